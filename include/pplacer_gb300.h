@@ -1,0 +1,260 @@
+/*
+ * pplacer_gb300 -- C ABI of the GB300 (sm_103a) placement-likelihood engine.
+ *
+ * Two layers, both plain C: pointers, sizes and status codes only.
+ *
+ * 1. The plain drop-in (pgb_* functions named after the linear_c.c symbol they
+ *    replace).  Each one has the argument meaning and order of the OCaml
+ *    external in pplacer_src/linear.ml:13-89; the OCaml bigarray dimensions
+ *    (Caml_ba_array_val(v)->dim[i]) become explicit int arguments.  All
+ *    pointers are HOST pointers to C-contiguous float64 / uint16 arrays with
+ *    the layout stated at pplacer_src/linear_c.c:6-12 (matrices [site][state],
+ *    tensors [rate][site][state]).  Each call copies its inputs to the GPU,
+ *    runs one sm_103a kernel in FP64 and copies the result back, so the
+ *    OCaml side keeps the FP64 values and exponent handling it relies on.
+ *    Like the reference, dimension mismatches are the caller's business and
+ *    log(0) yields -inf silently.  The CUDA context is created lazily on the
+ *    first call, so a process may fork before its first call (pplacer's
+ *    worker processes, pplacer_src/multiprocessing.ml:120-152).
+ *
+ * 2. The batched engine (pgb_engine_*): device-resident reference GLVs and
+ *    whole-query placement (pplacer_src/core.ml:222-557) in FP32 with exact
+ *    int32 per-site scaling exponents, stage-1 ranking, the baseball
+ *    heuristic, Brent or safeguarded-Newton branch-length optimisation and
+ *    the final refinement, for the Gamma-mixture (pplacer_src/gmix_model.ml)
+ *    and per-site CAT (pplacer_src/gcat_model.ml) models.
+ *
+ * Every function returns a pgb_status (or, for the drop-in log functions, the
+ * double result); pgb_last_error() describes the last failure of the calling
+ * thread.  A missing or unusable GPU is an error, never a silent CPU path.
+ */
+#ifndef PPLACER_GB300_H
+#define PPLACER_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  PGB_OK = 0,
+  PGB_ERR_ARG = 1,       /* invalid argument or size */
+  PGB_ERR_CUDA = 2,      /* CUDA runtime failure (no GPU, launch error, ...) */
+  PGB_ERR_NOMEM = 3,     /* device or host allocation failed */
+  PGB_ERR_STATE = 4,     /* call out of order (e.g. place before GLVs exist) */
+  PGB_ERR_QUERY = 5      /* query-level failure; see the per-query status */
+} pgb_status;
+
+const char *pgb_last_error(void);
+/* Number of kernels this library launched on the calling process's streams. */
+uint64_t pgb_kernel_launch_count(void);
+
+/* ----------------------------------------------------------------------------
+ * 1. Plain drop-in for pplacer_src/linear_c.c
+ * ------------------------------------------------------------------------- */
+
+/* gemmish_c (linear_c.c:29-90; linear.ml:13): dst[s,i] = sum_j a[i,j] b[s,j] */
+pgb_status pgb_gemmish(double *dst, const double *a, const double *b, int n_sites, int n_states);
+
+/* dediagonalize (linear_c.c:92-146; linear.ml:19):
+ * dst[i,j] = sum_k lambda[k] u[i,k] uit[j,k] */
+pgb_status pgb_dediagonalize(double *dst, const double *u, const double *lambda, const double *uit, int n);
+
+/* mat_log_like3_c (linear_c.c:170-216; linear.ml:28) */
+double pgb_mat_log_like3(const double *statd, const double *x, const double *y, const double *z, int n_sites,
+                         int n_states);
+
+/* mat_pairwise_prod_c (linear_c.c:218-230; linear.ml:31) */
+pgb_status pgb_mat_pairwise_prod(double *dst, const double *x, const double *y, int n_sites, int n_states);
+
+/* mat_statd_pairwise_prod_c (linear_c.c:232-249; linear.ml:34) */
+pgb_status pgb_mat_statd_pairwise_prod(const double *statd, double *dst, const double *a, const double *b,
+                                       int n_sites, int n_states);
+
+/* mat_masked_logdot_c (linear_c.c:251-296; linear.ml:40) */
+double pgb_mat_masked_logdot(const double *x, const double *y, const uint16_t *mask, int n_sites, int n_states);
+
+/* mat_bounded_logdot_c (linear_c.c:298-340; linear.ml:46) */
+double pgb_mat_bounded_logdot(const double *x, const double *y, int first, int last, int n_sites, int n_states);
+
+/* ten_log_like3_c (linear_c.c:367-424; linear.ml:55); util: n_sites scratch
+ * that receives the per-site likelihoods summed over rates, as the reference. */
+double pgb_ten_log_like3(const double *statd, const double *x, const double *y, const double *z, double *util,
+                         int n_rates, int n_sites, int n_states);
+
+/* ten_pairwise_prod_c (linear_c.c:426-441; linear.ml:58) */
+pgb_status pgb_ten_pairwise_prod(double *dst, const double *x, const double *y, int n_rates, int n_sites,
+                                 int n_states);
+
+/* ten_statd_pairwise_prod_c (linear_c.c:443-463; linear.ml:61) */
+pgb_status pgb_ten_statd_pairwise_prod(const double *statd, double *dst, const double *a, const double *b,
+                                       int n_rates, int n_sites, int n_states);
+
+/* ten_masked_logdot_c (linear_c.c:465-539; linear.ml:67) */
+double pgb_ten_masked_logdot(const double *x, const double *y, const uint16_t *mask, double *util, int n_rates,
+                             int n_sites, int n_states);
+
+/* ten_bounded_logdot_c (linear_c.c:541-605; linear.ml:73) */
+double pgb_ten_bounded_logdot(const double *x, const double *y, int first, int last, double *util, int n_rates,
+                              int n_sites, int n_states);
+
+/* vec_pairwise_prod_c (linear_c.c:607-618; linear.ml:76) */
+pgb_status pgb_vec_pairwise_prod(double *dst, const double *x, const double *y, int n);
+
+/* int_vec_tot_c (linear_c.c:620-630; linear.ml:80) */
+int pgb_int_vec_tot(const uint16_t *x, int n);
+
+/* int_vec_pairwise_prod_c (linear_c.c:632-642; linear.ml:83): uint16 wraps */
+pgb_status pgb_int_vec_pairwise_prod(uint16_t *dst, const uint16_t *x, const uint16_t *y, int n);
+
+/* float_mat_int_vec_mul_c (linear_c.c:644-670; linear.ml:89):
+ * dst[j] += sum_i mat[i,j] vec[i], mat is n x k.  The reference's
+ * caml_failwith on mismatched sizes is the stub's job (it has the dims). */
+pgb_status pgb_float_mat_int_vec_mul(double *dst, const double *mat, const uint16_t *vec, int n, int k);
+
+/* ----------------------------------------------------------------------------
+ * 2. Batched placement engine
+ * ------------------------------------------------------------------------- */
+
+typedef struct pgb_engine pgb_engine;
+
+/* Model (the fields of Gmix_model.Model.t / Gcat_model.Model.t,
+ * gmix_model.ml:10-16, gcat_model.ml:33-41): Diagd x, lambda, xit
+ * (diagd.ml:155-161) with x diag(lambda) x^-1 the rate matrix; statd; the
+ * Gamma category rates (Gmix) or the CAT category rates (Gcat). */
+typedef struct {
+  int n_states;               /* 4 (nucleotide) or 20 (amino acid) */
+  int n_rates;                /* Gamma categories, or CAT categories */
+  int gcat;                   /* 0: Gamma mixture; 1: per-site CAT categories */
+  int n_sites;                /* pre-masked alignment length */
+  const double *statd;        /* [n_states] */
+  const double *x;            /* [n_states * n_states] */
+  const double *lambda;       /* [n_states] */
+  const double *xit;          /* [n_states * n_states] */
+  const double *rates;        /* [n_rates] */
+  const int *site_categories; /* [n_sites] CAT category of each site (gcat), else NULL */
+} pgb_model_desc;
+
+/* Reference tree: n_nodes nodes numbered post-order (children before parents,
+ * children of a node in increasing id order -- pplacer's Newick numbering,
+ * newick_parser.mly:50-59); parent[root] = -1; bl[i] = length of the edge
+ * above node i (the root's is taken as 0, newick_gtree.ml:145-157). */
+typedef struct {
+  int n_nodes;
+  const int *parent;
+  const double *bl;
+} pgb_tree_desc;
+
+pgb_status pgb_engine_create(const pgb_model_desc *model, const pgb_tree_desc *tree, pgb_engine **out);
+pgb_status pgb_engine_destroy(pgb_engine *e);
+
+/* Compute darr / parr / snodes on the GPU from the reference alignment
+ * (Like_stree.calc_distal_and_proximal, like_stree.ml:43-110; pull exponents
+ * at -10 and Glv_arr.prep_supernodes, pplacer_run.ml:332-340).  leaf_row[i] is
+ * the row of leaf i in seqs (n_rows x n_sites characters), -1 for inner nodes.
+ * Arithmetic in FP64; the placement copies are then stored in FP32 with int32
+ * exponents. */
+pgb_status pgb_engine_precompute(pgb_engine *e, const int *leaf_row, const char *seqs, int n_rows);
+
+/* Upload darr / parr / snodes that the caller computed (FP64 GLVs
+ * [n_nodes][R][n_sites][n_states] with int32 exponents [n_nodes][n_sites]; R
+ * is 1 for gcat).  snodes may be NULL, in which case they are rebuilt on the
+ * GPU from darr and parr. */
+pgb_status pgb_engine_set_glvs(pgb_engine *e, const double *darr, const int *darr_e, const double *parr,
+                               const int *parr_e, const double *snodes, const int *snodes_e);
+
+/* Read back one GLV of the stored FP32 copies as FP64 (which: 0 darr, 1 parr,
+ * 2 snode); a: [R][n_sites][n_states], ex: [n_sites]. */
+pgb_status pgb_engine_get_glv(pgb_engine *e, int which, int node, double *a, int *ex);
+
+/* Placement preferences (pplacer_src/prefs.ml:76-114 defaults in brackets). */
+typedef struct {
+  double start_pend;         /* [0.1] */
+  double max_pend;           /* [2.0] */
+  double initial_tolerance;  /* [0.01] stage-2 tolerance; the final pass uses 1e-5 (core.ml:160) */
+  int max_strikes;           /* [6]; 0 evaluates every edge */
+  double strike_box;         /* [3.0] */
+  int max_pitches;           /* [40] */
+  int keep_at_most;          /* [7] */
+  double keep_factor;        /* [0.01] */
+  int optimizer;             /* 0: Brent as the reference (minimization.ml:83-101);
+                                1: batched safeguarded Newton on the adjoint */
+} pgb_prefs;
+
+void pgb_prefs_default(pgb_prefs *p);
+
+/* One placement (pplacer_src/placement.ml:168-175 fields). */
+typedef struct {
+  int edge;       /* edge_num: node id below the edge */
+  int pad;
+  double like;    /* likelihood (log) */
+  double lwr;     /* like_weight_ratio */
+  double dist;    /* distal_length */
+  double pend;    /* pendant_length */
+} pgb_placement;
+
+/* Per-query status codes. */
+enum {
+  PGB_Q_OK = 0,
+  PGB_Q_NO_INFORMATIVE = 1, /* no informative site (core.ml:303-304) */
+  PGB_Q_EMPTY = 2,          /* every location failed (core.ml:465-467) */
+  PGB_Q_BAD_CHAR = 3,       /* unknown character (pplacer_run.ml:63-69) */
+  PGB_Q_START_FAILURE = 4   /* Brent start finder failure (minimization.ml:11-13,35-36) */
+};
+
+/* Place n_queries pre-masked query rows (n_queries x n_sites characters, host
+ * memory).  out: n_queries * keep_at_most slots, sorted by like_weight_ratio
+ * as Pquery.make_ml_sorted (pquery.ml:86-92); n_out[q] placements written;
+ * qstatus[q] a PGB_Q_* code.  Host buffers in, host buffers out. */
+pgb_status pgb_place(pgb_engine *e, const pgb_prefs *prefs, int n_queries, const char *seqs, pgb_placement *out,
+                     int *n_out, int *qstatus);
+
+/* The same placement split so the device part can be timed alone: load
+ * queries to the device, run the placement on them (no host traffic), fetch
+ * the results. */
+pgb_status pgb_queries_load(pgb_engine *e, int n_queries, const char *seqs);
+pgb_status pgb_queries_run(pgb_engine *e, const pgb_prefs *prefs);
+pgb_status pgb_queries_fetch(pgb_engine *e, pgb_placement *out, int *n_out, int *qstatus);
+
+/* Stage 1 alone on the loaded queries (Glv.masked_logdot against every
+ * supernode, core.ml:333-343): scores[q][i] for the i-th non-root node in
+ * increasing id order. */
+pgb_status pgb_queries_stage1(pgb_engine *e, const pgb_prefs *prefs, double *scores);
+
+/* Branch-length optimisation of explicit (query, location) trials on the
+ * loaded queries (Three_tax.optimize from the given start, core.ml:401-425 with
+ * the retry from default lengths).  optimizer: 0 Brent, 1 Newton;
+ * mode 0 optimises, mode 1 only evaluates logL and its derivatives at the
+ * start point (the forward/backward pair).  Outputs per trial:
+ * like, pend, dist, status (0 ok, 1 max-iter, 2 failed), n_evals, and
+ * derivs[6] = dL/dpend, dL/ddist, d2L/dpend2, d2L/ddist2, d2L/dpend ddist,
+ * (unused) at the final point. */
+typedef struct {
+  int query;
+  int edge;
+  double pend0, dist0;
+  double tol;
+} pgb_trial;
+
+typedef struct {
+  double like, pend, dist;
+  double derivs[6];
+  int status;
+  int n_evals;
+} pgb_trial_out;
+
+pgb_status pgb_queries_trials(pgb_engine *e, const pgb_prefs *prefs, int optimizer, int mode, int n_trials,
+                              const pgb_trial *trials, pgb_trial_out *out);
+
+/* Device time of the last pgb_queries_run by phase, from CUDA events on the
+ * engine's stream: [0] query prep, [1] stage-1 tables, [2] stage-1 scores and
+ * ranking, [3] stage-2 trials, [4] refinement and output; [5] total.
+ * counts[0..3]: stage-1 (query, edge) pairs, stage-2 trials, stage-2 objective
+ * evaluations, stage-2 site evaluations. */
+pgb_status pgb_engine_timings(pgb_engine *e, double *ms, double *counts);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

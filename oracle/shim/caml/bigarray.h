@@ -1,0 +1,1 @@
+#include "ocaml_shim.h"

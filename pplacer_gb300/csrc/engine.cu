@@ -1,0 +1,2022 @@
+// Batched placement engine (sm_103a).
+//
+// Device layout (HBM):
+//   darr, parr, snode : float [n_nodes][n_sites][planes][n_states]   site-major,
+//                       one site of all rate planes is contiguous (64 B for DNA G4)
+//   dexp, pexp, sexp  : int32 [n_nodes][n_sites] exact per-site scaling exponents
+//   lt                : float [n_edges][prim][n_sites] stage-1 log table
+//   queries           : codes, masked-site index lists (reind) and codes, lengths
+//
+// Pipeline of one placement call (pplacer_src/core.ml:222-557):
+//   query prep -> stage-1 log table (once per start_pend) -> stage-1 scores
+//   -> per-query ranking -> baseball rounds of speculative stage-2 trials ->
+//   keep / refine trials -> like_weight_ratio and output.
+#include <math.h>
+
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "pgb_common.cuh"
+
+namespace pgb {
+namespace {
+
+constexpr int kTrialThreads = 256;
+constexpr int kTrialWarps = kTrialThreads / 32;
+constexpr double kLn2 = 0.69314718055994530942;
+
+enum { ST_OK = 0, ST_MAXITER = 1, ST_FAILED = 2, ST_STARTFAIL = 3 };
+enum { BR_OK = 0, BR_GSLERR = 1, BR_MAXITER = 2, BR_STARTFAIL = 3 };
+
+// ---------------------------------------------------------------------------
+// Precompute kernels (FP64): like_stree.ml:43-110, pplacer_run.ml:332-340
+// ---------------------------------------------------------------------------
+
+// P_m(t) = X diag(exp(rate_m t lambda)) Xit^T for every node (diagd.ml:201-220,
+// exp((rate * bl) * l_k) then dediagonalize's (l_k X_ik) Xit_jk order).
+__global__ void k_node_pmats(double *pm, const double *__restrict__ bl, double scale, int n_nodes, int NM, int K,
+                             const double *__restrict__ X, const double *__restrict__ Xit,
+                             const double *__restrict__ lam, const double *__restrict__ rates) {
+  long n = (long)n_nodes * NM * K * K;
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+    int j = (int)(t % K);
+    int i = (int)((t / K) % K);
+    int m = (int)((t / (K * K)) % NM);
+    long node = t / ((long)K * K * NM);
+    double rb = rates[m] * (bl[node] * scale);
+    double acc = 0;
+    for (int k = 0; k < K; k++) acc += exp(rb * lam[k]) * X[i * K + k] * Xit[j * K + k];
+    pm[t] = acc;
+  }
+}
+
+// Pull the per-site exponent when the site's max (over planes and states) has
+// frexp exponent below thr (gmix_model.ml:163-187, gcat_model.ml:195-212).
+__device__ __forceinline__ void pull_site(double *v, int n, int *e, int thr) {
+  double mx = v[0];
+  for (int i = 1; i < n; i++) mx = fmax(mx, v[i]);
+  int te;
+  frexp(mx, &te);
+  if (te < thr) {
+    double f = ldexp(0.5, -te + 1);
+    for (int i = 0; i < n; i++) v[i] *= f;
+    *e += te;
+  }
+}
+
+// evolve one site of all planes: out[r][k] = sum_j P_m[k][j] in[r][j]
+__device__ __forceinline__ void evolve_site(double *out, const double *in, const double *pm_node, int RP, int K,
+                                            int gcat_cat) {
+  for (int r = 0; r < RP; r++) {
+    int m = gcat_cat >= 0 ? gcat_cat : r;
+    const double *P = pm_node + (long)m * K * K;
+    for (int k = 0; k < K; k++) {
+      double acc = 0;
+      for (int j = 0; j < K; j++) acc += P[k * K + j] * in[r * K + j];
+      out[r * K + k] = acc;
+    }
+  }
+}
+
+struct PreCtx {
+  int S, RP, K, NM, gcat;
+  const uint8_t *site_cat;
+  const double *lvd;     // [ncode][K]
+  const double *pm;      // [n_nodes][NM][K][K] at bl
+  const double *pmh;     // at bl/2
+  const double *statd;
+  double *distal, *evd, *prox;  // [n_nodes][S][RP][K]
+  int *de, *ee, *pe;            // [n_nodes][S]
+};
+
+// Leaves: distal = LV broadcast to every plane, evd = P distal.
+__global__ void k_leaves(PreCtx c, const int *__restrict__ leaves, int n_leaves, const uint8_t *__restrict__ codes) {
+  long n = (long)n_leaves * c.S;
+  int RK = c.RP * c.K;
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+    int li = (int)(t / c.S), s = (int)(t - (long)li * c.S);
+    int node = leaves[li];
+    long base = ((long)node * c.S + s) * RK;
+    int code = codes[(long)li * c.S + s];
+    for (int r = 0; r < c.RP; r++)
+      for (int k = 0; k < c.K; k++) c.distal[base + r * c.K + k] = c.lvd[code * c.K + k];
+    c.de[(long)node * c.S + s] = 0;
+    c.ee[(long)node * c.S + s] = 0;
+    evolve_site(c.evd + base, c.distal + base, c.pm + (long)node * c.NM * c.K * c.K, c.RP, c.K,
+                c.gcat ? c.site_cat[s] : -1);
+  }
+}
+
+// One post-order level: distal = product of children's evd in child order,
+// pull at -50, evd = P(bl) distal (like_stree.ml:148-174).
+__global__ void k_distal_level(PreCtx c, const int *__restrict__ nodes, int n_nodes_lvl,
+                               const int *__restrict__ ch_start, const int *__restrict__ ch_list) {
+  long n = (long)n_nodes_lvl * c.S;
+  int RK = c.RP * c.K;
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+    int ni = (int)(t / c.S), s = (int)(t - (long)ni * c.S);
+    int node = nodes[ni];
+    long base = ((long)node * c.S + s) * RK;
+    double *d = c.distal + base;
+    int c0 = ch_list[ch_start[node]];
+    int e = c.ee[(long)c0 * c.S + s];
+    long b0 = ((long)c0 * c.S + s) * RK;
+    for (int i = 0; i < RK; i++) d[i] = c.evd[b0 + i];
+    for (int ci = ch_start[node] + 1; ci < ch_start[node + 1]; ci++) {
+      int ch = ch_list[ci];
+      long bc = ((long)ch * c.S + s) * RK;
+      for (int i = 0; i < RK; i++) d[i] = d[i] * c.evd[bc + i];
+      e += c.ee[(long)ch * c.S + s];
+    }
+    pull_site(d, RK, &e, -50);
+    c.de[(long)node * c.S + s] = e;
+    c.ee[(long)node * c.S + s] = e;
+    evolve_site(c.evd + base, d, c.pm + (long)node * c.NM * c.K * c.K, c.RP, c.K, c.gcat ? c.site_cat[s] : -1);
+  }
+}
+
+// One pre-order level: prox[child] = P(bl_parent) prox[parent] times the
+// siblings' evd in child order, pull at -50 (like_stree.ml:179-205).
+__global__ void k_prox_level(PreCtx c, const int *__restrict__ nodes, int n_nodes_lvl, const int *__restrict__ parent,
+                             const int *__restrict__ ch_start, const int *__restrict__ ch_list) {
+  long n = (long)n_nodes_lvl * c.S;
+  int RK = c.RP * c.K;
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+    int ni = (int)(t / c.S), s = (int)(t - (long)ni * c.S);
+    int node = nodes[ni];
+    int p = parent[node];
+    long base = ((long)node * c.S + s) * RK;
+    double *out = c.prox + base;
+    evolve_site(out, c.prox + ((long)p * c.S + s) * RK, c.pm + (long)p * c.NM * c.K * c.K, c.RP, c.K,
+                c.gcat ? c.site_cat[s] : -1);
+    int e = c.pe[(long)p * c.S + s];
+    for (int ci = ch_start[p]; ci < ch_start[p + 1]; ci++) {
+      int sib = ch_list[ci];
+      if (sib == node) continue;
+      long bs = ((long)sib * c.S + s) * RK;
+      for (int i = 0; i < RK; i++) out[i] = out[i] * c.evd[bs + i];
+      e += c.ee[(long)sib * c.S + s];
+    }
+    pull_site(out, RK, &e, -50);
+    c.pe[(long)node * c.S + s] = e;
+  }
+}
+
+__global__ void k_set_unit(double *g, int *e, long n_vals, long n_exps) {
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n_vals; t += (long)gridDim.x * blockDim.x) {
+    g[t] = 1.0;
+    if (t < n_exps) e[t] = 0;
+  }
+}
+
+// Pull at -10, supernode = statd (P(bl/2) d) (P(bl/2) p), FP32 copies
+// (pplacer_run.ml:332-340, glv_arr.ml:92-102).
+__global__ void k_finish_glvs(PreCtx c, int n_nodes, float *d32, float *p32, float *s32, int *dexp, int *pexp,
+                              int *sexp) {
+  long n = (long)n_nodes * c.S;
+  int RK = c.RP * c.K;
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+    int node = (int)(t / c.S), s = (int)(t - (long)node * c.S);
+    long base = t * RK;
+    double *d = c.distal + base, *p = c.prox + base;
+    int ed = c.de[t], ep = c.pe[t];
+    pull_site(d, RK, &ed, -10);
+    pull_site(p, RK, &ep, -10);
+    dexp[t] = ed;
+    pexp[t] = ep;
+    int cat = c.gcat ? c.site_cat[s] : -1;
+    const double *P = c.pmh + (long)node * c.NM * c.K * c.K;
+    for (int r = 0; r < c.RP; r++) {
+      int m = cat >= 0 ? cat : r;
+      const double *Pm = P + (long)m * c.K * c.K;
+      for (int k = 0; k < c.K; k++) {
+        double ud = 0, up = 0;
+        for (int j = 0; j < c.K; j++) {
+          ud += Pm[k * c.K + j] * d[r * c.K + j];
+          up += Pm[k * c.K + j] * p[r * c.K + j];
+        }
+        s32[base + r * c.K + k] = (float)(c.statd[k] * ud * up);
+        d32[base + r * c.K + k] = (float)d[r * c.K + k];
+        p32[base + r * c.K + k] = (float)p[r * c.K + k];
+      }
+    }
+    sexp[t] = ed + ep;
+  }
+}
+
+// Caller-provided FP64 GLVs [node][R][S][K] -> FP32 site-major.
+__global__ void k_import_glv(const double *__restrict__ src, const int *__restrict__ se, float *dst, int *de,
+                             int n_nodes, int S, int RP, int K) {
+  long n = (long)n_nodes * RP * S * K;
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+    int k = (int)(t % K);
+    int s = (int)((t / K) % S);
+    int r = (int)((t / ((long)K * S)) % RP);
+    long node = t / ((long)K * S * RP);
+    dst[((node * S + s) * RP + r) * K + k] = (float)src[t];
+    if (r == 0 && k == 0) de[node * S + s] = se[node * S + s];
+  }
+}
+
+// Supernodes from FP64 darr/parr in the caller's [node][R][S][K] layout.
+__global__ void k_snodes_from(const double *__restrict__ d, const double *__restrict__ p, const int *__restrict__ de,
+                              const int *__restrict__ pe, const double *__restrict__ pmh,
+                              const double *__restrict__ statd, const uint8_t *__restrict__ site_cat, int gcat,
+                              float *s32, int *sexp, int n_nodes, int S, int RP, int K, int NM) {
+  long n = (long)n_nodes * S;
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+    long node = t / S;
+    int s = (int)(t - node * S);
+    for (int r = 0; r < RP; r++) {
+      int m = gcat ? site_cat[s] : r;
+      const double *Pm = pmh + (node * NM + m) * K * K;
+      const double *dv = d + ((node * RP + r) * S + s) * K, *pv = p + ((node * RP + r) * S + s) * K;
+      for (int k = 0; k < K; k++) {
+        double ud = 0, up = 0;
+        for (int j = 0; j < K; j++) {
+          ud += Pm[k * K + j] * dv[j];
+          up += Pm[k * K + j] * pv[j];
+        }
+        s32[(t * RP + r) * K + k] = (float)(statd[k] * ud * up);
+      }
+    }
+    sexp[t] = de[t] + pe[t];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Query preparation: character codes, informative mask, masked site lists
+// (core.ml:267-304).  One CTA per query.
+// ---------------------------------------------------------------------------
+__global__ void k_query_prep(const char *__restrict__ seqs, int S, const uint8_t *__restrict__ char_code,
+                             const uint8_t *__restrict__ informative, uint8_t *qcode, uint16_t *reind,
+                             uint8_t *mcode, int *qlen, int *qstatus) {
+  int q = blockIdx.x;
+  const char *seq = seqs + (long)q * S;
+  __shared__ int s_off;
+  __shared__ int s_bad;
+  __shared__ int s_warp[32];
+  if (threadIdx.x == 0) { s_off = 0; s_bad = 0; }
+  __syncthreads();
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int base = 0; base < S; base += blockDim.x) {
+    int s = base + threadIdx.x;
+    uint8_t c = kBadCode;
+    int inf = 0;
+    if (s < S) {
+      c = char_code[(uint8_t)seq[s]];
+      if (c == kBadCode) atomicOr(&s_bad, 1);
+      else inf = informative[c];
+      qcode[(long)q * S + s] = c;
+    }
+    unsigned bal = __ballot_sync(0xffffffffu, inf);
+    if (lane == 0) s_warp[w] = __popc(bal);
+    __syncthreads();
+    int before = 0, tot = 0;
+    for (int i = 0; i < nw; i++) {
+      if (i < w) before += s_warp[i];
+      tot += s_warp[i];
+    }
+    if (inf) {
+      int pos = s_off + before + __popc(bal & ((1u << lane) - 1u));
+      reind[(long)q * S + pos] = (uint16_t)s;
+      mcode[(long)q * S + pos] = c;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) s_off += tot;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    qlen[q] = s_off;
+    qstatus[q] = s_bad ? PGB_Q_BAD_CHAR : (s_off == 0 ? PGB_Q_NO_INFORMATIVE : PGB_Q_OK);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Stage 1 (core.ml:333-343, Glv.masked_logdot against every supernode).
+// The query side is the full query evolved by start_pend; its value at a
+// site depends only on the site's character, so log(sum_r sum_k qe_c * snode)
+// is tabulated per (edge, primary character, site) once per start_pend and the
+// per-(query, edge) score becomes a gather-sum over the query's informative
+// sites.  Characters outside the primary set are computed from the supernode.
+// ---------------------------------------------------------------------------
+struct S1Ctx {
+  int S, RP, K, NM, gcat, ncode, prim, n_edges;
+  const float *snode;        // [n_nodes][S][RP][K]
+  const int *sexp;           // [n_nodes][S]
+  const int *edge_nodes;     // [n_edges]
+  const float *qe;           // [NM][ncode][K] evolved query LV per character
+  const uint8_t *site_cat;
+  float *lt;                 // [n_edges][prim][S]
+  double log_nrates;         // log((float)R) (Gmix), 0 (Gcat)
+};
+
+__device__ __forceinline__ float s1_util(const S1Ctx &c, int node, int s, int code) {
+  const float *sn = c.snode + ((long)node * c.S + s) * c.RP * c.K;
+  float u = 0.f;
+  for (int r = 0; r < c.RP; r++) {
+    int m = c.gcat ? c.site_cat[s] : r;
+    const float *q = c.qe + ((long)m * c.ncode + code) * c.K;
+    for (int k = 0; k < c.K; k++) u += q[k] * sn[r * c.K + k];
+  }
+  return u;
+}
+
+__global__ void k_lt_build(S1Ctx c) {
+  long n = (long)c.n_edges * c.S;
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+    int ei = (int)(t / c.S), s = (int)(t - (long)ei * c.S);
+    int node = c.edge_nodes[ei];
+    for (int code = 0; code < c.prim; code++)
+      c.lt[((long)ei * c.prim + code) * c.S + s] = (float)log((double)s1_util(c, node, s, code));
+  }
+}
+
+// grid (edge tiles, query tiles); ET edges' log tables and exponents staged in
+// shared memory; one warp per query, lanes over the query's sites.
+template <int ET>
+__global__ void __launch_bounds__(256) k_stage1(S1Ctx c, int Q, int q_per_cta, const uint16_t *__restrict__ reind,
+                                                const uint8_t *__restrict__ mcode, const int *__restrict__ qlen,
+                                                const int *__restrict__ qstatus, double *scores) {
+  extern __shared__ float s1_smem[];
+  int e0 = blockIdx.x * ET;
+  int ne = min(ET, c.n_edges - e0);
+  float *slt = s1_smem;                                   // [ET][prim][S]
+  int *sex = reinterpret_cast<int *>(slt + (long)ET * c.prim * c.S);  // [ET][S]
+  for (int e = 0; e < ne; e++) {
+    const float *src = c.lt + (long)(e0 + e) * c.prim * c.S;
+    for (int i = threadIdx.x; i < c.prim * c.S; i += blockDim.x) slt[(long)e * c.prim * c.S + i] = src[i];
+    const int *xs = c.sexp + (long)c.edge_nodes[e0 + e] * c.S;
+    for (int i = threadIdx.x; i < c.S; i += blockDim.x) sex[(long)e * c.S + i] = xs[i];
+  }
+  __syncthreads();
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  int q0 = blockIdx.y * q_per_cta;
+  int q1 = min(Q, q0 + q_per_cta);
+  for (int q = q0 + w; q < q1; q += nw) {
+    if (qstatus[q] != PGB_Q_OK) continue;
+    int n = qlen[q];
+    const uint16_t *ri = reind + (long)q * c.S;
+    const uint8_t *mc = mcode + (long)q * c.S;
+    float acc[ET];
+    int eacc[ET];
+#pragma unroll
+    for (int e = 0; e < ET; e++) { acc[e] = 0.f; eacc[e] = 0; }
+    for (int i = lane; i < n; i += 32) {
+      int s = ri[i];
+      int code = mc[i];
+      if (code < c.prim) {
+#pragma unroll
+        for (int e = 0; e < ET; e++) {
+          acc[e] += slt[((long)e * c.prim + code) * c.S + s];
+          eacc[e] += sex[(long)e * c.S + s];
+        }
+      } else {
+#pragma unroll
+        for (int e = 0; e < ET; e++) {
+          if (e < ne) acc[e] += (float)log((double)s1_util(c, c.edge_nodes[e0 + e], s, code));
+          eacc[e] += sex[(long)e * c.S + s];
+        }
+      }
+    }
+#pragma unroll
+    for (int e = 0; e < ET; e++) {
+      double a = warp_sum_d((double)acc[e]);
+      long long x = warp_sum_ll((long long)eacc[e]);
+      if (lane == 0 && e < ne)
+        scores[(long)q * c.n_edges + e0 + e] = a - (double)(float)n * c.log_nrates + kLn2 * (double)x;
+    }
+  }
+}
+
+// Per-query ranking: the top rk edges by score, descending, ties to the lower
+// edge index (stable sort of the ascending edge list, fig.ml:143-147; NaN
+// sorts below every number as OCaml's compare does).
+__device__ __forceinline__ bool s1_better(double a, int ia, double b, int ib) {
+  bool na = isnan(a), nb = isnan(b);
+  if (na != nb) return nb;
+  if (!na && a != b) return a > b;
+  return ia < ib;
+}
+
+__global__ void k_rank(const double *__restrict__ scores, int n_edges, int rk, const int *__restrict__ qstatus,
+                       int *rank) {
+  int q = blockIdx.x;
+  if (qstatus[q] != PGB_Q_OK) return;
+  extern __shared__ unsigned rk_taken[];
+  int words = (n_edges + 31) / 32;
+  for (int i = threadIdx.x; i < words; i += blockDim.x) rk_taken[i] = 0u;
+  __shared__ double bw_s[32];
+  __shared__ int bw_i[32];
+  __syncthreads();
+  const double *sc = scores + (long)q * n_edges;
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int r = 0; r < rk; r++) {
+    double bs = 0;
+    int bi = -1;
+    for (int i = threadIdx.x; i < n_edges; i += blockDim.x) {
+      if (rk_taken[i >> 5] & (1u << (i & 31))) continue;
+      double v = sc[i];
+      if (bi < 0 || s1_better(v, i, bs, bi)) { bs = v; bi = i; }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      double os = __shfl_down_sync(0xffffffffu, bs, o);
+      int oi = __shfl_down_sync(0xffffffffu, bi, o);
+      if (oi >= 0 && (bi < 0 || s1_better(os, oi, bs, bi))) { bs = os; bi = oi; }
+    }
+    if (lane == 0) { bw_s[w] = bs; bw_i[w] = bi; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double b = 0;
+      int ii = -1;
+      for (int i = 0; i < nw; i++)
+        if (bw_i[i] >= 0 && (ii < 0 || s1_better(bw_s[i], bw_i[i], b, ii))) { b = bw_s[i]; ii = bw_i[i]; }
+      rank[(long)q * rk + r] = ii;
+      if (ii >= 0) rk_taken[ii >> 5] |= 1u << (ii & 31);
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Stage-2 trials: one CTA per (query, location) optimisation.
+// Warp 0 runs the scalar optimiser (Brent with GSL's conventions, or
+// safeguarded Newton) in FP64; every warp evaluates the objective over its
+// share of the query's informative sites.  The evaluation protocol uses named
+// barrier 1 with all threads of the CTA; warp 0 always ends the protocol with
+// a stop command, every loop in it is bounded.
+// ---------------------------------------------------------------------------
+struct TrialIn {
+  int q, node;
+  double pend0, dist0, tol;
+};
+struct TrialRes {
+  double like, pend, dist;
+  double der[6];
+  int status, n_evals;
+};
+
+struct TrialCtx {
+  const float *darr, *parr;
+  const int *dexp, *pexp;
+  int S, RP, K, NM, ncode, gcat;
+  const double *bl;
+  const uint16_t *reind;
+  const uint8_t *mcode;
+  const int *qlen;
+  const uint8_t *site_cat;
+  const float *X, *W, *Lt, *lvf, *statd, *lam, *rates;
+  double log_nrates;
+  double start_pend, max_pend;
+  int optimizer, mode;
+  int smem_win, cap;
+};
+
+struct Ctrl {
+  double pend, dist, prox;
+  int cmd;  // 0 stop, 1 value, 2 value + derivatives
+};
+
+__device__ __forceinline__ void bar1() { asm volatile("bar.sync 1, %0;" ::"r"(kTrialThreads) : "memory"); }
+
+// shared memory carve-up of one trial CTA
+struct TrialSmem {
+  float *D, *P;              // [RP][cap][K]
+  uint8_t *code, *cat;       // [cap]
+  float *Md, *Mp, *Md1, *Md2, *Mp1, *Mp2;  // [NM][K][K]
+  float *Z, *Z1, *Z2;        // [NM][ncode][K]
+  float *E, *Em1, *Lr;       // [3][NM][K], [3][NM][K], [NM][K]
+  float *red;                // [warps][8]
+  int *redi;                 // [warps]
+  Ctrl *ctrl;
+};
+
+__host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
+
+__host__ __device__ inline size_t trial_smem_bytes(int cap, int win, int RP, int K, int NM, int ncode) {
+  size_t b = 0;
+  if (win) b += 2 * align16((size_t)RP * cap * K * 4);
+  b += 2 * align16((size_t)cap);
+  b += 6 * align16((size_t)NM * K * K * 4);
+  b += 3 * align16((size_t)NM * ncode * K * 4);
+  b += 2 * align16((size_t)3 * NM * K * 4) + align16((size_t)NM * K * 4);
+  b += align16(kTrialWarps * 8 * 4) + align16(kTrialWarps * 4);
+  b += align16(sizeof(Ctrl));
+  return b;
+}
+
+__device__ inline TrialSmem carve(char *base, int cap, int win, int RP, int K, int NM, int ncode) {
+  TrialSmem s;
+  char *p = base;
+  auto take = [&](size_t bytes) { char *r = p; p += align16(bytes); return r; };
+  s.D = win ? (float *)take((size_t)RP * cap * K * 4) : nullptr;
+  s.P = win ? (float *)take((size_t)RP * cap * K * 4) : nullptr;
+  s.code = (uint8_t *)take(cap);
+  s.cat = (uint8_t *)take(cap);
+  size_t mb = (size_t)NM * K * K * 4;
+  s.Md = (float *)take(mb); s.Mp = (float *)take(mb); s.Md1 = (float *)take(mb);
+  s.Md2 = (float *)take(mb); s.Mp1 = (float *)take(mb); s.Mp2 = (float *)take(mb);
+  size_t zb = (size_t)NM * ncode * K * 4;
+  s.Z = (float *)take(zb); s.Z1 = (float *)take(zb); s.Z2 = (float *)take(zb);
+  s.E = (float *)take((size_t)3 * NM * K * 4);
+  s.Em1 = (float *)take((size_t)3 * NM * K * 4);
+  s.Lr = (float *)take((size_t)NM * K * 4);
+  s.red = (float *)take(kTrialWarps * 8 * 4);
+  s.redi = (int *)take(kTrialWarps * 4);
+  s.ctrl = (Ctrl *)take(sizeof(Ctrl));
+  return s;
+}
+
+struct EvalOut {
+  double L;
+  double g[2], h[3];
+};
+
+// All threads: one objective evaluation at ctrl (pend, dist, prox).  Contains
+// exactly three bar1() calls.  Warp 0 gets the combined values.
+template <int K>
+__device__ __noinline__ void eval_part(const TrialCtx &c, const TrialSmem &sm, int q, int node, int Sq, bool derivs,
+                                       double exp_const, EvalOut *out) {
+  const int tid = threadIdx.x;
+  const int NM = c.NM, nc = c.ncode;
+  const Ctrl ctl = *sm.ctrl;
+  // phase 1: exp factors for (dist, prox, pend)
+  for (int i = tid; i < 3 * NM * K; i += kTrialThreads) {
+    int which = i / (NM * K), mk = i - which * NM * K;
+    int m = mk / K, k = mk - m * K;
+    float lr = c.rates[m] * c.lam[k];
+    float t = (float)(which == 0 ? ctl.dist : (which == 1 ? ctl.prox : ctl.pend));
+    float a = lr * t;
+    sm.E[i] = expf(a);
+    sm.Em1[i] = expm1f(a);
+    if (which == 0) sm.Lr[mk] = lr;
+  }
+  bar1();
+  // phase 2: transition matrices P = I + X diag(expm1) Xit^T and derivatives;
+  // evolved query vectors per character with statd folded in
+  const int nmat = NM * K * K;
+  for (int i = tid; i < 2 * nmat; i += kTrialThreads) {
+    int which = i / nmat, r = i - which * nmat;
+    int m = r / (K * K), ij = r - m * K * K;
+    int ii = ij / K, jj = ij - ii * K;
+    const float *w = c.W + (long)ij * K;
+    const float *em = sm.Em1 + (which * NM + m) * K;
+    float acc = (ii == jj) ? 1.f : 0.f;
+#pragma unroll 4
+    for (int k = 0; k < K; k++) acc += w[k] * em[k];
+    (which == 0 ? sm.Md : sm.Mp)[r] = acc;
+    if (derivs) {
+      const float *e = sm.E + (which * NM + m) * K;
+      const float *lr = sm.Lr + m * K;
+      float a1 = 0.f, a2 = 0.f;
+#pragma unroll 4
+      for (int k = 0; k < K; k++) {
+        float t1 = w[k] * lr[k] * e[k];
+        a1 += t1;
+        a2 += t1 * lr[k];
+      }
+      (which == 0 ? sm.Md1 : sm.Mp1)[r] = a1;
+      (which == 0 ? sm.Md2 : sm.Mp2)[r] = a2;
+    }
+  }
+  const int nz = NM * nc * K;
+  for (int i = tid; i < nz; i += kTrialThreads) {
+    int m = i / (nc * K), ck = i - m * nc * K;
+    int code = ck / K, ii = ck - code * K;
+    const float *x = c.X + ii * K;
+    const float *lt = c.Lt + code * K;
+    const float *em = sm.Em1 + (2 * NM + m) * K;
+    float acc = c.lvf[code * K + ii];
+#pragma unroll 4
+    for (int k = 0; k < K; k++) acc += x[k] * em[k] * lt[k];
+    float pi = c.statd[ii];
+    sm.Z[i] = pi * acc;
+    if (derivs) {
+      const float *e = sm.E + (2 * NM + m) * K;
+      const float *lr = sm.Lr + m * K;
+      float a1 = 0.f, a2 = 0.f;
+#pragma unroll 4
+      for (int k = 0; k < K; k++) {
+        float t1 = x[k] * lr[k] * e[k] * lt[k];
+        a1 += t1;
+        a2 += t1 * lr[k];
+      }
+      sm.Z1[i] = pi * a1;
+      sm.Z2[i] = pi * a2;
+    }
+  }
+  bar1();
+  // phase 3: sites
+  float m_acc = 1.f;
+  int e_acc = 0;
+  float gp = 0.f, gd = 0.f, hpp = 0.f, hdd = 0.f, hpd = 0.f;
+  const float *gd_base = c.darr + (long)node * c.S * c.RP * K;
+  const float *gp_base = c.parr + (long)node * c.S * c.RP * K;
+  for (int i = tid; i < Sq; i += kTrialThreads) {
+    int code = sm.code[i];
+    float u = 0.f, ud = 0.f, udd = 0.f, up = 0.f, upp = 0.f, upd = 0.f;
+    int s = 0;
+    if (!c.smem_win) s = c.reind[(long)q * c.S + i];
+    for (int r = 0; r < c.RP; r++) {
+      int m = c.gcat ? sm.cat[i] : r;
+      float dv[K], pv[K];
+      const float *ds = c.smem_win ? sm.D + ((long)r * c.cap + i) * K : gd_base + ((long)s * c.RP + r) * K;
+      const float *ps = c.smem_win ? sm.P + ((long)r * c.cap + i) * K : gp_base + ((long)s * c.RP + r) * K;
+      if (K % 4 == 0) {
+#pragma unroll
+        for (int k = 0; k < K; k += 4) {
+          float4 a = *reinterpret_cast<const float4 *>(ds + k);
+          float4 b = *reinterpret_cast<const float4 *>(ps + k);
+          dv[k] = a.x; dv[k + 1] = a.y; dv[k + 2] = a.z; dv[k + 3] = a.w;
+          pv[k] = b.x; pv[k + 1] = b.y; pv[k + 2] = b.z; pv[k + 3] = b.w;
+        }
+      } else {
+#pragma unroll
+        for (int k = 0; k < K; k++) { dv[k] = ds[k]; pv[k] = ps[k]; }
+      }
+      const float *Md = sm.Md + m * K * K, *Mp = sm.Mp + m * K * K;
+      const float *z = sm.Z + (m * nc + code) * K;
+#pragma unroll(K <= 4 ? K : 1)
+      for (int ii = 0; ii < K; ii++) {
+        float x = 0.f, y = 0.f;
+#pragma unroll
+        for (int j = 0; j < K; j++) {
+          x += Md[ii * K + j] * dv[j];
+          y += Mp[ii * K + j] * pv[j];
+        }
+        float xy = x * y;
+        u += z[ii] * xy;
+        if (derivs) {
+          const float *Md1 = sm.Md1 + m * K * K, *Md2 = sm.Md2 + m * K * K;
+          const float *Mp1 = sm.Mp1 + m * K * K, *Mp2 = sm.Mp2 + m * K * K;
+          float x1 = 0.f, x2 = 0.f, y1 = 0.f, y2 = 0.f;
+#pragma unroll
+          for (int j = 0; j < K; j++) {
+            x1 += Md1[ii * K + j] * dv[j];
+            x2 += Md2[ii * K + j] * dv[j];
+            y1 += Mp1[ii * K + j] * pv[j];
+            y2 += Mp2[ii * K + j] * pv[j];
+          }
+          float z1 = sm.Z1[(m * nc + code) * K + ii], z2 = sm.Z2[(m * nc + code) * K + ii];
+          float a = x1 * y - x * y1;
+          float b = x2 * y - 2.f * x1 * y1 + x * y2;
+          ud += z[ii] * a;
+          udd += z[ii] * b;
+          up += z1 * xy;
+          upp += z2 * xy;
+          upd += z1 * a;
+        }
+      }
+    }
+    int eu;
+    float mu = frexpf(u, &eu);
+    m_acc *= mu;
+    e_acc += eu;
+    int em;
+    m_acc = frexpf(m_acc, &em);
+    e_acc += em;
+    if (derivs) {
+      float inv = 1.f / u;
+      float lp = up * inv, ld = ud * inv;
+      gp += lp;
+      gd += ld;
+      hpp += upp * inv - lp * lp;
+      hdd += udd * inv - ld * ld;
+      hpd += upd * inv - lp * ld;
+    }
+  }
+  // warp combine: mantissa product with exponent carry, derivative sums
+  for (int o = 16; o > 0; o >>= 1) {
+    float mo = __shfl_down_sync(0xffffffffu, m_acc, o);
+    int eo = __shfl_down_sync(0xffffffffu, e_acc, o);
+    m_acc *= mo;
+    e_acc += eo;
+    int em;
+    m_acc = frexpf(m_acc, &em);
+    e_acc += em;
+  }
+  if (derivs) {
+    gp = warp_sum_f(gp); gd = warp_sum_f(gd);
+    hpp = warp_sum_f(hpp); hdd = warp_sum_f(hdd); hpd = warp_sum_f(hpd);
+  }
+  int lane = tid & 31, w = tid >> 5;
+  if (lane == 0) {
+    sm.red[w * 8 + 0] = m_acc;
+    sm.redi[w] = e_acc;
+    sm.red[w * 8 + 1] = gp; sm.red[w * 8 + 2] = gd;
+    sm.red[w * 8 + 3] = hpp; sm.red[w * 8 + 4] = hdd; sm.red[w * 8 + 5] = hpd;
+  }
+  bar1();
+  if (w == 0) {
+    float mt = 1.f;
+    int et = 0;
+    double sg[5] = {0, 0, 0, 0, 0};
+    for (int i = 0; i < kTrialWarps; i++) {
+      mt *= sm.red[i * 8];
+      et += sm.redi[i];
+      int em;
+      mt = frexpf(mt, &em);
+      et += em;
+      if (derivs)
+        for (int k = 0; k < 5; k++) sg[k] += (double)sm.red[i * 8 + 1 + k];
+    }
+    out->L = (double)et * kLn2 + (double)logf(mt) - (double)(float)Sq * c.log_nrates + exp_const;
+    out->g[0] = sg[0]; out->g[1] = sg[1];
+    out->h[0] = sg[2]; out->h[1] = sg[3]; out->h[2] = sg[4];
+  }
+}
+
+// Warp-0 side of the protocol.
+template <int K>
+struct Evaluator {
+  const TrialCtx *c;
+  const TrialSmem *sm;
+  int q, node, Sq;
+  double exp_const;
+  double pend, dist, prox;  // three-taxon state (three_tax.ml:252-258)
+  double L_last;
+  int n_evals;
+  EvalOut last;
+
+  __device__ double eval(bool derivs) {
+    if ((threadIdx.x & 31) == 0) {
+      sm->ctrl->pend = pend;
+      sm->ctrl->dist = dist;
+      sm->ctrl->prox = prox;
+      sm->ctrl->cmd = derivs ? 2 : 1;
+    }
+    __syncwarp();
+    bar1();
+    eval_part<K>(*c, *sm, q, node, Sq, derivs, exp_const, &last);
+    n_evals++;
+    L_last = last.L;
+    return last.L;
+  }
+  __device__ void stop() {
+    if ((threadIdx.x & 31) == 0) sm->ctrl->cmd = 0;
+    __syncwarp();
+    bar1();
+  }
+};
+
+// Brent minimisation with GSL's conventions (minimization.ml:24-41,83-101;
+// gsl_min_fminimizer_brent).  f(v) sets the state and returns -logL.
+template <class F>
+__device__ int brent_dev(F &f, double raw_start, double left, double right, double tol, double *xout) {
+  const int max_iters = 100;
+  if (left >= raw_start || raw_start >= right) return BR_STARTFAIL;
+  double righty = f(right);
+  double lefty = f(left);
+  double smaller = lefty < righty ? left : right;
+  double miny = lefty <= righty ? lefty : righty;  // Stdlib.min
+  double prev = raw_start, pv;
+  for (int iter = 1;; iter++) {
+    pv = f(prev);
+    if (pv < miny) break;
+    if (fabs(prev - smaller) < tol) { *xout = smaller; return BR_OK; }  // FoundMin
+    if (iter > max_iters) return BR_STARTFAIL;
+    prev = (prev + smaller) / 2.;
+  }
+  double xl = left, xu = right, xm = prev;
+  double fl = lefty, fu = righty, fm = pv;
+  if (!isfinite(fl) || !isfinite(fu) || !isfinite(fm)) return BR_GSLERR;
+  if (xl > xu || xm >= xu || xm <= xl || fm >= fl || fm >= fu) return BR_GSLERR;
+  const double golden = 0.3819660;
+  double v = xl + golden * (xu - xl), w = v;
+  double fv = f(v);
+  if (!isfinite(fv)) return BR_GSLERR;
+  double fw = fv, d = 0, e = 0;
+  for (int step = 1;; step++) {
+    if (step > max_iters) return BR_MAXITER;
+    double z = xm, fz = fm;
+    double dd = e, ee = d;
+    double wl = z - xl, wu = xu - z;
+    double tolerance = 1.4901161193847656e-08 * fabs(z);
+    double p = 0, qq = 0, r = 0;
+    double mid = 0.5 * (xl + xu);
+    double u;
+    if (fabs(ee) > tolerance) {
+      r = (z - w) * (fz - fv);
+      qq = (z - v) * (fz - fw);
+      p = (z - v) * qq - (z - w) * r;
+      qq = 2 * (qq - r);
+      if (qq > 0) p = -p; else qq = -qq;
+      r = ee;
+      ee = dd;
+    }
+    if (fabs(p) < fabs(0.5 * qq * r) && p < qq * wl && p < qq * wu) {
+      double t2 = 2 * tolerance;
+      dd = p / qq;
+      u = z + dd;
+      if ((u - xl) < t2 || (xu - u) < t2) dd = (z < mid) ? tolerance : -tolerance;
+    } else {
+      ee = (z < mid) ? xu - z : -(z - xl);
+      dd = golden * ee;
+    }
+    if (fabs(dd) >= tolerance) u = z + dd;
+    else u = z + ((dd > 0) ? tolerance : -tolerance);
+    e = ee;
+    d = dd;
+    double fuv = f(u);
+    if (!isfinite(fuv)) return BR_GSLERR;
+    if (fuv <= fz) {
+      if (u < z) { xu = z; fu = fz; } else { xl = z; fl = fz; }
+      v = w; fv = fw; w = z; fw = fz;
+      xm = u; fm = fuv;
+    } else {
+      if (u < z) { xl = u; fl = fuv; } else { xu = u; fu = fuv; }
+      if (fuv <= fw || w == z) { v = w; fv = fw; w = u; fw = fuv; }
+      else if (fuv <= fv || v == z || v == w) { v = u; fv = fuv; }
+    }
+    if (xu - xl < tol) { *xout = xm; return BR_OK; }
+  }
+}
+
+// Three_tax.optimize (three_tax.ml:285-320; max_iter 200, core.ml:156)
+template <int K>
+__device__ int optimize_brent(Evaluator<K> &ev, double tol, double max_pend) {
+  double prev_pend = ev.pend, prev_dist = ev.dist;
+  for (int step = 1;; step++) {
+    if (step > 200) return BR_MAXITER;
+    double cp, cd;
+    auto fp = [&](double v) { ev.pend = v; return -ev.eval(false); };
+    if (1e-8 == max_pend) cp = ev.pend;
+    else { int st = brent_dev(fp, ev.pend, 1e-8, max_pend, tol, &cp); if (st != BR_OK) return st; }
+    double cut = ev.dist + ev.prox;
+    auto fd = [&](double v) {
+      double pb = (ev.dist + ev.prox) - v;
+      ev.dist = v;
+      ev.prox = pb;
+      return -ev.eval(false);
+    };
+    if (0.0 == cut) cd = ev.dist;
+    else { int st = brent_dev(fd, ev.dist, 0.0, cut, tol, &cd); if (st != BR_OK) return st; }
+    if (fabs(prev_pend - cp) > tol || fabs(prev_dist - cd) > tol) { prev_pend = cp; prev_dist = cd; }
+    else break;
+  }
+  return BR_OK;
+}
+
+// Safeguarded projected Newton on (pendant, distal) using the adjoint's
+// gradient and Hessian; box [1e-8, max_pend] x [0, cut].
+template <int K>
+__device__ int optimize_newton(Evaluator<K> &ev, double tol, double max_pend, double cut) {
+  const double pmin = 1e-8, pmax = max_pend, dmin = 0.0, dmax = cut;
+  const double tn = 0.01 * tol;
+  double p = ev.pend, d = fmin(fmax(ev.dist, dmin), dmax);
+  ev.dist = d;
+  ev.prox = cut - d;
+  double L = ev.eval(true);
+  if (!isfinite(L)) return BR_GSLERR;
+  EvalOut cur = ev.last;
+  for (int it = 0; it < 60; it++) {
+    double gp = cur.g[0], gd = cur.g[1], hpp = cur.h[0], hdd = cur.h[1], hpd = cur.h[2];
+    bool free_p = !((p <= pmin && gp <= 0) || (p >= pmax && gp >= 0));
+    bool free_d = (dmax > dmin) && !((d <= dmin && gd <= 0) || (d >= dmax && gd >= 0));
+    if (!free_p && !free_d) break;
+    double sp = 0, sd = 0;
+    double det = hpp * hdd - hpd * hpd;
+    if (free_p && free_d && hpp < 0 && hdd < 0 && det > 0) {
+      sp = -(hdd * gp - hpd * gd) / det;
+      sd = -(hpp * gd - hpd * gp) / det;
+    } else {
+      if (free_p) sp = hpp < 0 ? -gp / hpp : (gp > 0 ? 1.0 : -1.0) * fmax(0.5 * p, 0.01);
+      if (free_d) sd = hdd < 0 ? -gd / hdd : (gd > 0 ? 1.0 : -1.0) * 0.25 * (dmax - dmin);
+    }
+    double lim_p = fmax(2.0 * p, 0.05), lim_d = fmax(0.5 * (dmax - dmin), 1e-12);
+    if (fabs(sp) > lim_p) sp = copysign(lim_p, sp);
+    if (fabs(sd) > lim_d) sd = copysign(lim_d, sd);
+    double pred = gp * sp + gd * sd;  // first-order predicted gain
+    double allow = 1e-9 * fabs(L) + 1e-6;
+    bool accepted = false;
+    double np = p, nd = d;
+    for (int ls = 0; ls < 30; ls++) {
+      np = fmin(fmax(p + sp, pmin), pmax);
+      nd = fmin(fmax(d + sd, dmin), dmax);
+      if (np == p && nd == d) break;
+      ev.pend = np;
+      ev.dist = nd;
+      ev.prox = cut - nd;
+      double Ln = ev.eval(true);
+      if (isfinite(Ln) && Ln >= L - allow) {
+        accepted = true;
+        L = Ln;
+        cur = ev.last;
+        break;
+      }
+      sp *= 0.25;
+      sd *= 0.25;
+    }
+    double step = fmax(fabs(np - p), fabs(nd - d));
+    if (!accepted) {
+      // restore the state of the best point
+      ev.pend = p; ev.dist = d; ev.prox = cut - d;
+      ev.L_last = L;
+      ev.last = cur;
+      break;
+    }
+    p = np;
+    d = nd;
+    if (step < tn || fabs(pred) < allow * 1e-3) break;
+    if (it == 59) return BR_MAXITER;
+  }
+  ev.pend = p;
+  ev.dist = d;
+  ev.prox = cut - d;
+  ev.L_last = L;
+  ev.last = cur;
+  return BR_OK;
+}
+
+template <int K>
+__global__ void __launch_bounds__(kTrialThreads) k_trials(TrialCtx c, const TrialIn *__restrict__ trials,
+                                                          const int *__restrict__ order, int n, TrialRes *out) {
+  extern __shared__ __align__(16) char t_smem[];
+  int ti = order ? order[blockIdx.x] : blockIdx.x;
+  if (blockIdx.x >= n) return;
+  TrialIn tr = trials[ti];
+  const int tid = threadIdx.x;
+  TrialSmem sm = carve(t_smem, c.cap, c.smem_win, c.RP, K, c.NM, c.ncode);
+  const int q = tr.q, node = tr.node;
+  const int Sq = c.qlen[q];
+  // prologue: gather the query's informative sites of darr / parr[node]
+  long long esum = 0;
+  const long qo = (long)q * c.S;
+  for (int i = tid; i < Sq; i += kTrialThreads) {
+    int s = c.reind[qo + i];
+    sm.code[i] = c.mcode[qo + i];
+    if (c.gcat) sm.cat[i] = c.site_cat[s];
+    long go = ((long)node * c.S + s);
+    esum += (long long)c.dexp[go] + (long long)c.pexp[go];
+    if (c.smem_win) {
+      for (int r = 0; r < c.RP; r++) {
+        const float *ds = c.darr + (go * c.RP + r) * K;
+        const float *ps = c.parr + (go * c.RP + r) * K;
+        float *dd = sm.D + ((long)r * c.cap + i) * K;
+        float *pd = sm.P + ((long)r * c.cap + i) * K;
+        for (int k = 0; k < K; k += 4) {
+          *reinterpret_cast<float4 *>(dd + k) = *reinterpret_cast<const float4 *>(ds + k);
+          *reinterpret_cast<float4 *>(pd + k) = *reinterpret_cast<const float4 *>(ps + k);
+        }
+      }
+    }
+  }
+  esum = warp_sum_ll(esum);
+  if ((tid & 31) == 0) sm.red[(tid >> 5) * 8] = 0.f, sm.redi[tid >> 5] = 0;
+  __shared__ long long s_esum[kTrialWarps];
+  if ((tid & 31) == 0) s_esum[tid >> 5] = esum;
+  __syncthreads();
+  long long etot = 0;
+  for (int i = 0; i < kTrialWarps; i++) etot += s_esum[i];
+  const double exp_const = kLn2 * (double)etot;
+
+  if (tid >= 32) {
+    // worker warps: evaluate until warp 0 sends stop
+    EvalOut dummy;
+    for (int guard = 0; guard < (1 << 30); guard++) {
+      bar1();
+      int cmd = sm.ctrl->cmd;
+      if (cmd == 0) break;
+      eval_part<K>(c, sm, q, node, Sq, cmd == 2, exp_const, &dummy);
+    }
+    return;
+  }
+  // warp 0: the optimiser
+  Evaluator<K> ev;
+  ev.c = &c; ev.sm = &sm; ev.q = q; ev.node = node; ev.Sq = Sq; ev.exp_const = exp_const;
+  ev.n_evals = 0;
+  ev.L_last = NAN;
+  const double cut_bl = c.bl[node];
+  // set_tt_edges (core.ml:371-385)
+  ev.pend = tr.pend0;
+  ev.dist = tr.dist0;
+  ev.prox = cut_bl - tr.dist0;
+  int status = ST_OK;
+  if (c.mode == 1) {
+    ev.eval(true);
+  } else {
+    for (int attempt = 0; attempt < 2; attempt++) {
+      int st = c.optimizer == 0 ? optimize_brent<K>(ev, tr.tol, c.max_pend)
+                                : optimize_newton<K>(ev, tr.tol, c.max_pend, cut_bl);
+      if (st == BR_OK) { status = ST_OK; break; }
+      if (st == BR_MAXITER) { status = ST_MAXITER; break; }
+      if (st == BR_STARTFAIL) { status = ST_STARTFAIL; break; }
+      // GSL error: retry once from the default branch lengths (core.ml:418-425)
+      status = ST_FAILED;
+      ev.pend = c.start_pend;
+      ev.dist = cut_bl / 2.;
+      ev.prox = cut_bl - cut_bl / 2.;
+    }
+    if (ev.n_evals == 0) ev.eval(false);
+  }
+  ev.stop();
+  if (tid == 0) {
+    TrialRes r;
+    r.like = ev.L_last;
+    r.pend = ev.pend;
+    r.dist = ev.dist;
+    r.der[0] = ev.last.g[0]; r.der[1] = ev.last.g[1];
+    r.der[2] = ev.last.h[0]; r.der[3] = ev.last.h[1]; r.der[4] = ev.last.h[2];
+    r.der[5] = 0;
+    r.status = status;
+    r.n_evals = ev.n_evals;
+    out[ti] = r;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Baseball (core.ml:429-464) and keep / refine / like_weight_ratio
+// (core.ml:482-523, ppatteries.ml:175-183, pquery.ml:8-9,92).
+// ---------------------------------------------------------------------------
+struct BBState {
+  int next, strikes, nres, done;
+  double record;
+};
+struct ResEntry {
+  int edge, status;
+  double like, pend, dist;
+};
+struct BBCtx {
+  int Q, rk, maxr, n_edges, bins;
+  const int *rank;            // [Q][rk] edge indices
+  const int *edge_nodes;
+  const double *bl;
+  const int *qlen;
+  int *qstatus;
+  BBState *bb;
+  ResEntry *res;              // [Q][maxr]
+  int *tbase, *tcount;        // [Q]
+  TrialIn *trials;
+  int *bin_count;             // [bins]
+  int *bin_list;              // [bins][cap_trials]
+  const int *bin_limit;       // [bins] max Sq of each bin
+  int cap_trials;
+  int *n_active;
+  double start_pend, tol, strike_box;
+  long max_pitches, max_strikes;
+};
+
+__device__ int bin_of(const BBCtx &c, int sq) {
+  for (int b = 0; b < c.bins; b++)
+    if (sq <= c.bin_limit[b]) return b;
+  return c.bins - 1;
+}
+
+__global__ void k_bb_init(BBCtx c) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= c.Q) return;
+  BBState s;
+  s.next = 0; s.strikes = 0; s.nres = 0;
+  s.done = c.qstatus[q] != PGB_Q_OK;
+  s.record = -INFINITY;
+  c.bb[q] = s;
+}
+
+__global__ void k_bb_emit(BBCtx c, int B, int *counter) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= c.Q) return;
+  BBState s = c.bb[q];
+  c.tcount[q] = 0;
+  if (s.done) return;
+  int n = min(B, c.rk - s.next);
+  if (n <= 0) { c.bb[q].done = 1; return; }
+  int base = atomicAdd(counter, n);
+  if (base + n > c.cap_trials) { c.bb[q].done = 1; c.qstatus[q] = PGB_Q_EMPTY; return; }
+  c.tbase[q] = base;
+  c.tcount[q] = n;
+  int bin = bin_of(c, c.qlen[q]);
+  int bpos = atomicAdd(&c.bin_count[bin], n);
+  for (int j = 0; j < n; j++) {
+    int ei = c.rank[(long)q * c.rk + s.next + j];
+    int node = c.edge_nodes[ei];
+    TrialIn t;
+    t.q = q;
+    t.node = node;
+    t.pend0 = c.start_pend;
+    t.dist0 = c.bl[node] / 2.;
+    t.tol = c.tol;
+    c.trials[base + j] = t;
+    c.bin_list[(long)bin * c.cap_trials + bpos + j] = base + j;
+  }
+}
+
+__global__ void k_bb_update(BBCtx c, const TrialRes *__restrict__ tres) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= c.Q) return;
+  BBState s = c.bb[q];
+  int n = c.tcount[q];
+  if (s.done || n == 0) return;
+  int base = c.tbase[q];
+  for (int j = 0; j < n && !s.done; j++) {
+    TrialRes r = tres[base + j];
+    int ei = c.rank[(long)q * c.rk + s.next];
+    s.next++;
+    if (r.status == ST_STARTFAIL) { s.done = 1; c.qstatus[q] = PGB_Q_START_FAILURE; break; }
+    if (r.status == ST_FAILED) continue;  // skipped location (core.ml:435-443)
+    long before = s.nres;
+    if (s.nres < c.maxr) {
+      ResEntry e;
+      e.edge = ei; e.status = r.status; e.like = r.like; e.pend = r.pend; e.dist = r.dist;
+      c.res[(long)q * c.maxr + s.nres] = e;
+      s.nres++;
+    }
+    if (before >= c.max_pitches) { s.done = 1; break; }
+    if (r.like > s.record) s.record = r.like;
+    else if (r.like < s.record - c.strike_box) {
+      if (s.strikes + 1 >= c.max_strikes) { s.done = 1; break; }
+      s.strikes++;
+    }
+  }
+  if (!s.done && s.next >= c.rk) s.done = 1;
+  if (!s.done) atomicAdd(c.n_active, 1);
+  c.bb[q] = s;
+}
+
+// sort results by like (stable, descending), keep, emit refinement trials
+__global__ void k_keep_emit(BBCtx c, int keep_at_most, double log_keep_factor, int *keep_idx, int *keep_n,
+                            int *counter) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= c.Q) return;
+  keep_n[q] = 0;
+  c.tcount[q] = 0;
+  if (c.qstatus[q] != PGB_Q_OK) return;
+  int n = c.bb[q].nres;
+  if (n == 0) { c.qstatus[q] = PGB_Q_EMPTY; return; }
+  ResEntry *r = c.res + (long)q * c.maxr;
+  // insertion sort: stable, descending by like (NaN last)
+  for (int i = 1; i < n; i++) {
+    ResEntry x = r[i];
+    int j = i - 1;
+    while (j >= 0 && (isnan(r[j].like) ? !isnan(x.like) : (!isnan(x.like) && x.like > r[j].like))) {
+      r[j + 1] = r[j];
+      j--;
+    }
+    r[j + 1] = x;
+  }
+  double best = r[0].like;
+  int nk = 0;
+  for (int i = 0; i < n; i++)
+    if (i < keep_at_most && r[i].like >= log_keep_factor + best) keep_idx[(long)q * keep_at_most + nk++] = i;
+  keep_n[q] = nk;
+  int base = atomicAdd(counter, nk);
+  c.tbase[q] = base;
+  c.tcount[q] = nk;
+  int bin = bin_of(c, c.qlen[q]);
+  int bpos = atomicAdd(&c.bin_count[bin], nk);
+  for (int j = 0; j < nk; j++) {
+    ResEntry e = r[keep_idx[(long)q * keep_at_most + j]];
+    TrialIn t;
+    t.q = q;
+    t.node = c.edge_nodes[e.edge];
+    t.pend0 = e.pend;
+    t.dist0 = e.dist;
+    t.tol = 1e-5;  // final_tolerance (core.ml:160)
+    c.trials[base + j] = t;
+    c.bin_list[(long)bin * c.cap_trials + bpos + j] = base + j;
+  }
+}
+
+__global__ void k_finalize(BBCtx c, int keep_at_most, const int *__restrict__ keep_idx, const int *__restrict__ keep_n,
+                           const TrialRes *__restrict__ tres, pgb_placement *out, int *n_out) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= c.Q) return;
+  int nk = keep_n[q];
+  n_out[q] = 0;
+  if (c.qstatus[q] != PGB_Q_OK || nk == 0) return;
+  const ResEntry *r = c.res + (long)q * c.maxr;
+  pgb_placement *o = out + (long)q * keep_at_most;
+  double like[64];
+  int m = min(nk, 64);
+  for (int j = 0; j < m; j++) {
+    ResEntry e = r[keep_idx[(long)q * keep_at_most + j]];
+    TrialRes t = tres[c.tbase[q] + j];
+    pgb_placement p;
+    p.edge = c.edge_nodes[e.edge];
+    p.pad = 0;
+    if (t.status == ST_FAILED || t.status == ST_STARTFAIL) { p.like = e.like; p.pend = e.pend; p.dist = e.dist; }
+    else { p.like = t.like; p.pend = t.pend; p.dist = t.dist; }
+    like[j] = p.like;
+    o[j] = p;
+  }
+  for (int j = 0; j < m; j++) {
+    double tot = 0;
+    for (int k = 0; k < m; k++) tot += exp(like[k] - like[j]);
+    o[j].lwr = 1. / tot;
+  }
+  for (int i = 1; i < m; i++) {  // stable sort by lwr, descending
+    pgb_placement x = o[i];
+    int j = i - 1;
+    while (j >= 0 && x.lwr > o[j].lwr) { o[j + 1] = o[j]; j--; }
+    o[j + 1] = x;
+  }
+  n_out[q] = m;
+}
+
+}  // namespace
+}  // namespace pgb
+
+// ---------------------------------------------------------------------------
+// Engine object
+// ---------------------------------------------------------------------------
+using namespace pgb;
+
+struct pgb_engine {
+  int K = 4, NM = 1, gcat = 0, S = 0, n_nodes = 0, root = -1, n_edges = 0, RP = 1, ncode = 18, prim = 4;
+  int device = 0, n_sm = 0;
+  size_t smem_optin = 0;
+  cudaStream_t st = nullptr;
+  cudaEvent_t ev[8] = {};
+  std::vector<double> statd, X, lam, Xit, rates;
+  std::vector<int> site_cats, parent, ch_start, ch_list, edge_nodes;
+  std::vector<double> bl;
+  // device model / tree
+  double *d_bl = nullptr, *d_Xd = nullptr, *d_Xitd = nullptr, *d_lamd = nullptr, *d_ratesd = nullptr,
+         *d_statdd = nullptr, *d_lvd = nullptr, *d_pm = nullptr, *d_pmh = nullptr;
+  float *d_mf = nullptr;  // X, W, Lt, lvf, statd, lam, rates (float)
+  size_t off_X = 0, off_W = 0, off_Lt = 0, off_lv = 0, off_statd = 0, off_lam = 0, off_rates = 0;
+  uint8_t *d_site_cat = nullptr, *d_char_code = nullptr, *d_informative = nullptr;
+  int *d_edge_nodes = nullptr, *d_parent = nullptr, *d_ch_start = nullptr, *d_ch_list = nullptr;
+  // GLVs
+  float *d_darr = nullptr, *d_parr = nullptr, *d_snode = nullptr;
+  int *d_dexp = nullptr, *d_pexp = nullptr, *d_sexp = nullptr;
+  bool glvs_ready = false;
+  // stage-1 table
+  float *d_lt = nullptr, *d_qe = nullptr;
+  double lt_pend = -1;
+  // queries
+  int Q = 0, Qcap = 0;
+  char *d_seqs = nullptr;
+  uint8_t *d_qcode = nullptr, *d_mcode = nullptr;
+  uint16_t *d_reind = nullptr;
+  int *d_qlen = nullptr, *d_qstatus = nullptr;
+  std::vector<int> h_qlen;
+  // run buffers
+  double *d_scores = nullptr;
+  size_t scores_cap = 0;
+  int *d_rank = nullptr;
+  size_t rank_cap = 0;
+  BBState *d_bb = nullptr;
+  ResEntry *d_res = nullptr;
+  size_t res_cap = 0;
+  int *d_tbase = nullptr, *d_tcount = nullptr, *d_keep_idx = nullptr, *d_keep_n = nullptr;
+  TrialIn *d_trials = nullptr;
+  TrialRes *d_tres = nullptr;
+  int *d_bin_list = nullptr;
+  size_t trials_cap = 0;
+  int *d_small = nullptr;  // counters: [0] trial counter, [1] n_active, [2..2+bins) bin counts, then bin limits
+  pgb_placement *d_out = nullptr;
+  int *d_nout = nullptr;
+  int out_keep = 0;
+  // timings
+  double t_ms[6] = {0, 0, 0, 0, 0, 0};
+  double counts[4] = {0, 0, 0, 0};
+};
+
+namespace {
+
+constexpr int kBins = 6;
+
+template <class T>
+pgb_status dalloc(T **p, size_t n) {
+  if (*p) { cudaFree(*p); *p = nullptr; }
+  if (n == 0) n = 1;
+  PGB_CUDA(cudaMalloc((void **)p, n * sizeof(T)));
+  return PGB_OK;
+}
+template <class T>
+pgb_status upload(T **p, const T *h, size_t n, cudaStream_t st) {
+  pgb_status s = dalloc(p, n);
+  if (s) return s;
+  if (n) PGB_CUDA(cudaMemcpyAsync(*p, h, n * sizeof(T), cudaMemcpyHostToDevice, st));
+  return PGB_OK;
+}
+int grid_for(long n, int threads = 256) {
+  long b = (n + threads - 1) / threads;
+  return (int)std::max(1L, std::min(b, 152L * 32));
+}
+
+// Host P(t) for each matrix index (diagd.ml:201-220) in FP64.
+void host_pmats(const pgb_engine *e, double t, std::vector<double> &pm) {
+  int K = e->K;
+  pm.assign((size_t)e->NM * K * K, 0.0);
+  for (int m = 0; m < e->NM; m++)
+    for (int i = 0; i < K; i++)
+      for (int j = 0; j < K; j++) {
+        double acc = 0;
+        for (int k = 0; k < K; k++) acc += exp(e->rates[m] * t * e->lam[k]) * e->X[i * K + k] * e->Xit[j * K + k];
+        pm[((size_t)m * K + i) * K + j] = acc;
+      }
+}
+
+pgb_status ensure_queries(pgb_engine *e, int Q) {
+  if (Q <= e->Qcap) return PGB_OK;
+  size_t n = (size_t)Q * e->S;
+  pgb_status s;
+  if ((s = dalloc(&e->d_seqs, n)) || (s = dalloc(&e->d_qcode, n)) || (s = dalloc(&e->d_mcode, n)) ||
+      (s = dalloc(&e->d_reind, n)) || (s = dalloc(&e->d_qlen, Q)) || (s = dalloc(&e->d_qstatus, Q)))
+    return s;
+  e->Qcap = Q;
+  return PGB_OK;
+}
+
+pgb_status build_stage1_table(pgb_engine *e, double start_pend) {
+  if (e->d_lt && e->lt_pend == start_pend) return PGB_OK;
+  int K = e->K;
+  std::vector<double> pm;
+  host_pmats(e, start_pend, pm);
+  std::vector<float> qe((size_t)e->NM * e->ncode * K);
+  std::vector<double> lv(K);
+  for (int m = 0; m < e->NM; m++)
+    for (int c = 0; c < e->ncode; c++) {
+      code_lv(K, c, lv.data());
+      for (int k = 0; k < K; k++) {  // gemmish of the LV by P (linear_c.c:29-90)
+        double acc = 0;
+        for (int j = 0; j < K; j++) acc += pm[((size_t)m * K + k) * K + j] * lv[j];
+        qe[((size_t)m * e->ncode + c) * K + k] = (float)acc;
+      }
+    }
+  pgb_status s;
+  if ((s = upload(&e->d_qe, qe.data(), qe.size(), e->st))) return s;
+  if (!e->d_lt && (s = dalloc(&e->d_lt, (size_t)e->n_edges * e->prim * e->S))) return s;
+  S1Ctx c{};
+  c.S = e->S; c.RP = e->RP; c.K = K; c.NM = e->NM; c.gcat = e->gcat; c.ncode = e->ncode; c.prim = e->prim;
+  c.n_edges = e->n_edges; c.snode = e->d_snode; c.sexp = e->d_sexp; c.edge_nodes = e->d_edge_nodes; c.qe = e->d_qe;
+  c.site_cat = e->d_site_cat; c.lt = e->d_lt;
+  k_lt_build<<<grid_for((long)e->n_edges * e->S), 256, 0, e->st>>>(c);
+  PGB_LAUNCH_CHECK();
+  e->lt_pend = start_pend;
+  return PGB_OK;
+}
+
+S1Ctx stage1_ctx(pgb_engine *e) {
+  S1Ctx c{};
+  c.S = e->S; c.RP = e->RP; c.K = e->K; c.NM = e->NM; c.gcat = e->gcat; c.ncode = e->ncode; c.prim = e->prim;
+  c.n_edges = e->n_edges; c.snode = e->d_snode; c.sexp = e->d_sexp; c.edge_nodes = e->d_edge_nodes; c.qe = e->d_qe;
+  c.site_cat = e->d_site_cat; c.lt = e->d_lt;
+  c.log_nrates = e->gcat ? 0.0 : log((double)(float)e->NM);
+  return c;
+}
+
+template <int ET>
+pgb_status launch_stage1_t(pgb_engine *e, size_t smem) {
+  if (smem > 48 * 1024)
+    PGB_CUDA(cudaFuncSetAttribute(k_stage1<ET>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int etiles = (e->n_edges + ET - 1) / ET;
+  // query tiles: enough CTAs for a few waves, at least 32 queries per CTA
+  long want = std::max<long>(1, (long)e->n_sm * 4 / std::max(1, etiles));
+  int qpc = (int)std::max<long>(32, (e->Q + want - 1) / want);
+  int qtiles = (e->Q + qpc - 1) / qpc;
+  dim3 grid(etiles, qtiles);
+  k_stage1<ET><<<grid, 256, smem, e->st>>>(stage1_ctx(e), e->Q, qpc, e->d_reind, e->d_mcode, e->d_qlen,
+                                          e->d_qstatus, e->d_scores);
+  PGB_LAUNCH_CHECK();
+  return PGB_OK;
+}
+
+pgb_status run_stage1(pgb_engine *e) {
+  size_t per_edge = (size_t)e->S * (e->prim * 4 + 4);
+  size_t budget = e->smem_optin - 1024;
+  int et = (int)std::min<size_t>(8, budget / per_edge);
+  if (et < 1) { set_error("stage 1: alignment too long for the shared-memory tile"); return PGB_ERR_ARG; }
+  size_t scores_n = (size_t)e->Q * e->n_edges;
+  if (scores_n > e->scores_cap) {
+    pgb_status s = dalloc(&e->d_scores, scores_n);
+    if (s) return s;
+    e->scores_cap = scores_n;
+  }
+  switch (et) {
+    case 1: return launch_stage1_t<1>(e, per_edge * 1);
+    case 2: return launch_stage1_t<2>(e, per_edge * 2);
+    case 3: return launch_stage1_t<3>(e, per_edge * 3);
+    case 4: return launch_stage1_t<4>(e, per_edge * 4);
+    case 5: return launch_stage1_t<5>(e, per_edge * 5);
+    case 6: return launch_stage1_t<6>(e, per_edge * 6);
+    case 7: return launch_stage1_t<7>(e, per_edge * 7);
+    default: return launch_stage1_t<8>(e, per_edge * 8);
+  }
+}
+
+TrialCtx trial_ctx(pgb_engine *e, const pgb_prefs *p, int optimizer, int mode) {
+  TrialCtx c{};
+  c.darr = e->d_darr; c.parr = e->d_parr; c.dexp = e->d_dexp; c.pexp = e->d_pexp;
+  c.S = e->S; c.RP = e->RP; c.K = e->K; c.NM = e->NM; c.ncode = e->ncode; c.gcat = e->gcat;
+  c.bl = e->d_bl; c.reind = e->d_reind; c.mcode = e->d_mcode; c.qlen = e->d_qlen; c.site_cat = e->d_site_cat;
+  c.X = e->d_mf + e->off_X; c.W = e->d_mf + e->off_W; c.Lt = e->d_mf + e->off_Lt; c.lvf = e->d_mf + e->off_lv;
+  c.statd = e->d_mf + e->off_statd; c.lam = e->d_mf + e->off_lam; c.rates = e->d_mf + e->off_rates;
+  c.log_nrates = e->gcat ? 0.0 : log((double)(float)e->NM);
+  c.start_pend = p->start_pend;
+  c.max_pend = p->max_pend;
+  c.optimizer = optimizer;
+  c.mode = mode;
+  return c;
+}
+
+// window capacities of the trial bins (sites); the last bin reads the
+// windows from global memory
+void bin_limits(const pgb_engine *e, int *lim) {
+  static const int caps4[kBins] = {256, 512, 768, 1024, 1536, 1 << 30};
+  for (int b = 0; b < kBins; b++) lim[b] = caps4[b];
+  if (e->K != 4 || e->gcat) {  // wider sites: fewer smem-staged bins
+    lim[0] = 128; lim[1] = 256; lim[2] = 384; lim[3] = 512; lim[4] = 640; lim[5] = 1 << 30;
+  }
+}
+
+template <int K>
+pgb_status launch_trials_k(pgb_engine *e, TrialCtx c, const int *d_order, int n, int cap, bool win, TrialRes *out) {
+  c.smem_win = win ? 1 : 0;
+  c.cap = cap;
+  size_t smem = trial_smem_bytes(cap, c.smem_win, e->RP, K, e->NM, e->ncode);
+  if (smem > e->smem_optin) { set_error("trial shared memory %zu exceeds %zu", smem, e->smem_optin); return PGB_ERR_ARG; }
+  PGB_CUDA(cudaFuncSetAttribute(k_trials<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  k_trials<K><<<n, kTrialThreads, smem, e->st>>>(c, e->d_trials, d_order, n, out);
+  PGB_LAUNCH_CHECK();
+  return PGB_OK;
+}
+
+pgb_status launch_trials(pgb_engine *e, TrialCtx c, const int *d_order, int n, int cap, bool win, TrialRes *out) {
+  if (n <= 0) return PGB_OK;
+  if (e->K == 4) return launch_trials_k<4>(e, c, d_order, n, cap, win, out);
+  return launch_trials_k<20>(e, c, d_order, n, cap, win, out);
+}
+
+// Launch every non-empty bin of the trial lists.
+pgb_status run_bins(pgb_engine *e, TrialCtx c, const int *h_bin_count, int max_sq) {
+  int lim[kBins];
+  bin_limits(e, lim);
+  size_t win_budget = e->smem_optin - trial_smem_bytes(0, 0, e->RP, e->K, e->NM, e->ncode) - 2048;
+  for (int b = 0; b < kBins; b++) {
+    int n = h_bin_count[b];
+    if (n == 0) continue;
+    int cap = std::min(lim[b], max_sq);
+    bool win = (size_t)2 * e->RP * cap * e->K * 4 + 2 * (size_t)cap <= win_budget && b < kBins - 1;
+    if (!win) cap = std::max(cap, 1);
+    pgb_status s = launch_trials(e, c, e->d_bin_list + (long)b * e->trials_cap, n, win ? cap : std::max(max_sq, 1),
+                                 win, e->d_tres);
+    if (s) return s;
+  }
+  return PGB_OK;
+}
+
+pgb_status ensure_run_buffers(pgb_engine *e, const pgb_prefs *p, int rk, int maxr, size_t tcap) {
+  pgb_status s;
+  size_t rn = (size_t)e->Q * rk;
+  if (rn > e->rank_cap) { if ((s = dalloc(&e->d_rank, rn))) return s; e->rank_cap = rn; }
+  size_t resn = (size_t)e->Q * maxr;
+  if (resn > e->res_cap) { if ((s = dalloc(&e->d_res, resn))) return s; e->res_cap = resn; }
+  if ((s = dalloc(&e->d_bb, e->Q)) || (s = dalloc(&e->d_tbase, e->Q)) || (s = dalloc(&e->d_tcount, e->Q)) ||
+      (s = dalloc(&e->d_keep_n, e->Q)) || (s = dalloc(&e->d_keep_idx, (size_t)e->Q * p->keep_at_most)) ||
+      (s = dalloc(&e->d_nout, e->Q)) || (s = dalloc(&e->d_out, (size_t)e->Q * p->keep_at_most)))
+    return s;
+  if (tcap > e->trials_cap) {
+    if ((s = dalloc(&e->d_trials, tcap)) || (s = dalloc(&e->d_tres, tcap)) ||
+        (s = dalloc(&e->d_bin_list, tcap * kBins)))
+      return s;
+    e->trials_cap = tcap;
+  }
+  e->out_keep = p->keep_at_most;
+  return PGB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void pgb_prefs_default(pgb_prefs *p) {
+  p->start_pend = 0.1;
+  p->max_pend = 2.0;
+  p->initial_tolerance = 0.01;
+  p->max_strikes = 6;
+  p->strike_box = 3.0;
+  p->max_pitches = 40;
+  p->keep_at_most = 7;
+  p->keep_factor = 0.01;
+  p->optimizer = 1;
+}
+
+pgb_status pgb_engine_create(const pgb_model_desc *m, const pgb_tree_desc *t, pgb_engine **out) {
+  if (!m || !t || !out) { set_error("engine_create: null argument"); return PGB_ERR_ARG; }
+  if ((m->n_states != 4 && m->n_states != 20) || m->n_rates < 1 || m->n_rates > 64 || m->n_sites < 1 ||
+      m->n_sites > 65535 || t->n_nodes < 2) {
+    set_error("engine_create: unsupported sizes (n_states 4|20, n_rates 1..64, n_sites 1..65535)");
+    return PGB_ERR_ARG;
+  }
+  if (m->gcat && !m->site_categories) { set_error("engine_create: gcat needs site_categories"); return PGB_ERR_ARG; }
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+    set_error("engine_create: no CUDA device");
+    return PGB_ERR_CUDA;
+  }
+  pgb_engine *e = new pgb_engine();
+  e->K = m->n_states;
+  e->NM = m->n_rates;
+  e->gcat = m->gcat ? 1 : 0;
+  e->RP = e->gcat ? 1 : e->NM;
+  e->S = m->n_sites;
+  e->ncode = n_codes(e->K);
+  e->prim = e->K;
+  int K = e->K;
+  e->statd.assign(m->statd, m->statd + K);
+  e->X.assign(m->x, m->x + K * K);
+  e->lam.assign(m->lambda, m->lambda + K);
+  e->Xit.assign(m->xit, m->xit + K * K);
+  e->rates.assign(m->rates, m->rates + e->NM);
+  if (e->gcat) {
+    e->site_cats.assign(m->site_categories, m->site_categories + e->S);
+    for (int v : e->site_cats)
+      if (v < 0 || v >= e->NM) { set_error("engine_create: site category out of range"); delete e; return PGB_ERR_ARG; }
+  }
+  e->n_nodes = t->n_nodes;
+  e->parent.assign(t->parent, t->parent + t->n_nodes);
+  e->bl.assign(t->bl, t->bl + t->n_nodes);
+  std::vector<std::vector<int>> ch(e->n_nodes);
+  for (int i = 0; i < e->n_nodes; i++) {
+    int p = e->parent[i];
+    if (p < 0) {
+      if (e->root >= 0) { set_error("engine_create: more than one root"); delete e; return PGB_ERR_ARG; }
+      e->root = i;
+    } else if (p <= i || p >= e->n_nodes) {
+      set_error("engine_create: nodes must be numbered post-order (parent id > child id)");
+      delete e;
+      return PGB_ERR_ARG;
+    } else ch[p].push_back(i);
+  }
+  if (e->root < 0) { set_error("engine_create: no root"); delete e; return PGB_ERR_ARG; }
+  e->bl[e->root] = 0.0;
+  e->ch_start.assign(e->n_nodes + 1, 0);
+  for (int i = 0; i < e->n_nodes; i++) {
+    e->ch_start[i + 1] = e->ch_start[i] + (int)ch[i].size();
+    for (int c : ch[i]) e->ch_list.push_back(c);
+    if (i != e->root) e->edge_nodes.push_back(i);
+  }
+  if (e->ch_list.empty()) e->ch_list.push_back(0);
+  e->n_edges = (int)e->edge_nodes.size();
+
+  cudaError_t ce;
+  if ((ce = cudaGetDevice(&e->device)) != cudaSuccess || (ce = cudaStreamCreateWithFlags(&e->st, cudaStreamNonBlocking)) != cudaSuccess) {
+    set_error("engine_create: %s", cudaGetErrorString(ce));
+    delete e;
+    return PGB_ERR_CUDA;
+  }
+  int optin = 0;
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, e->device);
+  cudaDeviceGetAttribute(&e->n_sm, cudaDevAttrMultiProcessorCount, e->device);
+  e->smem_optin = (size_t)optin;
+  for (int i = 0; i < 8; i++) cudaEventCreate(&e->ev[i]);
+
+  // model constants
+  std::vector<float> mf;
+  auto put = [&](const std::vector<float> &v) { size_t o = mf.size(); mf.insert(mf.end(), v.begin(), v.end()); while (mf.size() % 4) mf.push_back(0.f); return o; };
+  std::vector<float> Xf(K * K), W((size_t)K * K * K), Lt((size_t)e->ncode * K), lvf((size_t)e->ncode * K), sf(K), lf(K),
+      rf(e->NM);
+  std::vector<double> lvd((size_t)e->ncode * K), lv(K);
+  for (int i = 0; i < K * K; i++) Xf[i] = (float)e->X[i];
+  for (int i = 0; i < K; i++)
+    for (int j = 0; j < K; j++)
+      for (int k = 0; k < K; k++) W[((size_t)i * K + j) * K + k] = (float)(e->X[i * K + k] * e->Xit[j * K + k]);
+  for (int c = 0; c < e->ncode; c++) {
+    code_lv(K, c, lv.data());
+    for (int k = 0; k < K; k++) {
+      double acc = 0;
+      for (int j = 0; j < K; j++) acc += e->Xit[j * K + k] * lv[j];
+      Lt[(size_t)c * K + k] = (float)acc;
+      lvf[(size_t)c * K + k] = (float)lv[k];
+      lvd[(size_t)c * K + k] = lv[k];
+    }
+  }
+  for (int i = 0; i < K; i++) { sf[i] = (float)e->statd[i]; lf[i] = (float)e->lam[i]; }
+  for (int i = 0; i < e->NM; i++) rf[i] = (float)e->rates[i];
+  e->off_X = put(Xf); e->off_W = put(W); e->off_Lt = put(Lt); e->off_lv = put(lvf);
+  e->off_statd = put(sf); e->off_lam = put(lf); e->off_rates = put(rf);
+  // character tables
+  std::vector<uint8_t> cc(256, kBadCode), inf(kMaxCodes, 0);
+  const char *alpha = code_alphabet(K);
+  for (int c = 0; c < e->ncode; c++) {
+    cc[(uint8_t)alpha[c]] = (uint8_t)c;
+    inf[c] = code_informative(K, c) ? 1 : 0;
+  }
+  std::vector<uint8_t> scat(e->S, 0);
+  if (e->gcat)
+    for (int s = 0; s < e->S; s++) scat[s] = (uint8_t)e->site_cats[s];
+  pgb_status s;
+  if ((s = upload(&e->d_mf, mf.data(), mf.size(), e->st)) || (s = upload(&e->d_bl, e->bl.data(), e->bl.size(), e->st)) ||
+      (s = upload(&e->d_Xd, e->X.data(), e->X.size(), e->st)) ||
+      (s = upload(&e->d_Xitd, e->Xit.data(), e->Xit.size(), e->st)) ||
+      (s = upload(&e->d_lamd, e->lam.data(), e->lam.size(), e->st)) ||
+      (s = upload(&e->d_ratesd, e->rates.data(), e->rates.size(), e->st)) ||
+      (s = upload(&e->d_statdd, e->statd.data(), e->statd.size(), e->st)) ||
+      (s = upload(&e->d_lvd, lvd.data(), lvd.size(), e->st)) ||
+      (s = upload(&e->d_site_cat, scat.data(), scat.size(), e->st)) ||
+      (s = upload(&e->d_char_code, cc.data(), cc.size(), e->st)) ||
+      (s = upload(&e->d_informative, inf.data(), inf.size(), e->st)) ||
+      (s = upload(&e->d_edge_nodes, e->edge_nodes.data(), e->edge_nodes.size(), e->st)) ||
+      (s = upload(&e->d_parent, e->parent.data(), e->parent.size(), e->st)) ||
+      (s = upload(&e->d_ch_start, e->ch_start.data(), e->ch_start.size(), e->st)) ||
+      (s = upload(&e->d_ch_list, e->ch_list.data(), e->ch_list.size(), e->st)) ||
+      (s = dalloc(&e->d_small, 64))) {
+    pgb_engine_destroy(e);
+    return s;
+  }
+  // P matrices of every node at bl and bl/2 (FP64)
+  size_t npm = (size_t)e->n_nodes * e->NM * K * K;
+  if ((s = dalloc(&e->d_pm, npm)) || (s = dalloc(&e->d_pmh, npm))) { pgb_engine_destroy(e); return s; }
+  k_node_pmats<<<grid_for((long)npm), 256, 0, e->st>>>(e->d_pm, e->d_bl, 1.0, e->n_nodes, e->NM, K, e->d_Xd,
+                                                       e->d_Xitd, e->d_lamd, e->d_ratesd);
+  count_launch();
+  k_node_pmats<<<grid_for((long)npm), 256, 0, e->st>>>(e->d_pmh, e->d_bl, 0.5, e->n_nodes, e->NM, K, e->d_Xd,
+                                                       e->d_Xitd, e->d_lamd, e->d_ratesd);
+  count_launch();
+  if (cudaStreamSynchronize(e->st) != cudaSuccess || cudaGetLastError() != cudaSuccess) {
+    set_error("engine_create: setup kernels failed");
+    pgb_engine_destroy(e);
+    return PGB_ERR_CUDA;
+  }
+  *out = e;
+  return PGB_OK;
+}
+
+pgb_status pgb_engine_destroy(pgb_engine *e) {
+  if (!e) return PGB_OK;
+  if (e->st) cudaStreamSynchronize(e->st);
+  void *ptrs[] = {e->d_bl, e->d_Xd, e->d_Xitd, e->d_lamd, e->d_ratesd, e->d_statdd, e->d_lvd, e->d_pm, e->d_pmh,
+                  e->d_mf, e->d_site_cat, e->d_char_code, e->d_informative, e->d_edge_nodes, e->d_parent,
+                  e->d_ch_start, e->d_ch_list, e->d_darr, e->d_parr, e->d_snode, e->d_dexp, e->d_pexp, e->d_sexp,
+                  e->d_lt, e->d_qe, e->d_seqs, e->d_qcode, e->d_mcode, e->d_reind, e->d_qlen, e->d_qstatus,
+                  e->d_scores, e->d_rank, e->d_bb, e->d_res, e->d_tbase, e->d_tcount, e->d_keep_idx, e->d_keep_n,
+                  e->d_trials, e->d_tres, e->d_bin_list, e->d_small, e->d_out, e->d_nout};
+  for (void *p : ptrs)
+    if (p) cudaFree(p);
+  for (int i = 0; i < 8; i++)
+    if (e->ev[i]) cudaEventDestroy(e->ev[i]);
+  if (e->st) cudaStreamDestroy(e->st);
+  delete e;
+  return PGB_OK;
+}
+
+static pgb_status alloc_glv_store(pgb_engine *e) {
+  size_t n = (size_t)e->n_nodes * e->S * e->RP * e->K, ne = (size_t)e->n_nodes * e->S;
+  pgb_status s;
+  if ((s = dalloc(&e->d_darr, n)) || (s = dalloc(&e->d_parr, n)) || (s = dalloc(&e->d_snode, n)) ||
+      (s = dalloc(&e->d_dexp, ne)) || (s = dalloc(&e->d_pexp, ne)) || (s = dalloc(&e->d_sexp, ne)))
+    return s;
+  e->lt_pend = -1;
+  return PGB_OK;
+}
+
+pgb_status pgb_engine_precompute(pgb_engine *e, const int *leaf_row, const char *seqs, int n_rows) {
+  if (!e || !leaf_row || !seqs || n_rows < 1) { set_error("precompute: bad argument"); return PGB_ERR_ARG; }
+  int K = e->K, S = e->S;
+  // leaves, their codes, and the post-order / pre-order levels
+  std::vector<int> leaves;
+  std::vector<uint8_t> codes;
+  const char *alpha = code_alphabet(K);
+  for (int i = 0; i < e->n_nodes; i++) {
+    if (e->ch_start[i + 1] != e->ch_start[i]) continue;
+    int row = leaf_row[i];
+    if (row < 0 || row >= n_rows) { set_error("precompute: leaf %d has no alignment row", i); return PGB_ERR_ARG; }
+    leaves.push_back(i);
+    for (int s = 0; s < S; s++) {
+      const char *p = strchr(alpha, seqs[(size_t)row * S + s]);
+      if (!p || !seqs[(size_t)row * S + s]) { set_error("precompute: unknown character in reference row %d", row); return PGB_ERR_ARG; }
+      codes.push_back((uint8_t)(p - alpha));
+    }
+  }
+  std::vector<int> height(e->n_nodes, 0), depth(e->n_nodes, 0);
+  int maxh = 0, maxd = 0;
+  for (int i = 0; i < e->n_nodes; i++)
+    for (int c = e->ch_start[i]; c < e->ch_start[i + 1]; c++) height[i] = std::max(height[i], height[e->ch_list[c]] + 1);
+  for (int i = e->n_nodes - 1; i >= 0; i--)
+    if (e->parent[i] >= 0) depth[i] = depth[e->parent[i]] + 1;
+  for (int i = 0; i < e->n_nodes; i++) { maxh = std::max(maxh, height[i]); maxd = std::max(maxd, depth[i]); }
+  std::vector<int> hlist, hstart(maxh + 2, 0), dlist, dstart(maxd + 2, 0);
+  for (int h = 1; h <= maxh; h++) {
+    hstart[h] = (int)hlist.size();
+    for (int i = 0; i < e->n_nodes; i++) if (height[i] == h) hlist.push_back(i);
+  }
+  hstart[maxh + 1] = (int)hlist.size();
+  for (int d = 1; d <= maxd; d++) {
+    dstart[d] = (int)dlist.size();
+    for (int i = 0; i < e->n_nodes; i++) if (depth[i] == d) dlist.push_back(i);
+  }
+  dstart[maxd + 1] = (int)dlist.size();
+  size_t n = (size_t)e->n_nodes * S * e->RP * K, ne = (size_t)e->n_nodes * S;
+  double *d_distal = nullptr, *d_evd = nullptr, *d_prox = nullptr;
+  int *d_de = nullptr, *d_ee = nullptr, *d_pe = nullptr, *d_leaves = nullptr, *d_hlist = nullptr, *d_dlist = nullptr;
+  uint8_t *d_codes = nullptr;
+  pgb_status s = PGB_OK;
+  auto cleanup = [&]() {
+    void *ps[] = {d_distal, d_evd, d_prox, d_de, d_ee, d_pe, d_leaves, d_hlist, d_dlist, d_codes};
+    for (void *p : ps) if (p) cudaFree(p);
+  };
+  if ((s = dalloc(&d_distal, n)) || (s = dalloc(&d_evd, n)) || (s = dalloc(&d_prox, n)) || (s = dalloc(&d_de, ne)) ||
+      (s = dalloc(&d_ee, ne)) || (s = dalloc(&d_pe, ne)) ||
+      (s = upload(&d_leaves, leaves.data(), leaves.size(), e->st)) ||
+      (s = upload(&d_codes, codes.data(), codes.size(), e->st)) ||
+      (s = upload(&d_hlist, hlist.data(), hlist.size(), e->st)) ||
+      (s = upload(&d_dlist, dlist.data(), dlist.size(), e->st)) || (s = alloc_glv_store(e))) {
+    cleanup();
+    return s;
+  }
+  PreCtx c{};
+  c.S = S; c.RP = e->RP; c.K = K; c.NM = e->NM; c.gcat = e->gcat; c.site_cat = e->d_site_cat; c.lvd = e->d_lvd;
+  c.pm = e->d_pm; c.pmh = e->d_pmh; c.statd = e->d_statdd; c.distal = d_distal; c.evd = d_evd; c.prox = d_prox;
+  c.de = d_de; c.ee = d_ee; c.pe = d_pe;
+  k_leaves<<<grid_for((long)leaves.size() * S), 256, 0, e->st>>>(c, d_leaves, (int)leaves.size(), d_codes);
+  count_launch();
+  for (int h = 1; h <= maxh; h++) {
+    int cnt = hstart[h + 1] - hstart[h];
+    if (!cnt) continue;
+    k_distal_level<<<grid_for((long)cnt * S), 256, 0, e->st>>>(c, d_hlist + hstart[h], cnt, e->d_ch_start,
+                                                               e->d_ch_list);
+    count_launch();
+  }
+  size_t root_off = (size_t)e->root * S * e->RP * K;
+  k_set_unit<<<grid_for((long)S * e->RP * K), 256, 0, e->st>>>(d_prox + root_off, d_pe + (size_t)e->root * S,
+                                                               (long)S * e->RP * K, (long)S);
+  count_launch();
+  for (int d = 1; d <= maxd; d++) {
+    int cnt = dstart[d + 1] - dstart[d];
+    if (!cnt) continue;
+    k_prox_level<<<grid_for((long)cnt * S), 256, 0, e->st>>>(c, d_dlist + dstart[d], cnt, e->d_parent,
+                                                             e->d_ch_start, e->d_ch_list);
+    count_launch();
+  }
+  k_finish_glvs<<<grid_for((long)e->n_nodes * S), 256, 0, e->st>>>(c, e->n_nodes, e->d_darr, e->d_parr, e->d_snode,
+                                                                   e->d_dexp, e->d_pexp, e->d_sexp);
+  count_launch();
+  cudaError_t ce = cudaStreamSynchronize(e->st);
+  if (ce == cudaSuccess) ce = cudaGetLastError();
+  cleanup();
+  if (ce != cudaSuccess) { set_error("precompute: %s", cudaGetErrorString(ce)); return PGB_ERR_CUDA; }
+  e->glvs_ready = true;
+  return PGB_OK;
+}
+
+pgb_status pgb_engine_set_glvs(pgb_engine *e, const double *darr, const int *darr_e, const double *parr,
+                               const int *parr_e, const double *snodes, const int *snodes_e) {
+  if (!e || !darr || !darr_e || !parr || !parr_e) { set_error("set_glvs: bad argument"); return PGB_ERR_ARG; }
+  size_t n = (size_t)e->n_nodes * e->RP * e->S * e->K, ne = (size_t)e->n_nodes * e->S;
+  pgb_status s = alloc_glv_store(e);
+  if (s) return s;
+  double *dd = nullptr, *dp = nullptr;
+  int *ed = nullptr, *ep = nullptr;
+  if ((s = upload(&dd, darr, n, e->st)) || (s = upload(&ed, darr_e, ne, e->st)) || (s = upload(&dp, parr, n, e->st)) ||
+      (s = upload(&ep, parr_e, ne, e->st))) {
+    cudaFree(dd); cudaFree(dp); cudaFree(ed); cudaFree(ep);
+    return s;
+  }
+  k_import_glv<<<grid_for((long)n), 256, 0, e->st>>>(dd, ed, e->d_darr, e->d_dexp, e->n_nodes, e->S, e->RP, e->K);
+  count_launch();
+  k_import_glv<<<grid_for((long)n), 256, 0, e->st>>>(dp, ep, e->d_parr, e->d_pexp, e->n_nodes, e->S, e->RP, e->K);
+  count_launch();
+  if (snodes && snodes_e) {
+    double *ds = nullptr;
+    int *es = nullptr;
+    if ((s = upload(&ds, snodes, n, e->st)) || (s = upload(&es, snodes_e, ne, e->st))) { cudaFree(ds); cudaFree(es); return s; }
+    k_import_glv<<<grid_for((long)n), 256, 0, e->st>>>(ds, es, e->d_snode, e->d_sexp, e->n_nodes, e->S, e->RP, e->K);
+    count_launch();
+    cudaStreamSynchronize(e->st);
+    cudaFree(ds);
+    cudaFree(es);
+  } else {
+    k_snodes_from<<<grid_for((long)ne), 256, 0, e->st>>>(dd, dp, ed, ep, e->d_pmh, e->d_statdd, e->d_site_cat,
+                                                         e->gcat, e->d_snode, e->d_sexp, e->n_nodes, e->S, e->RP,
+                                                         e->K, e->NM);
+    count_launch();
+  }
+  cudaError_t ce = cudaStreamSynchronize(e->st);
+  if (ce == cudaSuccess) ce = cudaGetLastError();
+  cudaFree(dd); cudaFree(dp); cudaFree(ed); cudaFree(ep);
+  if (ce != cudaSuccess) { set_error("set_glvs: %s", cudaGetErrorString(ce)); return PGB_ERR_CUDA; }
+  e->glvs_ready = true;
+  return PGB_OK;
+}
+
+pgb_status pgb_engine_get_glv(pgb_engine *e, int which, int node, double *a, int *ex) {
+  if (!e || !e->glvs_ready || node < 0 || node >= e->n_nodes || which < 0 || which > 2) {
+    set_error("get_glv: bad argument or no GLVs");
+    return PGB_ERR_ARG;
+  }
+  size_t per = (size_t)e->S * e->RP * e->K;
+  std::vector<float> buf(per);
+  const float *src = which == 0 ? e->d_darr : which == 1 ? e->d_parr : e->d_snode;
+  const int *esrc = which == 0 ? e->d_dexp : which == 1 ? e->d_pexp : e->d_sexp;
+  PGB_CUDA(cudaMemcpyAsync(buf.data(), src + per * node, per * 4, cudaMemcpyDeviceToHost, e->st));
+  PGB_CUDA(cudaMemcpyAsync(ex, esrc + (size_t)e->S * node, (size_t)e->S * 4, cudaMemcpyDeviceToHost, e->st));
+  PGB_CUDA(cudaStreamSynchronize(e->st));
+  for (int s = 0; s < e->S; s++)
+    for (int r = 0; r < e->RP; r++)
+      for (int k = 0; k < e->K; k++)
+        a[((size_t)r * e->S + s) * e->K + k] = buf[((size_t)s * e->RP + r) * e->K + k];
+  return PGB_OK;
+}
+
+pgb_status pgb_queries_load(pgb_engine *e, int n_queries, const char *seqs) {
+  if (!e || n_queries < 0 || (n_queries > 0 && !seqs)) { set_error("queries_load: bad argument"); return PGB_ERR_ARG; }
+  pgb_status s = ensure_queries(e, std::max(n_queries, 1));
+  if (s) return s;
+  e->Q = n_queries;
+  if (!n_queries) return PGB_OK;
+  PGB_CUDA(cudaMemcpyAsync(e->d_seqs, seqs, (size_t)n_queries * e->S, cudaMemcpyHostToDevice, e->st));
+  k_query_prep<<<n_queries, 256, 0, e->st>>>(e->d_seqs, e->S, e->d_char_code, e->d_informative, e->d_qcode,
+                                             e->d_reind, e->d_mcode, e->d_qlen, e->d_qstatus);
+  PGB_LAUNCH_CHECK();
+  e->h_qlen.resize(n_queries);
+  PGB_CUDA(cudaMemcpyAsync(e->h_qlen.data(), e->d_qlen, (size_t)n_queries * 4, cudaMemcpyDeviceToHost, e->st));
+  PGB_CUDA(cudaStreamSynchronize(e->st));
+  return PGB_OK;
+}
+
+static pgb_status check_prefs(const pgb_prefs *p) {
+  if (!p || p->keep_at_most < 1 || p->keep_at_most > 64 || p->max_pitches < 0 || p->max_strikes < 0 ||
+      !(p->max_pend > 1e-8) || !(p->start_pend > 0) || !(p->initial_tolerance > 0) || p->optimizer < 0 ||
+      p->optimizer > 1) {
+    set_error("invalid prefs (keep_at_most 1..64, max_pend > 1e-8, tolerances > 0, optimizer 0|1)");
+    return PGB_ERR_ARG;
+  }
+  return PGB_OK;
+}
+
+pgb_status pgb_queries_stage1(pgb_engine *e, const pgb_prefs *p, double *scores) {
+  if (!e || !e->glvs_ready || e->Q < 1) { set_error("stage1: no GLVs or no queries"); return PGB_ERR_STATE; }
+  pgb_status s;
+  if ((s = check_prefs(p)) || (s = build_stage1_table(e, p->start_pend)) || (s = run_stage1(e))) return s;
+  PGB_CUDA(cudaMemcpyAsync(scores, e->d_scores, (size_t)e->Q * e->n_edges * 8, cudaMemcpyDeviceToHost, e->st));
+  PGB_CUDA(cudaStreamSynchronize(e->st));
+  return PGB_OK;
+}
+
+pgb_status pgb_queries_run(pgb_engine *e, const pgb_prefs *p) {
+  if (!e || !e->glvs_ready) { set_error("run: no GLVs"); return PGB_ERR_STATE; }
+  pgb_status s;
+  if ((s = check_prefs(p))) return s;
+  if (e->Q < 1) return PGB_OK;
+  bool all_edges = p->max_strikes == 0;
+  int rk = all_edges ? e->n_edges : std::min(e->n_edges, p->max_pitches + 1 + 24);
+  int maxr = all_edges ? e->n_edges : std::min(e->n_edges, p->max_pitches + 1);
+  int max_sq = 1;
+  for (int v : e->h_qlen) max_sq = std::max(max_sq, v);
+  size_t tcap = (size_t)e->Q * std::max(8, std::min(rk, 16)) + (size_t)e->Q * p->keep_at_most + 64;
+  if (all_edges) tcap = std::max(tcap, (size_t)e->Q * e->n_edges + 64);
+  if ((s = ensure_run_buffers(e, p, rk, maxr, tcap))) return s;
+  for (int i = 0; i < 4; i++) e->counts[i] = 0;
+  PGB_CUDA(cudaEventRecord(e->ev[0], e->st));
+  if ((s = build_stage1_table(e, p->start_pend))) return s;
+  PGB_CUDA(cudaEventRecord(e->ev[1], e->st));
+  if ((s = run_stage1(e))) return s;
+  {
+    size_t smem = (size_t)((e->n_edges + 31) / 32) * 4;
+    if (smem > 48 * 1024) PGB_CUDA(cudaFuncSetAttribute(k_rank, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_rank<<<e->Q, 256, smem, e->st>>>(e->d_scores, e->n_edges, rk, e->d_qstatus, e->d_rank);
+    PGB_LAUNCH_CHECK();
+  }
+  PGB_CUDA(cudaEventRecord(e->ev[2], e->st));
+  e->counts[0] = (double)e->Q * e->n_edges;
+  // baseball rounds
+  BBCtx c{};
+  c.Q = e->Q; c.rk = rk; c.maxr = maxr; c.n_edges = e->n_edges; c.bins = kBins;
+  c.rank = e->d_rank; c.edge_nodes = e->d_edge_nodes; c.bl = e->d_bl; c.qlen = e->d_qlen; c.qstatus = e->d_qstatus;
+  c.bb = e->d_bb; c.res = e->d_res; c.tbase = e->d_tbase; c.tcount = e->d_tcount; c.trials = e->d_trials;
+  c.bin_count = e->d_small + 2; c.bin_list = e->d_bin_list; c.bin_limit = e->d_small + 2 + kBins;
+  c.cap_trials = (int)e->trials_cap; c.n_active = e->d_small + 1;
+  c.start_pend = p->start_pend; c.tol = p->initial_tolerance; c.strike_box = p->strike_box;
+  c.max_pitches = all_edges ? (1L << 40) : p->max_pitches;
+  c.max_strikes = all_edges ? (1L << 40) : p->max_strikes;
+  int lim[kBins];
+  bin_limits(e, lim);
+  int h_small[2 + 2 * kBins] = {0};
+  for (int b = 0; b < kBins; b++) h_small[2 + kBins + b] = lim[b];
+  TrialCtx tc = trial_ctx(e, p, p->optimizer, 0);
+  int n = e->Q;
+  k_bb_init<<<(n + 255) / 256, 256, 0, e->st>>>(c);
+  PGB_LAUNCH_CHECK();
+  double n_trials_total = 0;
+  for (int round = 0; round < 4096; round++) {
+    int B = all_edges ? rk : (round == 0 ? std::min(rk, p->max_strikes + 1) : 8);
+    PGB_CUDA(cudaMemcpyAsync(e->d_small, h_small, sizeof(h_small), cudaMemcpyHostToDevice, e->st));
+    k_bb_emit<<<(n + 255) / 256, 256, 0, e->st>>>(c, B, e->d_small);
+    PGB_LAUNCH_CHECK();
+    int got[2 + kBins];
+    PGB_CUDA(cudaMemcpyAsync(got, e->d_small, sizeof(got), cudaMemcpyDeviceToHost, e->st));
+    PGB_CUDA(cudaStreamSynchronize(e->st));
+    if (got[0] == 0) break;
+    n_trials_total += got[0];
+    if ((s = run_bins(e, tc, got + 2, max_sq))) return s;
+    k_bb_update<<<(n + 255) / 256, 256, 0, e->st>>>(c, e->d_tres);
+    PGB_LAUNCH_CHECK();
+    int active = 0;
+    PGB_CUDA(cudaMemcpyAsync(&active, e->d_small + 1, 4, cudaMemcpyDeviceToHost, e->st));
+    PGB_CUDA(cudaStreamSynchronize(e->st));
+    if (active == 0) break;
+  }
+  PGB_CUDA(cudaEventRecord(e->ev[3], e->st));
+  // keep + refine
+  PGB_CUDA(cudaMemcpyAsync(e->d_small, h_small, sizeof(h_small), cudaMemcpyHostToDevice, e->st));
+  k_keep_emit<<<(n + 255) / 256, 256, 0, e->st>>>(c, p->keep_at_most, log(p->keep_factor), e->d_keep_idx,
+                                                  e->d_keep_n, e->d_small);
+  PGB_LAUNCH_CHECK();
+  int got[2 + kBins];
+  PGB_CUDA(cudaMemcpyAsync(got, e->d_small, sizeof(got), cudaMemcpyDeviceToHost, e->st));
+  PGB_CUDA(cudaStreamSynchronize(e->st));
+  n_trials_total += got[0];
+  if ((s = run_bins(e, tc, got + 2, max_sq))) return s;
+  k_finalize<<<(n + 255) / 256, 256, 0, e->st>>>(c, p->keep_at_most, e->d_keep_idx, e->d_keep_n, e->d_tres,
+                                                 e->d_out, e->d_nout);
+  PGB_LAUNCH_CHECK();
+  PGB_CUDA(cudaEventRecord(e->ev[4], e->st));
+  PGB_CUDA(cudaEventSynchronize(e->ev[4]));
+  float ms;
+  cudaEventElapsedTime(&ms, e->ev[0], e->ev[1]); e->t_ms[1] = ms;
+  cudaEventElapsedTime(&ms, e->ev[1], e->ev[2]); e->t_ms[2] = ms;
+  cudaEventElapsedTime(&ms, e->ev[2], e->ev[3]); e->t_ms[3] = ms;
+  cudaEventElapsedTime(&ms, e->ev[3], e->ev[4]); e->t_ms[4] = ms;
+  cudaEventElapsedTime(&ms, e->ev[0], e->ev[4]); e->t_ms[5] = ms;
+  e->counts[1] = n_trials_total;
+  return PGB_OK;
+}
+
+pgb_status pgb_queries_fetch(pgb_engine *e, pgb_placement *out, int *n_out, int *qstatus) {
+  if (!e || e->Q < 1) return PGB_OK;
+  if (!e->d_out) { set_error("fetch: nothing run"); return PGB_ERR_STATE; }
+  PGB_CUDA(cudaMemcpyAsync(out, e->d_out, (size_t)e->Q * e->out_keep * sizeof(pgb_placement), cudaMemcpyDeviceToHost, e->st));
+  PGB_CUDA(cudaMemcpyAsync(n_out, e->d_nout, (size_t)e->Q * 4, cudaMemcpyDeviceToHost, e->st));
+  PGB_CUDA(cudaMemcpyAsync(qstatus, e->d_qstatus, (size_t)e->Q * 4, cudaMemcpyDeviceToHost, e->st));
+  PGB_CUDA(cudaStreamSynchronize(e->st));
+  return PGB_OK;
+}
+
+pgb_status pgb_place(pgb_engine *e, const pgb_prefs *p, int n_queries, const char *seqs, pgb_placement *out,
+                     int *n_out, int *qstatus) {
+  pgb_status s;
+  if ((s = pgb_queries_load(e, n_queries, seqs)) || (s = pgb_queries_run(e, p)) ||
+      (s = pgb_queries_fetch(e, out, n_out, qstatus)))
+    return s;
+  return PGB_OK;
+}
+
+pgb_status pgb_queries_trials(pgb_engine *e, const pgb_prefs *p, int optimizer, int mode, int n_trials,
+                              const pgb_trial *trials, pgb_trial_out *out) {
+  if (!e || !e->glvs_ready || e->Q < 1) { set_error("trials: no GLVs or no queries"); return PGB_ERR_STATE; }
+  pgb_status s;
+  if ((s = check_prefs(p))) return s;
+  if (optimizer < 0 || optimizer > 1 || mode < 0 || mode > 1 || n_trials < 0) { set_error("trials: bad mode"); return PGB_ERR_ARG; }
+  if (!n_trials) return PGB_OK;
+  std::vector<TrialIn> tin(n_trials);
+  int max_sq = 1;
+  for (int i = 0; i < n_trials; i++) {
+    const pgb_trial &t = trials[i];
+    if (t.query < 0 || t.query >= e->Q || t.edge < 0 || t.edge >= e->n_nodes || t.edge == e->root) {
+      set_error("trials: trial %d out of range", i);
+      return PGB_ERR_ARG;
+    }
+    if (e->h_qlen[t.query] < 1) { set_error("trials: query %d has no informative site", t.query); return PGB_ERR_ARG; }
+    tin[i] = TrialIn{t.query, t.edge, t.pend0, t.dist0, t.tol};
+    max_sq = std::max(max_sq, e->h_qlen[t.query]);
+  }
+  if ((size_t)n_trials > e->trials_cap) {
+    if ((s = dalloc(&e->d_trials, n_trials)) || (s = dalloc(&e->d_tres, n_trials)) ||
+        (s = dalloc(&e->d_bin_list, (size_t)n_trials * kBins)))
+      return s;
+    e->trials_cap = n_trials;
+  }
+  PGB_CUDA(cudaMemcpyAsync(e->d_trials, tin.data(), n_trials * sizeof(TrialIn), cudaMemcpyHostToDevice, e->st));
+  // bin on the host
+  int lim[kBins];
+  bin_limits(e, lim);
+  std::vector<std::vector<int>> bins(kBins);
+  for (int i = 0; i < n_trials; i++) {
+    int sq = e->h_qlen[tin[i].q], b = 0;
+    while (b < kBins - 1 && sq > lim[b]) b++;
+    bins[b].push_back(i);
+  }
+  int counts[kBins];
+  for (int b = 0; b < kBins; b++) {
+    counts[b] = (int)bins[b].size();
+    if (counts[b])
+      PGB_CUDA(cudaMemcpyAsync(e->d_bin_list + (size_t)b * e->trials_cap, bins[b].data(), counts[b] * 4,
+                               cudaMemcpyHostToDevice, e->st));
+  }
+  TrialCtx tc = trial_ctx(e, p, optimizer, mode);
+  if ((s = run_bins(e, tc, counts, max_sq))) return s;
+  std::vector<TrialRes> res(n_trials);
+  PGB_CUDA(cudaMemcpyAsync(res.data(), e->d_tres, n_trials * sizeof(TrialRes), cudaMemcpyDeviceToHost, e->st));
+  PGB_CUDA(cudaStreamSynchronize(e->st));
+  for (int i = 0; i < n_trials; i++) {
+    out[i].like = res[i].like;
+    out[i].pend = res[i].pend;
+    out[i].dist = res[i].dist;
+    for (int k = 0; k < 6; k++) out[i].derivs[k] = res[i].der[k];
+    out[i].status = res[i].status;
+    out[i].n_evals = res[i].n_evals;
+  }
+  return PGB_OK;
+}
+
+pgb_status pgb_engine_timings(pgb_engine *e, double *ms, double *counts) {
+  if (!e) return PGB_ERR_ARG;
+  for (int i = 0; i < 6; i++) ms[i] = e->t_ms[i];
+  for (int i = 0; i < 4; i++) counts[i] = e->counts[i];
+  return PGB_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,255 @@
+"""Batched GPU placement engine against the FP64 oracle.
+
+Tolerances (FP32 GLVs with exact int32 exponents, FP64 per-site log sums and
+scalar optimiser state):
+  * logL of a fixed (query, edge, pendant, distal) point: 2e-7 relative
+  * optimised logL: 1e-6 relative (the benchmark spec's bound)
+  * best edge identical for >= 99.9% of queries whose top two oracle
+    placements are not tied (tie: within 1e-6 relative)
+"""
+import math
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+LOGL_RTOL = 1e-6
+
+
+@pytest.fixture(scope="module")
+def small(oracle_lib):
+    from pplacer_gb300 import engine as E
+    from pplacer_gb300 import synth
+    w = synth.make_workload("cpu_small", n_queries=60)
+    O = oracle_lib
+    oref = O.Reference(O.Model(w.exch, w.statd, w.rates), w.parent, w.bl, w.leaf_row, w.ref_seqs)
+    eng = E.engine_for_workload(w)
+    eng.load_queries(w.query_seqs)
+    return w, oref, eng
+
+
+def _scaled_log(a, e):
+    with np.errstate(divide="ignore"):
+        return np.log(a) + math.log(2) * e[None, :, None]
+
+
+def test_precompute_matches_oracle(small):
+    w, oref, eng = small
+    for node in list(range(0, w.n_nodes, 17)) + [w.n_nodes - 1]:
+        for which in (0, 1, 2):
+            ga, ge = eng.get_glv(which, node)
+            oa, oe = oref.glv(which, node)
+            assert np.mean(ge == oe) >= 0.999
+            same = ge == oe
+            mx = oa.max(axis=(0, 2), keepdims=True)
+            sig = (oa >= 1e-6 * mx) & same[None, :, None]
+            np.testing.assert_allclose(ga[sig], oa[sig], rtol=2e-6)
+
+
+def test_stage1_scores_match_oracle(small, oracle_lib):
+    w, oref, eng = small
+    sc = eng.stage1()
+    edges = [i for i in range(w.n_nodes) if w.parent[i] >= 0]
+    for q in range(0, 60, 7):
+        st, ranking, _ = oref.trace(w.query_seqs[q], oracle_lib.make_prefs(max_strikes=1, max_pitches=0))
+        want = dict(ranking)
+        got = np.array([sc[q, i] for i in range(len(edges))])
+        ref = np.array([want[e] for e in edges])
+        np.testing.assert_allclose(got, ref, rtol=1e-6)
+
+
+def _trial_list(w, n, seed):
+    rng = np.random.default_rng(seed)
+    edges = np.where(w.parent >= 0)[0]
+    out = []
+    for _ in range(n):
+        q = int(rng.integers(len(w.query_seqs)))
+        e = int(rng.choice(edges))
+        out.append((q, e))
+    return out
+
+
+def test_loglike_at_fixed_points(small):
+    w, oref, eng = small
+    from pplacer_gb300 import engine as E
+    pairs = _trial_list(w, 40, 1)
+    rng = np.random.default_rng(2)
+    trials = []
+    for q, e in pairs:
+        trials.append((q, e, float(rng.uniform(1e-8, 0.5)), float(rng.uniform(0, w.bl[e])), 0.01))
+    got = eng.trials(trials, optimizer=E.NEWTON, mode=1)
+    for (q, e, p, d, _), g in zip(trials, got):
+        st, ref = oref.loglike_derivs(w.query_seqs[q], e, p, d)
+        assert st == 0
+        assert abs(g["like"] - ref[0]) <= 2e-7 * abs(ref[0]), (g["like"], ref[0])
+        # adjoint: gradient and Hessian against the FP64 oracle
+        hscale = math.sqrt(abs(ref[3] * ref[4])) + 1.0
+        for k, (gv, rv) in enumerate(zip(g["derivs"][:5], ref[1:6])):
+            tol = 2e-3 * abs(rv) + (1e-5 * abs(ref[3 + k]) + 1e-2 if k < 2 else 1e-3 * hscale + 1.0)
+            assert abs(gv - rv) <= tol, (k, gv, rv)
+
+
+def test_oracle_gradient_vs_central_fd(small):
+    """The FP64 analytic derivatives (the adjoint's reference) against central
+    finite differences with h = 1e-6."""
+    w, oref, _ = small
+    h = 1e-6
+    for q, e in _trial_list(w, 12, 3):
+        p, d = 0.05, 0.4 * w.bl[e]
+        s = w.query_seqs[q]
+        _, c = oref.loglike_derivs(s, e, p, d)
+        _, pp = oref.loglike_derivs(s, e, p + h, d)
+        _, pm = oref.loglike_derivs(s, e, p - h, d)
+        _, dp = oref.loglike_derivs(s, e, p, d + h)
+        _, dm = oref.loglike_derivs(s, e, p, d - h)
+        fd_gp = (pp[0] - pm[0]) / (2 * h)
+        fd_gd = (dp[0] - dm[0]) / (2 * h)
+        noise = 4e-16 * abs(c[0]) / h
+        assert abs(fd_gp - c[1]) <= 1e-6 * abs(c[1]) + noise
+        assert abs(fd_gd - c[2]) <= 1e-6 * abs(c[2]) + noise
+        fd_hpp = (pp[1] - pm[1]) / (2 * h)
+        assert abs(fd_hpp - c[3]) <= 1e-5 * abs(c[3]) + 1e-3
+
+
+def test_gpu_forward_vs_fd(small):
+    """The GPU adjoint against central differences of the GPU forward (FP32
+    forward: step sized to its noise, h = 1e-3 on the branch length)."""
+    w, oref, eng = small
+    from pplacer_gb300 import engine as E
+    h = 1e-3
+    trials = []
+    pairs = _trial_list(w, 10, 4)
+    for q, e in pairs:
+        p, d = 0.08, 0.5 * w.bl[e]
+        trials += [(q, e, p, d, 0.01), (q, e, p + h, d, 0.01), (q, e, p - h, d, 0.01),
+                   (q, e, p, d + h, 0.01), (q, e, p, d - h, 0.01)]
+    got = eng.trials(trials, optimizer=E.NEWTON, mode=1)
+    for i in range(len(pairs)):
+        c, pp, pm, dp, dm = got[5 * i:5 * i + 5]
+        fd_gp = (pp["like"] - pm["like"]) / (2 * h)
+        fd_gd = (dp["like"] - dm["like"]) / (2 * h)
+        assert abs(fd_gp - c["derivs"][0]) <= 1e-2 * abs(c["derivs"][0]) + 0.05
+        assert abs(fd_gd - c["derivs"][1]) <= 1e-2 * abs(c["derivs"][1]) + 0.05
+
+
+@pytest.mark.parametrize("optimizer", [0, 1])
+@pytest.mark.parametrize("tol", [0.01, 1e-5])
+def test_single_location_optimisation(small, optimizer, tol):
+    """Three_tax.optimize from the default start at one location
+    (core.ml:386-425): Brent replica and Newton against the oracle's Brent."""
+    w, oref, eng = small
+    pairs = _trial_list(w, 30, 5)
+    trials = [(q, e, 0.1, w.bl[e] / 2.0, tol) for q, e in pairs]
+    got = eng.trials(trials, optimizer=optimizer, mode=0)
+    for (q, e, p0, d0, _), g in zip(trials, got):
+        st, ref = oref.optimize_location(w.query_seqs[q], e, p0, d0, tol)
+        assert st == 0 and g["status"] in (0, 1)
+        rl = ref[0]
+        # Newton reaches the optimum; Brent stops within its tolerance of it
+        slack = LOGL_RTOL * abs(rl) if tol < 1e-3 else max(LOGL_RTOL * abs(rl), 0.05)
+        if optimizer == 1:
+            assert g["like"] >= rl - LOGL_RTOL * abs(rl), (g, ref)
+        assert abs(g["like"] - rl) <= slack, (g, ref)
+
+
+def _best_edge_agreement(res_gpu, res_orc):
+    agree = tied = total = 0
+    for g, o in zip(res_gpu, res_orc):
+        if not o:
+            continue
+        total += 1
+        if len(o) > 1 and abs(o[0][1] - o[1][1]) <= 1e-6 * abs(o[0][1]):
+            tied += 1
+            continue
+        agree += g and g[0][0] == o[0][0]
+    return agree, total - tied
+
+
+@pytest.mark.parametrize("optimizer", [0, 1])
+def test_place_all_edges_vs_oracle(small, oracle_lib, optimizer):
+    """cpu_small preferences: every edge goes to stage 2 (max_strikes 0)."""
+    from pplacer_gb300 import engine as E
+    w, oref, eng = small
+    O = oracle_lib
+    ores, ost = oref.place(w.query_seqs, O.make_prefs(max_strikes=0), n_threads=8)
+    gres, gst = eng.place(w.query_seqs, E.default_prefs(max_strikes=0, optimizer=optimizer))
+    assert list(gst) == list(ost)
+    agree, non_tied = _best_edge_agreement(gres, ores)
+    assert agree >= 0.999 * non_tied
+    for g, o in zip(gres, ores):
+        if not g or not o or g[0][0] != o[0][0]:
+            continue
+        assert abs(g[0][1] - o[0][1]) <= LOGL_RTOL * abs(o[0][1])
+        assert abs(g[0][2] - o[0][2]) <= 0.02  # like_weight_ratio
+
+
+def test_place_baseball_dna(oracle_lib):
+    """dna_1k preferences (keep 7, strikes 6) on a 60-query sample."""
+    from pplacer_gb300 import engine as E
+    from pplacer_gb300 import synth
+    O = oracle_lib
+    w = synth.make_workload("dna_1k", n_queries=60)
+    oref = O.Reference(O.Model(w.exch, w.statd, w.rates), w.parent, w.bl, w.leaf_row, w.ref_seqs)
+    ores, ost = oref.place(w.query_seqs, O.make_prefs(), n_threads=8)
+    eng = E.engine_for_workload(w)
+    for optimizer in (0, 1):
+        gres, gst = eng.place(w.query_seqs, E.default_prefs(optimizer=optimizer))
+        assert list(gst) == list(ost)
+        agree, non_tied = _best_edge_agreement(gres, ores)
+        assert agree >= 0.999 * non_tied, (optimizer, agree, non_tied)
+        for g, o in zip(gres, ores):
+            if g and o and g[0][0] == o[0][0]:
+                assert abs(g[0][1] - o[0][1]) <= LOGL_RTOL * abs(o[0][1])
+
+
+def test_place_gcat_and_protein(oracle_lib):
+    """Per-site CAT (Gcat_model) and 20-state Gamma models on small trees."""
+    from pplacer_gb300 import engine as E
+    from pplacer_gb300 import synth
+    O = oracle_lib
+    for name, kw in (("cat_5k", dict(taxa=120, sites=300, lo=60, hi=300)),
+                     ("aa_500", dict(taxa=60, sites=120, lo=40, hi=120))):
+        w = synth.make_workload(name, n_queries=30, **kw)
+        om = O.Model(w.exch, w.statd, w.rates, w.site_cats)
+        oref = O.Reference(om, w.parent, w.bl, w.leaf_row, w.ref_seqs)
+        ores, ost = oref.place(w.query_seqs, O.make_prefs(), n_threads=8)
+        eng = E.engine_for_workload(w)
+        gres, gst = eng.place(w.query_seqs, E.default_prefs(optimizer=1))
+        assert list(gst) == list(ost), name
+        agree, non_tied = _best_edge_agreement(gres, ores)
+        assert agree >= 0.999 * non_tied, (name, agree, non_tied)
+        for g, o in zip(gres, ores):
+            if g and o and g[0][0] == o[0][0]:
+                assert abs(g[0][1] - o[0][1]) <= LOGL_RTOL * abs(o[0][1]), name
+
+
+def test_edge_cases(small, oracle_lib):
+    """All-gap query, unknown character, ambiguity codes, a one-site query,
+    an empty batch, and a zero-length edge."""
+    from pplacer_gb300 import engine as E
+    w, oref, eng = small
+    S = w.n_sites
+    base = w.query_seqs[0]
+    amb = "".join(("N" if i % 7 == 0 else "R" if i % 11 == 0 else c) if c != "-" else c for i, c in enumerate(base))
+    one = "-" * 500 + base.strip("-")[0] + "-" * (S - 501)
+    qs = ["-" * S, base[:10] + "Z" + base[11:], amb, one]
+    gres, gst = eng.place(qs, E.default_prefs())
+    ores, ost = oref.place(qs, oracle_lib.make_prefs(), n_threads=4)
+    assert list(gst) == [1, 3, 0, 0] and list(ost) == [1, 3, 0, 0]
+    for i in (2, 3):
+        assert gres[i][0][0] == ores[i][0][0] or abs(gres[i][0][1] - ores[i][0][1]) <= 1e-6 * abs(ores[i][0][1])
+        assert abs(gres[i][0][1] - ores[i][0][1]) <= LOGL_RTOL * abs(ores[i][0][1])
+    r, s = eng.place([], E.default_prefs())
+    assert r == [] and len(s) == 0
+    # zero-length edge: distal is fixed at 0
+    from pplacer_gb300 import synth
+    w2 = synth.make_workload("cpu_small", n_queries=8, taxa=30, sites=200, lo=80, hi=200)
+    w2.bl[3] = 0.0
+    O = oracle_lib
+    oref2 = O.Reference(O.Model(w2.exch, w2.statd, w2.rates), w2.parent, w2.bl, w2.leaf_row, w2.ref_seqs)
+    eng2 = E.engine_for_workload(w2)
+    eng2.load_queries(w2.query_seqs)
+    got = eng2.trials([(0, 3, 0.1, 0.0, 1e-5)], optimizer=0)
+    st, ref = oref2.optimize_location(w2.query_seqs[0], 3, 0.1, 0.0, 1e-5)
+    assert got[0]["dist"] == 0.0 and abs(got[0]["like"] - ref[0]) <= LOGL_RTOL * abs(ref[0])
