@@ -1,0 +1,282 @@
+"""Placement throughput benchmark (query placements/s) on one GB300.
+
+Workload: dna_1k -- the batched-FP32 configuration: Yule tree of 1,000 taxa
+(branch lengths ~ Exp(0.05)), DNA GTR+G4, 1,500-site alignment, 10,000 queries
+of masked length U[100, 1500] with 2% substitution noise and 1% internal gaps,
+pplacer default placement preferences (keep-at-most 7, max-strikes 6,
+strike-box 3, max-pitches 40), seeded synthetic data (seed 1001).
+
+A step is the whole placement phase for all queries (stage-1 ranking of every
+edge, baseball stage-2 branch-length optimisation, final refinement at 1e-5,
+like_weight_ratio), after the reference-tree precompute, as pplacer times it.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--optimizer newton|brent] [--queries Q]
+
+value: placements/s with queries and GLVs already resident in HBM, timed with
+       CUDA events on the engine's stream; the GLV arrays (3 x 192 MB) exceed
+       the 129 MB L2, so no L2 flush is needed between steps.
+e2e:   placements/s through pgb_place (the C ABI call a caller makes) with the
+       query rows in host memory and the placements copied back every step.
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--optimizer", default="newton", choices=["newton", "brent"])
+    ap.add_argument("--queries", type=int, default=None)
+    ap.add_argument("--workload", default="dna_1k")
+    ap.add_argument("--cpu-sample", type=int, default=512, help="queries in the CPU-baseline sample")
+    return ap.parse_args()
+
+
+def dist_setup(n):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+        return rank, world, local, dist
+    return rank, world, local, None
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(dist, v):
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        med = sorted(sm)[len(sm) // 2] if sm else None
+        return {"sm_mhz": med, "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def load_peaks():
+    try:
+        with open(MEASURED_PEAKS) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def cpu_baseline(w, n_sample, prefs_kw):
+    """The oracle (FP64 CPU restatement of pplacer's path, with the reference's
+    own linear_c.c arithmetic) on a bounded sample, all host threads."""
+    from oracle import oracle as O
+    O.build(with_ref=True)
+    n = min(n_sample, len(w.query_seqs))
+    threads = os.cpu_count() or 1
+    ref = O.Reference(O.Model(w.exch, w.statd, w.rates, w.site_cats), w.parent, w.bl, w.leaf_row, w.ref_seqs)
+    t0 = time.perf_counter()
+    ref.place(w.query_seqs[:n], O.make_prefs(**prefs_kw), n_threads=threads)
+    dt = time.perf_counter() - t0
+    return n / dt, threads, n, dt
+
+
+def run_reference(args):
+    rank, world, local, dist = dist_setup(args.gpus)
+    if rank != 0:
+        return
+    from pplacer_gb300 import synth
+    w = synth.make_workload(args.workload, n_queries=args.queries)
+    prefs_kw = dict(w.prefs)
+    from oracle import oracle as O
+    O.build(with_ref=True)
+    threads = os.cpu_count() or 1
+    ref = O.Reference(O.Model(w.exch, w.statd, w.rates, w.site_cats), w.parent, w.bl, w.leaf_row, w.ref_seqs)
+    n = min(args.cpu_sample // 2, len(w.query_seqs))
+    for i in range(args.warmup):
+        ref.place(w.query_seqs[:max(8, n // 8)], O.make_prefs(**prefs_kw), n_threads=threads)
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        lo = (i * n) % len(w.query_seqs)
+        ref.place((w.query_seqs + w.query_seqs)[lo:lo + n], O.make_prefs(**prefs_kw), n_threads=threads)
+    dt = time.perf_counter() - t0
+    v = n * args.steps / dt
+    line = {"metric": "query placements/s", "value": v, "unit": "placements/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "impl": "reference",
+            "config": {"workload": args.workload, "queries_per_step": n, "taxa": (w.n_nodes + 1) // 2,
+                       "sites": w.n_sites},
+            "cpu_baseline": {"value": v, "unit": "placements/s", "cores": threads, "kind": "port",
+                             "sample": "%d queries of %s per step" % (n, args.workload)},
+            "e2e": {"value": v, "unit": "placements/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def run_ours(args):
+    rank, world, local, dist = dist_setup(args.gpus)
+    import numpy as np
+    from pplacer_gb300 import build as B
+    B.build()
+    from pplacer_gb300 import engine as E
+    from pplacer_gb300 import lib as L
+    from pplacer_gb300 import synth
+    w = synth.make_workload(args.workload, n_queries=args.queries)
+    Q, S = len(w.query_seqs), w.n_sites
+    eng = E.engine_for_workload(w)
+    prefs = E.default_prefs(optimizer=1 if args.optimizer == "newton" else 0, **w.prefs)
+    lib = L.load()
+    # ---- device-resident value ----
+    eng.load_queries(w.query_seqs)
+    for _ in range(args.warmup):
+        eng.run(prefs)
+    barrier(dist)
+    sampler = ClockSampler(local) if rank == 0 else None
+    if sampler:
+        sampler.start()
+    n0 = lib.pgb_kernel_launch_count()
+    ms_steps, phase = [], np.zeros(6)
+    counts = np.zeros(4)
+    for _ in range(args.steps):
+        eng.run(prefs)
+        ms, cnt = eng.timings()
+        ms_steps.append(ms[5])
+        phase += ms
+        counts += cnt
+    launches = lib.pgb_kernel_launch_count() - n0
+    barrier(dist)
+    clocks = sampler.stop() if sampler else None
+    t_dev = max_over_ranks(dist, sum(ms_steps) / 1e3)
+    value = Q * world * args.steps / t_dev
+    # ---- end to end through pgb_place, host buffers ----
+    seqs = "".join(w.query_seqs).encode()
+    kam = prefs.keep_at_most
+    out = (L.Placement * (Q * kam))()
+    n_out = np.zeros(Q, dtype=np.int32)
+    qst = np.zeros(Q, dtype=np.int32)
+    lib.pgb_place(eng.h, C.byref(prefs), Q, seqs, C.addressof(out), n_out.ctypes.data, qst.ctypes.data)
+    barrier(dist)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        L.check(lib.pgb_place(eng.h, C.byref(prefs), Q, seqs, C.addressof(out), n_out.ctypes.data,
+                              qst.ctypes.data), "pgb_place")
+    t_e2e = max_over_ranks(dist, time.perf_counter() - t0)
+    e2e = Q * world * args.steps / t_e2e
+    if rank != 0:
+        return
+    # ---- roofline of the dominant kernel (stage-2 trials) ----
+    # algorithmic bytes per objective evaluation: the distal and proximal GLV
+    # windows of the query's informative sites (FP32 + int32 exponent per site)
+    # and one query code byte per site: S_q * (2 * (4*R*K + 4) + 1).
+    R, K = len(w.rates) if w.site_cats is None else 1, w.K
+    bytes_per_site_eval = 2 * (4 * R * K + 4) + 1
+    site_evals = counts[3]
+    t_trials = phase[3] / 1e3 / args.steps
+    peak, peak_kind = load_peaks()
+    achieved = bytes_per_site_eval * site_evals / args.steps / t_trials / 1e9 if t_trials > 0 else 0.0
+    cpu_v, cpu_threads, cpu_n, cpu_dt = cpu_baseline(w, args.cpu_sample, dict(w.prefs))
+    line = {
+        "metric": "query placements/s", "value": value, "unit": "placements/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": args.workload, "taxa": (w.n_nodes + 1) // 2, "sites": S, "queries": Q,
+                   "model": "GTR+G4" if w.site_cats is None else "GTR+CAT20",
+                   "optimizer": args.optimizer, "keep_at_most": prefs.keep_at_most,
+                   "max_strikes": prefs.max_strikes, "l2": "GLV arrays 3x%.0f MB exceed L2, no flush" %
+                   (w.n_nodes * S * R * K * 4 / 1e6), "seed": w.seed},
+        "edge_evals": {"stage1_pairs_per_s": counts[0] / (phase[2] / 1e3),
+                       "stage2_evals_per_s": counts[2] / (phase[3] / 1e3),
+                       "stage2_trials_per_step": counts[1] / args.steps,
+                       "phase_ms": {"stage1_table": phase[1] / args.steps, "stage1_rank": phase[2] / args.steps,
+                                    "stage2": phase[3] / args.steps, "refine_out": phase[4] / args.steps}},
+        "roofline": {"kernel": "k_trials (stage 2)", "bound": "hbm", "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak, "traffic": None, "peak_source": peak_kind},
+        "cpu_baseline": {"value": cpu_v, "unit": "placements/s", "cores": cpu_threads, "kind": "port",
+                         "sample": "%d queries of %s (%.1f s)" % (cpu_n, args.workload, cpu_dt)},
+        "e2e": {"value": e2e, "unit": "placements/s", "h2d_bytes_per_step": Q * S,
+                "d2h_bytes_per_step": Q * kam * C.sizeof(L.Placement) + 8 * Q},
+        "gpu_launches": int(launches),
+        "clocks": clocks,
+    }
+    print(json.dumps(line))
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

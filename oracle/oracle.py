@@ -311,3 +311,45 @@ def model_from_fixture(fx):
 def reference_from_fixture(fx, model=None):
     model = model or model_from_fixture(fx)
     return Reference(model, fx["parent"], fx["bl"], fx["leaf_row"], fx["seqs"])
+
+
+def polish(ref, seq, loc, pend, dist, max_pend=2.0, iters=100):
+    """FP64 projected Newton on (pendant, distal) from (pend, dist) to the
+    stationary point of the likelihood at location loc (box [1e-8, max_pend]
+    x [0, bl]); returns (logL, pend, dist).  Used by tests to measure how far
+    the reference's alternating Brent stops from the optimum."""
+    cut = float(ref.bl[loc])
+    p, d = float(pend), min(max(float(dist), 0.0), cut)
+    st, v = ref.loglike_derivs(seq, loc, p, d)
+    for _ in range(iters):
+        L, gp, gd, hpp, hdd, hpd = v
+        fp = not ((p <= 1e-8 and gp <= 0) or (p >= max_pend and gp >= 0))
+        fd = cut > 0 and not ((d <= 0 and gd <= 0) or (d >= cut and gd >= 0))
+        if not fp and not fd:
+            break
+        sp = sd = 0.0
+        det = hpp * hdd - hpd * hpd
+        if fp and fd and hpp < 0 and hdd < 0 and det > 0:
+            sp = -(hdd * gp - hpd * gd) / det
+            sd = -(hpp * gd - hpd * gp) / det
+        else:
+            if fp:
+                sp = -gp / hpp if hpp < 0 else np.sign(gp) * max(0.5 * p, 0.01)
+            if fd:
+                sd = -gd / hdd if hdd < 0 else np.sign(gd) * 0.25 * cut
+        ok = False
+        for _ls in range(60):
+            np_, nd = min(max(p + sp, 1e-8), max_pend), min(max(d + sd, 0.0), cut)
+            st, nv = ref.loglike_derivs(seq, loc, np_, nd)
+            if nv[0] >= L - 1e-12 * abs(L):
+                ok = True
+                break
+            sp *= 0.5
+            sd *= 0.5
+        if not ok:
+            break
+        step = max(abs(np_ - p), abs(nd - d))
+        p, d, v = np_, nd, nv
+        if step < 1e-10:
+            break
+    return v[0], p, d

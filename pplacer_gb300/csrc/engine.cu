@@ -471,10 +471,11 @@ struct TrialCtx {
   double start_pend, max_pend;
   int optimizer, mode;
   int smem_win, cap;
+  unsigned long long *stats;  // [0] objective evaluations, [1] site evaluations
 };
 
 struct Ctrl {
-  double pend, dist, prox;
+  float pend, dist, prox;
   int cmd;  // 0 stop, 1 value, 2 value + derivatives
 };
 
@@ -528,16 +529,23 @@ __device__ inline TrialSmem carve(char *base, int cap, int win, int RP, int K, i
   return s;
 }
 
+// One evaluation: logL = ex * ln2 + lm + (trial constant); derivatives in FP32.
 struct EvalOut {
-  double L;
-  double g[2], h[3];
+  int ex;
+  float lm;
+  float g[2], h[3];
 };
+
+// logL difference a - b without FP64 (exact exponent difference)
+__device__ __forceinline__ float dlogl(const EvalOut &a, const EvalOut &b) {
+  return (float)(a.ex - b.ex) * 0.69314718f + (a.lm - b.lm);
+}
 
 // All threads: one objective evaluation at ctrl (pend, dist, prox).  Contains
 // exactly three bar1() calls.  Warp 0 gets the combined values.
 template <int K>
 __device__ __noinline__ void eval_part(const TrialCtx &c, const TrialSmem &sm, int q, int node, int Sq, bool derivs,
-                                       double exp_const, EvalOut *out) {
+                                       EvalOut *out) {
   const int tid = threadIdx.x;
   const int NM = c.NM, nc = c.ncode;
   const Ctrl ctl = *sm.ctrl;
@@ -546,7 +554,7 @@ __device__ __noinline__ void eval_part(const TrialCtx &c, const TrialSmem &sm, i
     int which = i / (NM * K), mk = i - which * NM * K;
     int m = mk / K, k = mk - m * K;
     float lr = c.rates[m] * c.lam[k];
-    float t = (float)(which == 0 ? ctl.dist : (which == 1 ? ctl.prox : ctl.pend));
+    float t = which == 0 ? ctl.dist : (which == 1 ? ctl.prox : ctl.pend);
     float a = lr * t;
     sm.E[i] = expf(a);
     sm.Em1[i] = expm1f(a);
@@ -711,7 +719,7 @@ __device__ __noinline__ void eval_part(const TrialCtx &c, const TrialSmem &sm, i
   if (w == 0) {
     float mt = 1.f;
     int et = 0;
-    double sg[5] = {0, 0, 0, 0, 0};
+    float sg[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
     for (int i = 0; i < kTrialWarps; i++) {
       mt *= sm.red[i * 8];
       et += sm.redi[i];
@@ -719,9 +727,11 @@ __device__ __noinline__ void eval_part(const TrialCtx &c, const TrialSmem &sm, i
       mt = frexpf(mt, &em);
       et += em;
       if (derivs)
-        for (int k = 0; k < 5; k++) sg[k] += (double)sm.red[i * 8 + 1 + k];
+#pragma unroll
+        for (int k = 0; k < 5; k++) sg[k] += sm.red[i * 8 + 1 + k];
     }
-    out->L = (double)et * kLn2 + (double)logf(mt) - (double)(float)Sq * c.log_nrates + exp_const;
+    out->ex = et;
+    out->lm = logf(mt);
     out->g[0] = sg[0]; out->g[1] = sg[1];
     out->h[0] = sg[2]; out->h[1] = sg[3]; out->h[2] = sg[4];
   }
@@ -733,25 +743,30 @@ struct Evaluator {
   const TrialCtx *c;
   const TrialSmem *sm;
   int q, node, Sq;
-  double exp_const;
+  double cst;               // exponent and -S log R terms of logL
   double pend, dist, prox;  // three-taxon state (three_tax.ml:252-258)
   double L_last;
   int n_evals;
   EvalOut last;
 
-  __device__ double eval(bool derivs) {
+  __device__ void eval_raw(float p, float d, float x, bool derivs) {
     if ((threadIdx.x & 31) == 0) {
-      sm->ctrl->pend = pend;
-      sm->ctrl->dist = dist;
-      sm->ctrl->prox = prox;
+      sm->ctrl->pend = p;
+      sm->ctrl->dist = d;
+      sm->ctrl->prox = x;
       sm->ctrl->cmd = derivs ? 2 : 1;
     }
     __syncwarp();
     bar1();
-    eval_part<K>(*c, *sm, q, node, Sq, derivs, exp_const, &last);
+    eval_part<K>(*c, *sm, q, node, Sq, derivs, &last);
     n_evals++;
-    L_last = last.L;
-    return last.L;
+  }
+  __device__ double full(const EvalOut &o) const { return (double)o.ex * kLn2 + (double)o.lm + cst; }
+  // FP64 value at the double state (Brent replica)
+  __device__ double eval(bool derivs) {
+    eval_raw((float)pend, (float)dist, (float)prox, derivs);
+    L_last = full(last);
+    return L_last;
   }
   __device__ void stop() {
     if ((threadIdx.x & 31) == 0) sm->ctrl->cmd = 0;
@@ -859,74 +874,68 @@ __device__ int optimize_brent(Evaluator<K> &ev, double tol, double max_pend) {
 }
 
 // Safeguarded projected Newton on (pendant, distal) using the adjoint's
-// gradient and Hessian; box [1e-8, max_pend] x [0, cut].
+// gradient and Hessian; box [1e-8, max_pend] x [0, cut].  The control state
+// is FP32: branch lengths need ~1e-9 resolution, and likelihoods are compared
+// through exact exponent differences (dlogl), so no FP64 arithmetic (64-cycle
+// latency on this part) sits on the optimiser's critical path.
 template <int K>
-__device__ int optimize_newton(Evaluator<K> &ev, double tol, double max_pend, double cut) {
-  const double pmin = 1e-8, pmax = max_pend, dmin = 0.0, dmax = cut;
-  const double tn = 0.01 * tol;
-  double p = ev.pend, d = fmin(fmax(ev.dist, dmin), dmax);
-  ev.dist = d;
-  ev.prox = cut - d;
-  double L = ev.eval(true);
-  if (!isfinite(L)) return BR_GSLERR;
+__device__ int optimize_newton(Evaluator<K> &ev, double tol, double max_pend, double cut_d) {
+  const float pmin = 1e-8f, pmax = (float)max_pend, cut = (float)cut_d, dmax = cut;
+  const float tn = (float)(0.01 * tol);
+  float p = fminf(fmaxf((float)ev.pend, pmin), pmax);
+  float d = fminf(fmaxf((float)ev.dist, 0.f), dmax);
+  ev.eval_raw(p, d, cut - d, true);
   EvalOut cur = ev.last;
+  if (!isfinite(cur.lm)) return BR_GSLERR;
+  // noise allowance for accepting a step: 1e-6 absolute + 1e-9 relative
+  const float allow = 1e-6f + 1e-9f * fabsf((float)cur.ex * 0.69314718f + (float)ev.cst);
+  int status = BR_OK;
   for (int it = 0; it < 60; it++) {
-    double gp = cur.g[0], gd = cur.g[1], hpp = cur.h[0], hdd = cur.h[1], hpd = cur.h[2];
-    bool free_p = !((p <= pmin && gp <= 0) || (p >= pmax && gp >= 0));
-    bool free_d = (dmax > dmin) && !((d <= dmin && gd <= 0) || (d >= dmax && gd >= 0));
+    float gp = cur.g[0], gd = cur.g[1], hpp = cur.h[0], hdd = cur.h[1], hpd = cur.h[2];
+    bool free_p = !((p <= pmin && gp <= 0.f) || (p >= pmax && gp >= 0.f));
+    bool free_d = (dmax > 0.f) && !((d <= 0.f && gd <= 0.f) || (d >= dmax && gd >= 0.f));
     if (!free_p && !free_d) break;
-    double sp = 0, sd = 0;
-    double det = hpp * hdd - hpd * hpd;
-    if (free_p && free_d && hpp < 0 && hdd < 0 && det > 0) {
+    float sp = 0.f, sd = 0.f;
+    float det = hpp * hdd - hpd * hpd;
+    if (free_p && free_d && hpp < 0.f && hdd < 0.f && det > 0.f) {
       sp = -(hdd * gp - hpd * gd) / det;
       sd = -(hpp * gd - hpd * gp) / det;
     } else {
-      if (free_p) sp = hpp < 0 ? -gp / hpp : (gp > 0 ? 1.0 : -1.0) * fmax(0.5 * p, 0.01);
-      if (free_d) sd = hdd < 0 ? -gd / hdd : (gd > 0 ? 1.0 : -1.0) * 0.25 * (dmax - dmin);
+      if (free_p) sp = hpp < 0.f ? -gp / hpp : copysignf(fmaxf(0.5f * p, 0.01f), gp);
+      if (free_d) sd = hdd < 0.f ? -gd / hdd : copysignf(0.25f * dmax, gd);
     }
-    double lim_p = fmax(2.0 * p, 0.05), lim_d = fmax(0.5 * (dmax - dmin), 1e-12);
-    if (fabs(sp) > lim_p) sp = copysign(lim_p, sp);
-    if (fabs(sd) > lim_d) sd = copysign(lim_d, sd);
-    double pred = gp * sp + gd * sd;  // first-order predicted gain
-    double allow = 1e-9 * fabs(L) + 1e-6;
+    float lim_p = fmaxf(2.f * p, 0.05f), lim_d = fmaxf(0.5f * dmax, 1e-12f);
+    if (fabsf(sp) > lim_p) sp = copysignf(lim_p, sp);
+    if (fabsf(sd) > lim_d) sd = copysignf(lim_d, sd);
+    float pred = gp * sp + gd * sd;  // first-order predicted gain
     bool accepted = false;
-    double np = p, nd = d;
+    float np = p, nd = d;
     for (int ls = 0; ls < 30; ls++) {
-      np = fmin(fmax(p + sp, pmin), pmax);
-      nd = fmin(fmax(d + sd, dmin), dmax);
+      np = fminf(fmaxf(p + sp, pmin), pmax);
+      nd = fminf(fmaxf(d + sd, 0.f), dmax);
       if (np == p && nd == d) break;
-      ev.pend = np;
-      ev.dist = nd;
-      ev.prox = cut - nd;
-      double Ln = ev.eval(true);
-      if (isfinite(Ln) && Ln >= L - allow) {
+      ev.eval_raw(np, nd, cut - nd, true);
+      if (isfinite(ev.last.lm) && dlogl(ev.last, cur) >= -allow) {
         accepted = true;
-        L = Ln;
-        cur = ev.last;
         break;
       }
-      sp *= 0.25;
-      sd *= 0.25;
+      sp *= 0.25f;
+      sd *= 0.25f;
     }
-    double step = fmax(fabs(np - p), fabs(nd - d));
-    if (!accepted) {
-      // restore the state of the best point
-      ev.pend = p; ev.dist = d; ev.prox = cut - d;
-      ev.L_last = L;
-      ev.last = cur;
-      break;
-    }
+    if (!accepted) break;
+    float step = fmaxf(fabsf(np - p), fabsf(nd - d));
     p = np;
     d = nd;
-    if (step < tn || fabs(pred) < allow * 1e-3) break;
-    if (it == 59) return BR_MAXITER;
+    cur = ev.last;
+    if (step < tn || fabsf(pred) < 1e-3f * allow) break;
+    if (it == 59) status = BR_MAXITER;
   }
   ev.pend = p;
   ev.dist = d;
-  ev.prox = cut - d;
-  ev.L_last = L;
+  ev.prox = (double)(cut - d);
   ev.last = cur;
-  return BR_OK;
+  ev.L_last = ev.full(cur);
+  return status;
 }
 
 template <int K>
@@ -978,13 +987,14 @@ __global__ void __launch_bounds__(kTrialThreads) k_trials(TrialCtx c, const Tria
       bar1();
       int cmd = sm.ctrl->cmd;
       if (cmd == 0) break;
-      eval_part<K>(c, sm, q, node, Sq, cmd == 2, exp_const, &dummy);
+      eval_part<K>(c, sm, q, node, Sq, cmd == 2, &dummy);
     }
     return;
   }
   // warp 0: the optimiser
   Evaluator<K> ev;
-  ev.c = &c; ev.sm = &sm; ev.q = q; ev.node = node; ev.Sq = Sq; ev.exp_const = exp_const;
+  ev.c = &c; ev.sm = &sm; ev.q = q; ev.node = node; ev.Sq = Sq;
+  ev.cst = exp_const - (double)(float)Sq * c.log_nrates;
   ev.n_evals = 0;
   ev.L_last = NAN;
   const double cut_bl = c.bl[node];
@@ -996,6 +1006,7 @@ __global__ void __launch_bounds__(kTrialThreads) k_trials(TrialCtx c, const Tria
   if (c.mode == 1) {
     ev.eval(true);
   } else {
+    ev.last.g[0] = ev.last.g[1] = ev.last.h[0] = ev.last.h[1] = ev.last.h[2] = 0.f;
     for (int attempt = 0; attempt < 2; attempt++) {
       int st = c.optimizer == 0 ? optimize_brent<K>(ev, tr.tol, c.max_pend)
                                 : optimize_newton<K>(ev, tr.tol, c.max_pend, cut_bl);
@@ -1022,6 +1033,10 @@ __global__ void __launch_bounds__(kTrialThreads) k_trials(TrialCtx c, const Tria
     r.status = status;
     r.n_evals = ev.n_evals;
     out[ti] = r;
+    if (c.stats) {
+      atomicAdd(&c.stats[0], (unsigned long long)ev.n_evals);
+      atomicAdd(&c.stats[1], (unsigned long long)ev.n_evals * (unsigned long long)Sq);
+    }
   }
 }
 
@@ -1264,6 +1279,7 @@ struct pgb_engine {
   TrialRes *d_tres = nullptr;
   int *d_bin_list = nullptr;
   size_t trials_cap = 0;
+  unsigned long long *d_stats = nullptr;  // trial-kernel evaluation counters
   int *d_small = nullptr;  // counters: [0] trial counter, [1] n_active, [2..2+bins) bin counts, then bin limits
   pgb_placement *d_out = nullptr;
   int *d_nout = nullptr;
@@ -1409,6 +1425,7 @@ TrialCtx trial_ctx(pgb_engine *e, const pgb_prefs *p, int optimizer, int mode) {
   c.max_pend = p->max_pend;
   c.optimizer = optimizer;
   c.mode = mode;
+  c.stats = e->d_stats;
   return c;
 }
 
@@ -1613,7 +1630,7 @@ pgb_status pgb_engine_create(const pgb_model_desc *m, const pgb_tree_desc *t, pg
       (s = upload(&e->d_parent, e->parent.data(), e->parent.size(), e->st)) ||
       (s = upload(&e->d_ch_start, e->ch_start.data(), e->ch_start.size(), e->st)) ||
       (s = upload(&e->d_ch_list, e->ch_list.data(), e->ch_list.size(), e->st)) ||
-      (s = dalloc(&e->d_small, 64))) {
+      (s = dalloc(&e->d_small, 64)) || (s = dalloc(&e->d_stats, 4))) {
     pgb_engine_destroy(e);
     return s;
   }
@@ -1643,7 +1660,7 @@ pgb_status pgb_engine_destroy(pgb_engine *e) {
                   e->d_ch_start, e->d_ch_list, e->d_darr, e->d_parr, e->d_snode, e->d_dexp, e->d_pexp, e->d_sexp,
                   e->d_lt, e->d_qe, e->d_seqs, e->d_qcode, e->d_mcode, e->d_reind, e->d_qlen, e->d_qstatus,
                   e->d_scores, e->d_rank, e->d_bb, e->d_res, e->d_tbase, e->d_tcount, e->d_keep_idx, e->d_keep_n,
-                  e->d_trials, e->d_tres, e->d_bin_list, e->d_small, e->d_out, e->d_nout};
+                  e->d_trials, e->d_tres, e->d_bin_list, e->d_small, e->d_out, e->d_nout, e->d_stats};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   for (int i = 0; i < 8; i++)
@@ -1860,6 +1877,7 @@ pgb_status pgb_queries_run(pgb_engine *e, const pgb_prefs *p) {
   if (all_edges) tcap = std::max(tcap, (size_t)e->Q * e->n_edges + 64);
   if ((s = ensure_run_buffers(e, p, rk, maxr, tcap))) return s;
   for (int i = 0; i < 4; i++) e->counts[i] = 0;
+  PGB_CUDA(cudaMemsetAsync(e->d_stats, 0, 4 * sizeof(unsigned long long), e->st));
   PGB_CUDA(cudaEventRecord(e->ev[0], e->st));
   if ((s = build_stage1_table(e, p->start_pend))) return s;
   PGB_CUDA(cudaEventRecord(e->ev[1], e->st));
@@ -1932,6 +1950,10 @@ pgb_status pgb_queries_run(pgb_engine *e, const pgb_prefs *p) {
   cudaEventElapsedTime(&ms, e->ev[3], e->ev[4]); e->t_ms[4] = ms;
   cudaEventElapsedTime(&ms, e->ev[0], e->ev[4]); e->t_ms[5] = ms;
   e->counts[1] = n_trials_total;
+  unsigned long long st_h[2] = {0, 0};
+  PGB_CUDA(cudaMemcpy(st_h, e->d_stats, sizeof st_h, cudaMemcpyDeviceToHost));
+  e->counts[2] = (double)st_h[0];
+  e->counts[3] = (double)st_h[1];
   return PGB_OK;
 }
 
