@@ -46,8 +46,7 @@ def _compile(src, verbose_ptxas=False):
 
 def build(force=False, verbose_ptxas=False):
     os.makedirs(OUT_DIR, exist_ok=True)
-    srcs = [os.path.join(CSRC, s) for s in SOURCES] + [os.path.join(CSRC, "pgb_common.cuh"),
-                                                       os.path.join(ROOT, "include", "pplacer_gb300.h")]
+    srcs = [os.path.join(CSRC, s) for s in os.listdir(CSRC)] + [os.path.join(ROOT, "include", "pplacer_gb300.h")]
     if not force and os.path.exists(LIB):
         t = os.path.getmtime(LIB)
         if all(os.path.getmtime(s) <= t for s in srcs):

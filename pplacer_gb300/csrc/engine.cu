@@ -22,8 +22,6 @@
 namespace pgb {
 namespace {
 
-constexpr int kTrialThreads = 256;
-constexpr int kTrialWarps = kTrialThreads / 32;
 constexpr double kLn2 = 0.69314718055994530942;
 
 enum { ST_OK = 0, ST_MAXITER = 1, ST_FAILED = 2, ST_STARTFAIL = 3 };
@@ -439,606 +437,7 @@ __global__ void k_rank(const double *__restrict__ scores, int n_edges, int rk, c
   }
 }
 
-// ---------------------------------------------------------------------------
-// Stage-2 trials: one CTA per (query, location) optimisation.
-// Warp 0 runs the scalar optimiser (Brent with GSL's conventions, or
-// safeguarded Newton) in FP64; every warp evaluates the objective over its
-// share of the query's informative sites.  The evaluation protocol uses named
-// barrier 1 with all threads of the CTA; warp 0 always ends the protocol with
-// a stop command, every loop in it is bounded.
-// ---------------------------------------------------------------------------
-struct TrialIn {
-  int q, node;
-  double pend0, dist0, tol;
-};
-struct TrialRes {
-  double like, pend, dist;
-  double der[6];
-  int status, n_evals;
-};
-
-struct TrialCtx {
-  const float *darr, *parr;
-  const int *dexp, *pexp;
-  int S, RP, K, NM, ncode, gcat;
-  const double *bl;
-  const uint16_t *reind;
-  const uint8_t *mcode;
-  const int *qlen;
-  const uint8_t *site_cat;
-  const float *X, *W, *Lt, *lvf, *statd, *lam, *rates;
-  double log_nrates;
-  double start_pend, max_pend;
-  int optimizer, mode;
-  int smem_win, cap;
-  unsigned long long *stats;  // [0] objective evaluations, [1] site evaluations
-};
-
-struct Ctrl {
-  float pend, dist, prox;
-  int cmd;  // 0 stop, 1 value, 2 value + derivatives
-};
-
-__device__ __forceinline__ void bar1() { asm volatile("bar.sync 1, %0;" ::"r"(kTrialThreads) : "memory"); }
-
-// shared memory carve-up of one trial CTA
-struct TrialSmem {
-  float *D, *P;              // [RP][cap][K]
-  uint8_t *code, *cat;       // [cap]
-  float *Md, *Mp, *Md1, *Md2, *Mp1, *Mp2;  // [NM][K][K]
-  float *Z, *Z1, *Z2;        // [NM][ncode][K]
-  float *E, *Em1, *Lr;       // [3][NM][K], [3][NM][K], [NM][K]
-  float *red;                // [warps][8]
-  int *redi;                 // [warps]
-  Ctrl *ctrl;
-};
-
-__host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
-
-__host__ __device__ inline size_t trial_smem_bytes(int cap, int win, int RP, int K, int NM, int ncode) {
-  size_t b = 0;
-  if (win) b += 2 * align16((size_t)RP * cap * K * 4);
-  b += 2 * align16((size_t)cap);
-  b += 6 * align16((size_t)NM * K * K * 4);
-  b += 3 * align16((size_t)NM * ncode * K * 4);
-  b += 2 * align16((size_t)3 * NM * K * 4) + align16((size_t)NM * K * 4);
-  b += align16(kTrialWarps * 8 * 4) + align16(kTrialWarps * 4);
-  b += align16(sizeof(Ctrl));
-  return b;
-}
-
-__device__ inline TrialSmem carve(char *base, int cap, int win, int RP, int K, int NM, int ncode) {
-  TrialSmem s;
-  char *p = base;
-  auto take = [&](size_t bytes) { char *r = p; p += align16(bytes); return r; };
-  s.D = win ? (float *)take((size_t)RP * cap * K * 4) : nullptr;
-  s.P = win ? (float *)take((size_t)RP * cap * K * 4) : nullptr;
-  s.code = (uint8_t *)take(cap);
-  s.cat = (uint8_t *)take(cap);
-  size_t mb = (size_t)NM * K * K * 4;
-  s.Md = (float *)take(mb); s.Mp = (float *)take(mb); s.Md1 = (float *)take(mb);
-  s.Md2 = (float *)take(mb); s.Mp1 = (float *)take(mb); s.Mp2 = (float *)take(mb);
-  size_t zb = (size_t)NM * ncode * K * 4;
-  s.Z = (float *)take(zb); s.Z1 = (float *)take(zb); s.Z2 = (float *)take(zb);
-  s.E = (float *)take((size_t)3 * NM * K * 4);
-  s.Em1 = (float *)take((size_t)3 * NM * K * 4);
-  s.Lr = (float *)take((size_t)NM * K * 4);
-  s.red = (float *)take(kTrialWarps * 8 * 4);
-  s.redi = (int *)take(kTrialWarps * 4);
-  s.ctrl = (Ctrl *)take(sizeof(Ctrl));
-  return s;
-}
-
-// One evaluation: logL = ex * ln2 + lm + (trial constant); derivatives in FP32.
-struct EvalOut {
-  int ex;
-  float lm;
-  float g[2], h[3];
-};
-
-// logL difference a - b without FP64 (exact exponent difference)
-__device__ __forceinline__ float dlogl(const EvalOut &a, const EvalOut &b) {
-  return (float)(a.ex - b.ex) * 0.69314718f + (a.lm - b.lm);
-}
-
-// All threads: one objective evaluation at ctrl (pend, dist, prox).  Contains
-// exactly three bar1() calls.  Warp 0 gets the combined values.
-template <int K>
-__device__ __noinline__ void eval_part(const TrialCtx &c, const TrialSmem &sm, int q, int node, int Sq, bool derivs,
-                                       EvalOut *out) {
-  const int tid = threadIdx.x;
-  const int NM = c.NM, nc = c.ncode;
-  const Ctrl ctl = *sm.ctrl;
-  // phase 1: exp factors for (dist, prox, pend)
-  for (int i = tid; i < 3 * NM * K; i += kTrialThreads) {
-    int which = i / (NM * K), mk = i - which * NM * K;
-    int m = mk / K, k = mk - m * K;
-    float lr = c.rates[m] * c.lam[k];
-    float t = which == 0 ? ctl.dist : (which == 1 ? ctl.prox : ctl.pend);
-    float a = lr * t;
-    sm.E[i] = expf(a);
-    sm.Em1[i] = expm1f(a);
-    if (which == 0) sm.Lr[mk] = lr;
-  }
-  bar1();
-  // phase 2: transition matrices P = I + X diag(expm1) Xit^T and derivatives;
-  // evolved query vectors per character with statd folded in
-  const int nmat = NM * K * K;
-  for (int i = tid; i < 2 * nmat; i += kTrialThreads) {
-    int which = i / nmat, r = i - which * nmat;
-    int m = r / (K * K), ij = r - m * K * K;
-    int ii = ij / K, jj = ij - ii * K;
-    const float *w = c.W + (long)ij * K;
-    const float *em = sm.Em1 + (which * NM + m) * K;
-    float acc = (ii == jj) ? 1.f : 0.f;
-#pragma unroll 4
-    for (int k = 0; k < K; k++) acc += w[k] * em[k];
-    (which == 0 ? sm.Md : sm.Mp)[r] = acc;
-    if (derivs) {
-      const float *e = sm.E + (which * NM + m) * K;
-      const float *lr = sm.Lr + m * K;
-      float a1 = 0.f, a2 = 0.f;
-#pragma unroll 4
-      for (int k = 0; k < K; k++) {
-        float t1 = w[k] * lr[k] * e[k];
-        a1 += t1;
-        a2 += t1 * lr[k];
-      }
-      (which == 0 ? sm.Md1 : sm.Mp1)[r] = a1;
-      (which == 0 ? sm.Md2 : sm.Mp2)[r] = a2;
-    }
-  }
-  const int nz = NM * nc * K;
-  for (int i = tid; i < nz; i += kTrialThreads) {
-    int m = i / (nc * K), ck = i - m * nc * K;
-    int code = ck / K, ii = ck - code * K;
-    const float *x = c.X + ii * K;
-    const float *lt = c.Lt + code * K;
-    const float *em = sm.Em1 + (2 * NM + m) * K;
-    float acc = c.lvf[code * K + ii];
-#pragma unroll 4
-    for (int k = 0; k < K; k++) acc += x[k] * em[k] * lt[k];
-    float pi = c.statd[ii];
-    sm.Z[i] = pi * acc;
-    if (derivs) {
-      const float *e = sm.E + (2 * NM + m) * K;
-      const float *lr = sm.Lr + m * K;
-      float a1 = 0.f, a2 = 0.f;
-#pragma unroll 4
-      for (int k = 0; k < K; k++) {
-        float t1 = x[k] * lr[k] * e[k] * lt[k];
-        a1 += t1;
-        a2 += t1 * lr[k];
-      }
-      sm.Z1[i] = pi * a1;
-      sm.Z2[i] = pi * a2;
-    }
-  }
-  bar1();
-  // phase 3: sites
-  float m_acc = 1.f;
-  int e_acc = 0;
-  float gp = 0.f, gd = 0.f, hpp = 0.f, hdd = 0.f, hpd = 0.f;
-  const float *gd_base = c.darr + (long)node * c.S * c.RP * K;
-  const float *gp_base = c.parr + (long)node * c.S * c.RP * K;
-  for (int i = tid; i < Sq; i += kTrialThreads) {
-    int code = sm.code[i];
-    float u = 0.f, ud = 0.f, udd = 0.f, up = 0.f, upp = 0.f, upd = 0.f;
-    int s = 0;
-    if (!c.smem_win) s = c.reind[(long)q * c.S + i];
-    for (int r = 0; r < c.RP; r++) {
-      int m = c.gcat ? sm.cat[i] : r;
-      float dv[K], pv[K];
-      const float *ds = c.smem_win ? sm.D + ((long)r * c.cap + i) * K : gd_base + ((long)s * c.RP + r) * K;
-      const float *ps = c.smem_win ? sm.P + ((long)r * c.cap + i) * K : gp_base + ((long)s * c.RP + r) * K;
-      if (K % 4 == 0) {
-#pragma unroll
-        for (int k = 0; k < K; k += 4) {
-          float4 a = *reinterpret_cast<const float4 *>(ds + k);
-          float4 b = *reinterpret_cast<const float4 *>(ps + k);
-          dv[k] = a.x; dv[k + 1] = a.y; dv[k + 2] = a.z; dv[k + 3] = a.w;
-          pv[k] = b.x; pv[k + 1] = b.y; pv[k + 2] = b.z; pv[k + 3] = b.w;
-        }
-      } else {
-#pragma unroll
-        for (int k = 0; k < K; k++) { dv[k] = ds[k]; pv[k] = ps[k]; }
-      }
-      const float *Md = sm.Md + m * K * K, *Mp = sm.Mp + m * K * K;
-      const float *z = sm.Z + (m * nc + code) * K;
-#pragma unroll(K <= 4 ? K : 1)
-      for (int ii = 0; ii < K; ii++) {
-        float x = 0.f, y = 0.f;
-#pragma unroll
-        for (int j = 0; j < K; j++) {
-          x += Md[ii * K + j] * dv[j];
-          y += Mp[ii * K + j] * pv[j];
-        }
-        float xy = x * y;
-        u += z[ii] * xy;
-        if (derivs) {
-          const float *Md1 = sm.Md1 + m * K * K, *Md2 = sm.Md2 + m * K * K;
-          const float *Mp1 = sm.Mp1 + m * K * K, *Mp2 = sm.Mp2 + m * K * K;
-          float x1 = 0.f, x2 = 0.f, y1 = 0.f, y2 = 0.f;
-#pragma unroll
-          for (int j = 0; j < K; j++) {
-            x1 += Md1[ii * K + j] * dv[j];
-            x2 += Md2[ii * K + j] * dv[j];
-            y1 += Mp1[ii * K + j] * pv[j];
-            y2 += Mp2[ii * K + j] * pv[j];
-          }
-          float z1 = sm.Z1[(m * nc + code) * K + ii], z2 = sm.Z2[(m * nc + code) * K + ii];
-          float a = x1 * y - x * y1;
-          float b = x2 * y - 2.f * x1 * y1 + x * y2;
-          ud += z[ii] * a;
-          udd += z[ii] * b;
-          up += z1 * xy;
-          upp += z2 * xy;
-          upd += z1 * a;
-        }
-      }
-    }
-    int eu;
-    float mu = frexpf(u, &eu);
-    m_acc *= mu;
-    e_acc += eu;
-    int em;
-    m_acc = frexpf(m_acc, &em);
-    e_acc += em;
-    if (derivs) {
-      float inv = 1.f / u;
-      float lp = up * inv, ld = ud * inv;
-      gp += lp;
-      gd += ld;
-      hpp += upp * inv - lp * lp;
-      hdd += udd * inv - ld * ld;
-      hpd += upd * inv - lp * ld;
-    }
-  }
-  // warp combine: mantissa product with exponent carry, derivative sums
-  for (int o = 16; o > 0; o >>= 1) {
-    float mo = __shfl_down_sync(0xffffffffu, m_acc, o);
-    int eo = __shfl_down_sync(0xffffffffu, e_acc, o);
-    m_acc *= mo;
-    e_acc += eo;
-    int em;
-    m_acc = frexpf(m_acc, &em);
-    e_acc += em;
-  }
-  if (derivs) {
-    gp = warp_sum_f(gp); gd = warp_sum_f(gd);
-    hpp = warp_sum_f(hpp); hdd = warp_sum_f(hdd); hpd = warp_sum_f(hpd);
-  }
-  int lane = tid & 31, w = tid >> 5;
-  if (lane == 0) {
-    sm.red[w * 8 + 0] = m_acc;
-    sm.redi[w] = e_acc;
-    sm.red[w * 8 + 1] = gp; sm.red[w * 8 + 2] = gd;
-    sm.red[w * 8 + 3] = hpp; sm.red[w * 8 + 4] = hdd; sm.red[w * 8 + 5] = hpd;
-  }
-  bar1();
-  if (w == 0) {
-    float mt = 1.f;
-    int et = 0;
-    float sg[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
-    for (int i = 0; i < kTrialWarps; i++) {
-      mt *= sm.red[i * 8];
-      et += sm.redi[i];
-      int em;
-      mt = frexpf(mt, &em);
-      et += em;
-      if (derivs)
-#pragma unroll
-        for (int k = 0; k < 5; k++) sg[k] += sm.red[i * 8 + 1 + k];
-    }
-    out->ex = et;
-    out->lm = logf(mt);
-    out->g[0] = sg[0]; out->g[1] = sg[1];
-    out->h[0] = sg[2]; out->h[1] = sg[3]; out->h[2] = sg[4];
-  }
-}
-
-// Warp-0 side of the protocol.
-template <int K>
-struct Evaluator {
-  const TrialCtx *c;
-  const TrialSmem *sm;
-  int q, node, Sq;
-  double cst;               // exponent and -S log R terms of logL
-  double pend, dist, prox;  // three-taxon state (three_tax.ml:252-258)
-  double L_last;
-  int n_evals;
-  EvalOut last;
-
-  __device__ void eval_raw(float p, float d, float x, bool derivs) {
-    if ((threadIdx.x & 31) == 0) {
-      sm->ctrl->pend = p;
-      sm->ctrl->dist = d;
-      sm->ctrl->prox = x;
-      sm->ctrl->cmd = derivs ? 2 : 1;
-    }
-    __syncwarp();
-    bar1();
-    eval_part<K>(*c, *sm, q, node, Sq, derivs, &last);
-    n_evals++;
-  }
-  __device__ double full(const EvalOut &o) const { return (double)o.ex * kLn2 + (double)o.lm + cst; }
-  // FP64 value at the double state (Brent replica)
-  __device__ double eval(bool derivs) {
-    eval_raw((float)pend, (float)dist, (float)prox, derivs);
-    L_last = full(last);
-    return L_last;
-  }
-  __device__ void stop() {
-    if ((threadIdx.x & 31) == 0) sm->ctrl->cmd = 0;
-    __syncwarp();
-    bar1();
-  }
-};
-
-// Brent minimisation with GSL's conventions (minimization.ml:24-41,83-101;
-// gsl_min_fminimizer_brent).  f(v) sets the state and returns -logL.
-template <class F>
-__device__ int brent_dev(F &f, double raw_start, double left, double right, double tol, double *xout) {
-  const int max_iters = 100;
-  if (left >= raw_start || raw_start >= right) return BR_STARTFAIL;
-  double righty = f(right);
-  double lefty = f(left);
-  double smaller = lefty < righty ? left : right;
-  double miny = lefty <= righty ? lefty : righty;  // Stdlib.min
-  double prev = raw_start, pv;
-  for (int iter = 1;; iter++) {
-    pv = f(prev);
-    if (pv < miny) break;
-    if (fabs(prev - smaller) < tol) { *xout = smaller; return BR_OK; }  // FoundMin
-    if (iter > max_iters) return BR_STARTFAIL;
-    prev = (prev + smaller) / 2.;
-  }
-  double xl = left, xu = right, xm = prev;
-  double fl = lefty, fu = righty, fm = pv;
-  if (!isfinite(fl) || !isfinite(fu) || !isfinite(fm)) return BR_GSLERR;
-  if (xl > xu || xm >= xu || xm <= xl || fm >= fl || fm >= fu) return BR_GSLERR;
-  const double golden = 0.3819660;
-  double v = xl + golden * (xu - xl), w = v;
-  double fv = f(v);
-  if (!isfinite(fv)) return BR_GSLERR;
-  double fw = fv, d = 0, e = 0;
-  for (int step = 1;; step++) {
-    if (step > max_iters) return BR_MAXITER;
-    double z = xm, fz = fm;
-    double dd = e, ee = d;
-    double wl = z - xl, wu = xu - z;
-    double tolerance = 1.4901161193847656e-08 * fabs(z);
-    double p = 0, qq = 0, r = 0;
-    double mid = 0.5 * (xl + xu);
-    double u;
-    if (fabs(ee) > tolerance) {
-      r = (z - w) * (fz - fv);
-      qq = (z - v) * (fz - fw);
-      p = (z - v) * qq - (z - w) * r;
-      qq = 2 * (qq - r);
-      if (qq > 0) p = -p; else qq = -qq;
-      r = ee;
-      ee = dd;
-    }
-    if (fabs(p) < fabs(0.5 * qq * r) && p < qq * wl && p < qq * wu) {
-      double t2 = 2 * tolerance;
-      dd = p / qq;
-      u = z + dd;
-      if ((u - xl) < t2 || (xu - u) < t2) dd = (z < mid) ? tolerance : -tolerance;
-    } else {
-      ee = (z < mid) ? xu - z : -(z - xl);
-      dd = golden * ee;
-    }
-    if (fabs(dd) >= tolerance) u = z + dd;
-    else u = z + ((dd > 0) ? tolerance : -tolerance);
-    e = ee;
-    d = dd;
-    double fuv = f(u);
-    if (!isfinite(fuv)) return BR_GSLERR;
-    if (fuv <= fz) {
-      if (u < z) { xu = z; fu = fz; } else { xl = z; fl = fz; }
-      v = w; fv = fw; w = z; fw = fz;
-      xm = u; fm = fuv;
-    } else {
-      if (u < z) { xl = u; fl = fuv; } else { xu = u; fu = fuv; }
-      if (fuv <= fw || w == z) { v = w; fv = fw; w = u; fw = fuv; }
-      else if (fuv <= fv || v == z || v == w) { v = u; fv = fuv; }
-    }
-    if (xu - xl < tol) { *xout = xm; return BR_OK; }
-  }
-}
-
-// Three_tax.optimize (three_tax.ml:285-320; max_iter 200, core.ml:156)
-template <int K>
-__device__ int optimize_brent(Evaluator<K> &ev, double tol, double max_pend) {
-  double prev_pend = ev.pend, prev_dist = ev.dist;
-  for (int step = 1;; step++) {
-    if (step > 200) return BR_MAXITER;
-    double cp, cd;
-    auto fp = [&](double v) { ev.pend = v; return -ev.eval(false); };
-    if (1e-8 == max_pend) cp = ev.pend;
-    else { int st = brent_dev(fp, ev.pend, 1e-8, max_pend, tol, &cp); if (st != BR_OK) return st; }
-    double cut = ev.dist + ev.prox;
-    auto fd = [&](double v) {
-      double pb = (ev.dist + ev.prox) - v;
-      ev.dist = v;
-      ev.prox = pb;
-      return -ev.eval(false);
-    };
-    if (0.0 == cut) cd = ev.dist;
-    else { int st = brent_dev(fd, ev.dist, 0.0, cut, tol, &cd); if (st != BR_OK) return st; }
-    if (fabs(prev_pend - cp) > tol || fabs(prev_dist - cd) > tol) { prev_pend = cp; prev_dist = cd; }
-    else break;
-  }
-  return BR_OK;
-}
-
-// Safeguarded projected Newton on (pendant, distal) using the adjoint's
-// gradient and Hessian; box [1e-8, max_pend] x [0, cut].  The control state
-// is FP32: branch lengths need ~1e-9 resolution, and likelihoods are compared
-// through exact exponent differences (dlogl), so no FP64 arithmetic (64-cycle
-// latency on this part) sits on the optimiser's critical path.
-template <int K>
-__device__ int optimize_newton(Evaluator<K> &ev, double tol, double max_pend, double cut_d) {
-  const float pmin = 1e-8f, pmax = (float)max_pend, cut = (float)cut_d, dmax = cut;
-  const float tn = (float)(0.01 * tol);
-  float p = fminf(fmaxf((float)ev.pend, pmin), pmax);
-  float d = fminf(fmaxf((float)ev.dist, 0.f), dmax);
-  ev.eval_raw(p, d, cut - d, true);
-  EvalOut cur = ev.last;
-  if (!isfinite(cur.lm)) return BR_GSLERR;
-  // noise allowance for accepting a step: 1e-6 absolute + 1e-9 relative
-  const float allow = 1e-6f + 1e-9f * fabsf((float)cur.ex * 0.69314718f + (float)ev.cst);
-  int status = BR_OK;
-  for (int it = 0; it < 60; it++) {
-    float gp = cur.g[0], gd = cur.g[1], hpp = cur.h[0], hdd = cur.h[1], hpd = cur.h[2];
-    bool free_p = !((p <= pmin && gp <= 0.f) || (p >= pmax && gp >= 0.f));
-    bool free_d = (dmax > 0.f) && !((d <= 0.f && gd <= 0.f) || (d >= dmax && gd >= 0.f));
-    if (!free_p && !free_d) break;
-    float sp = 0.f, sd = 0.f;
-    float det = hpp * hdd - hpd * hpd;
-    if (free_p && free_d && hpp < 0.f && hdd < 0.f && det > 0.f) {
-      sp = -(hdd * gp - hpd * gd) / det;
-      sd = -(hpp * gd - hpd * gp) / det;
-    } else {
-      if (free_p) sp = hpp < 0.f ? -gp / hpp : copysignf(fmaxf(0.5f * p, 0.01f), gp);
-      if (free_d) sd = hdd < 0.f ? -gd / hdd : copysignf(0.25f * dmax, gd);
-    }
-    float lim_p = fmaxf(2.f * p, 0.05f), lim_d = fmaxf(0.5f * dmax, 1e-12f);
-    if (fabsf(sp) > lim_p) sp = copysignf(lim_p, sp);
-    if (fabsf(sd) > lim_d) sd = copysignf(lim_d, sd);
-    float pred = gp * sp + gd * sd;  // first-order predicted gain
-    bool accepted = false;
-    float np = p, nd = d;
-    for (int ls = 0; ls < 30; ls++) {
-      np = fminf(fmaxf(p + sp, pmin), pmax);
-      nd = fminf(fmaxf(d + sd, 0.f), dmax);
-      if (np == p && nd == d) break;
-      ev.eval_raw(np, nd, cut - nd, true);
-      if (isfinite(ev.last.lm) && dlogl(ev.last, cur) >= -allow) {
-        accepted = true;
-        break;
-      }
-      sp *= 0.25f;
-      sd *= 0.25f;
-    }
-    if (!accepted) break;
-    float step = fmaxf(fabsf(np - p), fabsf(nd - d));
-    p = np;
-    d = nd;
-    cur = ev.last;
-    if (step < tn || fabsf(pred) < 1e-3f * allow) break;
-    if (it == 59) status = BR_MAXITER;
-  }
-  ev.pend = p;
-  ev.dist = d;
-  ev.prox = (double)(cut - d);
-  ev.last = cur;
-  ev.L_last = ev.full(cur);
-  return status;
-}
-
-template <int K>
-__global__ void __launch_bounds__(kTrialThreads) k_trials(TrialCtx c, const TrialIn *__restrict__ trials,
-                                                          const int *__restrict__ order, int n, TrialRes *out) {
-  extern __shared__ __align__(16) char t_smem[];
-  int ti = order ? order[blockIdx.x] : blockIdx.x;
-  if (blockIdx.x >= n) return;
-  TrialIn tr = trials[ti];
-  const int tid = threadIdx.x;
-  TrialSmem sm = carve(t_smem, c.cap, c.smem_win, c.RP, K, c.NM, c.ncode);
-  const int q = tr.q, node = tr.node;
-  const int Sq = c.qlen[q];
-  // prologue: gather the query's informative sites of darr / parr[node]
-  long long esum = 0;
-  const long qo = (long)q * c.S;
-  for (int i = tid; i < Sq; i += kTrialThreads) {
-    int s = c.reind[qo + i];
-    sm.code[i] = c.mcode[qo + i];
-    if (c.gcat) sm.cat[i] = c.site_cat[s];
-    long go = ((long)node * c.S + s);
-    esum += (long long)c.dexp[go] + (long long)c.pexp[go];
-    if (c.smem_win) {
-      for (int r = 0; r < c.RP; r++) {
-        const float *ds = c.darr + (go * c.RP + r) * K;
-        const float *ps = c.parr + (go * c.RP + r) * K;
-        float *dd = sm.D + ((long)r * c.cap + i) * K;
-        float *pd = sm.P + ((long)r * c.cap + i) * K;
-        for (int k = 0; k < K; k += 4) {
-          *reinterpret_cast<float4 *>(dd + k) = *reinterpret_cast<const float4 *>(ds + k);
-          *reinterpret_cast<float4 *>(pd + k) = *reinterpret_cast<const float4 *>(ps + k);
-        }
-      }
-    }
-  }
-  esum = warp_sum_ll(esum);
-  if ((tid & 31) == 0) sm.red[(tid >> 5) * 8] = 0.f, sm.redi[tid >> 5] = 0;
-  __shared__ long long s_esum[kTrialWarps];
-  if ((tid & 31) == 0) s_esum[tid >> 5] = esum;
-  __syncthreads();
-  long long etot = 0;
-  for (int i = 0; i < kTrialWarps; i++) etot += s_esum[i];
-  const double exp_const = kLn2 * (double)etot;
-
-  if (tid >= 32) {
-    // worker warps: evaluate until warp 0 sends stop
-    EvalOut dummy;
-    for (int guard = 0; guard < (1 << 30); guard++) {
-      bar1();
-      int cmd = sm.ctrl->cmd;
-      if (cmd == 0) break;
-      eval_part<K>(c, sm, q, node, Sq, cmd == 2, &dummy);
-    }
-    return;
-  }
-  // warp 0: the optimiser
-  Evaluator<K> ev;
-  ev.c = &c; ev.sm = &sm; ev.q = q; ev.node = node; ev.Sq = Sq;
-  ev.cst = exp_const - (double)(float)Sq * c.log_nrates;
-  ev.n_evals = 0;
-  ev.L_last = NAN;
-  const double cut_bl = c.bl[node];
-  // set_tt_edges (core.ml:371-385)
-  ev.pend = tr.pend0;
-  ev.dist = tr.dist0;
-  ev.prox = cut_bl - tr.dist0;
-  int status = ST_OK;
-  if (c.mode == 1) {
-    ev.eval(true);
-  } else {
-    ev.last.g[0] = ev.last.g[1] = ev.last.h[0] = ev.last.h[1] = ev.last.h[2] = 0.f;
-    for (int attempt = 0; attempt < 2; attempt++) {
-      int st = c.optimizer == 0 ? optimize_brent<K>(ev, tr.tol, c.max_pend)
-                                : optimize_newton<K>(ev, tr.tol, c.max_pend, cut_bl);
-      if (st == BR_OK) { status = ST_OK; break; }
-      if (st == BR_MAXITER) { status = ST_MAXITER; break; }
-      if (st == BR_STARTFAIL) { status = ST_STARTFAIL; break; }
-      // GSL error: retry once from the default branch lengths (core.ml:418-425)
-      status = ST_FAILED;
-      ev.pend = c.start_pend;
-      ev.dist = cut_bl / 2.;
-      ev.prox = cut_bl - cut_bl / 2.;
-    }
-    if (ev.n_evals == 0) ev.eval(false);
-  }
-  ev.stop();
-  if (tid == 0) {
-    TrialRes r;
-    r.like = ev.L_last;
-    r.pend = ev.pend;
-    r.dist = ev.dist;
-    r.der[0] = ev.last.g[0]; r.der[1] = ev.last.g[1];
-    r.der[2] = ev.last.h[0]; r.der[3] = ev.last.h[1]; r.der[4] = ev.last.h[2];
-    r.der[5] = 0;
-    r.status = status;
-    r.n_evals = ev.n_evals;
-    out[ti] = r;
-    if (c.stats) {
-      atomicAdd(&c.stats[0], (unsigned long long)ev.n_evals);
-      atomicAdd(&c.stats[1], (unsigned long long)ev.n_evals * (unsigned long long)Sq);
-    }
-  }
-}
+#include "trials.cuh"
 
 // ---------------------------------------------------------------------------
 // Baseball (core.ml:429-464) and keep / refine / like_weight_ratio

@@ -1,0 +1,808 @@
+// Stage-2 trials: one CTA per (query, location) branch-length optimisation
+// (Three_tax.optimize, pplacer_src/three_tax.ml:285-320, with the retry from
+// default lengths of core.ml:418-425).  Included by engine.cu inside its
+// anonymous namespace.
+//
+// Structure of the kernel: the query's informative sites of darr / parr[node]
+// are gathered into shared memory once.  Warp 0 runs the optimiser as a state
+// machine (a coroutine: each resume consumes one objective value and yields
+// the next point); all warps then evaluate that point together.  One
+// evaluation is three block barriers:
+//   warp 0: decide next point, exp factors   | barrier A
+//   all:    P(t) and derivative matrices,    | barrier B
+//           evolved query vectors per character
+//   all:    sites -> warp partials           | barrier C
+//   warp 0: combine partials
+// Every loop is bounded and every path through warp 0 ends with the stop
+// command, so the barriers always complete.
+
+constexpr int kTrialThreads = 256;
+constexpr int kTrialWarps = kTrialThreads / 32;
+constexpr int kMaxTrialEvals = 200000;
+
+struct TrialIn {
+  int q, node;
+  double pend0, dist0, tol;
+};
+struct TrialRes {
+  double like, pend, dist;
+  double der[6];
+  int status, n_evals;
+};
+
+struct TrialCtx {
+  const float *darr, *parr;
+  const int *dexp, *pexp;
+  int S, RP, K, NM, ncode, gcat;
+  const double *bl;
+  const uint16_t *reind;
+  const uint8_t *mcode;
+  const int *qlen;
+  const uint8_t *site_cat;
+  const float *X, *W, *Lt, *lvf, *statd, *lam, *rates;
+  double log_nrates;
+  double start_pend, max_pend;
+  int optimizer, mode;
+  int smem_win, cap;
+  unsigned long long *stats;  // [0] objective evaluations, [1] site evaluations
+};
+
+struct Ctrl {
+  float pend, dist, prox;
+  int cmd;  // 0 stop, 1 value, 2 value + derivatives
+};
+
+// One evaluation: logL = ex * ln2 + lm + (trial constant); derivatives FP32.
+struct EvalOut {
+  int ex;
+  float lm;
+  float g[2], h[3];
+};
+
+// logL difference a - b without FP64 (exact exponent difference)
+__device__ __forceinline__ float dlogl(const EvalOut &a, const EvalOut &b) {
+  return (float)(a.ex - b.ex) * 0.69314718f + (a.lm - b.lm);
+}
+
+__host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
+
+// shared memory of one trial CTA
+struct TrialSmem {
+  float *D, *P;              // [RP][cap][K] windows (smem_win)
+  uint8_t *code, *cat;       // [cap]
+  float *Md, *Mp, *Md1, *Md2, *Mp1, *Mp2;  // [NM][K][K]
+  float *Z, *Z1, *Z2;        // [NM][ncode][K] statd-weighted evolved query vectors
+  float *E, *Em1, *Lr;       // exp / expm1 factors [3][NM][K]; rate * lambda [NM][K]
+  float *X, *W, *Lt, *lv, *statd;  // model constants (W only for K = 4)
+  float *red;                // [warps][8]
+  int *redi;                 // [warps]
+  Ctrl *ctrl;
+};
+
+__host__ __device__ inline size_t trial_smem_bytes(int cap, int win, int RP, int K, int NM, int ncode) {
+  size_t b = 0;
+  if (win) b += 2 * align16((size_t)RP * cap * K * 4);
+  b += 2 * align16((size_t)cap);
+  b += 6 * align16((size_t)NM * K * K * 4);
+  b += 3 * align16((size_t)NM * ncode * K * 4);
+  b += 2 * align16((size_t)3 * NM * K * 4) + align16((size_t)NM * K * 4);
+  b += align16((size_t)K * K * 4) + (K == 4 ? align16((size_t)K * K * K * 4) : 0) +
+       2 * align16((size_t)ncode * K * 4) + align16((size_t)K * 4);
+  b += align16(kTrialWarps * 8 * 4) + align16(kTrialWarps * 4);
+  b += align16(sizeof(Ctrl));
+  return b;
+}
+
+__device__ inline TrialSmem carve(char *base, int cap, int win, int RP, int K, int NM, int ncode) {
+  TrialSmem s;
+  char *p = base;
+  auto take = [&](size_t bytes) { char *r = p; p += align16(bytes); return r; };
+  s.D = win ? (float *)take((size_t)RP * cap * K * 4) : nullptr;
+  s.P = win ? (float *)take((size_t)RP * cap * K * 4) : nullptr;
+  s.code = (uint8_t *)take(cap);
+  s.cat = (uint8_t *)take(cap);
+  size_t mb = (size_t)NM * K * K * 4;
+  s.Md = (float *)take(mb); s.Mp = (float *)take(mb); s.Md1 = (float *)take(mb);
+  s.Md2 = (float *)take(mb); s.Mp1 = (float *)take(mb); s.Mp2 = (float *)take(mb);
+  size_t zb = (size_t)NM * ncode * K * 4;
+  s.Z = (float *)take(zb); s.Z1 = (float *)take(zb); s.Z2 = (float *)take(zb);
+  s.E = (float *)take((size_t)3 * NM * K * 4);
+  s.Em1 = (float *)take((size_t)3 * NM * K * 4);
+  s.Lr = (float *)take((size_t)NM * K * 4);
+  s.X = (float *)take((size_t)K * K * 4);
+  s.W = K == 4 ? (float *)take((size_t)K * K * K * 4) : nullptr;
+  s.Lt = (float *)take((size_t)ncode * K * 4);
+  s.lv = (float *)take((size_t)ncode * K * 4);
+  s.statd = (float *)take((size_t)K * 4);
+  s.red = (float *)take(kTrialWarps * 8 * 4);
+  s.redi = (int *)take(kTrialWarps * 4);
+  s.ctrl = (Ctrl *)take(sizeof(Ctrl));
+  return s;
+}
+
+// ---------------------------------------------------------------------------
+// Warp-0 optimiser state machines.  next(res) consumes the value of the last
+// requested point (res == nullptr on the first call) and either sets the next
+// request (req_*) and returns true, or finishes and returns false.
+// ---------------------------------------------------------------------------
+#define PGB_YIELD(label) \
+  do {                   \
+    pc = label;          \
+    return true;         \
+    case label:;         \
+  } while (0)
+
+struct Optimiser {
+  // inputs
+  int optimizer, mode;
+  double cut, tol, max_pend, start_pend, pend0, dist0, cst;
+  // outputs
+  int status, n_evals;
+  double pend, dist, prox;  // three-taxon state (three_tax.ml:252-258)
+  double L_last;
+  EvalOut last;
+  // request
+  float req_p, req_d, req_x;
+  bool req_derivs;
+  // coroutine
+  int pc;
+  int attempt;
+  // Brent replica state
+  int outer, which, iter, bstep, err;
+  double prev_pend, prev_dist, cres[2];
+  double raw, left, right, lefty, righty, smaller, miny, prevx, pv;
+  double xl, xu, xm, fl, fu, fm, v, w, fv, fw, bd, be, u, fz, z, probe_dx, fval, fx;
+  bool probe;
+  // Newton state
+  int it, ls;
+  float p, d, sp, sd, np, nd, allow, pred;
+  bool accepted;
+  EvalOut cur;
+
+  __device__ double full(const EvalOut &o) const { return (double)o.ex * kLn2 + (double)o.lm + cst; }
+
+  __device__ void request(double pp, double dd, double xx, bool derivs) {
+    req_p = (float)pp;
+    req_d = (float)dd;
+    req_x = (float)xx;
+    req_derivs = derivs;
+  }
+
+  // set_pend_bl / set_dist_bl (three_tax.ml:275-282)
+  __device__ void set_coord(int wh, double val) {
+    if (wh == 0) {
+      pend = val;
+    } else {
+      double pb = (dist + prox) - val;
+      dist = val;
+      prox = pb;
+    }
+  }
+
+  __device__ void record(const EvalOut *res) {
+    last = *res;
+    L_last = full(*res);
+    n_evals++;
+  }
+
+  __device__ bool next(const EvalOut *res) {
+    if (res) record(res);
+    switch (pc) {
+      case 0:
+        status = ST_OK;
+        attempt = 0;
+        pend = pend0;
+        dist = dist0;
+        prox = cut - dist0;  // set_tt_edges (core.ml:371-385)
+        if (mode == 1) {
+          request(pend, dist, prox, true);
+          PGB_YIELD(1);
+          return false;
+        }
+        if (optimizer == 1) goto NEWTON;
+        // ---------------- Brent replica (three_tax.ml:285-320) ----------------
+      BRENT_ATTEMPT:
+        prev_pend = pend;
+        prev_dist = dist;
+        for (outer = 1;; outer++) {
+          if (outer > 200) { status = ST_MAXITER; goto BRENT_DONE; }
+          for (which = 0; which < 2; which++) {
+            raw = which == 0 ? pend : dist;
+            left = which == 0 ? 1e-8 : 0.0;
+            right = which == 0 ? max_pend : dist + prox;
+            if (left == right) { cres[which] = raw; continue; }
+            // bisection_start_finder (minimization.ml:11-41)
+            if (left >= raw || raw >= right) { status = ST_STARTFAIL; goto BRENT_DONE; }
+            fx = right;
+            set_coord(which, fx);
+            request(pend, dist, prox, false);
+            PGB_YIELD(10);
+            righty = -L_last;
+            fx = left;
+            set_coord(which, fx);
+            request(pend, dist, prox, false);
+            PGB_YIELD(11);
+            lefty = -L_last;
+            smaller = lefty < righty ? left : right;
+            miny = lefty <= righty ? lefty : righty;  // Stdlib.min
+            prevx = raw;
+            for (iter = 1;; iter++) {
+              set_coord(which, prevx);
+              request(pend, dist, prox, false);
+              PGB_YIELD(12);
+              pv = -L_last;
+              if (pv < miny) break;
+              if (fabs(prevx - smaller) < tol) { cres[which] = smaller; goto SEARCH_DONE; }  // FoundMin
+              if (iter > 100) { status = ST_STARTFAIL; goto BRENT_DONE; }
+              prevx = (prevx + smaller) / 2.;
+            }
+            // gsl_min_fminimizer_set (values of the finder's evaluations)
+            xl = left; xu = right; xm = prevx;
+            fl = lefty; fu = righty; fm = pv;
+            if (!isfinite(fl) || !isfinite(fu) || !isfinite(fm)) { err = 1; goto BRENT_ERR; }
+            if (xl > xu || xm >= xu || xm <= xl || fm >= fl || fm >= fu) { err = 1; goto BRENT_ERR; }
+            v = xl + 0.3819660 * (xu - xl);
+            w = v;
+            set_coord(which, v);
+            request(pend, dist, prox, false);
+            PGB_YIELD(13);
+            fv = -L_last;
+            if (!isfinite(fv)) { err = 1; goto BRENT_ERR; }
+            fw = fv;
+            bd = 0;
+            be = 0;
+            for (bstep = 1;; bstep++) {
+              if (bstep > 100) { status = ST_MAXITER; goto BRENT_DONE; }
+              {
+                // one GSL Brent iteration (parabolic step, else golden section)
+                z = xm;
+                fz = fm;
+                double dd = be, ee = bd;
+                double wl = z - xl, wu = xu - z;
+                double tolerance = 1.4901161193847656e-08 * fabs(z);
+                double pp = 0, qq = 0, r = 0;
+                double mid = 0.5 * (xl + xu);
+                if (fabs(ee) > tolerance) {
+                  r = (z - w) * (fz - fv);
+                  qq = (z - v) * (fz - fw);
+                  pp = (z - v) * qq - (z - w) * r;
+                  qq = 2 * (qq - r);
+                  if (qq > 0) pp = -pp; else qq = -qq;
+                  r = ee;
+                  ee = dd;
+                }
+                if (fabs(pp) < fabs(0.5 * qq * r) && pp < qq * wl && pp < qq * wu) {
+                  double t2 = 2 * tolerance;
+                  dd = pp / qq;
+                  u = z + dd;
+                  if ((u - xl) < t2 || (xu - u) < t2) dd = (z < mid) ? tolerance : -tolerance;
+                } else {
+                  ee = (z < mid) ? xu - z : -(z - xl);
+                  dd = 0.3819660 * ee;
+                }
+                if (fabs(dd) >= tolerance) u = z + dd;
+                else u = z + ((dd > 0) ? tolerance : -tolerance);
+                be = ee;
+                bd = dd;
+              }
+              // A probe closer to z than the FP32 objective resolves is
+              // decided by the adjoint's first-order model instead of by
+              // two values equal to rounding.
+              probe_dx = u - z;
+              probe = fabs(probe_dx) < 1e-6;
+              set_coord(which, u);
+              request(pend, dist, prox, probe);
+              PGB_YIELD(14);
+              fval = probe ? fz - (double)last.g[which] * probe_dx : -L_last;
+              if (!isfinite(fval)) { err = 1; goto BRENT_ERR; }
+              if (fval <= fz) {
+                if (u < z) { xu = z; fu = fz; } else { xl = z; fl = fz; }
+                v = w; fv = fw; w = z; fw = fz;
+                xm = u; fm = fval;
+              } else {
+                if (u < z) { xl = u; fl = fval; } else { xu = u; fu = fval; }
+                if (fval <= fw || w == z) { v = w; fv = fw; w = u; fw = fval; }
+                else if (fval <= fv || v == z || v == w) { v = u; fv = fval; }
+              }
+              if (xu - xl < tol) { cres[which] = xm; break; }
+            }
+          SEARCH_DONE:;
+          }
+          if (fabs(prev_pend - cres[0]) > tol || fabs(prev_dist - cres[1]) > tol) {
+            prev_pend = cres[0];
+            prev_dist = cres[1];
+          } else {
+            break;
+          }
+        }
+        goto BRENT_DONE;
+      BRENT_ERR:
+        if (attempt == 0) {  // retry from the default branch lengths (core.ml:418-425)
+          attempt = 1;
+          pend = start_pend;
+          dist = cut / 2.;
+          prox = cut - cut / 2.;
+          goto BRENT_ATTEMPT;
+        }
+        status = ST_FAILED;
+      BRENT_DONE:
+        if (n_evals == 0) {
+          request(pend, dist, prox, false);
+          PGB_YIELD(15);
+        }
+        return false;
+        // ---------------- safeguarded projected Newton ----------------
+      NEWTON:
+        p = fminf(fmaxf((float)pend, 1e-8f), (float)max_pend);
+        d = fminf(fmaxf((float)dist, 0.f), (float)cut);
+        request(p, d, (float)cut - d, true);
+        PGB_YIELD(20);
+        cur = last;
+        if (!isfinite(cur.lm)) {
+          if (attempt == 0) {
+            attempt = 1;
+            pend = start_pend;
+            dist = cut / 2.;
+            goto NEWTON;
+          }
+          status = ST_FAILED;
+          pend = p; dist = d; prox = (double)((float)cut - d);
+          return false;
+        }
+        allow = 1e-6f + 1e-9f * fabsf((float)L_last);
+        for (it = 0; it < 60; it++) {
+          {
+            const float pmin = 1e-8f, pmax = (float)max_pend, dmax = (float)cut;
+            float gp = cur.g[0], gd = cur.g[1], hpp = cur.h[0], hdd = cur.h[1], hpd = cur.h[2];
+            bool free_p = !((p <= pmin && gp <= 0.f) || (p >= pmax && gp >= 0.f));
+            bool free_d = (dmax > 0.f) && !((d <= 0.f && gd <= 0.f) || (d >= dmax && gd >= 0.f));
+            if (!free_p && !free_d) break;
+            sp = 0.f;
+            sd = 0.f;
+            float det = hpp * hdd - hpd * hpd;
+            if (free_p && free_d && hpp < 0.f && hdd < 0.f && det > 0.f) {
+              sp = -(hdd * gp - hpd * gd) / det;
+              sd = -(hpp * gd - hpd * gp) / det;
+            } else {
+              if (free_p) sp = hpp < 0.f ? -gp / hpp : copysignf(fmaxf(0.5f * p, 0.01f), gp);
+              if (free_d) sd = hdd < 0.f ? -gd / hdd : copysignf(0.25f * dmax, gd);
+            }
+            float lim_p = fmaxf(2.f * p, 0.05f), lim_d = fmaxf(0.5f * dmax, 1e-12f);
+            if (fabsf(sp) > lim_p) sp = copysignf(lim_p, sp);
+            if (fabsf(sd) > lim_d) sd = copysignf(lim_d, sd);
+            pred = gp * sp + gd * sd;
+          }
+          accepted = false;
+          for (ls = 0; ls < 30; ls++) {
+            np = fminf(fmaxf(p + sp, 1e-8f), (float)max_pend);
+            nd = fminf(fmaxf(d + sd, 0.f), (float)cut);
+            if (np == p && nd == d) break;
+            request(np, nd, (float)cut - nd, true);
+            PGB_YIELD(21);
+            if (isfinite(last.lm) && dlogl(last, cur) >= -allow) {
+              accepted = true;
+              break;
+            }
+            sp *= 0.25f;
+            sd *= 0.25f;
+          }
+          if (!accepted) break;
+          {
+            float step = fmaxf(fabsf(np - p), fabsf(nd - d));
+            p = np;
+            d = nd;
+            cur = last;
+            if (step < (float)(0.01 * tol) || fabsf(pred) < 1e-3f * allow) break;
+          }
+          if (it == 59) status = ST_MAXITER;
+        }
+        pend = p;
+        dist = d;
+        prox = (double)((float)cut - d);
+        last = cur;
+        L_last = full(cur);
+        return false;
+      default:
+        return false;
+    }
+  }
+};
+#undef PGB_YIELD
+
+// ---------------------------------------------------------------------------
+// The kernel
+// ---------------------------------------------------------------------------
+
+// per-site likelihood and its derivatives -> running (mantissa, exponent)
+// product and derivative sums of the thread
+struct SiteAcc {
+  float m;
+  int e;
+  float gp, gd, hpp, hdd, hpd;
+  __device__ void init() { m = 1.f; e = 0; gp = gd = hpp = hdd = hpd = 0.f; }
+  __device__ void add(float u, float ud, float udd, float up, float upp, float upd, bool derivs) {
+    int eu;
+    float mu = frexpf(u, &eu);
+    m *= mu;
+    e += eu;
+    int em;
+    m = frexpf(m, &em);
+    e += em;
+    if (derivs) {
+      float inv = 1.f / u;
+      float lp = up * inv, ld = ud * inv;
+      gp += lp;
+      gd += ld;
+      hpp += upp * inv - lp * lp;
+      hdd += udd * inv - ld * ld;
+      hpd += upd * inv - lp * ld;
+    }
+  }
+};
+
+// Sites of the DNA Gamma-mixture model: rates outer, the rate's transition
+// matrices held in registers, the thread's sites inner.
+template <bool DER>
+__device__ __forceinline__ void sites_dna_gmix(const TrialCtx &c, const TrialSmem &sm, int q, int node, int Sq,
+                                               SiteAcc &acc) {
+  constexpr int K = 4;
+  const int tid = threadIdx.x, nc = c.ncode;
+  const float *gdb = c.darr + (long)node * c.S * c.RP * K;
+  const float *gpb = c.parr + (long)node * c.S * c.RP * K;
+  for (int base = 0; base < Sq; base += 4 * kTrialThreads) {
+    float a0[4], ad[4], add[4], ap[4], app[4], apd[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) a0[j] = ad[j] = add[j] = ap[j] = app[j] = apd[j] = 0.f;
+    for (int r = 0; r < c.RP; r++) {
+      float md[16], mp[16], md1[DER ? 16 : 1], md2[DER ? 16 : 1], mp1[DER ? 16 : 1], mp2[DER ? 16 : 1];
+#pragma unroll
+      for (int t = 0; t < 16; t += 4) {
+        float4 a = *reinterpret_cast<const float4 *>(sm.Md + r * 16 + t);
+        float4 b = *reinterpret_cast<const float4 *>(sm.Mp + r * 16 + t);
+        md[t] = a.x; md[t + 1] = a.y; md[t + 2] = a.z; md[t + 3] = a.w;
+        mp[t] = b.x; mp[t + 1] = b.y; mp[t + 2] = b.z; mp[t + 3] = b.w;
+        if (DER) {
+          float4 c1 = *reinterpret_cast<const float4 *>(sm.Md1 + r * 16 + t);
+          float4 c2 = *reinterpret_cast<const float4 *>(sm.Md2 + r * 16 + t);
+          float4 e1 = *reinterpret_cast<const float4 *>(sm.Mp1 + r * 16 + t);
+          float4 e2 = *reinterpret_cast<const float4 *>(sm.Mp2 + r * 16 + t);
+          md1[t] = c1.x; md1[t + 1] = c1.y; md1[t + 2] = c1.z; md1[t + 3] = c1.w;
+          md2[t] = c2.x; md2[t + 1] = c2.y; md2[t + 2] = c2.z; md2[t + 3] = c2.w;
+          mp1[t] = e1.x; mp1[t + 1] = e1.y; mp1[t + 2] = e1.z; mp1[t + 3] = e1.w;
+          mp2[t] = e2.x; mp2[t + 1] = e2.y; mp2[t + 2] = e2.z; mp2[t + 3] = e2.w;
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        int i = base + tid + j * kTrialThreads;
+        if (i < Sq) {
+          int code = sm.code[i];
+          float4 D4, P4;
+          if (c.smem_win) {
+            D4 = *reinterpret_cast<const float4 *>(sm.D + ((long)r * c.cap + i) * K);
+            P4 = *reinterpret_cast<const float4 *>(sm.P + ((long)r * c.cap + i) * K);
+          } else {
+            long s = c.reind[(long)q * c.S + i];
+            D4 = __ldg(reinterpret_cast<const float4 *>(gdb + (s * c.RP + r) * K));
+            P4 = __ldg(reinterpret_cast<const float4 *>(gpb + (s * c.RP + r) * K));
+          }
+          const float dv[4] = {D4.x, D4.y, D4.z, D4.w}, pv[4] = {P4.x, P4.y, P4.z, P4.w};
+          float4 Z4 = *reinterpret_cast<const float4 *>(sm.Z + (r * nc + code) * K);
+          const float z[4] = {Z4.x, Z4.y, Z4.z, Z4.w};
+          float z1[4], z2[4];
+          if (DER) {
+            float4 a = *reinterpret_cast<const float4 *>(sm.Z1 + (r * nc + code) * K);
+            float4 b = *reinterpret_cast<const float4 *>(sm.Z2 + (r * nc + code) * K);
+            z1[0] = a.x; z1[1] = a.y; z1[2] = a.z; z1[3] = a.w;
+            z2[0] = b.x; z2[1] = b.y; z2[2] = b.z; z2[3] = b.w;
+          }
+#pragma unroll
+          for (int ii = 0; ii < 4; ii++) {
+            float x = 0.f, y = 0.f;
+#pragma unroll
+            for (int jj = 0; jj < 4; jj++) {
+              x = fmaf(md[ii * 4 + jj], dv[jj], x);
+              y = fmaf(mp[ii * 4 + jj], pv[jj], y);
+            }
+            float xy = x * y;
+            a0[j] = fmaf(z[ii], xy, a0[j]);
+            if (DER) {
+              float x1 = 0.f, x2 = 0.f, y1 = 0.f, y2 = 0.f;
+#pragma unroll
+              for (int jj = 0; jj < 4; jj++) {
+                x1 = fmaf(md1[ii * 4 + jj], dv[jj], x1);
+                x2 = fmaf(md2[ii * 4 + jj], dv[jj], x2);
+                y1 = fmaf(mp1[ii * 4 + jj], pv[jj], y1);
+                y2 = fmaf(mp2[ii * 4 + jj], pv[jj], y2);
+              }
+              float aa = x1 * y - x * y1;
+              float bb = x2 * y - 2.f * x1 * y1 + x * y2;
+              ad[j] = fmaf(z[ii], aa, ad[j]);
+              add[j] = fmaf(z[ii], bb, add[j]);
+              ap[j] = fmaf(z1[ii], xy, ap[j]);
+              app[j] = fmaf(z2[ii], xy, app[j]);
+              apd[j] = fmaf(z1[ii], aa, apd[j]);
+            }
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < 4; j++)
+      if (base + tid + j * kTrialThreads < Sq) acc.add(a0[j], ad[j], add[j], ap[j], app[j], apd[j], DER);
+  }
+}
+
+// Generic sites: any K, Gamma mixture or per-site CAT category matrices read
+// from shared memory.
+template <int K, bool DER>
+__device__ __forceinline__ void sites_generic(const TrialCtx &c, const TrialSmem &sm, int q, int node, int Sq,
+                                              SiteAcc &acc) {
+  const int tid = threadIdx.x, nc = c.ncode;
+  const float *gdb = c.darr + (long)node * c.S * c.RP * K;
+  const float *gpb = c.parr + (long)node * c.S * c.RP * K;
+  for (int i = tid; i < Sq; i += kTrialThreads) {
+    int code = sm.code[i];
+    float u = 0.f, ud = 0.f, udd = 0.f, up = 0.f, upp = 0.f, upd = 0.f;
+    long s = c.smem_win ? 0 : (long)c.reind[(long)q * c.S + i];
+    for (int r = 0; r < c.RP; r++) {
+      int m = c.gcat ? sm.cat[i] : r;
+      float dv[K], pv[K];
+      const float *ds = c.smem_win ? sm.D + ((long)r * c.cap + i) * K : gdb + (s * c.RP + r) * K;
+      const float *ps = c.smem_win ? sm.P + ((long)r * c.cap + i) * K : gpb + (s * c.RP + r) * K;
+#pragma unroll
+      for (int k = 0; k < K; k += 4) {
+        float4 a = *reinterpret_cast<const float4 *>(ds + k);
+        float4 b = *reinterpret_cast<const float4 *>(ps + k);
+        dv[k] = a.x; dv[k + 1] = a.y; dv[k + 2] = a.z; dv[k + 3] = a.w;
+        pv[k] = b.x; pv[k + 1] = b.y; pv[k + 2] = b.z; pv[k + 3] = b.w;
+      }
+      const float *Md = sm.Md + m * K * K, *Mp = sm.Mp + m * K * K;
+      const float *z = sm.Z + (m * nc + code) * K;
+#pragma unroll(K <= 4 ? K : 1)
+      for (int ii = 0; ii < K; ii++) {
+        float x = 0.f, y = 0.f;
+#pragma unroll
+        for (int jj = 0; jj < K; jj++) {
+          x = fmaf(Md[ii * K + jj], dv[jj], x);
+          y = fmaf(Mp[ii * K + jj], pv[jj], y);
+        }
+        float xy = x * y;
+        u = fmaf(z[ii], xy, u);
+        if (DER) {
+          const float *Md1 = sm.Md1 + m * K * K, *Md2 = sm.Md2 + m * K * K;
+          const float *Mp1 = sm.Mp1 + m * K * K, *Mp2 = sm.Mp2 + m * K * K;
+          float x1 = 0.f, x2 = 0.f, y1 = 0.f, y2 = 0.f;
+#pragma unroll
+          for (int jj = 0; jj < K; jj++) {
+            x1 = fmaf(Md1[ii * K + jj], dv[jj], x1);
+            x2 = fmaf(Md2[ii * K + jj], dv[jj], x2);
+            y1 = fmaf(Mp1[ii * K + jj], pv[jj], y1);
+            y2 = fmaf(Mp2[ii * K + jj], pv[jj], y2);
+          }
+          float z1 = sm.Z1[(m * nc + code) * K + ii], z2 = sm.Z2[(m * nc + code) * K + ii];
+          float aa = x1 * y - x * y1;
+          float bb = x2 * y - 2.f * x1 * y1 + x * y2;
+          ud = fmaf(z[ii], aa, ud);
+          udd = fmaf(z[ii], bb, udd);
+          up = fmaf(z1, xy, up);
+          upp = fmaf(z2, xy, upp);
+          upd = fmaf(z1, aa, upd);
+        }
+      }
+    }
+    acc.add(u, ud, udd, up, upp, upd, DER);
+  }
+}
+
+template <int K>
+__global__ void __launch_bounds__(kTrialThreads, 1) k_trials(TrialCtx c, const TrialIn *__restrict__ trials,
+                                                             const int *__restrict__ order, int n, TrialRes *out) {
+  extern __shared__ __align__(16) char t_smem[];
+  if (blockIdx.x >= n) return;
+  const int ti = order ? order[blockIdx.x] : blockIdx.x;
+  const TrialIn tr = trials[ti];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const TrialSmem sm = carve(t_smem, c.cap, c.smem_win, c.RP, K, c.NM, c.ncode);
+  const int q = tr.q, node = tr.node;
+  const int Sq = c.qlen[q];
+  const int NM = c.NM, nc = c.ncode;
+  // ---- prologue: model constants and the query's sites of darr / parr ----
+  for (int i = tid; i < K * K; i += kTrialThreads) sm.X[i] = c.X[i];
+  if (K == 4)
+    for (int i = tid; i < K * K * K; i += kTrialThreads) sm.W[i] = c.W[i];
+  for (int i = tid; i < nc * K; i += kTrialThreads) { sm.Lt[i] = c.Lt[i]; sm.lv[i] = c.lvf[i]; }
+  for (int i = tid; i < NM * K; i += kTrialThreads) sm.Lr[i] = c.rates[i / K] * c.lam[i % K];
+  if (tid < K) sm.statd[tid] = c.statd[tid];
+  long long esum = 0;
+  const long qo = (long)q * c.S;
+  for (int i = tid; i < Sq; i += kTrialThreads) {
+    int s = c.reind[qo + i];
+    sm.code[i] = c.mcode[qo + i];
+    if (c.gcat) sm.cat[i] = c.site_cat[s];
+    long go = ((long)node * c.S + s);
+    esum += (long long)c.dexp[go] + (long long)c.pexp[go];
+    if (c.smem_win) {
+      for (int r = 0; r < c.RP; r++) {
+        const float *ds = c.darr + (go * c.RP + r) * K;
+        const float *ps = c.parr + (go * c.RP + r) * K;
+        float *dd = sm.D + ((long)r * c.cap + i) * K;
+        float *pd = sm.P + ((long)r * c.cap + i) * K;
+#pragma unroll
+        for (int k = 0; k < K; k += 4) {
+          *reinterpret_cast<float4 *>(dd + k) = __ldg(reinterpret_cast<const float4 *>(ds + k));
+          *reinterpret_cast<float4 *>(pd + k) = __ldg(reinterpret_cast<const float4 *>(ps + k));
+        }
+      }
+    }
+  }
+  esum = warp_sum_ll(esum);
+  __shared__ long long s_esum[kTrialWarps];
+  if (lane == 0) s_esum[warp] = esum;
+  __syncthreads();
+  long long etot = 0;
+  for (int i = 0; i < kTrialWarps; i++) etot += s_esum[i];
+
+  Optimiser opt;
+  if (warp == 0) {
+    opt.optimizer = c.optimizer;
+    opt.mode = c.mode;
+    opt.cut = c.bl[node];
+    opt.tol = tr.tol;
+    opt.max_pend = c.max_pend;
+    opt.start_pend = c.start_pend;
+    opt.pend0 = tr.pend0;
+    opt.dist0 = tr.dist0;
+    opt.cst = kLn2 * (double)etot - (double)(float)Sq * c.log_nrates;
+    opt.n_evals = 0;
+    opt.pc = 0;
+    opt.L_last = NAN;
+    opt.last.ex = 0; opt.last.lm = 0.f;
+    opt.last.g[0] = opt.last.g[1] = opt.last.h[0] = opt.last.h[1] = opt.last.h[2] = 0.f;
+  }
+  EvalOut res;
+  for (int ev = 0; ev < kMaxTrialEvals; ev++) {
+    // ---- warp 0: next point, exp factors ----
+    if (warp == 0) {
+      bool more = opt.next(ev == 0 ? nullptr : &res);
+      if (lane == 0) {
+        sm.ctrl->cmd = more ? (opt.req_derivs ? 2 : 1) : 0;
+        sm.ctrl->pend = opt.req_p;
+        sm.ctrl->dist = opt.req_d;
+        sm.ctrl->prox = opt.req_x;
+      }
+      if (more) {
+        for (int i = lane; i < 3 * NM * K; i += 32) {
+          int wh = i / (NM * K), mk = i - wh * NM * K;
+          float t = wh == 0 ? opt.req_d : (wh == 1 ? opt.req_x : opt.req_p);
+          float a = sm.Lr[mk] * t;
+          sm.E[i] = expf(a);
+          sm.Em1[i] = expm1f(a);
+        }
+      }
+    }
+    __syncthreads();  // A
+    const Ctrl ctl = *sm.ctrl;
+    if (ctl.cmd == 0) break;
+    const bool derivs = ctl.cmd == 2;
+    // ---- P(t) = I + X diag(expm1(r lambda t)) X^-T and derivatives; query vectors ----
+    const float *W = K == 4 ? sm.W : c.W;
+    const int nmat = NM * K * K;
+    for (int i = tid; i < 2 * nmat; i += kTrialThreads) {
+      int wh = i / nmat, r = i - wh * nmat;
+      int m = r / (K * K), ij = r - m * K * K;
+      int ii = ij / K, jj = ij - ii * K;
+      const float *w = W + (long)ij * K;
+      const float *em = sm.Em1 + (wh * NM + m) * K;
+      float a = (ii == jj) ? 1.f : 0.f;
+#pragma unroll 4
+      for (int k = 0; k < K; k++) a = fmaf(w[k], em[k], a);
+      (wh == 0 ? sm.Md : sm.Mp)[r] = a;
+      if (derivs) {
+        const float *e = sm.E + (wh * NM + m) * K;
+        const float *lr = sm.Lr + m * K;
+        float a1 = 0.f, a2 = 0.f;
+#pragma unroll 4
+        for (int k = 0; k < K; k++) {
+          float t1 = w[k] * lr[k] * e[k];
+          a1 += t1;
+          a2 = fmaf(t1, lr[k], a2);
+        }
+        (wh == 0 ? sm.Md1 : sm.Mp1)[r] = a1;
+        (wh == 0 ? sm.Md2 : sm.Mp2)[r] = a2;
+      }
+    }
+    const int nz = NM * nc * K;
+    for (int i = tid; i < nz; i += kTrialThreads) {
+      int m = i / (nc * K), ck = i - m * nc * K;
+      int code = ck / K, ii = ck - code * K;
+      const float *x = sm.X + ii * K;
+      const float *lt = sm.Lt + code * K;
+      const float *em = sm.Em1 + (2 * NM + m) * K;
+      float a = sm.lv[code * K + ii];
+#pragma unroll 4
+      for (int k = 0; k < K; k++) a = fmaf(x[k] * em[k], lt[k], a);
+      float pi = sm.statd[ii];
+      sm.Z[i] = pi * a;
+      if (derivs) {
+        const float *e = sm.E + (2 * NM + m) * K;
+        const float *lr = sm.Lr + m * K;
+        float a1 = 0.f, a2 = 0.f;
+#pragma unroll 4
+        for (int k = 0; k < K; k++) {
+          float t1 = x[k] * lr[k] * e[k] * lt[k];
+          a1 += t1;
+          a2 = fmaf(t1, lr[k], a2);
+        }
+        sm.Z1[i] = pi * a1;
+        sm.Z2[i] = pi * a2;
+      }
+    }
+    __syncthreads();  // B
+    // ---- sites ----
+    SiteAcc acc;
+    acc.init();
+    if (K == 4 && !c.gcat) {
+      if (derivs) sites_dna_gmix<true>(c, sm, q, node, Sq, acc);
+      else sites_dna_gmix<false>(c, sm, q, node, Sq, acc);
+    } else {
+      if (derivs) sites_generic<K, true>(c, sm, q, node, Sq, acc);
+      else sites_generic<K, false>(c, sm, q, node, Sq, acc);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      float mo = __shfl_down_sync(0xffffffffu, acc.m, o);
+      int eo = __shfl_down_sync(0xffffffffu, acc.e, o);
+      acc.m *= mo;
+      acc.e += eo;
+      int em;
+      acc.m = frexpf(acc.m, &em);
+      acc.e += em;
+    }
+    if (derivs) {
+      acc.gp = warp_sum_f(acc.gp); acc.gd = warp_sum_f(acc.gd);
+      acc.hpp = warp_sum_f(acc.hpp); acc.hdd = warp_sum_f(acc.hdd); acc.hpd = warp_sum_f(acc.hpd);
+    }
+    if (lane == 0) {
+      sm.red[warp * 8 + 0] = acc.m;
+      sm.redi[warp] = acc.e;
+      sm.red[warp * 8 + 1] = acc.gp; sm.red[warp * 8 + 2] = acc.gd;
+      sm.red[warp * 8 + 3] = acc.hpp; sm.red[warp * 8 + 4] = acc.hdd; sm.red[warp * 8 + 5] = acc.hpd;
+    }
+    __syncthreads();  // C
+    if (warp == 0) {
+      float mt = 1.f;
+      int et = 0;
+      float sg[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+      for (int i = 0; i < kTrialWarps; i++) {
+        mt *= sm.red[i * 8];
+        et += sm.redi[i];
+        int em;
+        mt = frexpf(mt, &em);
+        et += em;
+#pragma unroll
+        for (int k = 0; k < 5; k++) sg[k] += sm.red[i * 8 + 1 + k];
+      }
+      res.ex = et;
+      res.lm = logf(mt);
+      res.g[0] = sg[0]; res.g[1] = sg[1];
+      res.h[0] = sg[2]; res.h[1] = sg[3]; res.h[2] = sg[4];
+    }
+  }
+  if (tid == 0) {
+    TrialRes r;
+    r.like = opt.L_last;
+    r.pend = opt.pend;
+    r.dist = opt.dist;
+    r.der[0] = opt.last.g[0]; r.der[1] = opt.last.g[1];
+    r.der[2] = opt.last.h[0]; r.der[3] = opt.last.h[1]; r.der[4] = opt.last.h[2];
+    r.der[5] = 0;
+    r.status = opt.status;
+    r.n_evals = opt.n_evals;
+    out[ti] = r;
+    if (c.stats) {
+      atomicAdd(&c.stats[0], (unsigned long long)opt.n_evals);
+      atomicAdd(&c.stats[1], (unsigned long long)opt.n_evals * (unsigned long long)Sq);
+    }
+  }
+}
