@@ -17,6 +17,9 @@
 #include <cstring>
 #include <vector>
 
+#include <cublas_v2.h>
+#include <cuda_bf16.h>
+
 #include "pgb_common.cuh"
 
 namespace pgb {
@@ -247,15 +250,16 @@ __global__ void k_snodes_from(const double *__restrict__ d, const double *__rest
 // Query preparation: character codes, informative mask, masked site lists
 // (core.ml:267-304).  One CTA per query.
 // ---------------------------------------------------------------------------
-__global__ void k_query_prep(const char *__restrict__ seqs, int S, const uint8_t *__restrict__ char_code,
+__global__ void k_query_prep(const char *__restrict__ seqs, int S, int prim, const uint8_t *__restrict__ char_code,
                              const uint8_t *__restrict__ informative, uint8_t *qcode, uint16_t *reind,
-                             uint8_t *mcode, int *qlen, int *qstatus) {
+                             uint8_t *mcode, int *qlen, int *qstatus, int *qamb) {
   int q = blockIdx.x;
   const char *seq = seqs + (long)q * S;
   __shared__ int s_off;
   __shared__ int s_bad;
+  __shared__ int s_amb;
   __shared__ int s_warp[32];
-  if (threadIdx.x == 0) { s_off = 0; s_bad = 0; }
+  if (threadIdx.x == 0) { s_off = 0; s_bad = 0; s_amb = 0; }
   __syncthreads();
   int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
   for (int base = 0; base < S; base += blockDim.x) {
@@ -266,6 +270,7 @@ __global__ void k_query_prep(const char *__restrict__ seqs, int S, const uint8_t
       c = char_code[(uint8_t)seq[s]];
       if (c == kBadCode) atomicOr(&s_bad, 1);
       else inf = informative[c];
+      if (inf && c >= prim) atomicAdd(&s_amb, 1);
       qcode[(long)q * S + s] = c;
     }
     unsigned bal = __ballot_sync(0xffffffffu, inf);
@@ -287,27 +292,32 @@ __global__ void k_query_prep(const char *__restrict__ seqs, int S, const uint8_t
   }
   if (threadIdx.x == 0) {
     qlen[q] = s_off;
+    qamb[q] = s_amb;
     qstatus[q] = s_bad ? PGB_Q_BAD_CHAR : (s_off == 0 ? PGB_Q_NO_INFORMATIVE : PGB_Q_OK);
   }
 }
 
 // ---------------------------------------------------------------------------
 // Stage 1 (core.ml:333-343, Glv.masked_logdot against every supernode).
-// The query side is the full query evolved by start_pend; its value at a
-// site depends only on the site's character, so log(sum_r sum_k qe_c * snode)
-// is tabulated per (edge, primary character, site) once per start_pend and the
-// per-(query, edge) score becomes a gather-sum over the query's informative
-// sites.  Characters outside the primary set are computed from the supernode.
+// The query side is the full query evolved by start_pend, so its value at a
+// site depends only on the site's character.  With
+//   T[e][c][s] = log(sum_r sum_k qe_c[r][k] snode_e[s][r][k])
+// the score of (query q, edge e) is sum over q's informative sites of
+// T[e][code(q, s)][s]: a dense product of the one-hot query matrix
+// A[q][c*Sp + s] with T, done as a bf16 tensor-core GEMM with FP32
+// accumulation on T split into three bf16 terms (hi + mid + lo carry 24
+// mantissa bits).  The exact integer exponent sums come from two more GEMMs
+// of the informative-site mask with the supernode exponents split into
+// base-256 digits (exact in bf16, exact FP32 sums).  Sites with ambiguity
+// characters (outside the one-hot primary set) are added by k_s1_ambig.
 // ---------------------------------------------------------------------------
 struct S1Ctx {
-  int S, RP, K, NM, gcat, ncode, prim, n_edges;
+  int S, Sp, RP, K, NM, gcat, ncode, prim, n_edges;
   const float *snode;        // [n_nodes][S][RP][K]
   const int *sexp;           // [n_nodes][S]
   const int *edge_nodes;     // [n_edges]
   const float *qe;           // [NM][ncode][K] evolved query LV per character
   const uint8_t *site_cat;
-  float *lt;                 // [n_edges][prim][S]
-  double log_nrates;         // log((float)R) (Gmix), 0 (Gcat)
 };
 
 __device__ __forceinline__ float s1_util(const S1Ctx &c, int node, int s, int code) {
@@ -316,81 +326,132 @@ __device__ __forceinline__ float s1_util(const S1Ctx &c, int node, int s, int co
   for (int r = 0; r < c.RP; r++) {
     int m = c.gcat ? c.site_cat[s] : r;
     const float *q = c.qe + ((long)m * c.ncode + code) * c.K;
-    for (int k = 0; k < c.K; k++) u += q[k] * sn[r * c.K + k];
+    for (int k = 0; k < c.K; k++) u = fmaf(q[k], sn[r * c.K + k], u);
   }
   return u;
 }
 
-__global__ void k_lt_build(S1Ctx c) {
-  long n = (long)c.n_edges * c.S;
+// Edge-side tables, once per start_pend: B3 = hi/mid/lo bf16 of T,
+// [3][n_edges][prim * Sp]; BX = base-256 digits of the exponents, [2][n_edges][Sp].
+__global__ void k_s1_tables(S1Ctx c, __nv_bfloat16 *B3, __nv_bfloat16 *BX) {
+  long n = (long)c.n_edges * c.Sp;
+  long K4 = (long)c.prim * c.Sp;
+  long plane = (long)c.n_edges * K4;
   for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
-    int ei = (int)(t / c.S), s = (int)(t - (long)ei * c.S);
+    int ei = (int)(t / c.Sp), s = (int)(t - (long)ei * c.Sp);
     int node = c.edge_nodes[ei];
-    for (int code = 0; code < c.prim; code++)
-      c.lt[((long)ei * c.prim + code) * c.S + s] = (float)log((double)s1_util(c, node, s, code));
+    for (int code = 0; code < c.prim; code++) {
+      float v = 0.f;
+      if (s < c.S) {
+        double lg = log((double)s1_util(c, node, s, code));
+        if (!(lg > -1e30)) lg = -1e30;  // log 0 (and NaN) -> a finite -1e30: 0 * inf would poison the GEMM
+        if (lg > 1e30) lg = 1e30;
+        v = (float)lg;
+      }
+      __nv_bfloat16 hi = __float2bfloat16_rn(v);
+      float r1 = v - __bfloat162float(hi);
+      __nv_bfloat16 mid = __float2bfloat16_rn(r1);
+      __nv_bfloat16 lo = __float2bfloat16_rn(r1 - __bfloat162float(mid));
+      long o = (long)ei * K4 + (long)code * c.Sp + s;
+      B3[o] = hi;
+      B3[plane + o] = mid;
+      B3[2 * plane + o] = lo;
+    }
+    int ex = s < c.S ? c.sexp[(long)node * c.S + s] : 0;
+    int ehi = ex >> 8;          // floor(ex / 256)
+    int elo = ex - (ehi << 8);  // 0..255
+    BX[(long)ei * c.Sp + s] = __float2bfloat16_rn((float)ehi);
+    BX[(long)c.n_edges * c.Sp + (long)ei * c.Sp + s] = __float2bfloat16_rn((float)elo);
   }
 }
 
-// grid (edge tiles, query tiles); ET edges' log tables and exponents staged in
-// shared memory; one warp per query, lanes over the query's sites.
-template <int ET>
-__global__ void __launch_bounds__(256) k_stage1(S1Ctx c, int Q, int q_per_cta, const uint16_t *__restrict__ reind,
-                                                const uint8_t *__restrict__ mcode, const int *__restrict__ qlen,
-                                                const int *__restrict__ qstatus, double *scores) {
-  extern __shared__ float s1_smem[];
-  int e0 = blockIdx.x * ET;
-  int ne = min(ET, c.n_edges - e0);
-  float *slt = s1_smem;                                   // [ET][prim][S]
-  int *sex = reinterpret_cast<int *>(slt + (long)ET * c.prim * c.S);  // [ET][S]
-  for (int e = 0; e < ne; e++) {
-    const float *src = c.lt + (long)(e0 + e) * c.prim * c.S;
-    for (int i = threadIdx.x; i < c.prim * c.S; i += blockDim.x) slt[(long)e * c.prim * c.S + i] = src[i];
-    const int *xs = c.sexp + (long)c.edge_nodes[e0 + e] * c.S;
-    for (int i = threadIdx.x; i < c.S; i += blockDim.x) sex[(long)e * c.S + i] = xs[i];
+// Query side: one-hot rows A[q][c * Sp + s] and the informative mask M[q][s].
+__global__ void k_s1_query(int S, int Sp, int prim, const uint8_t *__restrict__ qcode,
+                           const uint8_t *__restrict__ informative, const int *__restrict__ qstatus,
+                           __nv_bfloat16 *A, __nv_bfloat16 *M) {
+  int q = blockIdx.x;
+  bool ok = qstatus[q] == PGB_Q_OK;
+  const __nv_bfloat16 one = __float2bfloat16_rn(1.f), zero = __float2bfloat16_rn(0.f);
+  long K4 = (long)prim * Sp;
+  for (int s = threadIdx.x; s < Sp; s += blockDim.x) {
+    int code = (ok && s < S) ? qcode[(long)q * S + s] : kBadCode;
+    bool inf = code != kBadCode && informative[code];
+    for (int c = 0; c < prim; c++) A[(long)q * K4 + (long)c * Sp + s] = (inf && code == c) ? one : zero;
+    M[(long)q * Sp + s] = inf ? one : zero;
+  }
+}
+
+// scores = T-sum - n log R + ln2 * exponent sum
+__global__ void k_s1_epilogue(int Q, int E, const float *__restrict__ C, const float *__restrict__ Xhi,
+                              const float *__restrict__ Xlo, const int *__restrict__ qlen,
+                              const int *__restrict__ qstatus, double log_nrates, double *scores) {
+  long n = (long)Q * E;
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+    int q = (int)(t / E);
+    if (qstatus[q] != PGB_Q_OK) continue;
+    long long ex = 256LL * __float2ll_rn(Xhi[t]) + __float2ll_rn(Xlo[t]);
+    scores[t] = (double)C[t] - (double)(float)qlen[q] * log_nrates + kLn2 * (double)ex;
+  }
+}
+
+// Ambiguity characters of the listed queries, every edge.
+__global__ void k_s1_ambig(S1Ctx c, const int *__restrict__ qlist, const uint16_t *__restrict__ reind,
+                           const uint8_t *__restrict__ mcode, const int *__restrict__ qlen, double *scores) {
+  int q = qlist[blockIdx.x];
+  int ei = blockIdx.y * blockDim.x + threadIdx.x;
+  if (ei >= c.n_edges) return;
+  int node = c.edge_nodes[ei];
+  double acc = 0;
+  for (int i = 0; i < qlen[q]; i++) {
+    int code = mcode[(long)q * c.S + i];
+    if (code >= c.prim) acc += log((double)s1_util(c, node, reind[(long)q * c.S + i], code));
+  }
+  scores[(long)q * c.n_edges + ei] += acc;
+}
+
+// Per-query ranking: edges by score, descending, ties to the lower edge index
+// (stable sort of the ascending edge list, fig.ml:143-147); NaN sorts below
+// every number as OCaml's compare does.  Scores map to order-preserving
+// 64-bit keys; a bitonic sort in shared memory orders (key, index) pairs.
+__device__ __forceinline__ unsigned long long s1_key(double v) {
+  if (isnan(v)) return 0ull;
+  unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+
+__global__ void __launch_bounds__(1024) k_rank_bitonic(const double *__restrict__ scores, int E, int N, int rk,
+                                                       const int *__restrict__ qstatus, int *rank) {
+  extern __shared__ unsigned long long rk_key[];
+  int *rk_idx = reinterpret_cast<int *>(rk_key + N);
+  int q = blockIdx.x;
+  if (qstatus[q] != PGB_Q_OK) return;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    rk_key[i] = i < E ? s1_key(scores[(long)q * E + i]) : 0ull;
+    rk_idx[i] = i < E ? i : 0x7fffffff;
   }
   __syncthreads();
-  int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  int q0 = blockIdx.y * q_per_cta;
-  int q1 = min(Q, q0 + q_per_cta);
-  for (int q = q0 + w; q < q1; q += nw) {
-    if (qstatus[q] != PGB_Q_OK) continue;
-    int n = qlen[q];
-    const uint16_t *ri = reind + (long)q * c.S;
-    const uint8_t *mc = mcode + (long)q * c.S;
-    float acc[ET];
-    int eacc[ET];
-#pragma unroll
-    for (int e = 0; e < ET; e++) { acc[e] = 0.f; eacc[e] = 0; }
-    for (int i = lane; i < n; i += 32) {
-      int s = ri[i];
-      int code = mc[i];
-      if (code < c.prim) {
-#pragma unroll
-        for (int e = 0; e < ET; e++) {
-          acc[e] += slt[((long)e * c.prim + code) * c.S + s];
-          eacc[e] += sex[(long)e * c.S + s];
-        }
-      } else {
-#pragma unroll
-        for (int e = 0; e < ET; e++) {
-          if (e < ne) acc[e] += (float)log((double)s1_util(c, c.edge_nodes[e0 + e], s, code));
-          eacc[e] += sex[(long)e * c.S + s];
+  for (int k = 2; k <= N; k <<= 1) {
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int i = threadIdx.x; i < N; i += blockDim.x) {
+        int l = i ^ j;
+        if (l > i) {
+          unsigned long long ki = rk_key[i], kl = rk_key[l];
+          int ii = rk_idx[i], il = rk_idx[l];
+          bool l_first = kl > ki || (kl == ki && il < ii);  // l precedes i in the final order
+          bool i_first = ki > kl || (ki == kl && ii < il);
+          bool up = (i & k) == 0;
+          if (up ? l_first : i_first) {
+            rk_key[i] = kl; rk_key[l] = ki;
+            rk_idx[i] = il; rk_idx[l] = ii;
+          }
         }
       }
-    }
-#pragma unroll
-    for (int e = 0; e < ET; e++) {
-      double a = warp_sum_d((double)acc[e]);
-      long long x = warp_sum_ll((long long)eacc[e]);
-      if (lane == 0 && e < ne)
-        scores[(long)q * c.n_edges + e0 + e] = a - (double)(float)n * c.log_nrates + kLn2 * (double)x;
+      __syncthreads();
     }
   }
+  for (int r = threadIdx.x; r < rk; r += blockDim.x) rank[(long)q * rk + r] = rk_idx[r];
 }
 
-// Per-query ranking: the top rk edges by score, descending, ties to the lower
-// edge index (stable sort of the ascending edge list, fig.ml:143-147; NaN
-// sorts below every number as OCaml's compare does).
 __device__ __forceinline__ bool s1_better(double a, int ia, double b, int ib) {
   bool na = isnan(a), nb = isnan(b);
   if (na != nb) return nb;
@@ -398,6 +459,7 @@ __device__ __forceinline__ bool s1_better(double a, int ia, double b, int ib) {
   return ia < ib;
 }
 
+// Selection ranking for edge counts beyond the bitonic shared-memory tile.
 __global__ void k_rank(const double *__restrict__ scores, int n_edges, int rk, const int *__restrict__ qstatus,
                        int *rank) {
   int q = blockIdx.x;
@@ -655,8 +717,15 @@ struct pgb_engine {
   float *d_darr = nullptr, *d_parr = nullptr, *d_snode = nullptr;
   int *d_dexp = nullptr, *d_pexp = nullptr, *d_sexp = nullptr;
   bool glvs_ready = false;
-  // stage-1 table
-  float *d_lt = nullptr, *d_qe = nullptr;
+  // stage 1: edge tables (bf16 GEMM operands), query operands, GEMM outputs
+  cublasHandle_t blas = nullptr;
+  int Sp = 0;                       // sites padded to a multiple of 8
+  float *d_qe = nullptr;
+  __nv_bfloat16 *d_B3 = nullptr, *d_BX = nullptr, *d_A = nullptr, *d_M = nullptr;
+  float *d_C = nullptr, *d_Xhi = nullptr, *d_Xlo = nullptr;
+  size_t a_cap = 0, c_cap = 0;
+  int *d_qamb = nullptr, *d_amb_list = nullptr;
+  std::vector<int> h_qamb;
   double lt_pend = -1;
   // queries
   int Q = 0, Qcap = 0;
@@ -729,14 +798,23 @@ pgb_status ensure_queries(pgb_engine *e, int Q) {
   size_t n = (size_t)Q * e->S;
   pgb_status s;
   if ((s = dalloc(&e->d_seqs, n)) || (s = dalloc(&e->d_qcode, n)) || (s = dalloc(&e->d_mcode, n)) ||
-      (s = dalloc(&e->d_reind, n)) || (s = dalloc(&e->d_qlen, Q)) || (s = dalloc(&e->d_qstatus, Q)))
+      (s = dalloc(&e->d_reind, n)) || (s = dalloc(&e->d_qlen, Q)) || (s = dalloc(&e->d_qstatus, Q)) ||
+      (s = dalloc(&e->d_qamb, Q)) || (s = dalloc(&e->d_amb_list, Q)))
     return s;
   e->Qcap = Q;
   return PGB_OK;
 }
 
+S1Ctx stage1_ctx(pgb_engine *e) {
+  S1Ctx c{};
+  c.S = e->S; c.Sp = e->Sp; c.RP = e->RP; c.K = e->K; c.NM = e->NM; c.gcat = e->gcat; c.ncode = e->ncode;
+  c.prim = e->prim; c.n_edges = e->n_edges; c.snode = e->d_snode; c.sexp = e->d_sexp;
+  c.edge_nodes = e->d_edge_nodes; c.qe = e->d_qe; c.site_cat = e->d_site_cat;
+  return c;
+}
+
 pgb_status build_stage1_table(pgb_engine *e, double start_pend) {
-  if (e->d_lt && e->lt_pend == start_pend) return PGB_OK;
+  if (e->d_B3 && e->lt_pend == start_pend) return PGB_OK;
   int K = e->K;
   std::vector<double> pm;
   host_pmats(e, start_pend, pm);
@@ -753,63 +831,89 @@ pgb_status build_stage1_table(pgb_engine *e, double start_pend) {
     }
   pgb_status s;
   if ((s = upload(&e->d_qe, qe.data(), qe.size(), e->st))) return s;
-  if (!e->d_lt && (s = dalloc(&e->d_lt, (size_t)e->n_edges * e->prim * e->S))) return s;
-  S1Ctx c{};
-  c.S = e->S; c.RP = e->RP; c.K = K; c.NM = e->NM; c.gcat = e->gcat; c.ncode = e->ncode; c.prim = e->prim;
-  c.n_edges = e->n_edges; c.snode = e->d_snode; c.sexp = e->d_sexp; c.edge_nodes = e->d_edge_nodes; c.qe = e->d_qe;
-  c.site_cat = e->d_site_cat; c.lt = e->d_lt;
-  k_lt_build<<<grid_for((long)e->n_edges * e->S), 256, 0, e->st>>>(c);
+  size_t K4 = (size_t)e->prim * e->Sp;
+  if (!e->d_B3 && ((s = dalloc(&e->d_B3, 3 * (size_t)e->n_edges * K4)) ||
+                   (s = dalloc(&e->d_BX, 2 * (size_t)e->n_edges * e->Sp))))
+    return s;
+  k_s1_tables<<<grid_for((long)e->n_edges * e->Sp), 256, 0, e->st>>>(stage1_ctx(e), e->d_B3, e->d_BX);
   PGB_LAUNCH_CHECK();
   e->lt_pend = start_pend;
   return PGB_OK;
 }
 
-S1Ctx stage1_ctx(pgb_engine *e) {
-  S1Ctx c{};
-  c.S = e->S; c.RP = e->RP; c.K = e->K; c.NM = e->NM; c.gcat = e->gcat; c.ncode = e->ncode; c.prim = e->prim;
-  c.n_edges = e->n_edges; c.snode = e->d_snode; c.sexp = e->d_sexp; c.edge_nodes = e->d_edge_nodes; c.qe = e->d_qe;
-  c.site_cat = e->d_site_cat; c.lt = e->d_lt;
-  c.log_nrates = e->gcat ? 0.0 : log((double)(float)e->NM);
-  return c;
-}
-
-template <int ET>
-pgb_status launch_stage1_t(pgb_engine *e, size_t smem) {
-  if (smem > 48 * 1024)
-    PGB_CUDA(cudaFuncSetAttribute(k_stage1<ET>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  int etiles = (e->n_edges + ET - 1) / ET;
-  // query tiles: enough CTAs for a few waves, at least 32 queries per CTA
-  long want = std::max<long>(1, (long)e->n_sm * 4 / std::max(1, etiles));
-  int qpc = (int)std::max<long>(32, (e->Q + want - 1) / want);
-  int qtiles = (e->Q + qpc - 1) / qpc;
-  dim3 grid(etiles, qtiles);
-  k_stage1<ET><<<grid, 256, smem, e->st>>>(stage1_ctx(e), e->Q, qpc, e->d_reind, e->d_mcode, e->d_qlen,
-                                          e->d_qstatus, e->d_scores);
-  PGB_LAUNCH_CHECK();
+pgb_status gemm_bf16(pgb_engine *e, const __nv_bfloat16 *B, const __nv_bfloat16 *A, float *C, int m, int n, int k,
+                     float beta) {
+  // row-major C[n][m] = A[n][k] * B[m][k]^T, i.e. column-major C' = B'^T A'
+  const float alpha = 1.f;
+  cublasStatus_t st = cublasGemmEx(e->blas, CUBLAS_OP_T, CUBLAS_OP_N, m, n, k, &alpha, B, CUDA_R_16BF, k, A,
+                                   CUDA_R_16BF, k, &beta, C, CUDA_R_32F, m, CUBLAS_COMPUTE_32F, CUBLAS_GEMM_DEFAULT);
+  if (st != CUBLAS_STATUS_SUCCESS) {
+    set_error("stage 1: cublasGemmEx failed (%d)", (int)st);
+    return PGB_ERR_CUDA;
+  }
   return PGB_OK;
 }
 
 pgb_status run_stage1(pgb_engine *e) {
-  size_t per_edge = (size_t)e->S * (e->prim * 4 + 4);
-  size_t budget = e->smem_optin - 1024;
-  int et = (int)std::min<size_t>(8, budget / per_edge);
-  if (et < 1) { set_error("stage 1: alignment too long for the shared-memory tile"); return PGB_ERR_ARG; }
-  size_t scores_n = (size_t)e->Q * e->n_edges;
-  if (scores_n > e->scores_cap) {
-    pgb_status s = dalloc(&e->d_scores, scores_n);
-    if (s) return s;
-    e->scores_cap = scores_n;
+  pgb_status s;
+  size_t K4 = (size_t)e->prim * e->Sp;
+  size_t qe_n = (size_t)e->Q * e->n_edges;
+  if (qe_n > e->scores_cap) {
+    if ((s = dalloc(&e->d_scores, qe_n))) return s;
+    e->scores_cap = qe_n;
   }
-  switch (et) {
-    case 1: return launch_stage1_t<1>(e, per_edge * 1);
-    case 2: return launch_stage1_t<2>(e, per_edge * 2);
-    case 3: return launch_stage1_t<3>(e, per_edge * 3);
-    case 4: return launch_stage1_t<4>(e, per_edge * 4);
-    case 5: return launch_stage1_t<5>(e, per_edge * 5);
-    case 6: return launch_stage1_t<6>(e, per_edge * 6);
-    case 7: return launch_stage1_t<7>(e, per_edge * 7);
-    default: return launch_stage1_t<8>(e, per_edge * 8);
+  if ((size_t)e->Q > e->a_cap) {
+    if ((s = dalloc(&e->d_A, (size_t)e->Q * K4)) || (s = dalloc(&e->d_M, (size_t)e->Q * e->Sp))) return s;
+    e->a_cap = e->Q;
   }
+  if (qe_n > e->c_cap) {
+    if ((s = dalloc(&e->d_C, qe_n)) || (s = dalloc(&e->d_Xhi, qe_n)) || (s = dalloc(&e->d_Xlo, qe_n))) return s;
+    e->c_cap = qe_n;
+  }
+  k_s1_query<<<e->Q, 256, 0, e->st>>>(e->S, e->Sp, e->prim, e->d_qcode, e->d_informative, e->d_qstatus, e->d_A,
+                                      e->d_M);
+  PGB_LAUNCH_CHECK();
+  size_t plane = (size_t)e->n_edges * K4;
+  for (int piece = 0; piece < 3; piece++)
+    if ((s = gemm_bf16(e, e->d_B3 + piece * plane, e->d_A, e->d_C, e->n_edges, e->Q, (int)K4, piece ? 1.f : 0.f)))
+      return s;
+  if ((s = gemm_bf16(e, e->d_BX, e->d_M, e->d_Xhi, e->n_edges, e->Q, e->Sp, 0.f)) ||
+      (s = gemm_bf16(e, e->d_BX + (size_t)e->n_edges * e->Sp, e->d_M, e->d_Xlo, e->n_edges, e->Q, e->Sp, 0.f)))
+    return s;
+  double log_nrates = e->gcat ? 0.0 : log((double)(float)e->NM);
+  k_s1_epilogue<<<grid_for((long)qe_n), 256, 0, e->st>>>(e->Q, e->n_edges, e->d_C, e->d_Xhi, e->d_Xlo, e->d_qlen,
+                                                         e->d_qstatus, log_nrates, e->d_scores);
+  PGB_LAUNCH_CHECK();
+  std::vector<int> amb;
+  for (int q = 0; q < e->Q; q++)
+    if (e->h_qamb[q] > 0) amb.push_back(q);
+  if (!amb.empty()) {
+    PGB_CUDA(cudaMemcpyAsync(e->d_amb_list, amb.data(), amb.size() * 4, cudaMemcpyHostToDevice, e->st));
+    dim3 grid((unsigned)amb.size(), (unsigned)((e->n_edges + 127) / 128));
+    k_s1_ambig<<<grid, 128, 0, e->st>>>(stage1_ctx(e), e->d_amb_list, e->d_reind, e->d_mcode, e->d_qlen,
+                                        e->d_scores);
+    PGB_LAUNCH_CHECK();
+  }
+  return PGB_OK;
+}
+
+pgb_status run_rank(pgb_engine *e, int rk) {
+  int N = 1;
+  while (N < e->n_edges) N <<= 1;
+  size_t smem = (size_t)N * 12;
+  if (N <= 16384 && smem <= e->smem_optin) {
+    if (smem > 48 * 1024)
+      PGB_CUDA(cudaFuncSetAttribute(k_rank_bitonic, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_rank_bitonic<<<e->Q, std::min(1024, std::max(32, N / 2)), smem, e->st>>>(e->d_scores, e->n_edges, N, rk,
+                                                                            e->d_qstatus, e->d_rank);
+    PGB_LAUNCH_CHECK();
+    return PGB_OK;
+  }
+  size_t sm2 = (size_t)((e->n_edges + 31) / 32) * 4;
+  if (sm2 > 48 * 1024) PGB_CUDA(cudaFuncSetAttribute(k_rank, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2));
+  k_rank<<<e->Q, 256, sm2, e->st>>>(e->d_scores, e->n_edges, rk, e->d_qstatus, e->d_rank);
+  PGB_LAUNCH_CHECK();
+  return PGB_OK;
 }
 
 TrialCtx trial_ctx(pgb_engine *e, const pgb_prefs *p, int optimizer, int mode) {
@@ -931,6 +1035,7 @@ pgb_status pgb_engine_create(const pgb_model_desc *m, const pgb_tree_desc *t, pg
   e->S = m->n_sites;
   e->ncode = n_codes(e->K);
   e->prim = e->K;
+  e->Sp = (e->S + 7) & ~7;
   int K = e->K;
   e->statd.assign(m->statd, m->statd + K);
   e->X.assign(m->x, m->x + K * K);
@@ -972,6 +1077,11 @@ pgb_status pgb_engine_create(const pgb_model_desc *m, const pgb_tree_desc *t, pg
   if ((ce = cudaGetDevice(&e->device)) != cudaSuccess || (ce = cudaStreamCreateWithFlags(&e->st, cudaStreamNonBlocking)) != cudaSuccess) {
     set_error("engine_create: %s", cudaGetErrorString(ce));
     delete e;
+    return PGB_ERR_CUDA;
+  }
+  if (cublasCreate(&e->blas) != CUBLAS_STATUS_SUCCESS || cublasSetStream(e->blas, e->st) != CUBLAS_STATUS_SUCCESS) {
+    set_error("engine_create: cuBLAS initialisation failed");
+    pgb_engine_destroy(e);
     return PGB_ERR_CUDA;
   }
   int optin = 0;
@@ -1057,13 +1167,15 @@ pgb_status pgb_engine_destroy(pgb_engine *e) {
   void *ptrs[] = {e->d_bl, e->d_Xd, e->d_Xitd, e->d_lamd, e->d_ratesd, e->d_statdd, e->d_lvd, e->d_pm, e->d_pmh,
                   e->d_mf, e->d_site_cat, e->d_char_code, e->d_informative, e->d_edge_nodes, e->d_parent,
                   e->d_ch_start, e->d_ch_list, e->d_darr, e->d_parr, e->d_snode, e->d_dexp, e->d_pexp, e->d_sexp,
-                  e->d_lt, e->d_qe, e->d_seqs, e->d_qcode, e->d_mcode, e->d_reind, e->d_qlen, e->d_qstatus,
+                  e->d_qe, e->d_B3, e->d_BX, e->d_A, e->d_M, e->d_C, e->d_Xhi, e->d_Xlo, e->d_qamb,
+                  e->d_amb_list, e->d_seqs, e->d_qcode, e->d_mcode, e->d_reind, e->d_qlen, e->d_qstatus,
                   e->d_scores, e->d_rank, e->d_bb, e->d_res, e->d_tbase, e->d_tcount, e->d_keep_idx, e->d_keep_n,
                   e->d_trials, e->d_tres, e->d_bin_list, e->d_small, e->d_out, e->d_nout, e->d_stats};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   for (int i = 0; i < 8; i++)
     if (e->ev[i]) cudaEventDestroy(e->ev[i]);
+  if (e->blas) cublasDestroy(e->blas);
   if (e->st) cudaStreamDestroy(e->st);
   delete e;
   return PGB_OK;
@@ -1234,11 +1346,14 @@ pgb_status pgb_queries_load(pgb_engine *e, int n_queries, const char *seqs) {
   e->Q = n_queries;
   if (!n_queries) return PGB_OK;
   PGB_CUDA(cudaMemcpyAsync(e->d_seqs, seqs, (size_t)n_queries * e->S, cudaMemcpyHostToDevice, e->st));
-  k_query_prep<<<n_queries, 256, 0, e->st>>>(e->d_seqs, e->S, e->d_char_code, e->d_informative, e->d_qcode,
-                                             e->d_reind, e->d_mcode, e->d_qlen, e->d_qstatus);
+  k_query_prep<<<n_queries, 256, 0, e->st>>>(e->d_seqs, e->S, e->prim, e->d_char_code, e->d_informative,
+                                             e->d_qcode, e->d_reind, e->d_mcode, e->d_qlen, e->d_qstatus,
+                                             e->d_qamb);
   PGB_LAUNCH_CHECK();
   e->h_qlen.resize(n_queries);
   PGB_CUDA(cudaMemcpyAsync(e->h_qlen.data(), e->d_qlen, (size_t)n_queries * 4, cudaMemcpyDeviceToHost, e->st));
+  e->h_qamb.resize(n_queries);
+  PGB_CUDA(cudaMemcpyAsync(e->h_qamb.data(), e->d_qamb, (size_t)n_queries * 4, cudaMemcpyDeviceToHost, e->st));
   PGB_CUDA(cudaStreamSynchronize(e->st));
   return PGB_OK;
 }
@@ -1281,12 +1396,7 @@ pgb_status pgb_queries_run(pgb_engine *e, const pgb_prefs *p) {
   if ((s = build_stage1_table(e, p->start_pend))) return s;
   PGB_CUDA(cudaEventRecord(e->ev[1], e->st));
   if ((s = run_stage1(e))) return s;
-  {
-    size_t smem = (size_t)((e->n_edges + 31) / 32) * 4;
-    if (smem > 48 * 1024) PGB_CUDA(cudaFuncSetAttribute(k_rank, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k_rank<<<e->Q, 256, smem, e->st>>>(e->d_scores, e->n_edges, rk, e->d_qstatus, e->d_rank);
-    PGB_LAUNCH_CHECK();
-  }
+  if ((s = run_rank(e, rk))) return s;
   PGB_CUDA(cudaEventRecord(e->ev[2], e->st));
   e->counts[0] = (double)e->Q * e->n_edges;
   // baseball rounds
