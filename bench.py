@@ -204,7 +204,7 @@ def run_ours(args):
         sampler.start()
     n0 = lib.pgb_kernel_launch_count()
     ms_steps, phase = [], np.zeros(6)
-    counts = np.zeros(4)
+    counts = np.zeros(8)
     for _ in range(args.steps):
         eng.run(prefs)
         ms, cnt = eng.timings()
@@ -255,7 +255,10 @@ def run_ours(args):
                    (w.n_nodes * S * R * K * 4 / 1e6), "seed": w.seed},
         "edge_evals": {"stage1_pairs_per_s": counts[0] / (phase[2] / 1e3),
                        "stage2_evals_per_s": counts[2] / (phase[3] / 1e3),
-                       "stage2_trials_per_step": counts[1] / args.steps,
+                       "trials_per_step": counts[1] / args.steps,
+                       "stage2_trials_launched": counts[4] / args.steps,
+                       "stage2_trials_consumed": counts[5] / args.steps,
+                       "refine_trials": counts[6] / args.steps, "rounds": counts[7] / args.steps,
                        "phase_ms": {"stage1_table": phase[1] / args.steps, "stage1_rank": phase[2] / args.steps,
                                     "stage2": phase[3] / args.steps, "refine_out": phase[4] / args.steps}},
         "roofline": {"kernel": "k_trials (stage 2)", "bound": "hbm", "achieved": achieved, "peak": peak,

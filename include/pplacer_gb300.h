@@ -250,8 +250,10 @@ pgb_status pgb_queries_trials(pgb_engine *e, const pgb_prefs *prefs, int optimiz
 /* Device time of the last pgb_queries_run by phase, from CUDA events on the
  * engine's stream: [0] query prep, [1] stage-1 tables, [2] stage-1 scores and
  * ranking, [3] stage-2 trials, [4] refinement and output; [5] total.
- * counts[0..3]: stage-1 (query, edge) pairs, stage-2 trials, stage-2 objective
- * evaluations, stage-2 site evaluations. */
+ * counts[0..7]: stage-1 (query, edge) pairs, stage-2 + refinement trials,
+ * objective evaluations, site evaluations (both trial passes), stage-2 trials
+ * launched, stage-2 trials consumed by the baseball stop rule, refinement
+ * trials, baseball rounds. */
 pgb_status pgb_engine_timings(pgb_engine *e, double *ms, double *counts);
 
 #ifdef __cplusplus

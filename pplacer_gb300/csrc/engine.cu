@@ -703,6 +703,8 @@ struct pgb_engine {
   size_t smem_optin = 0;
   cudaStream_t st = nullptr;
   cudaEvent_t ev[8] = {};
+  cudaStream_t bin_st[8] = {};   // the trial bins run concurrently, one stream each
+  cudaEvent_t bin_ev[9] = {};
   std::vector<double> statd, X, lam, Xit, rates;
   std::vector<int> site_cats, parent, ch_start, ch_list, edge_nodes;
   std::vector<double> bl;
@@ -754,7 +756,7 @@ struct pgb_engine {
   int out_keep = 0;
   // timings
   double t_ms[6] = {0, 0, 0, 0, 0, 0};
-  double counts[4] = {0, 0, 0, 0};
+  double counts[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 };
 
 namespace {
@@ -943,21 +945,23 @@ void bin_limits(const pgb_engine *e, int *lim) {
 }
 
 template <int K>
-pgb_status launch_trials_k(pgb_engine *e, TrialCtx c, const int *d_order, int n, int cap, bool win, TrialRes *out) {
+pgb_status launch_trials_k(pgb_engine *e, cudaStream_t st, TrialCtx c, const int *d_order, int n, int cap, bool win,
+                           TrialRes *out) {
   c.smem_win = win ? 1 : 0;
   c.cap = cap;
   size_t smem = trial_smem_bytes(cap, c.smem_win, e->RP, K, e->NM, e->ncode);
   if (smem > e->smem_optin) { set_error("trial shared memory %zu exceeds %zu", smem, e->smem_optin); return PGB_ERR_ARG; }
   PGB_CUDA(cudaFuncSetAttribute(k_trials<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  k_trials<K><<<n, kTrialThreads, smem, e->st>>>(c, e->d_trials, d_order, n, out);
+  k_trials<K><<<n, kTrialThreads, smem, st>>>(c, e->d_trials, d_order, n, out);
   PGB_LAUNCH_CHECK();
   return PGB_OK;
 }
 
-pgb_status launch_trials(pgb_engine *e, TrialCtx c, const int *d_order, int n, int cap, bool win, TrialRes *out) {
+pgb_status launch_trials(pgb_engine *e, cudaStream_t st, TrialCtx c, const int *d_order, int n, int cap, bool win,
+                         TrialRes *out) {
   if (n <= 0) return PGB_OK;
-  if (e->K == 4) return launch_trials_k<4>(e, c, d_order, n, cap, win, out);
-  return launch_trials_k<20>(e, c, d_order, n, cap, win, out);
+  if (e->K == 4) return launch_trials_k<4>(e, st, c, d_order, n, cap, win, out);
+  return launch_trials_k<20>(e, st, c, d_order, n, cap, win, out);
 }
 
 // Launch every non-empty bin of the trial lists.
@@ -965,16 +969,24 @@ pgb_status run_bins(pgb_engine *e, TrialCtx c, const int *h_bin_count, int max_s
   int lim[kBins];
   bin_limits(e, lim);
   size_t win_budget = e->smem_optin - trial_smem_bytes(0, 0, e->RP, e->K, e->NM, e->ncode) - 2048;
-  for (int b = 0; b < kBins; b++) {
+  // fork the bins off the engine stream, longest windows first, and join
+  PGB_CUDA(cudaEventRecord(e->bin_ev[8], e->st));
+  int used[kBins], nu = 0;
+  for (int b = kBins - 1; b >= 0; b--) {
     int n = h_bin_count[b];
     if (n == 0) continue;
     int cap = std::min(lim[b], max_sq);
     bool win = (size_t)2 * e->RP * cap * e->K * 4 + 2 * (size_t)cap <= win_budget && b < kBins - 1;
     if (!win) cap = std::max(cap, 1);
-    pgb_status s = launch_trials(e, c, e->d_bin_list + (long)b * e->trials_cap, n, win ? cap : std::max(max_sq, 1),
-                                 win, e->d_tres);
+    cudaStream_t bs = e->bin_st[b];
+    PGB_CUDA(cudaStreamWaitEvent(bs, e->bin_ev[8], 0));
+    pgb_status s = launch_trials(e, bs, c, e->d_bin_list + (long)b * e->trials_cap, n,
+                                 win ? cap : std::max(max_sq, 1), win, e->d_tres);
     if (s) return s;
+    PGB_CUDA(cudaEventRecord(e->bin_ev[b], bs));
+    used[nu++] = b;
   }
+  for (int i = 0; i < nu; i++) PGB_CUDA(cudaStreamWaitEvent(e->st, e->bin_ev[used[i]], 0));
   return PGB_OK;
 }
 
@@ -1089,6 +1101,8 @@ pgb_status pgb_engine_create(const pgb_model_desc *m, const pgb_tree_desc *t, pg
   cudaDeviceGetAttribute(&e->n_sm, cudaDevAttrMultiProcessorCount, e->device);
   e->smem_optin = (size_t)optin;
   for (int i = 0; i < 8; i++) cudaEventCreate(&e->ev[i]);
+  for (int i = 0; i < 8; i++) cudaStreamCreateWithFlags(&e->bin_st[i], cudaStreamNonBlocking);
+  for (int i = 0; i < 9; i++) cudaEventCreateWithFlags(&e->bin_ev[i], cudaEventDisableTiming);
 
   // model constants
   std::vector<float> mf;
@@ -1175,6 +1189,10 @@ pgb_status pgb_engine_destroy(pgb_engine *e) {
     if (p) cudaFree(p);
   for (int i = 0; i < 8; i++)
     if (e->ev[i]) cudaEventDestroy(e->ev[i]);
+  for (int i = 0; i < 8; i++)
+    if (e->bin_st[i]) cudaStreamDestroy(e->bin_st[i]);
+  for (int i = 0; i < 9; i++)
+    if (e->bin_ev[i]) cudaEventDestroy(e->bin_ev[i]);
   if (e->blas) cublasDestroy(e->blas);
   if (e->st) cudaStreamDestroy(e->st);
   delete e;
@@ -1390,7 +1408,7 @@ pgb_status pgb_queries_run(pgb_engine *e, const pgb_prefs *p) {
   size_t tcap = (size_t)e->Q * std::max(8, std::min(rk, 16)) + (size_t)e->Q * p->keep_at_most + 64;
   if (all_edges) tcap = std::max(tcap, (size_t)e->Q * e->n_edges + 64);
   if ((s = ensure_run_buffers(e, p, rk, maxr, tcap))) return s;
-  for (int i = 0; i < 4; i++) e->counts[i] = 0;
+  for (int i = 0; i < 8; i++) e->counts[i] = 0;
   PGB_CUDA(cudaMemsetAsync(e->d_stats, 0, 4 * sizeof(unsigned long long), e->st));
   PGB_CUDA(cudaEventRecord(e->ev[0], e->st));
   if ((s = build_stage1_table(e, p->start_pend))) return s;
@@ -1418,8 +1436,18 @@ pgb_status pgb_queries_run(pgb_engine *e, const pgb_prefs *p) {
   k_bb_init<<<(n + 255) / 256, 256, 0, e->st>>>(c);
   PGB_LAUNCH_CHECK();
   double n_trials_total = 0;
+  int rounds = 0, last_active = e->Q;
   for (int round = 0; round < 4096; round++) {
-    int B = all_edges ? rk : (round == 0 ? std::min(rk, p->max_strikes + 1) : 8);
+    rounds = round + 1;
+    // speculative width: round 0 evaluates the minimum any query needs
+    // (max_strikes + 1); later rounds are narrow since most queries that
+    // continue stop within a few more pitches
+    // later rounds widen as fewer queries remain: enough trials to keep every
+    // SM busy for a couple of waves, at least 3 per query
+    int B;
+    if (all_edges) B = rk;
+    else if (round == 0) B = std::min(rk, p->max_strikes + 1);
+    else B = std::max(3, std::min(16, (2 * e->n_sm + last_active - 1) / std::max(1, last_active)));
     PGB_CUDA(cudaMemcpyAsync(e->d_small, h_small, sizeof(h_small), cudaMemcpyHostToDevice, e->st));
     k_bb_emit<<<(n + 255) / 256, 256, 0, e->st>>>(c, B, e->d_small);
     PGB_LAUNCH_CHECK();
@@ -1435,8 +1463,19 @@ pgb_status pgb_queries_run(pgb_engine *e, const pgb_prefs *p) {
     PGB_CUDA(cudaMemcpyAsync(&active, e->d_small + 1, 4, cudaMemcpyDeviceToHost, e->st));
     PGB_CUDA(cudaStreamSynchronize(e->st));
     if (active == 0) break;
+    last_active = active;
   }
   PGB_CUDA(cudaEventRecord(e->ev[3], e->st));
+  {  // speculation accounting: stage-2 trials emitted vs consumed by the stop rule
+    std::vector<BBState> bbh(e->Q);
+    PGB_CUDA(cudaMemcpyAsync(bbh.data(), e->d_bb, e->Q * sizeof(BBState), cudaMemcpyDeviceToHost, e->st));
+    PGB_CUDA(cudaStreamSynchronize(e->st));
+    double consumed = 0;
+    for (const BBState &b : bbh) consumed += b.next;
+    e->counts[4] = n_trials_total;
+    e->counts[5] = consumed;
+    e->counts[7] = rounds;
+  }
   // keep + refine
   PGB_CUDA(cudaMemcpyAsync(e->d_small, h_small, sizeof(h_small), cudaMemcpyHostToDevice, e->st));
   k_keep_emit<<<(n + 255) / 256, 256, 0, e->st>>>(c, p->keep_at_most, log(p->keep_factor), e->d_keep_idx,
@@ -1446,6 +1485,7 @@ pgb_status pgb_queries_run(pgb_engine *e, const pgb_prefs *p) {
   PGB_CUDA(cudaMemcpyAsync(got, e->d_small, sizeof(got), cudaMemcpyDeviceToHost, e->st));
   PGB_CUDA(cudaStreamSynchronize(e->st));
   n_trials_total += got[0];
+  e->counts[6] = got[0];
   if ((s = run_bins(e, tc, got + 2, max_sq))) return s;
   k_finalize<<<(n + 255) / 256, 256, 0, e->st>>>(c, p->keep_at_most, e->d_keep_idx, e->d_keep_n, e->d_tres,
                                                  e->d_out, e->d_nout);
@@ -1546,7 +1586,7 @@ pgb_status pgb_queries_trials(pgb_engine *e, const pgb_prefs *p, int optimizer, 
 pgb_status pgb_engine_timings(pgb_engine *e, double *ms, double *counts) {
   if (!e) return PGB_ERR_ARG;
   for (int i = 0; i < 6; i++) ms[i] = e->t_ms[i];
-  for (int i = 0; i < 4; i++) counts[i] = e->counts[i];
+  for (int i = 0; i < 8; i++) counts[i] = e->counts[i];
   return PGB_OK;
 }
 

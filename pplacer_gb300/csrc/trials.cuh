@@ -161,6 +161,14 @@ struct Optimiser {
 
   __device__ double full(const EvalOut &o) const { return (double)o.ex * kLn2 + (double)o.lm + cst; }
 
+  // Newton stops when the first-order gain of its last step, g . s, is below
+  // this (logL units): 1e-3 in the stage-2 pass (pplacer's tolerance 0.01,
+  // whose Brent stops within about 0.05 logL of the optimum), 1e-7 in the
+  // final 1e-5 pass -- plus the evaluation's rounding allowance.  A step-size
+  // rule alone is unsound here: near a zero pendant the curvature is huge and
+  // Newton steps are tiny while the gradient is not.
+  __device__ float newton_gain_tol() const { return tol >= 1e-3 ? 1e-3f : 1e-7f; }
+
   __device__ void request(double pp, double dd, double xx, bool derivs) {
     req_p = (float)pp;
     req_d = (float)dd;
@@ -185,7 +193,7 @@ struct Optimiser {
     n_evals++;
   }
 
-  __device__ bool next(const EvalOut *res) {
+  __device__ __forceinline__ bool next(const EvalOut *res) {
     if (res) record(res);
     switch (pc) {
       case 0:
@@ -392,7 +400,7 @@ struct Optimiser {
             p = np;
             d = nd;
             cur = last;
-            if (step < (float)(0.01 * tol) || fabsf(pred) < 1e-3f * allow) break;
+            if (fabsf(pred) < newton_gain_tol() + allow || step < 1e-9f) break;
           }
           if (it == 59) status = ST_MAXITER;
         }
@@ -671,20 +679,21 @@ __global__ void __launch_bounds__(kTrialThreads, 1) k_trials(TrialCtx c, const T
         sm.ctrl->dist = opt.req_d;
         sm.ctrl->prox = opt.req_x;
       }
-      if (more) {
-        for (int i = lane; i < 3 * NM * K; i += 32) {
-          int wh = i / (NM * K), mk = i - wh * NM * K;
-          float t = wh == 0 ? opt.req_d : (wh == 1 ? opt.req_x : opt.req_p);
-          float a = sm.Lr[mk] * t;
-          sm.E[i] = expf(a);
-          sm.Em1[i] = expm1f(a);
-        }
-      }
     }
     __syncthreads();  // A
     const Ctrl ctl = *sm.ctrl;
     if (ctl.cmd == 0) break;
     const bool derivs = ctl.cmd == 2;
+    // exp factors of (dist, prox, pend), spread over all threads
+
+    for (int i = tid; i < 3 * NM * K; i += kTrialThreads) {
+      int wh = i / (NM * K), mk = i - wh * NM * K;
+      float t = wh == 0 ? ctl.dist : (wh == 1 ? ctl.prox : ctl.pend);
+      float a = sm.Lr[mk] * t;
+      sm.E[i] = expf(a);
+      sm.Em1[i] = expm1f(a);
+    }
+    __syncthreads();  // A2: exp factors
     // ---- P(t) = I + X diag(expm1(r lambda t)) X^-T and derivatives; query vectors ----
     const float *W = K == 4 ? sm.W : c.W;
     const int nmat = NM * K * K;
@@ -770,19 +779,29 @@ __global__ void __launch_bounds__(kTrialThreads, 1) k_trials(TrialCtx c, const T
     }
     __syncthreads();  // C
     if (warp == 0) {
-      float mt = 1.f;
-      int et = 0;
-      float sg[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+      // lanes 0..warps-1 hold one warp's partials; shuffle tree
+      bool have = lane < kTrialWarps;
+      float mt = have ? sm.red[lane * 8] : 1.f;
+      int et = have ? sm.redi[lane] : 0;
+      float sg[5];
 #pragma unroll
-      for (int i = 0; i < kTrialWarps; i++) {
-        mt *= sm.red[i * 8];
-        et += sm.redi[i];
+      for (int k = 0; k < 5; k++) sg[k] = have ? sm.red[lane * 8 + 1 + k] : 0.f;
+#pragma unroll
+      for (int o = kTrialWarps / 2; o > 0; o >>= 1) {
+        float mo = __shfl_xor_sync(0xffffffffu, mt, o);
+        int eo = __shfl_xor_sync(0xffffffffu, et, o);
+        mt *= mo;
+        et += eo;
         int em;
         mt = frexpf(mt, &em);
         et += em;
 #pragma unroll
-        for (int k = 0; k < 5; k++) sg[k] += sm.red[i * 8 + 1 + k];
+        for (int k = 0; k < 5; k++) sg[k] += __shfl_xor_sync(0xffffffffu, sg[k], o);
       }
+      mt = __shfl_sync(0xffffffffu, mt, 0);
+      et = __shfl_sync(0xffffffffu, et, 0);
+#pragma unroll
+      for (int k = 0; k < 5; k++) sg[k] = __shfl_sync(0xffffffffu, sg[k], 0);
       res.ex = et;
       res.lm = logf(mt);
       res.g[0] = sg[0]; res.g[1] = sg[1];

@@ -132,7 +132,7 @@ class Engine:
 
     def timings(self):
         ms = np.zeros(6)
-        cnt = np.zeros(4)
+        cnt = np.zeros(8)
         _L.check(_L.load().pgb_engine_timings(self.h, ms.ctypes.data, cnt.ctypes.data), "pgb_engine_timings")
         return ms, cnt
 
