@@ -113,6 +113,21 @@ pgb_status pgb_int_vec_pairwise_prod(uint16_t *dst, const uint16_t *x, const uin
  * caml_failwith on mismatched sizes is the stub's job (it has the dims). */
 pgb_status pgb_float_mat_int_vec_mul(double *dst, const double *mat, const uint16_t *vec, int n, int k);
 
+/* Allocation-free ten_log_like3 on device buffers.  No counterpart in the
+ * reference: it is for callers that cannot allocate device memory when they
+ * need a likelihood -- their GPU memory belongs to another runtime's pool, or
+ * they allocate only at start-up.  statd ([n_states]), x, y, z
+ * ([n_rates][n_sites][n_states]) and result (one double) are DEVICE pointers;
+ * stream is a cudaStream_t (NULL: the default stream) and the call is
+ * asynchronous on it.  The reduction's scratch is a fixed array inside the
+ * library, held by every GPU that loads it: n_sites <= 65,536, larger sizes
+ * return PGB_ERR_ARG.  All calls on a device share that array, so calls that
+ * overlap on the GPU race.  The first call on a device looks up the array's
+ * address; make it before any stream capture.  Calls no cudaMalloc or
+ * cudaFree. */
+pgb_status pgb_ten_log_like3_noalloc(const double *statd, const double *x, const double *y, const double *z,
+                                     int n_rates, int n_sites, int n_states, double *result, void *stream);
+
 /* ----------------------------------------------------------------------------
  * 2. Batched placement engine
  * ------------------------------------------------------------------------- */
