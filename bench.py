@@ -196,6 +196,7 @@ def run_ours(args):
     lib = L.load()
     # ---- device-resident value ----
     eng.load_queries(w.query_seqs)
+    tune = eng.autotune(prefs)
     for _ in range(args.warmup):
         eng.run(prefs)
     barrier(dist)
@@ -251,7 +252,9 @@ def run_ours(args):
         "config": {"workload": args.workload, "taxa": (w.n_nodes + 1) // 2, "sites": S, "queries": Q,
                    "model": "GTR+G4" if w.site_cats is None else "GTR+CAT20",
                    "optimizer": args.optimizer, "keep_at_most": prefs.keep_at_most,
-                   "max_strikes": prefs.max_strikes, "l2": "GLV arrays 3x%.0f MB exceed L2, no flush" %
+                   "max_strikes": prefs.max_strikes,
+                   "trial_tuning": {"threads": [int(v) for v in tune[0]], "smem_windows": [int(v) for v in tune[1]]},
+                   "l2": "GLV arrays 3x%.0f MB exceed L2, no flush" %
                    (w.n_nodes * S * R * K * 4 / 1e6), "seed": w.seed},
         "edge_evals": {"stage1_pairs_per_s": counts[0] / (phase[2] / 1e3),
                        "stage2_evals_per_s": counts[2] / (phase[3] / 1e3),

@@ -262,6 +262,15 @@ typedef struct {
 pgb_status pgb_queries_trials(pgb_engine *e, const pgb_prefs *prefs, int optimizer, int mode, int n_trials,
                               const pgb_trial *trials, pgb_trial_out *out);
 
+/* Autotuner of the stage-2 trial kernel: for each of the 6 query-length bins
+ * (<= 256, 512, 768, 1024, 1536 informative sites, longer), time every shape
+ * -- 128 or 256 threads per CTA, the query's sites of darr / parr staged in
+ * shared memory or read from L2 -- on the loaded queries' first baseball
+ * round, and keep the fastest for later runs.  get_tuning reports the table
+ * (threads[6], smem_windows[6]). */
+pgb_status pgb_engine_autotune(pgb_engine *e, const pgb_prefs *prefs);
+pgb_status pgb_engine_get_tuning(pgb_engine *e, int *threads, int *smem_windows);
+
 /* Device time of the last pgb_queries_run by phase, from CUDA events on the
  * engine's stream: [0] query prep, [1] stage-1 tables, [2] stage-1 scores and
  * ranking, [3] stage-2 trials, [4] refinement and output; [5] total.

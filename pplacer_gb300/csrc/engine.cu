@@ -754,6 +754,10 @@ struct pgb_engine {
   pgb_placement *d_out = nullptr;
   int *d_nout = nullptr;
   int out_keep = 0;
+  // trial-kernel shape per length bin: threads per CTA, shared-memory windows
+  // allowed (1) or read from L2 (0); set by pgb_engine_autotune
+  int tune_threads[8] = {256, 256, 256, 256, 256, 256, 256, 256};
+  int tune_win[8] = {1, 1, 1, 1, 1, 1, 1, 1};
   // timings
   double t_ms[6] = {0, 0, 0, 0, 0, 0};
   double counts[8] = {0, 0, 0, 0, 0, 0, 0, 0};
@@ -944,44 +948,54 @@ void bin_limits(const pgb_engine *e, int *lim) {
   }
 }
 
-template <int K>
-pgb_status launch_trials_k(pgb_engine *e, cudaStream_t st, TrialCtx c, const int *d_order, int n, int cap, bool win,
-                           TrialRes *out) {
+template <int K, int T>
+pgb_status launch_trials_kt(pgb_engine *e, cudaStream_t st, TrialCtx c, const int *d_order, int n, int cap, bool win,
+                            TrialRes *out) {
   c.smem_win = win ? 1 : 0;
   c.cap = cap;
   size_t smem = trial_smem_bytes(cap, c.smem_win, e->RP, K, e->NM, e->ncode);
   if (smem > e->smem_optin) { set_error("trial shared memory %zu exceeds %zu", smem, e->smem_optin); return PGB_ERR_ARG; }
-  PGB_CUDA(cudaFuncSetAttribute(k_trials<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  k_trials<K><<<n, kTrialThreads, smem, st>>>(c, e->d_trials, d_order, n, out);
+  PGB_CUDA(cudaFuncSetAttribute(k_trials<K, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  k_trials<K, T><<<n, T, smem, st>>>(c, e->d_trials, d_order, n, out);
   PGB_LAUNCH_CHECK();
   return PGB_OK;
 }
 
 pgb_status launch_trials(pgb_engine *e, cudaStream_t st, TrialCtx c, const int *d_order, int n, int cap, bool win,
-                         TrialRes *out) {
+                         TrialRes *out, int threads) {
   if (n <= 0) return PGB_OK;
-  if (e->K == 4) return launch_trials_k<4>(e, st, c, d_order, n, cap, win, out);
-  return launch_trials_k<20>(e, st, c, d_order, n, cap, win, out);
+  if (e->K == 4)
+    return threads == 128 ? launch_trials_kt<4, 128>(e, st, c, d_order, n, cap, win, out)
+                          : launch_trials_kt<4, 256>(e, st, c, d_order, n, cap, win, out);
+  return threads == 128 ? launch_trials_kt<20, 128>(e, st, c, d_order, n, cap, win, out)
+                        : launch_trials_kt<20, 256>(e, st, c, d_order, n, cap, win, out);
 }
 
-// Launch every non-empty bin of the trial lists.
-pgb_status run_bins(pgb_engine *e, TrialCtx c, const int *h_bin_count, int max_sq) {
+// window capacity of bin b and whether it is staged in shared memory
+void bin_shape(const pgb_engine *e, int b, int max_sq, int allow_win, int *cap, bool *win) {
   int lim[kBins];
   bin_limits(e, lim);
   size_t win_budget = e->smem_optin - trial_smem_bytes(0, 0, e->RP, e->K, e->NM, e->ncode) - 2048;
-  // fork the bins off the engine stream, longest windows first, and join
+  int c0 = std::min(lim[b], max_sq);
+  *win = allow_win && b < kBins - 1 && (size_t)2 * e->RP * c0 * e->K * 4 + 2 * (size_t)c0 <= win_budget;
+  *cap = *win ? std::max(c0, 1) : std::max(max_sq, 1);
+}
+
+// Launch every non-empty bin of the trial lists, concurrently (one stream
+// each, longest windows first), and join them on the engine stream.
+pgb_status run_bins(pgb_engine *e, TrialCtx c, const int *h_bin_count, int max_sq) {
   PGB_CUDA(cudaEventRecord(e->bin_ev[8], e->st));
   int used[kBins], nu = 0;
   for (int b = kBins - 1; b >= 0; b--) {
     int n = h_bin_count[b];
     if (n == 0) continue;
-    int cap = std::min(lim[b], max_sq);
-    bool win = (size_t)2 * e->RP * cap * e->K * 4 + 2 * (size_t)cap <= win_budget && b < kBins - 1;
-    if (!win) cap = std::max(cap, 1);
+    int cap;
+    bool win;
+    bin_shape(e, b, max_sq, e->tune_win[b], &cap, &win);
     cudaStream_t bs = e->bin_st[b];
     PGB_CUDA(cudaStreamWaitEvent(bs, e->bin_ev[8], 0));
-    pgb_status s = launch_trials(e, bs, c, e->d_bin_list + (long)b * e->trials_cap, n,
-                                 win ? cap : std::max(max_sq, 1), win, e->d_tres);
+    pgb_status s = launch_trials(e, bs, c, e->d_bin_list + (long)b * e->trials_cap, n, cap, win, e->d_tres,
+                                 e->tune_threads[b]);
     if (s) return s;
     PGB_CUDA(cudaEventRecord(e->bin_ev[b], bs));
     used[nu++] = b;
@@ -1503,6 +1517,84 @@ pgb_status pgb_queries_run(pgb_engine *e, const pgb_prefs *p) {
   PGB_CUDA(cudaMemcpy(st_h, e->d_stats, sizeof st_h, cudaMemcpyDeviceToHost));
   e->counts[2] = (double)st_h[0];
   e->counts[3] = (double)st_h[1];
+  return PGB_OK;
+}
+
+// Time every (threads, window placement) shape of the trial kernel on the
+// loaded queries' first-round trials, bin by bin, and keep the fastest.
+pgb_status pgb_engine_autotune(pgb_engine *e, const pgb_prefs *p) {
+  if (!e || !e->glvs_ready || e->Q < 1) { set_error("autotune: no GLVs or no queries"); return PGB_ERR_STATE; }
+  pgb_status s;
+  if ((s = check_prefs(p))) return s;
+  bool all_edges = p->max_strikes == 0;
+  int rk = all_edges ? e->n_edges : std::min(e->n_edges, p->max_pitches + 1 + 24);
+  int maxr = all_edges ? e->n_edges : std::min(e->n_edges, p->max_pitches + 1);
+  int max_sq = 1;
+  for (int v : e->h_qlen) max_sq = std::max(max_sq, v);
+  size_t tcap = (size_t)e->Q * std::max(8, std::min(rk, 16)) + (size_t)e->Q * p->keep_at_most + 64;
+  if (all_edges) tcap = std::max(tcap, (size_t)e->Q * e->n_edges + 64);
+  if ((s = ensure_run_buffers(e, p, rk, maxr, tcap)) || (s = build_stage1_table(e, p->start_pend)) ||
+      (s = run_stage1(e)) || (s = run_rank(e, rk)))
+    return s;
+  BBCtx c{};
+  c.Q = e->Q; c.rk = rk; c.maxr = maxr; c.n_edges = e->n_edges; c.bins = kBins;
+  c.rank = e->d_rank; c.edge_nodes = e->d_edge_nodes; c.bl = e->d_bl; c.qlen = e->d_qlen; c.qstatus = e->d_qstatus;
+  c.bb = e->d_bb; c.res = e->d_res; c.tbase = e->d_tbase; c.tcount = e->d_tcount; c.trials = e->d_trials;
+  c.bin_count = e->d_small + 2; c.bin_list = e->d_bin_list; c.bin_limit = e->d_small + 2 + kBins;
+  c.cap_trials = (int)e->trials_cap; c.n_active = e->d_small + 1;
+  c.start_pend = p->start_pend; c.tol = p->initial_tolerance; c.strike_box = p->strike_box;
+  c.max_pitches = all_edges ? (1L << 40) : p->max_pitches;
+  c.max_strikes = all_edges ? (1L << 40) : p->max_strikes;
+  int lim[kBins];
+  bin_limits(e, lim);
+  int h_small[2 + 2 * kBins] = {0};
+  for (int b = 0; b < kBins; b++) h_small[2 + kBins + b] = lim[b];
+  k_bb_init<<<(e->Q + 255) / 256, 256, 0, e->st>>>(c);
+  PGB_LAUNCH_CHECK();
+  PGB_CUDA(cudaMemcpyAsync(e->d_small, h_small, sizeof(h_small), cudaMemcpyHostToDevice, e->st));
+  int B = all_edges ? rk : std::min(rk, p->max_strikes + 1);
+  k_bb_emit<<<(e->Q + 255) / 256, 256, 0, e->st>>>(c, B, e->d_small);
+  PGB_LAUNCH_CHECK();
+  int got[2 + kBins];
+  PGB_CUDA(cudaMemcpyAsync(got, e->d_small, sizeof(got), cudaMemcpyDeviceToHost, e->st));
+  PGB_CUDA(cudaStreamSynchronize(e->st));
+  TrialCtx tc = trial_ctx(e, p, p->optimizer, 0);
+  tc.stats = nullptr;
+  const int cand_threads[2] = {256, 128};
+  for (int b = 0; b < kBins; b++) {
+    int n = got[2 + b];
+    if (n == 0) continue;
+    float best = 1e30f;
+    int bt = e->tune_threads[b], bw = e->tune_win[b];
+    for (int ti = 0; ti < 2; ti++)
+      for (int w = 1; w >= 0; w--) {
+        int cap;
+        bool win;
+        bin_shape(e, b, max_sq, w, &cap, &win);
+        if (w == 1 && !win) continue;  // window does not fit: same as w == 0
+        float ms_best = 1e30f;
+        for (int rep = 0; rep < 2; rep++) {
+          PGB_CUDA(cudaEventRecord(e->ev[6], e->st));
+          if ((s = launch_trials(e, e->st, tc, e->d_bin_list + (long)b * e->trials_cap, n, cap, win, e->d_tres,
+                                 cand_threads[ti])))
+            return s;
+          PGB_CUDA(cudaEventRecord(e->ev[7], e->st));
+          PGB_CUDA(cudaEventSynchronize(e->ev[7]));
+          float ms;
+          cudaEventElapsedTime(&ms, e->ev[6], e->ev[7]);
+          ms_best = std::min(ms_best, ms);
+        }
+        if (ms_best < best) { best = ms_best; bt = cand_threads[ti]; bw = w; }
+      }
+    e->tune_threads[b] = bt;
+    e->tune_win[b] = bw;
+  }
+  return PGB_OK;
+}
+
+pgb_status pgb_engine_get_tuning(pgb_engine *e, int *threads, int *smem_windows) {
+  if (!e) return PGB_ERR_ARG;
+  for (int b = 0; b < kBins; b++) { threads[b] = e->tune_threads[b]; smem_windows[b] = e->tune_win[b]; }
   return PGB_OK;
 }
 

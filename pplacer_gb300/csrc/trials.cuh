@@ -16,8 +16,7 @@
 // Every loop is bounded and every path through warp 0 ends with the stop
 // command, so the barriers always complete.
 
-constexpr int kTrialThreads = 256;
-constexpr int kTrialWarps = kTrialThreads / 32;
+constexpr int kTrialMaxWarps = 8;  // CTAs of 128 or 256 threads (autotuned per bin)
 constexpr int kMaxTrialEvals = 200000;
 
 struct TrialIn {
@@ -88,7 +87,7 @@ __host__ __device__ inline size_t trial_smem_bytes(int cap, int win, int RP, int
   b += 2 * align16((size_t)3 * NM * K * 4) + align16((size_t)NM * K * 4);
   b += align16((size_t)K * K * 4) + (K == 4 ? align16((size_t)K * K * K * 4) : 0) +
        2 * align16((size_t)ncode * K * 4) + align16((size_t)K * 4);
-  b += align16(kTrialWarps * 8 * 4) + align16(kTrialWarps * 4);
+  b += align16(kTrialMaxWarps * 8 * 4) + align16(kTrialMaxWarps * 4);
   b += align16(sizeof(Ctrl));
   return b;
 }
@@ -114,8 +113,8 @@ __device__ inline TrialSmem carve(char *base, int cap, int win, int RP, int K, i
   s.Lt = (float *)take((size_t)ncode * K * 4);
   s.lv = (float *)take((size_t)ncode * K * 4);
   s.statd = (float *)take((size_t)K * 4);
-  s.red = (float *)take(kTrialWarps * 8 * 4);
-  s.redi = (int *)take(kTrialWarps * 4);
+  s.red = (float *)take(kTrialMaxWarps * 8 * 4);
+  s.redi = (int *)take(kTrialMaxWarps * 4);
   s.ctrl = (Ctrl *)take(sizeof(Ctrl));
   return s;
 }
@@ -450,14 +449,14 @@ struct SiteAcc {
 
 // Sites of the DNA Gamma-mixture model: rates outer, the rate's transition
 // matrices held in registers, the thread's sites inner.
-template <bool DER>
+template <int T, bool DER>
 __device__ __forceinline__ void sites_dna_gmix(const TrialCtx &c, const TrialSmem &sm, int q, int node, int Sq,
                                                SiteAcc &acc) {
   constexpr int K = 4;
   const int tid = threadIdx.x, nc = c.ncode;
   const float *gdb = c.darr + (long)node * c.S * c.RP * K;
   const float *gpb = c.parr + (long)node * c.S * c.RP * K;
-  for (int base = 0; base < Sq; base += 4 * kTrialThreads) {
+  for (int base = 0; base < Sq; base += 4 * T) {
     float a0[4], ad[4], add[4], ap[4], app[4], apd[4];
 #pragma unroll
     for (int j = 0; j < 4; j++) a0[j] = ad[j] = add[j] = ap[j] = app[j] = apd[j] = 0.f;
@@ -482,7 +481,7 @@ __device__ __forceinline__ void sites_dna_gmix(const TrialCtx &c, const TrialSme
       }
 #pragma unroll
       for (int j = 0; j < 4; j++) {
-        int i = base + tid + j * kTrialThreads;
+        int i = base + tid + j * T;
         if (i < Sq) {
           int code = sm.code[i];
           float4 D4, P4;
@@ -537,19 +536,19 @@ __device__ __forceinline__ void sites_dna_gmix(const TrialCtx &c, const TrialSme
     }
 #pragma unroll
     for (int j = 0; j < 4; j++)
-      if (base + tid + j * kTrialThreads < Sq) acc.add(a0[j], ad[j], add[j], ap[j], app[j], apd[j], DER);
+      if (base + tid + j * T < Sq) acc.add(a0[j], ad[j], add[j], ap[j], app[j], apd[j], DER);
   }
 }
 
 // Generic sites: any K, Gamma mixture or per-site CAT category matrices read
 // from shared memory.
-template <int K, bool DER>
+template <int K, int T, bool DER>
 __device__ __forceinline__ void sites_generic(const TrialCtx &c, const TrialSmem &sm, int q, int node, int Sq,
                                               SiteAcc &acc) {
   const int tid = threadIdx.x, nc = c.ncode;
   const float *gdb = c.darr + (long)node * c.S * c.RP * K;
   const float *gpb = c.parr + (long)node * c.S * c.RP * K;
-  for (int i = tid; i < Sq; i += kTrialThreads) {
+  for (int i = tid; i < Sq; i += T) {
     int code = sm.code[i];
     float u = 0.f, ud = 0.f, udd = 0.f, up = 0.f, upp = 0.f, upd = 0.f;
     long s = c.smem_win ? 0 : (long)c.reind[(long)q * c.S + i];
@@ -603,8 +602,8 @@ __device__ __forceinline__ void sites_generic(const TrialCtx &c, const TrialSmem
   }
 }
 
-template <int K>
-__global__ void __launch_bounds__(kTrialThreads, 1) k_trials(TrialCtx c, const TrialIn *__restrict__ trials,
+template <int K, int T>
+__global__ void __launch_bounds__(T, 1) k_trials(TrialCtx c, const TrialIn *__restrict__ trials,
                                                              const int *__restrict__ order, int n, TrialRes *out) {
   extern __shared__ __align__(16) char t_smem[];
   if (blockIdx.x >= n) return;
@@ -616,15 +615,15 @@ __global__ void __launch_bounds__(kTrialThreads, 1) k_trials(TrialCtx c, const T
   const int Sq = c.qlen[q];
   const int NM = c.NM, nc = c.ncode;
   // ---- prologue: model constants and the query's sites of darr / parr ----
-  for (int i = tid; i < K * K; i += kTrialThreads) sm.X[i] = c.X[i];
+  for (int i = tid; i < K * K; i += T) sm.X[i] = c.X[i];
   if (K == 4)
-    for (int i = tid; i < K * K * K; i += kTrialThreads) sm.W[i] = c.W[i];
-  for (int i = tid; i < nc * K; i += kTrialThreads) { sm.Lt[i] = c.Lt[i]; sm.lv[i] = c.lvf[i]; }
-  for (int i = tid; i < NM * K; i += kTrialThreads) sm.Lr[i] = c.rates[i / K] * c.lam[i % K];
+    for (int i = tid; i < K * K * K; i += T) sm.W[i] = c.W[i];
+  for (int i = tid; i < nc * K; i += T) { sm.Lt[i] = c.Lt[i]; sm.lv[i] = c.lvf[i]; }
+  for (int i = tid; i < NM * K; i += T) sm.Lr[i] = c.rates[i / K] * c.lam[i % K];
   if (tid < K) sm.statd[tid] = c.statd[tid];
   long long esum = 0;
   const long qo = (long)q * c.S;
-  for (int i = tid; i < Sq; i += kTrialThreads) {
+  for (int i = tid; i < Sq; i += T) {
     int s = c.reind[qo + i];
     sm.code[i] = c.mcode[qo + i];
     if (c.gcat) sm.cat[i] = c.site_cat[s];
@@ -645,11 +644,11 @@ __global__ void __launch_bounds__(kTrialThreads, 1) k_trials(TrialCtx c, const T
     }
   }
   esum = warp_sum_ll(esum);
-  __shared__ long long s_esum[kTrialWarps];
+  __shared__ long long s_esum[(T / 32)];
   if (lane == 0) s_esum[warp] = esum;
   __syncthreads();
   long long etot = 0;
-  for (int i = 0; i < kTrialWarps; i++) etot += s_esum[i];
+  for (int i = 0; i < (T / 32); i++) etot += s_esum[i];
 
   Optimiser opt;
   if (warp == 0) {
@@ -686,7 +685,7 @@ __global__ void __launch_bounds__(kTrialThreads, 1) k_trials(TrialCtx c, const T
     const bool derivs = ctl.cmd == 2;
     // exp factors of (dist, prox, pend), spread over all threads
 
-    for (int i = tid; i < 3 * NM * K; i += kTrialThreads) {
+    for (int i = tid; i < 3 * NM * K; i += T) {
       int wh = i / (NM * K), mk = i - wh * NM * K;
       float t = wh == 0 ? ctl.dist : (wh == 1 ? ctl.prox : ctl.pend);
       float a = sm.Lr[mk] * t;
@@ -697,7 +696,7 @@ __global__ void __launch_bounds__(kTrialThreads, 1) k_trials(TrialCtx c, const T
     // ---- P(t) = I + X diag(expm1(r lambda t)) X^-T and derivatives; query vectors ----
     const float *W = K == 4 ? sm.W : c.W;
     const int nmat = NM * K * K;
-    for (int i = tid; i < 2 * nmat; i += kTrialThreads) {
+    for (int i = tid; i < 2 * nmat; i += T) {
       int wh = i / nmat, r = i - wh * nmat;
       int m = r / (K * K), ij = r - m * K * K;
       int ii = ij / K, jj = ij - ii * K;
@@ -722,7 +721,7 @@ __global__ void __launch_bounds__(kTrialThreads, 1) k_trials(TrialCtx c, const T
       }
     }
     const int nz = NM * nc * K;
-    for (int i = tid; i < nz; i += kTrialThreads) {
+    for (int i = tid; i < nz; i += T) {
       int m = i / (nc * K), ck = i - m * nc * K;
       int code = ck / K, ii = ck - code * K;
       const float *x = sm.X + ii * K;
@@ -752,11 +751,11 @@ __global__ void __launch_bounds__(kTrialThreads, 1) k_trials(TrialCtx c, const T
     SiteAcc acc;
     acc.init();
     if (K == 4 && !c.gcat) {
-      if (derivs) sites_dna_gmix<true>(c, sm, q, node, Sq, acc);
-      else sites_dna_gmix<false>(c, sm, q, node, Sq, acc);
+      if (derivs) sites_dna_gmix<T, true>(c, sm, q, node, Sq, acc);
+      else sites_dna_gmix<T, false>(c, sm, q, node, Sq, acc);
     } else {
-      if (derivs) sites_generic<K, true>(c, sm, q, node, Sq, acc);
-      else sites_generic<K, false>(c, sm, q, node, Sq, acc);
+      if (derivs) sites_generic<K, T, true>(c, sm, q, node, Sq, acc);
+      else sites_generic<K, T, false>(c, sm, q, node, Sq, acc);
     }
     for (int o = 16; o > 0; o >>= 1) {
       float mo = __shfl_down_sync(0xffffffffu, acc.m, o);
@@ -780,14 +779,14 @@ __global__ void __launch_bounds__(kTrialThreads, 1) k_trials(TrialCtx c, const T
     __syncthreads();  // C
     if (warp == 0) {
       // lanes 0..warps-1 hold one warp's partials; shuffle tree
-      bool have = lane < kTrialWarps;
+      bool have = lane < (T / 32);
       float mt = have ? sm.red[lane * 8] : 1.f;
       int et = have ? sm.redi[lane] : 0;
       float sg[5];
 #pragma unroll
       for (int k = 0; k < 5; k++) sg[k] = have ? sm.red[lane * 8 + 1 + k] : 0.f;
 #pragma unroll
-      for (int o = kTrialWarps / 2; o > 0; o >>= 1) {
+      for (int o = (T / 32) / 2; o > 0; o >>= 1) {
         float mo = __shfl_xor_sync(0xffffffffu, mt, o);
         int eo = __shfl_xor_sync(0xffffffffu, et, o);
         mt *= mo;

@@ -130,6 +130,15 @@ class Engine:
         return [dict(like=t.like, pend=t.pend, dist=t.dist, derivs=list(t.derivs), status=t.status,
                      n_evals=t.n_evals) for t in tout[:n]]
 
+    def autotune(self, prefs=None):
+        """Pick the trial-kernel shape per query-length bin on the loaded queries."""
+        prefs = prefs or default_prefs()
+        _L.check(_L.load().pgb_engine_autotune(self.h, C.byref(prefs)), "pgb_engine_autotune")
+        th = np.zeros(6, dtype=np.int32)
+        wi = np.zeros(6, dtype=np.int32)
+        _L.check(_L.load().pgb_engine_get_tuning(self.h, th.ctypes.data, wi.ctypes.data), "pgb_engine_get_tuning")
+        return list(th), list(wi)
+
     def timings(self):
         ms = np.zeros(6)
         cnt = np.zeros(8)
