@@ -500,6 +500,7 @@ __global__ void k_rank(const double *__restrict__ scores, int n_edges, int rk, c
 }
 
 #include "trials.cuh"
+#include "trials_warp.cuh"
 
 // ---------------------------------------------------------------------------
 // Baseball (core.ml:429-464) and keep / refine / like_weight_ratio
@@ -961,9 +962,43 @@ pgb_status launch_trials_kt(pgb_engine *e, cudaStream_t st, TrialCtx c, const in
   return PGB_OK;
 }
 
+// the warp-per-trial kernel covers nucleotide Gamma mixtures of 1, 2, 4 or 8 rates
+bool warp_trials_ok(const pgb_engine *e) {
+  return e->K == 4 && !e->gcat && e->NM == e->RP && (e->RP == 1 || e->RP == 2 || e->RP == 4 || e->RP == 8);
+}
+
+template <int RP>
+pgb_status launch_trials_warp_rp(pgb_engine *e, cudaStream_t st, TrialCtx c, const int *d_order, int n,
+                                 TrialRes *out) {
+  size_t smem = warp_trial_smem_bytes(e->NM, e->ncode);
+  if (smem > e->smem_optin) { set_error("warp trial shared memory %zu exceeds %zu", smem, e->smem_optin); return PGB_ERR_ARG; }
+  PGB_CUDA(cudaFuncSetAttribute(k_trials_warp<RP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int grid = (n + kWarpTrialWarps - 1) / kWarpTrialWarps;
+  k_trials_warp<RP><<<grid, 32 * kWarpTrialWarps, smem, st>>>(c, e->d_trials, d_order, n, out);
+  PGB_LAUNCH_CHECK();
+  return PGB_OK;
+}
+
+pgb_status launch_trials_warp(pgb_engine *e, cudaStream_t st, TrialCtx c, const int *d_order, int n, TrialRes *out) {
+  c.smem_win = 0;
+  c.cap = 0;
+  switch (e->RP) {
+    case 1: return launch_trials_warp_rp<1>(e, st, c, d_order, n, out);
+    case 2: return launch_trials_warp_rp<2>(e, st, c, d_order, n, out);
+    case 4: return launch_trials_warp_rp<4>(e, st, c, d_order, n, out);
+    default: return launch_trials_warp_rp<8>(e, st, c, d_order, n, out);
+  }
+}
+
+// threads: 32 selects the warp-per-trial kernel where it applies, else the
+// CTA-per-trial kernel with 128 or 256 threads
 pgb_status launch_trials(pgb_engine *e, cudaStream_t st, TrialCtx c, const int *d_order, int n, int cap, bool win,
                          TrialRes *out, int threads) {
   if (n <= 0) return PGB_OK;
+  if (threads == 32) {
+    if (warp_trials_ok(e)) return launch_trials_warp(e, st, c, d_order, n, out);
+    threads = 256;
+  }
   if (e->K == 4)
     return threads == 128 ? launch_trials_kt<4, 128>(e, st, c, d_order, n, cap, win, out)
                           : launch_trials_kt<4, 256>(e, st, c, d_order, n, cap, win, out);
@@ -1114,6 +1149,8 @@ pgb_status pgb_engine_create(const pgb_model_desc *m, const pgb_tree_desc *t, pg
   cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, e->device);
   cudaDeviceGetAttribute(&e->n_sm, cudaDevAttrMultiProcessorCount, e->device);
   e->smem_optin = (size_t)optin;
+  if (warp_trials_ok(e))  // one warp per trial unless the autotuner finds better
+    for (int b = 0; b < kBins; b++) { e->tune_threads[b] = 32; e->tune_win[b] = 0; }
   for (int i = 0; i < 8; i++) cudaEventCreate(&e->ev[i]);
   for (int i = 0; i < 8; i++) cudaStreamCreateWithFlags(&e->bin_st[i], cudaStreamNonBlocking);
   for (int i = 0; i < 9; i++) cudaEventCreateWithFlags(&e->bin_ev[i], cudaEventDisableTiming);
@@ -1560,16 +1597,18 @@ pgb_status pgb_engine_autotune(pgb_engine *e, const pgb_prefs *p) {
   PGB_CUDA(cudaStreamSynchronize(e->st));
   TrialCtx tc = trial_ctx(e, p, p->optimizer, 0);
   tc.stats = nullptr;
-  const int cand_threads[2] = {256, 128};
+  const int cand_threads[3] = {32, 256, 128};
+  const int n_cand = warp_trials_ok(e) ? 3 : 2, c0 = warp_trials_ok(e) ? 0 : 1;
   for (int b = 0; b < kBins; b++) {
     int n = got[2 + b];
     if (n == 0) continue;
     float best = 1e30f;
     int bt = e->tune_threads[b], bw = e->tune_win[b];
-    for (int ti = 0; ti < 2; ti++)
+    for (int ti = c0; ti < c0 + n_cand && ti < 3; ti++)
       for (int w = 1; w >= 0; w--) {
         int cap;
         bool win;
+        if (cand_threads[ti] == 32 && w == 1) continue;  // the warp kernel reads windows from L2
         bin_shape(e, b, max_sq, w, &cap, &win);
         if (w == 1 && !win) continue;  // window does not fit: same as w == 0
         float ms_best = 1e30f;
@@ -1589,12 +1628,53 @@ pgb_status pgb_engine_autotune(pgb_engine *e, const pgb_prefs *p) {
     e->tune_threads[b] = bt;
     e->tune_win[b] = bw;
   }
+  // In a run the bins execute concurrently, so a form that loses on a bin
+  // alone can win on the whole round (its tail overlaps the other bins).
+  // Time the whole round for the per-bin choice and for each uniform form.
+  int per_bin_t[kBins], per_bin_w[kBins];
+  for (int b = 0; b < kBins; b++) { per_bin_t[b] = e->tune_threads[b]; per_bin_w[b] = e->tune_win[b]; }
+  const int uni_t[3] = {32, 128, 256}, uni_w[3] = {0, 1, 1};
+  float best = 1e30f;
+  int best_cfg = -1;
+  for (int cfg = -1; cfg < 3; cfg++) {
+    if (cfg == 0 && !warp_trials_ok(e)) continue;
+    for (int b = 0; b < kBins; b++) {
+      e->tune_threads[b] = cfg < 0 ? per_bin_t[b] : uni_t[cfg];
+      e->tune_win[b] = cfg < 0 ? per_bin_w[b] : uni_w[cfg];
+    }
+    float ms_best = 1e30f;
+    for (int rep = 0; rep < 2; rep++) {
+      PGB_CUDA(cudaEventRecord(e->ev[6], e->st));
+      if ((s = run_bins(e, tc, got + 2, max_sq))) return s;
+      PGB_CUDA(cudaEventRecord(e->ev[7], e->st));
+      PGB_CUDA(cudaEventSynchronize(e->ev[7]));
+      float ms;
+      cudaEventElapsedTime(&ms, e->ev[6], e->ev[7]);
+      ms_best = std::min(ms_best, ms);
+    }
+    if (ms_best < best) { best = ms_best; best_cfg = cfg; }
+  }
+  for (int b = 0; b < kBins; b++) {
+    e->tune_threads[b] = best_cfg < 0 ? per_bin_t[b] : uni_t[best_cfg];
+    e->tune_win[b] = best_cfg < 0 ? per_bin_w[b] : uni_w[best_cfg];
+  }
   return PGB_OK;
 }
 
 pgb_status pgb_engine_get_tuning(pgb_engine *e, int *threads, int *smem_windows) {
   if (!e) return PGB_ERR_ARG;
   for (int b = 0; b < kBins; b++) { threads[b] = e->tune_threads[b]; smem_windows[b] = e->tune_win[b]; }
+  return PGB_OK;
+}
+
+pgb_status pgb_engine_set_tuning(pgb_engine *e, const int *threads, const int *smem_windows) {
+  if (!e || !threads || !smem_windows) { set_error("set_tuning: null argument"); return PGB_ERR_ARG; }
+  for (int b = 0; b < kBins; b++)
+    if ((threads[b] != 32 && threads[b] != 128 && threads[b] != 256) || (smem_windows[b] & ~1)) {
+      set_error("set_tuning: bin %d: threads must be 32, 128 or 256 and smem_windows 0 or 1", b);
+      return PGB_ERR_ARG;
+    }
+  for (int b = 0; b < kBins; b++) { e->tune_threads[b] = threads[b]; e->tune_win[b] = smem_windows[b]; }
   return PGB_OK;
 }
 

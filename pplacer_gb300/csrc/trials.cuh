@@ -153,7 +153,7 @@ struct Optimiser {
   double xl, xu, xm, fl, fu, fm, v, w, fv, fw, bd, be, u, fz, z, probe_dx, fval, fx;
   bool probe;
   // Newton state
-  int it, ls;
+  int it, ls, stall;
   float p, d, sp, sd, np, nd, allow, pred;
   bool accepted;
   EvalOut cur;
@@ -357,6 +357,7 @@ struct Optimiser {
           return false;
         }
         allow = 1e-6f + 1e-9f * fabsf((float)L_last);
+        stall = 0;
         for (it = 0; it < 60; it++) {
           {
             const float pmin = 1e-8f, pmax = (float)max_pend, dmax = (float)cut;
@@ -374,9 +375,18 @@ struct Optimiser {
               if (free_p) sp = hpp < 0.f ? -gp / hpp : copysignf(fmaxf(0.5f * p, 0.01f), gp);
               if (free_d) sd = hdd < 0.f ? -gd / hdd : copysignf(0.25f * dmax, gd);
             }
+            // Trust region: one factor for both coordinates, so the step
+            // keeps the direction of the Newton (or diagonal) step, which is
+            // an ascent direction.  Clipping each coordinate on its own can
+            // turn it downhill -- on short edges the distal limit is tiny
+            // while the pendant step is not -- and the line search then
+            // shrinks it to nothing, iteration after iteration.
             float lim_p = fmaxf(2.f * p, 0.05f), lim_d = fmaxf(0.5f * dmax, 1e-12f);
-            if (fabsf(sp) > lim_p) sp = copysignf(lim_p, sp);
-            if (fabsf(sd) > lim_d) sd = copysignf(lim_d, sd);
+            float f = 1.f;
+            if (fabsf(sp) > lim_p) f = fminf(f, lim_p / fabsf(sp));
+            if (fabsf(sd) > lim_d) f = fminf(f, lim_d / fabsf(sd));
+            sp *= f;
+            sd *= f;
             pred = gp * sp + gd * sd;
           }
           accepted = false;
@@ -395,11 +405,15 @@ struct Optimiser {
           }
           if (!accepted) break;
           {
+            // three accepted steps in a row that gain less than the
+            // evaluation's rounding allowance: the objective's noise floor
+            float gain = dlogl(last, cur);
             float step = fmaxf(fabsf(np - p), fabsf(nd - d));
             p = np;
             d = nd;
             cur = last;
-            if (fabsf(pred) < newton_gain_tol() + allow || step < 1e-9f) break;
+            stall = gain < allow ? stall + 1 : 0;
+            if (fabsf(pred) < newton_gain_tol() + allow || step < 1e-9f || stall >= 3) break;
           }
           if (it == 59) status = ST_MAXITER;
         }
@@ -417,6 +431,81 @@ struct Optimiser {
 #undef PGB_YIELD
 
 // ---------------------------------------------------------------------------
+// Per-evaluation tables, shared by the CTA and the warp kernels.  Threads
+// i0, i0 + stride, ... of the group fill them; the caller synchronises the
+// group between trial_exps and trial_tables and before the sites read them.
+// ---------------------------------------------------------------------------
+
+// exp / expm1 of rate * lambda * t for t = dist, prox, pend: E, Em1 [3][NM][K]
+__device__ __forceinline__ void trial_exps(const TrialSmem &sm, int NM, int K, const Ctrl &ctl, int i0, int stride) {
+  for (int i = i0; i < 3 * NM * K; i += stride) {
+    int wh = i / (NM * K), mk = i - wh * NM * K;
+    float t = wh == 0 ? ctl.dist : (wh == 1 ? ctl.prox : ctl.pend);
+    float a = sm.Lr[mk] * t;
+    sm.E[i] = expf(a);
+    sm.Em1[i] = expm1f(a);
+  }
+}
+
+// P(t) = I + X diag(expm1(r lambda t)) X^-T for the distal and proximal
+// lengths, its first and second derivatives, and the statd-weighted evolved
+// query vectors Z (and d/dpend, d2/dpend2) of every character code.
+__device__ __forceinline__ void trial_tables(const TrialSmem &sm, const float *W, int NM, int nc, int K, bool derivs,
+                                             int i0, int stride) {
+  const int nmat = NM * K * K;
+  for (int i = i0; i < 2 * nmat; i += stride) {
+    int wh = i / nmat, r = i - wh * nmat;
+    int m = r / (K * K), ij = r - m * K * K;
+    int ii = ij / K, jj = ij - ii * K;
+    const float *w = W + (long)ij * K;
+    const float *em = sm.Em1 + (wh * NM + m) * K;
+    float a = (ii == jj) ? 1.f : 0.f;
+#pragma unroll 4
+    for (int k = 0; k < K; k++) a = fmaf(w[k], em[k], a);
+    (wh == 0 ? sm.Md : sm.Mp)[r] = a;
+    if (derivs) {
+      const float *e = sm.E + (wh * NM + m) * K;
+      const float *lr = sm.Lr + m * K;
+      float a1 = 0.f, a2 = 0.f;
+#pragma unroll 4
+      for (int k = 0; k < K; k++) {
+        float t1 = w[k] * lr[k] * e[k];
+        a1 += t1;
+        a2 = fmaf(t1, lr[k], a2);
+      }
+      (wh == 0 ? sm.Md1 : sm.Mp1)[r] = a1;
+      (wh == 0 ? sm.Md2 : sm.Mp2)[r] = a2;
+    }
+  }
+  const int nz = NM * nc * K;
+  for (int i = i0; i < nz; i += stride) {
+    int m = i / (nc * K), ck = i - m * nc * K;
+    int code = ck / K, ii = ck - code * K;
+    const float *x = sm.X + ii * K;
+    const float *lt = sm.Lt + code * K;
+    const float *em = sm.Em1 + (2 * NM + m) * K;
+    float a = sm.lv[code * K + ii];
+#pragma unroll 4
+    for (int k = 0; k < K; k++) a = fmaf(x[k] * em[k], lt[k], a);
+    float pi = sm.statd[ii];
+    sm.Z[i] = pi * a;
+    if (derivs) {
+      const float *e = sm.E + (2 * NM + m) * K;
+      const float *lr = sm.Lr + m * K;
+      float a1 = 0.f, a2 = 0.f;
+#pragma unroll 4
+      for (int k = 0; k < K; k++) {
+        float t1 = x[k] * lr[k] * e[k] * lt[k];
+        a1 += t1;
+        a2 = fmaf(t1, lr[k], a2);
+      }
+      sm.Z1[i] = pi * a1;
+      sm.Z2[i] = pi * a2;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
 // The kernel
 // ---------------------------------------------------------------------------
 
@@ -427,16 +516,30 @@ struct SiteAcc {
   int e;
   float gp, gd, hpp, hdd, hpd;
   __device__ void init() { m = 1.f; e = 0; gp = gd = hpp = hdd = hpd = 0.f; }
-  __device__ void add(float u, float ud, float udd, float up, float upp, float upd, bool derivs) {
-    int eu;
-    float mu = frexpf(u, &eu);
+  __device__ __forceinline__ void add(float u, float ud, float udd, float up, float upp, float upd, bool derivs) {
+    // u = 2^eu * mu with mu in [0.5, 1): read from the bits for positive
+    // normal u; zero, subnormal, negative and non-finite u take frexpf and a
+    // full division, so a zero or NaN site still reaches the product.
+    const unsigned bu = __float_as_uint(u);
+    float mu, inv = 0.f;
+    if ((bu >> 23) - 1u < 254u) {
+      e += (int)(bu >> 23) - 126;
+      mu = __uint_as_float((bu & 0x007fffffu) | 0x3f000000u);
+      if (derivs) inv = __fdividef(1.f, u);
+    } else {
+      int eu;
+      mu = frexpf(u, &eu);
+      e += eu;
+      if (derivs) inv = 1.f / u;
+    }
+    // m, mu in [0.5, 1): the product is a positive normal number or zero
     m *= mu;
-    e += eu;
-    int em;
-    m = frexpf(m, &em);
-    e += em;
+    const unsigned bm = __float_as_uint(m);
+    if (bm != 0u && (bm >> 23) < 255u) {
+      e += (int)(bm >> 23) - 126;
+      m = __uint_as_float((bm & 0x007fffffu) | 0x3f000000u);
+    }
     if (derivs) {
-      float inv = 1.f / u;
       float lp = up * inv, ld = ud * inv;
       gp += lp;
       gd += ld;
@@ -683,69 +786,9 @@ __global__ void __launch_bounds__(T, 1) k_trials(TrialCtx c, const TrialIn *__re
     const Ctrl ctl = *sm.ctrl;
     if (ctl.cmd == 0) break;
     const bool derivs = ctl.cmd == 2;
-    // exp factors of (dist, prox, pend), spread over all threads
-
-    for (int i = tid; i < 3 * NM * K; i += T) {
-      int wh = i / (NM * K), mk = i - wh * NM * K;
-      float t = wh == 0 ? ctl.dist : (wh == 1 ? ctl.prox : ctl.pend);
-      float a = sm.Lr[mk] * t;
-      sm.E[i] = expf(a);
-      sm.Em1[i] = expm1f(a);
-    }
+    trial_exps(sm, NM, K, ctl, tid, T);
     __syncthreads();  // A2: exp factors
-    // ---- P(t) = I + X diag(expm1(r lambda t)) X^-T and derivatives; query vectors ----
-    const float *W = K == 4 ? sm.W : c.W;
-    const int nmat = NM * K * K;
-    for (int i = tid; i < 2 * nmat; i += T) {
-      int wh = i / nmat, r = i - wh * nmat;
-      int m = r / (K * K), ij = r - m * K * K;
-      int ii = ij / K, jj = ij - ii * K;
-      const float *w = W + (long)ij * K;
-      const float *em = sm.Em1 + (wh * NM + m) * K;
-      float a = (ii == jj) ? 1.f : 0.f;
-#pragma unroll 4
-      for (int k = 0; k < K; k++) a = fmaf(w[k], em[k], a);
-      (wh == 0 ? sm.Md : sm.Mp)[r] = a;
-      if (derivs) {
-        const float *e = sm.E + (wh * NM + m) * K;
-        const float *lr = sm.Lr + m * K;
-        float a1 = 0.f, a2 = 0.f;
-#pragma unroll 4
-        for (int k = 0; k < K; k++) {
-          float t1 = w[k] * lr[k] * e[k];
-          a1 += t1;
-          a2 = fmaf(t1, lr[k], a2);
-        }
-        (wh == 0 ? sm.Md1 : sm.Mp1)[r] = a1;
-        (wh == 0 ? sm.Md2 : sm.Mp2)[r] = a2;
-      }
-    }
-    const int nz = NM * nc * K;
-    for (int i = tid; i < nz; i += T) {
-      int m = i / (nc * K), ck = i - m * nc * K;
-      int code = ck / K, ii = ck - code * K;
-      const float *x = sm.X + ii * K;
-      const float *lt = sm.Lt + code * K;
-      const float *em = sm.Em1 + (2 * NM + m) * K;
-      float a = sm.lv[code * K + ii];
-#pragma unroll 4
-      for (int k = 0; k < K; k++) a = fmaf(x[k] * em[k], lt[k], a);
-      float pi = sm.statd[ii];
-      sm.Z[i] = pi * a;
-      if (derivs) {
-        const float *e = sm.E + (2 * NM + m) * K;
-        const float *lr = sm.Lr + m * K;
-        float a1 = 0.f, a2 = 0.f;
-#pragma unroll 4
-        for (int k = 0; k < K; k++) {
-          float t1 = x[k] * lr[k] * e[k] * lt[k];
-          a1 += t1;
-          a2 = fmaf(t1, lr[k], a2);
-        }
-        sm.Z1[i] = pi * a1;
-        sm.Z2[i] = pi * a2;
-      }
-    }
+    trial_tables(sm, K == 4 ? sm.W : c.W, NM, nc, K, derivs, tid, T);
     __syncthreads();  // B
     // ---- sites ----
     SiteAcc acc;

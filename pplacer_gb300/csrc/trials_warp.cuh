@@ -1,0 +1,339 @@
+// Stage-2 trials, one WARP per (query, location) optimisation: the form for
+// nucleotide models with Gamma rate mixtures (K = 4, RP = 1, 2, 4 or 8 rates).
+// Included by engine.cu after trials.cuh, inside its anonymous namespace.
+//
+// The CTA-per-trial kernel (trials.cuh) stages the query's sites in shared
+// memory and evaluates them with all the CTA's warps; between evaluations
+// the optimiser step, the exp factors and the matrices are short serial
+// phases that leave most warps waiting at block barriers.  Here each warp
+// owns a whole trial, so those phases of one trial overlap the site loops of
+// the other trials resident on the SM, and no block barrier is taken after
+// the prologue.  The windows are read from global memory in every
+// evaluation, streamed by cp.async into a per-warp ring of kWarpRing
+// iterations, so each lane has that many site loads in flight without
+// holding them in registers.
+//
+// Lane layout: lane = slot * RP + r.  A lane evaluates rate r of sites
+// slot, slot + 32 / RP, ...; it holds rate r's six 4x4 matrices in
+// registers for the whole evaluation.  The RP lanes of a site add their rate
+// terms with shuffles: for 2 and 4 rates a reduce-scatter over RP
+// consecutive iterations leaves each lane one whole site per group to
+// accumulate; for 8 rates an all-reduce, lane r == 0 accumulating; a single
+// rate needs none.  The evaluation's final xor all-reduce leaves the
+// warp's sums identical in every lane, so every lane runs the same optimiser
+// step; the request is still broadcast from lane 0 so control flow stays
+// uniform by construction.
+
+constexpr int kWarpTrialWarps = 1;  // warps (trials) per CTA
+constexpr int kWarpTrialMinCtas = 11;  // resident CTAs per SM: at most 186 registers
+constexpr int kWarpRing = 8;        // site iterations in flight per warp
+
+__host__ __device__ inline size_t warp_trial_const_floats(int NM, int ncode) {
+  return 16 + 64 + 2 * (size_t)ncode * 4 + 4 + (size_t)NM * 4;
+}
+__host__ __device__ inline size_t warp_trial_table_floats(int NM, int ncode) {
+  return 6 * (size_t)NM * 16 + 3 * (size_t)NM * ncode * 4 + 2 * 3 * (size_t)NM * 4;
+}
+// per warp: its tables, then the ring of D / P float4s [2][kWarpRing][32]
+__host__ __device__ inline size_t warp_trial_warp_bytes(int NM, int ncode) {
+  return align16(4 * warp_trial_table_floats(NM, ncode)) + 2 * kWarpRing * 32 * 16;
+}
+__host__ __device__ inline size_t warp_trial_smem_bytes(int NM, int ncode) {
+  return align16(4 * warp_trial_const_floats(NM, ncode)) + kWarpTrialWarps * warp_trial_warp_bytes(NM, ncode);
+}
+
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+  unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+// sites of one evaluation; the lane's partial (mantissa, exponent) product
+// and derivative sums accumulate into acc (lanes r == 0 only)
+template <int RP, bool DER>
+__device__ __forceinline__ void sites_warp(const TrialCtx &c, const TrialSmem &sm, float4 *ring, int q, int node,
+                                           int Sq, int lane, SiteAcc &acc) {
+  constexpr int K = 4, SPW = 32 / RP;
+  const int r = lane & (RP - 1), slot = lane / RP, nc = c.ncode;
+  float md[16], mp[16], md1[DER ? 16 : 1], md2[DER ? 16 : 1], mp1[DER ? 16 : 1], mp2[DER ? 16 : 1];
+#pragma unroll
+  for (int t = 0; t < 16; t += 4) {
+    float4 a = *reinterpret_cast<const float4 *>(sm.Md + r * 16 + t);
+    float4 b = *reinterpret_cast<const float4 *>(sm.Mp + r * 16 + t);
+    md[t] = a.x; md[t + 1] = a.y; md[t + 2] = a.z; md[t + 3] = a.w;
+    mp[t] = b.x; mp[t + 1] = b.y; mp[t + 2] = b.z; mp[t + 3] = b.w;
+    if (DER) {
+      float4 c1 = *reinterpret_cast<const float4 *>(sm.Md1 + r * 16 + t);
+      float4 c2 = *reinterpret_cast<const float4 *>(sm.Md2 + r * 16 + t);
+      float4 e1 = *reinterpret_cast<const float4 *>(sm.Mp1 + r * 16 + t);
+      float4 e2 = *reinterpret_cast<const float4 *>(sm.Mp2 + r * 16 + t);
+      md1[t] = c1.x; md1[t + 1] = c1.y; md1[t + 2] = c1.z; md1[t + 3] = c1.w;
+      md2[t] = c2.x; md2[t + 1] = c2.y; md2[t + 2] = c2.z; md2[t + 3] = c2.w;
+      mp1[t] = e1.x; mp1[t + 1] = e1.y; mp1[t + 2] = e1.z; mp1[t + 3] = e1.w;
+      mp2[t] = e2.x; mp2[t + 1] = e2.y; mp2[t + 2] = e2.z; mp2[t + 3] = e2.w;
+    }
+  }
+  const float *gd = c.darr + (long)node * c.S * RP * K + r * K;
+  const float *gp = c.parr + (long)node * c.S * RP * K + r * K;
+  const uint16_t *ri = c.reind + (long)q * c.S;
+  const uint8_t *mc = c.mcode + (long)q * c.S;
+  const float *Zr = sm.Z + r * nc * K, *Z1r = sm.Z1 + r * nc * K, *Z2r = sm.Z2 + r * nc * K;
+  const int last = Sq - 1;
+  // Ring stage of iteration it: it % kWarpRing; iteration it covers the
+  // sites it * SPW + slot.  Iterations past the end copy the last site and
+  // are not accumulated.  Copies run kWarpRing - 1 iterations ahead; the
+  // column of the next copy is loaded one iteration before it is issued.
+  // A lane reads back only the ring entries it copied itself, so the
+  // per-thread wait_group is the only synchronisation the ring needs.
+#pragma unroll
+  for (int k = 0; k < kWarpRing - 1; k++) {
+    int s0 = ri[min(k * SPW + slot, last)];
+    cp_async16(ring + (k * 32 + lane), gd + (long)s0 * RP * K);
+    cp_async16(ring + ((kWarpRing + k) * 32 + lane), gp + (long)s0 * RP * K);
+    cp_async_commit();
+  }
+  int col = ri[min((kWarpRing - 1) * SPW + slot, last)];
+  int code = mc[min(slot, last)];
+  int st_w = kWarpRing - 1, st_r = 0;
+  // one ring iteration: copy ahead, wait for this iteration's window entry,
+  // and the lane's six rate terms of its site
+  auto iteration = [&](int i, bool live, float *v) {
+    cp_async16(ring + (st_w * 32 + lane), gd + (long)col * RP * K);
+    cp_async16(ring + ((kWarpRing + st_w) * 32 + lane), gp + (long)col * RP * K);
+    cp_async_commit();
+    col = ri[min(i + kWarpRing * SPW, last)];
+    const int coden = mc[min(i + SPW, last)];
+    cp_async_wait<kWarpRing - 1>();  // this iteration's copies have landed
+    const float4 dcur = ring[st_r * 32 + lane];
+    const float4 pcur = ring[(kWarpRing + st_r) * 32 + lane];
+    st_w = st_w + 1 == kWarpRing ? 0 : st_w + 1;
+    st_r = st_r + 1 == kWarpRing ? 0 : st_r + 1;
+#pragma unroll
+    for (int k = 0; k < 6; k++) v[k] = 0.f;
+    if (live) {  // uniform over the warp
+      const float dv[4] = {dcur.x, dcur.y, dcur.z, dcur.w}, pv[4] = {pcur.x, pcur.y, pcur.z, pcur.w};
+      const float4 Z4 = *reinterpret_cast<const float4 *>(Zr + code * K);
+      const float z[4] = {Z4.x, Z4.y, Z4.z, Z4.w};
+      float z1[4], z2[4];
+      if (DER) {
+        float4 a = *reinterpret_cast<const float4 *>(Z1r + code * K);
+        float4 b = *reinterpret_cast<const float4 *>(Z2r + code * K);
+        z1[0] = a.x; z1[1] = a.y; z1[2] = a.z; z1[3] = a.w;
+        z2[0] = b.x; z2[1] = b.y; z2[2] = b.z; z2[3] = b.w;
+      }
+#pragma unroll
+      for (int ii = 0; ii < 4; ii++) {
+        float x = 0.f, y = 0.f;
+#pragma unroll
+        for (int jj = 0; jj < 4; jj++) {
+          x = fmaf(md[ii * 4 + jj], dv[jj], x);
+          y = fmaf(mp[ii * 4 + jj], pv[jj], y);
+        }
+        float xy = x * y;
+        v[0] = fmaf(z[ii], xy, v[0]);
+        if (DER) {
+          float x1 = 0.f, x2 = 0.f, y1 = 0.f, y2 = 0.f;
+#pragma unroll
+          for (int jj = 0; jj < 4; jj++) {
+            x1 = fmaf(md1[ii * 4 + jj], dv[jj], x1);
+            x2 = fmaf(md2[ii * 4 + jj], dv[jj], x2);
+            y1 = fmaf(mp1[ii * 4 + jj], pv[jj], y1);
+            y2 = fmaf(mp2[ii * 4 + jj], pv[jj], y2);
+          }
+          float aa = x1 * y - x * y1;
+          float bb = x2 * y - 2.f * x1 * y1 + x * y2;
+          v[1] = fmaf(z[ii], aa, v[1]);
+          v[2] = fmaf(z[ii], bb, v[2]);
+          v[3] = fmaf(z1[ii], xy, v[3]);
+          v[4] = fmaf(z2[ii], xy, v[4]);
+          v[5] = fmaf(z1[ii], aa, v[5]);
+        }
+      }
+    }
+    code = coden;
+  };
+  constexpr int NV = DER ? 6 : 1;
+  if (RP == 2 || RP == 4) {
+    // Reduce-scatter over groups of RP iterations: after the exchange lane r
+    // holds the rate sum of its slot's site in iteration r of the group, so
+    // every lane accumulates one site per group.  Stage xor 1 pairs
+    // iterations (0, 1) and (2, 3); stage xor 2 pairs the two halves.
+    const bool b0 = r & 1, b1 = (r >> 1) & 1;
+    for (int base = 0; base < Sq; base += RP * SPW) {
+      float h[2][6];
+#pragma unroll
+      for (int half = 0; half < RP / 2; half++) {
+        float v0[6], v1[6];
+        const int i0 = base + (2 * half) * SPW + slot;
+        iteration(i0, i0 - slot < Sq, v0);
+        iteration(i0 + SPW, i0 + SPW - slot < Sq, v1);
+#pragma unroll
+        for (int k = 0; k < NV; k++) {
+          float keep = b0 ? v1[k] : v0[k], send = b0 ? v0[k] : v1[k];
+          h[half][k] = keep + __shfl_xor_sync(0xffffffffu, send, 1);
+        }
+      }
+      float f[6];
+#pragma unroll
+      for (int k = 0; k < NV; k++) {
+        if (RP == 4) {
+          float keep = b1 ? h[1][k] : h[0][k], send = b1 ? h[0][k] : h[1][k];
+          f[k] = keep + __shfl_xor_sync(0xffffffffu, send, 2);
+        } else {
+          f[k] = h[0][k];
+        }
+      }
+      if (base + r * SPW + slot < Sq) acc.add(f[0], f[1], f[2], f[3], f[4], f[5], DER);
+    }
+  } else {
+    // RP = 1: a lane's site needs no exchange; RP = 8: xor all-reduce of
+    // the site's rate terms, lane r == 0 accumulates
+    for (int base = 0; base < Sq; base += SPW) {
+      float v[6];
+      iteration(base + slot, true, v);
+#pragma unroll
+      for (int o = 1; o < RP; o <<= 1)
+#pragma unroll
+        for (int k = 0; k < NV; k++) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+      if (r == 0 && base + slot < Sq) acc.add(v[0], v[1], v[2], v[3], v[4], v[5], DER);
+    }
+  }
+  cp_async_wait<0>();  // drain the copies issued past the end
+}
+
+template <int RP>
+__global__ void __launch_bounds__(32 * kWarpTrialWarps, kWarpTrialMinCtas)
+    k_trials_warp(TrialCtx c, const TrialIn *__restrict__ trials, const int *__restrict__ order, int n,
+                  TrialRes *out) {
+  constexpr int K = 4;
+  extern __shared__ __align__(16) char t_smem[];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int NM = c.NM, nc = c.ncode;
+  // ---- CTA constants, then one barrier; the warps are independent after it ----
+  float *cst = reinterpret_cast<float *>(t_smem);
+  TrialSmem sm{};
+  sm.X = cst;
+  sm.W = cst + 16;
+  sm.Lt = cst + 80;
+  sm.lv = sm.Lt + nc * K;
+  sm.statd = sm.lv + nc * K;
+  sm.Lr = sm.statd + 4;
+  for (int i = tid; i < 16; i += blockDim.x) sm.X[i] = c.X[i];
+  for (int i = tid; i < 64; i += blockDim.x) sm.W[i] = c.W[i];
+  for (int i = tid; i < nc * K; i += blockDim.x) { sm.Lt[i] = c.Lt[i]; sm.lv[i] = c.lvf[i]; }
+  for (int i = tid; i < NM * K; i += blockDim.x) sm.Lr[i] = c.rates[i / K] * c.lam[i % K];
+  if (tid < K) sm.statd[tid] = c.statd[tid];
+  float4 *ring;
+  {
+    char *wb = t_smem + align16(4 * warp_trial_const_floats(NM, nc)) + warp * warp_trial_warp_bytes(NM, nc);
+    float *tb = reinterpret_cast<float *>(wb);
+    ring = reinterpret_cast<float4 *>(wb + align16(4 * warp_trial_table_floats(NM, nc)));
+    const int mb = NM * 16, zb = NM * nc * K;
+    sm.Md = tb; sm.Mp = tb + mb; sm.Md1 = tb + 2 * mb; sm.Md2 = tb + 3 * mb; sm.Mp1 = tb + 4 * mb;
+    sm.Mp2 = tb + 5 * mb;
+    sm.Z = tb + 6 * mb; sm.Z1 = sm.Z + zb; sm.Z2 = sm.Z1 + zb;
+    sm.E = sm.Z2 + zb; sm.Em1 = sm.E + 3 * NM * K;
+  }
+  __syncthreads();
+  const int t = blockIdx.x * kWarpTrialWarps + warp;
+  if (t >= n) return;
+  const int ti = order ? order[t] : t;
+  const TrialIn tr = trials[ti];
+  const int q = tr.q, node = tr.node;
+  const int Sq = c.qlen[q];
+  // exponent sum of the query's sites of darr / parr[node]
+  long long esum = 0;
+  const long qo = (long)q * c.S;
+  for (int i0 = lane; i0 < Sq; i0 += 8 * 32) {  // eight gathers in flight per lane
+    int col8[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) col8[k] = i0 + 32 * k < Sq ? (int)c.reind[qo + i0 + 32 * k] : -1;
+#pragma unroll
+    for (int k = 0; k < 8; k++)
+      if (col8[k] >= 0) {
+        long go = (long)node * c.S + col8[k];
+        esum += (long long)c.dexp[go] + (long long)c.pexp[go];
+      }
+  }
+  for (int o = 16; o > 0; o >>= 1) esum += __shfl_xor_sync(0xffffffffu, esum, o);
+
+  Optimiser opt;
+  opt.optimizer = c.optimizer;
+  opt.mode = c.mode;
+  opt.cut = c.bl[node];
+  opt.tol = tr.tol;
+  opt.max_pend = c.max_pend;
+  opt.start_pend = c.start_pend;
+  opt.pend0 = tr.pend0;
+  opt.dist0 = tr.dist0;
+  opt.cst = kLn2 * (double)esum - (double)(float)Sq * c.log_nrates;
+  opt.n_evals = 0;
+  opt.pc = 0;
+  opt.L_last = NAN;
+  opt.last.ex = 0; opt.last.lm = 0.f;
+  opt.last.g[0] = opt.last.g[1] = opt.last.h[0] = opt.last.h[1] = opt.last.h[2] = 0.f;
+  EvalOut res;
+  for (int ev = 0; ev < kMaxTrialEvals; ev++) {
+    bool more = opt.next(ev == 0 ? nullptr : &res);
+    Ctrl ctl;
+    ctl.cmd = __shfl_sync(0xffffffffu, more ? (opt.req_derivs ? 2 : 1) : 0, 0);
+    if (ctl.cmd == 0) break;
+    ctl.pend = __shfl_sync(0xffffffffu, opt.req_p, 0);
+    ctl.dist = __shfl_sync(0xffffffffu, opt.req_d, 0);
+    ctl.prox = __shfl_sync(0xffffffffu, opt.req_x, 0);
+    const bool derivs = ctl.cmd == 2;
+    __syncwarp();  // the previous evaluation's sites have read the tables
+    trial_exps(sm, NM, K, ctl, lane, 32);
+    __syncwarp();
+    trial_tables(sm, sm.W, NM, nc, K, derivs, lane, 32);
+    __syncwarp();
+    SiteAcc acc;
+    acc.init();
+    if (Sq > 0) {
+      if (derivs) sites_warp<RP, true>(c, sm, ring, q, node, Sq, lane, acc);
+      else sites_warp<RP, false>(c, sm, ring, q, node, Sq, lane, acc);
+    }
+    // xor all-reduce: every lane ends with the same bits
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      float mo = __shfl_xor_sync(0xffffffffu, acc.m, o);
+      int eo = __shfl_xor_sync(0xffffffffu, acc.e, o);
+      acc.m *= mo;
+      acc.e += eo;
+      int em;
+      acc.m = frexpf(acc.m, &em);
+      acc.e += em;
+      if (derivs) {
+        acc.gp += __shfl_xor_sync(0xffffffffu, acc.gp, o);
+        acc.gd += __shfl_xor_sync(0xffffffffu, acc.gd, o);
+        acc.hpp += __shfl_xor_sync(0xffffffffu, acc.hpp, o);
+        acc.hdd += __shfl_xor_sync(0xffffffffu, acc.hdd, o);
+        acc.hpd += __shfl_xor_sync(0xffffffffu, acc.hpd, o);
+      }
+    }
+    res.ex = acc.e;
+    res.lm = logf(acc.m);
+    res.g[0] = acc.gp; res.g[1] = acc.gd;
+    res.h[0] = acc.hpp; res.h[1] = acc.hdd; res.h[2] = acc.hpd;
+  }
+  if (lane == 0) {
+    TrialRes rr;
+    rr.like = opt.L_last;
+    rr.pend = opt.pend;
+    rr.dist = opt.dist;
+    rr.der[0] = opt.last.g[0]; rr.der[1] = opt.last.g[1];
+    rr.der[2] = opt.last.h[0]; rr.der[3] = opt.last.h[1]; rr.der[4] = opt.last.h[2];
+    rr.der[5] = 0;
+    rr.status = opt.status;
+    rr.n_evals = opt.n_evals;
+    out[ti] = rr;
+    if (c.stats) {
+      atomicAdd(&c.stats[0], (unsigned long long)opt.n_evals);
+      atomicAdd(&c.stats[1], (unsigned long long)opt.n_evals * (unsigned long long)Sq);
+    }
+  }
+}

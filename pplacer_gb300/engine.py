@@ -134,10 +134,19 @@ class Engine:
         """Pick the trial-kernel shape per query-length bin on the loaded queries."""
         prefs = prefs or default_prefs()
         _L.check(_L.load().pgb_engine_autotune(self.h, C.byref(prefs)), "pgb_engine_autotune")
+        return self.get_tuning()
+
+    def get_tuning(self):
         th = np.zeros(6, dtype=np.int32)
         wi = np.zeros(6, dtype=np.int32)
         _L.check(_L.load().pgb_engine_get_tuning(self.h, th.ctypes.data, wi.ctypes.data), "pgb_engine_get_tuning")
         return list(th), list(wi)
+
+    def set_tuning(self, threads, smem_windows):
+        """Impose the trial-kernel shape per query-length bin (threads 32 = one warp per trial)."""
+        th = np.ascontiguousarray(np.broadcast_to(threads, 6), dtype=np.int32)
+        wi = np.ascontiguousarray(np.broadcast_to(smem_windows, 6), dtype=np.int32)
+        _L.check(_L.load().pgb_engine_set_tuning(self.h, th.ctypes.data, wi.ctypes.data), "pgb_engine_set_tuning")
 
     def timings(self):
         ms = np.zeros(6)

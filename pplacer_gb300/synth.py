@@ -210,6 +210,7 @@ def make_workload(name, n_queries=None, **overrides):
                        noise=0.0, gaps=0.0, cat=True, alpha=0.0, prefs=dict()),
     }
     sp = dict(specs[name])
+    sp.setdefault("n_rates", 4)
     sp.update(overrides)
     rng = np.random.default_rng(sp["seed"])
     K = sp["K"]
@@ -230,13 +231,13 @@ def make_workload(name, n_queries=None, **overrides):
         site_rate = cat_rates[site_cats]
     else:
         from scipy.special import gammaincinv, gammainc
-        a = sp["alpha"]
+        a, nr = sp["alpha"], sp["n_rates"]
         # discrete Gamma(a, a) category means (Yang 1994), mean one
-        cuts = [0.0] + [gammaincinv(a, i / 4) for i in range(1, 4)] + [np.inf]
+        cuts = [0.0] + [gammaincinv(a, i / nr) for i in range(1, nr)] + [np.inf]
         fr = [gammainc(a + 1, c) if np.isfinite(c) else 1.0 for c in cuts]
-        rates = np.array([fr[i + 1] - fr[i] for i in range(4)]) * 4
+        rates = np.array([fr[i + 1] - fr[i] for i in range(nr)]) * nr
         site_cats = None
-        site_rate = rates[rng.integers(0, 4, size=S)]
+        site_rate = rates[rng.integers(0, nr, size=S)]
     states = simulate(rng, parent, bl, Qm, statd, site_rate, S)
     alpha_arr = np.frombuffer(alphabet.encode(), dtype=np.uint8)
     is_leaf = np.ones(len(parent), dtype=bool)

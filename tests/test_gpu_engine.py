@@ -17,14 +17,20 @@ pytestmark = pytest.mark.gpu
 LOGL_RTOL = 1e-6
 
 
-@pytest.fixture(scope="module")
-def small(oracle_lib):
+# trial-kernel forms: one CTA (256 threads, windows in shared memory) or one
+# warp per trial
+FORMS = {"cta": (256, 1), "warp": (32, 0)}
+
+
+@pytest.fixture(scope="module", params=sorted(FORMS))
+def small(request, oracle_lib):
     from pplacer_gb300 import engine as E
     from pplacer_gb300 import synth
     w = synth.make_workload("cpu_small", n_queries=60)
     O = oracle_lib
     oref = O.Reference(O.Model(w.exch, w.statd, w.rates), w.parent, w.bl, w.leaf_row, w.ref_seqs)
     eng = E.engine_for_workload(w)
+    eng.set_tuning(*FORMS[request.param])
     eng.load_queries(w.query_seqs)
     return w, oref, eng
 
@@ -207,7 +213,8 @@ def test_place_all_edges_vs_oracle(small, oracle_lib, optimizer):
         assert abs(sum(p[2] for p in g) - 1.0) < 1e-9 and all(a[2] >= b[2] for a, b in zip(g, g[1:]))
 
 
-def test_place_baseball_dna(oracle_lib):
+@pytest.mark.parametrize("form", sorted(FORMS))
+def test_place_baseball_dna(oracle_lib, form):
     """dna_1k preferences (keep 7, strikes 6) on a 60-query sample.  The
     Brent replica follows the reference's search, whose path FP32 rounding can
     change, so it may end on a different coordinate-wise stopping point for
@@ -219,10 +226,30 @@ def test_place_baseball_dna(oracle_lib):
     oref = O.Reference(O.Model(w.exch, w.statd, w.rates), w.parent, w.bl, w.leaf_row, w.ref_seqs)
     ores, ost = oref.place(w.query_seqs, O.make_prefs(), n_threads=8)
     eng = E.engine_for_workload(w)
+    eng.set_tuning(*FORMS[form])
     for optimizer, frac in ((1, 1.0), (0, 0.95)):
         gres, gst = eng.place(w.query_seqs, E.default_prefs(optimizer=optimizer))
         assert list(gst) == list(ost)
         _compare_placements(O, oref, w.query_seqs, gres, ores, min_logl_frac=frac)
+
+
+@pytest.mark.parametrize("form", sorted(FORMS))
+@pytest.mark.parametrize("n_rates", [1, 2, 8])
+def test_place_rate_counts(oracle_lib, n_rates, form):
+    """Gamma mixtures of 1, 2 and 8 rates (the warp form's lane layout
+    changes with the rate count)."""
+    from pplacer_gb300 import engine as E
+    from pplacer_gb300 import synth
+    O = oracle_lib
+    w = synth.make_workload("dna_1k", n_queries=25, taxa=80, sites=400, lo=60, hi=400, n_rates=n_rates)
+    assert len(w.rates) == n_rates
+    oref = O.Reference(O.Model(w.exch, w.statd, w.rates), w.parent, w.bl, w.leaf_row, w.ref_seqs)
+    ores, ost = oref.place(w.query_seqs, O.make_prefs(), n_threads=8)
+    eng = E.engine_for_workload(w)
+    eng.set_tuning(*FORMS[form])
+    gres, gst = eng.place(w.query_seqs, E.default_prefs(optimizer=1))
+    assert list(gst) == list(ost)
+    _compare_placements(O, oref, w.query_seqs, gres, ores)
 
 
 def test_place_gcat_and_protein(oracle_lib):
@@ -267,6 +294,7 @@ def test_edge_cases(small, oracle_lib):
     O = oracle_lib
     oref2 = O.Reference(O.Model(w2.exch, w2.statd, w2.rates), w2.parent, w2.bl, w2.leaf_row, w2.ref_seqs)
     eng2 = E.engine_for_workload(w2)
+    eng2.set_tuning(*eng.get_tuning())
     eng2.load_queries(w2.query_seqs)
     got = eng2.trials([(0, 3, 0.1, 0.0, 1e-5)], optimizer=0)
     st, ref = oref2.optimize_location(w2.query_seqs[0], 3, 0.1, 0.0, 1e-5)
