@@ -237,6 +237,12 @@ pgb_status pgb_queries_fetch(pgb_engine *e, pgb_placement *out, int *n_out, int 
  * increasing id order. */
 pgb_status pgb_queries_stage1(pgb_engine *e, const pgb_prefs *prefs, double *scores);
 
+/* Stage 1 and its ranking (core.ml:341-343, fig.ml:143-147): rank[q][r] for
+ * r < rk (rk <= the number of edges) is the index, in the order of
+ * pgb_queries_stage1's columns, of the query's r-th best edge: scores
+ * descending, equal scores by increasing index, NaN below every number. */
+pgb_status pgb_queries_rank(pgb_engine *e, const pgb_prefs *prefs, int rk, int *rank);
+
 /* Branch-length optimisation of explicit (query, location) trials on the
  * loaded queries (Three_tax.optimize from the given start, core.ml:401-425 with
  * the retry from default lengths).  optimizer: 0 Brent, 1 Newton;

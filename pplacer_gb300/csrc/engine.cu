@@ -252,7 +252,7 @@ __global__ void k_snodes_from(const double *__restrict__ d, const double *__rest
 // ---------------------------------------------------------------------------
 __global__ void k_query_prep(const char *__restrict__ seqs, int S, int prim, const uint8_t *__restrict__ char_code,
                              const uint8_t *__restrict__ informative, uint8_t *qcode, uint16_t *reind,
-                             uint8_t *mcode, int *qlen, int *qstatus, int *qamb) {
+                             uint8_t *mcode, uint32_t *rcode, int *qlen, int *qstatus, int *qamb) {
   int q = blockIdx.x;
   const char *seq = seqs + (long)q * S;
   __shared__ int s_off;
@@ -285,6 +285,7 @@ __global__ void k_query_prep(const char *__restrict__ seqs, int S, int prim, con
       int pos = s_off + before + __popc(bal & ((1u << lane) - 1u));
       reind[(long)q * S + pos] = (uint16_t)s;
       mcode[(long)q * S + pos] = c;
+      rcode[(long)q * S + pos] = ((uint32_t)s << 8) | c;
     }
     __syncthreads();
     if (threadIdx.x == 0) s_off += tot;
@@ -313,6 +314,7 @@ __global__ void k_query_prep(const char *__restrict__ seqs, int S, int prim, con
 // ---------------------------------------------------------------------------
 struct S1Ctx {
   int S, Sp, RP, K, NM, gcat, ncode, prim, n_edges;
+  int Ep;  // edge rows of the tables: n_edges rounded up to 16 (zero rows past n_edges)
   const float *snode;        // [n_nodes][S][RP][K]
   const int *sexp;           // [n_nodes][S]
   const int *edge_nodes;     // [n_edges]
@@ -332,11 +334,11 @@ __device__ __forceinline__ float s1_util(const S1Ctx &c, int node, int s, int co
 }
 
 // Edge-side tables, once per start_pend: B3 = hi/mid/lo bf16 of T,
-// [3][n_edges][prim * Sp]; BX = base-256 digits of the exponents, [2][n_edges][Sp].
+// [3][Ep][prim * Sp]; BX = base-256 digits of the exponents, [2][Ep][Sp].
 __global__ void k_s1_tables(S1Ctx c, __nv_bfloat16 *B3, __nv_bfloat16 *BX) {
   long n = (long)c.n_edges * c.Sp;
   long K4 = (long)c.prim * c.Sp;
-  long plane = (long)c.n_edges * K4;
+  long plane = (long)c.Ep * K4;
   for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
     int ei = (int)(t / c.Sp), s = (int)(t - (long)ei * c.Sp);
     int node = c.edge_nodes[ei];
@@ -361,7 +363,7 @@ __global__ void k_s1_tables(S1Ctx c, __nv_bfloat16 *B3, __nv_bfloat16 *BX) {
     int ehi = ex >> 8;          // floor(ex / 256)
     int elo = ex - (ehi << 8);  // 0..255
     BX[(long)ei * c.Sp + s] = __float2bfloat16_rn((float)ehi);
-    BX[(long)c.n_edges * c.Sp + (long)ei * c.Sp + s] = __float2bfloat16_rn((float)elo);
+    BX[(long)c.Ep * c.Sp + (long)ei * c.Sp + s] = __float2bfloat16_rn((float)elo);
   }
 }
 
@@ -382,15 +384,16 @@ __global__ void k_s1_query(int S, int Sp, int prim, const uint8_t *__restrict__ 
 }
 
 // scores = T-sum - n log R + ln2 * exponent sum
-__global__ void k_s1_epilogue(int Q, int E, const float *__restrict__ C, const float *__restrict__ Xhi,
+__global__ void k_s1_epilogue(int Q, int E, int Ep, const float *__restrict__ C, const float *__restrict__ Xhi,
                               const float *__restrict__ Xlo, const int *__restrict__ qlen,
                               const int *__restrict__ qstatus, double log_nrates, double *scores) {
   long n = (long)Q * E;
   for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
     int q = (int)(t / E);
     if (qstatus[q] != PGB_Q_OK) continue;
-    long long ex = 256LL * __float2ll_rn(Xhi[t]) + __float2ll_rn(Xlo[t]);
-    scores[t] = (double)C[t] - (double)(float)qlen[q] * log_nrates + kLn2 * (double)ex;
+    long tp = (long)q * Ep + (t - (long)q * E);
+    long long ex = 256LL * __float2ll_rn(Xhi[tp]) + __float2ll_rn(Xlo[tp]);
+    scores[t] = (double)C[tp] - (double)(float)qlen[q] * log_nrates + kLn2 * (double)ex;
   }
 }
 
@@ -412,90 +415,84 @@ __global__ void k_s1_ambig(S1Ctx c, const int *__restrict__ qlist, const uint16_
 // Per-query ranking: edges by score, descending, ties to the lower edge index
 // (stable sort of the ascending edge list, fig.ml:143-147); NaN sorts below
 // every number as OCaml's compare does.  Scores map to order-preserving
-// 64-bit keys; a bitonic sort in shared memory orders (key, index) pairs.
+// 64-bit keys.  Only the rk best edges are needed, so each query takes one
+// warp and extracts them by repeated arg-max: lane L owns edges L, L + 32,
+// ... and keeps its best remaining (key, edge); the warp's winner is the
+// arg-max over lanes (an xor butterfly, identical in every lane), and only
+// the winner's owner lane marks it taken and rescans its edges.
 __device__ __forceinline__ unsigned long long s1_key(double v) {
   if (isnan(v)) return 0ull;
   unsigned long long b = (unsigned long long)__double_as_longlong(v);
   return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
 }
 
-__global__ void __launch_bounds__(1024) k_rank_bitonic(const double *__restrict__ scores, int E, int N, int rk,
-                                                       const int *__restrict__ qstatus, int *rank) {
-  extern __shared__ unsigned long long rk_key[];
-  int *rk_idx = reinterpret_cast<int *>(rk_key + N);
-  int q = blockIdx.x;
-  if (qstatus[q] != PGB_Q_OK) return;
-  for (int i = threadIdx.x; i < N; i += blockDim.x) {
-    rk_key[i] = i < E ? s1_key(scores[(long)q * E + i]) : 0ull;
-    rk_idx[i] = i < E ? i : 0x7fffffff;
-  }
-  __syncthreads();
-  for (int k = 2; k <= N; k <<= 1) {
-    for (int j = k >> 1; j > 0; j >>= 1) {
-      for (int i = threadIdx.x; i < N; i += blockDim.x) {
-        int l = i ^ j;
-        if (l > i) {
-          unsigned long long ki = rk_key[i], kl = rk_key[l];
-          int ii = rk_idx[i], il = rk_idx[l];
-          bool l_first = kl > ki || (kl == ki && il < ii);  // l precedes i in the final order
-          bool i_first = ki > kl || (ki == kl && ii < il);
-          bool up = (i & k) == 0;
-          if (up ? l_first : i_first) {
-            rk_key[i] = kl; rk_key[l] = ki;
-            rk_idx[i] = il; rk_idx[l] = ii;
-          }
+// keys in shared memory when a warp's row fits (E * 8 bytes), else read
+// from global memory.  Each lane keeps a sorted cache of its kRankCache best
+// remaining edges; a lane that wins pops its cache and, when it runs dry,
+// refills it from its edges ranked after the last one it gave out, so most
+// lanes scan their edges once.
+constexpr int kRankCache = 4;
+
+__device__ __forceinline__ bool rank_before(unsigned long long ka, int ia, unsigned long long kb, int ib) {
+  return ka > kb || (ka == kb && ia < ib);
+}
+
+__global__ void __launch_bounds__(128) k_rank_warp(const double *__restrict__ scores, int E, int rk, int Q,
+                                                   const int *__restrict__ qstatus, int *rank, int keys_in_smem) {
+  extern __shared__ unsigned long long rk_smem[];
+  const int nw = blockDim.x >> 5, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int q = blockIdx.x * nw + w;
+  if (q >= Q || qstatus[q] != PGB_Q_OK) return;
+  unsigned long long *keys = rk_smem + (long)w * E;
+  const double *sc = scores + (long)q * E;
+  if (keys_in_smem)
+    for (int i = lane; i < E; i += 32) keys[i] = s1_key(sc[i]);
+  __syncwarp();
+  unsigned long long ck[kRankCache];
+  int ci[kRankCache];
+  unsigned long long lk = 0ull;  // last edge this lane gave out (li < 0: none yet)
+  int li = -1;
+  auto refill = [&]() {  // the kRankCache best of the lane's edges ranked after (lk, li)
+#pragma unroll
+    for (int c = 0; c < kRankCache; c++) { ck[c] = 0ull; ci[c] = -1; }
+    for (int i = lane; i < E; i += 32) {
+      unsigned long long k = keys_in_smem ? keys[i] : s1_key(sc[i]);
+      if (li >= 0 && !rank_before(lk, li, k, i)) continue;
+      if (ci[kRankCache - 1] >= 0 && !rank_before(k, i, ck[kRankCache - 1], ci[kRankCache - 1])) continue;
+      // insert into the sorted cache
+      unsigned long long kk = k;
+      int ii = i;
+#pragma unroll
+      for (int c = 0; c < kRankCache; c++) {
+        if (ci[c] < 0 || rank_before(kk, ii, ck[c], ci[c])) {
+          unsigned long long tk = ck[c];
+          int ti = ci[c];
+          ck[c] = kk; ci[c] = ii;
+          kk = tk; ii = ti;
         }
       }
-      __syncthreads();
     }
-  }
-  for (int r = threadIdx.x; r < rk; r += blockDim.x) rank[(long)q * rk + r] = rk_idx[r];
-}
-
-__device__ __forceinline__ bool s1_better(double a, int ia, double b, int ib) {
-  bool na = isnan(a), nb = isnan(b);
-  if (na != nb) return nb;
-  if (!na && a != b) return a > b;
-  return ia < ib;
-}
-
-// Selection ranking for edge counts beyond the bitonic shared-memory tile.
-__global__ void k_rank(const double *__restrict__ scores, int n_edges, int rk, const int *__restrict__ qstatus,
-                       int *rank) {
-  int q = blockIdx.x;
-  if (qstatus[q] != PGB_Q_OK) return;
-  extern __shared__ unsigned rk_taken[];
-  int words = (n_edges + 31) / 32;
-  for (int i = threadIdx.x; i < words; i += blockDim.x) rk_taken[i] = 0u;
-  __shared__ double bw_s[32];
-  __shared__ int bw_i[32];
-  __syncthreads();
-  const double *sc = scores + (long)q * n_edges;
-  int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  };
+  refill();
   for (int r = 0; r < rk; r++) {
-    double bs = 0;
-    int bi = -1;
-    for (int i = threadIdx.x; i < n_edges; i += blockDim.x) {
-      if (rk_taken[i >> 5] & (1u << (i & 31))) continue;
-      double v = sc[i];
-      if (bi < 0 || s1_better(v, i, bs, bi)) { bs = v; bi = i; }
-    }
+    unsigned long long wk = ck[0];
+    int wi = ci[0];
+#pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-      double os = __shfl_down_sync(0xffffffffu, bs, o);
-      int oi = __shfl_down_sync(0xffffffffu, bi, o);
-      if (oi >= 0 && (bi < 0 || s1_better(os, oi, bs, bi))) { bs = os; bi = oi; }
+      unsigned long long ok = __shfl_xor_sync(0xffffffffu, wk, o);
+      int oi = __shfl_xor_sync(0xffffffffu, wi, o);
+      if (oi >= 0 && (wi < 0 || rank_before(ok, oi, wk, wi))) { wk = ok; wi = oi; }
     }
-    if (lane == 0) { bw_s[w] = bs; bw_i[w] = bi; }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      double b = 0;
-      int ii = -1;
-      for (int i = 0; i < nw; i++)
-        if (bw_i[i] >= 0 && (ii < 0 || s1_better(bw_s[i], bw_i[i], b, ii))) { b = bw_s[i]; ii = bw_i[i]; }
-      rank[(long)q * rk + r] = ii;
-      if (ii >= 0) rk_taken[ii >> 5] |= 1u << (ii & 31);
+    if (lane == 0) rank[(long)q * rk + r] = wi;
+    if (wi >= 0 && wi == ci[0]) {  // this lane's head: pop it
+      lk = ck[0];
+      li = ci[0];
+#pragma unroll
+      for (int c = 0; c + 1 < kRankCache; c++) { ck[c] = ck[c + 1]; ci[c] = ci[c + 1]; }
+      ck[kRankCache - 1] = 0ull;
+      ci[kRankCache - 1] = -1;
+      if (ci[0] < 0) refill();
     }
-    __syncthreads();
   }
 }
 
@@ -735,6 +732,7 @@ struct pgb_engine {
   char *d_seqs = nullptr;
   uint8_t *d_qcode = nullptr, *d_mcode = nullptr;
   uint16_t *d_reind = nullptr;
+  uint32_t *d_rcode = nullptr;  // (alignment column << 8) | code per informative site
   int *d_qlen = nullptr, *d_qstatus = nullptr;
   std::vector<int> h_qlen;
   // run buffers
@@ -805,7 +803,8 @@ pgb_status ensure_queries(pgb_engine *e, int Q) {
   size_t n = (size_t)Q * e->S;
   pgb_status s;
   if ((s = dalloc(&e->d_seqs, n)) || (s = dalloc(&e->d_qcode, n)) || (s = dalloc(&e->d_mcode, n)) ||
-      (s = dalloc(&e->d_reind, n)) || (s = dalloc(&e->d_qlen, Q)) || (s = dalloc(&e->d_qstatus, Q)) ||
+      (s = dalloc(&e->d_reind, n)) || (s = dalloc(&e->d_rcode, n)) || (s = dalloc(&e->d_qlen, Q)) ||
+      (s = dalloc(&e->d_qstatus, Q)) ||
       (s = dalloc(&e->d_qamb, Q)) || (s = dalloc(&e->d_amb_list, Q)))
     return s;
   e->Qcap = Q;
@@ -815,7 +814,7 @@ pgb_status ensure_queries(pgb_engine *e, int Q) {
 S1Ctx stage1_ctx(pgb_engine *e) {
   S1Ctx c{};
   c.S = e->S; c.Sp = e->Sp; c.RP = e->RP; c.K = e->K; c.NM = e->NM; c.gcat = e->gcat; c.ncode = e->ncode;
-  c.prim = e->prim; c.n_edges = e->n_edges; c.snode = e->d_snode; c.sexp = e->d_sexp;
+  c.prim = e->prim; c.n_edges = e->n_edges; c.Ep = (e->n_edges + 15) & ~15; c.snode = e->d_snode; c.sexp = e->d_sexp;
   c.edge_nodes = e->d_edge_nodes; c.qe = e->d_qe; c.site_cat = e->d_site_cat;
   return c;
 }
@@ -839,9 +838,12 @@ pgb_status build_stage1_table(pgb_engine *e, double start_pend) {
   pgb_status s;
   if ((s = upload(&e->d_qe, qe.data(), qe.size(), e->st))) return s;
   size_t K4 = (size_t)e->prim * e->Sp;
-  if (!e->d_B3 && ((s = dalloc(&e->d_B3, 3 * (size_t)e->n_edges * K4)) ||
-                   (s = dalloc(&e->d_BX, 2 * (size_t)e->n_edges * e->Sp))))
-    return s;
+  const size_t Ep = (size_t)((e->n_edges + 15) & ~15);
+  if (!e->d_B3) {
+    if ((s = dalloc(&e->d_B3, 3 * Ep * K4)) || (s = dalloc(&e->d_BX, 2 * Ep * e->Sp))) return s;
+    PGB_CUDA(cudaMemsetAsync(e->d_B3, 0, 3 * Ep * K4 * sizeof(__nv_bfloat16), e->st));  // zero pad rows
+    PGB_CUDA(cudaMemsetAsync(e->d_BX, 0, 2 * Ep * e->Sp * sizeof(__nv_bfloat16), e->st));
+  }
   k_s1_tables<<<grid_for((long)e->n_edges * e->Sp), 256, 0, e->st>>>(stage1_ctx(e), e->d_B3, e->d_BX);
   PGB_LAUNCH_CHECK();
   e->lt_pend = start_pend;
@@ -849,11 +851,11 @@ pgb_status build_stage1_table(pgb_engine *e, double start_pend) {
 }
 
 pgb_status gemm_bf16(pgb_engine *e, const __nv_bfloat16 *B, const __nv_bfloat16 *A, float *C, int m, int n, int k,
-                     float beta) {
-  // row-major C[n][m] = A[n][k] * B[m][k]^T, i.e. column-major C' = B'^T A'
+                     int ldc, float beta) {
+  // row-major C[n][ldc] = A[n][k] * B[m][k]^T, i.e. column-major C' = B'^T A'
   const float alpha = 1.f;
   cublasStatus_t st = cublasGemmEx(e->blas, CUBLAS_OP_T, CUBLAS_OP_N, m, n, k, &alpha, B, CUDA_R_16BF, k, A,
-                                   CUDA_R_16BF, k, &beta, C, CUDA_R_32F, m, CUBLAS_COMPUTE_32F, CUBLAS_GEMM_DEFAULT);
+                                   CUDA_R_16BF, k, &beta, C, CUDA_R_32F, ldc, CUBLAS_COMPUTE_32F, CUBLAS_GEMM_DEFAULT);
   if (st != CUBLAS_STATUS_SUCCESS) {
     set_error("stage 1: cublasGemmEx failed (%d)", (int)st);
     return PGB_ERR_CUDA;
@@ -873,22 +875,28 @@ pgb_status run_stage1(pgb_engine *e) {
     if ((s = dalloc(&e->d_A, (size_t)e->Q * K4)) || (s = dalloc(&e->d_M, (size_t)e->Q * e->Sp))) return s;
     e->a_cap = e->Q;
   }
-  if (qe_n > e->c_cap) {
-    if ((s = dalloc(&e->d_C, qe_n)) || (s = dalloc(&e->d_Xhi, qe_n)) || (s = dalloc(&e->d_Xlo, qe_n))) return s;
-    e->c_cap = qe_n;
+  // FP32 products in rows of Ep = n_edges rounded up to 16: 64-byte aligned
+  // rows let the GEMM use its widest vector loads and stores
+  const int Ep = (e->n_edges + 15) & ~15;
+  size_t qep_n = (size_t)e->Q * Ep;
+  if (qep_n > e->c_cap) {
+    if ((s = dalloc(&e->d_C, qep_n)) || (s = dalloc(&e->d_Xhi, qep_n)) || (s = dalloc(&e->d_Xlo, qep_n))) return s;
+    e->c_cap = qep_n;
   }
   k_s1_query<<<e->Q, 256, 0, e->st>>>(e->S, e->Sp, e->prim, e->d_qcode, e->d_informative, e->d_qstatus, e->d_A,
                                       e->d_M);
   PGB_LAUNCH_CHECK();
-  size_t plane = (size_t)e->n_edges * K4;
+  // m = Ep rows (the pad rows are zero): every extent and leading dimension
+  // a multiple of 16 elements
+  size_t plane = (size_t)Ep * K4;
   for (int piece = 0; piece < 3; piece++)
-    if ((s = gemm_bf16(e, e->d_B3 + piece * plane, e->d_A, e->d_C, e->n_edges, e->Q, (int)K4, piece ? 1.f : 0.f)))
+    if ((s = gemm_bf16(e, e->d_B3 + piece * plane, e->d_A, e->d_C, Ep, e->Q, (int)K4, Ep, piece ? 1.f : 0.f)))
       return s;
-  if ((s = gemm_bf16(e, e->d_BX, e->d_M, e->d_Xhi, e->n_edges, e->Q, e->Sp, 0.f)) ||
-      (s = gemm_bf16(e, e->d_BX + (size_t)e->n_edges * e->Sp, e->d_M, e->d_Xlo, e->n_edges, e->Q, e->Sp, 0.f)))
+  if ((s = gemm_bf16(e, e->d_BX, e->d_M, e->d_Xhi, Ep, e->Q, e->Sp, Ep, 0.f)) ||
+      (s = gemm_bf16(e, e->d_BX + (size_t)Ep * e->Sp, e->d_M, e->d_Xlo, Ep, e->Q, e->Sp, Ep, 0.f)))
     return s;
   double log_nrates = e->gcat ? 0.0 : log((double)(float)e->NM);
-  k_s1_epilogue<<<grid_for((long)qe_n), 256, 0, e->st>>>(e->Q, e->n_edges, e->d_C, e->d_Xhi, e->d_Xlo, e->d_qlen,
+  k_s1_epilogue<<<grid_for((long)qe_n), 256, 0, e->st>>>(e->Q, e->n_edges, Ep, e->d_C, e->d_Xhi, e->d_Xlo, e->d_qlen,
                                                          e->d_qstatus, log_nrates, e->d_scores);
   PGB_LAUNCH_CHECK();
   std::vector<int> amb;
@@ -905,20 +913,17 @@ pgb_status run_stage1(pgb_engine *e) {
 }
 
 pgb_status run_rank(pgb_engine *e, int rk) {
-  int N = 1;
-  while (N < e->n_edges) N <<= 1;
-  size_t smem = (size_t)N * 12;
-  if (N <= 16384 && smem <= e->smem_optin) {
-    if (smem > 48 * 1024)
-      PGB_CUDA(cudaFuncSetAttribute(k_rank_bitonic, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k_rank_bitonic<<<e->Q, std::min(1024, std::max(32, N / 2)), smem, e->st>>>(e->d_scores, e->n_edges, N, rk,
-                                                                            e->d_qstatus, e->d_rank);
-    PGB_LAUNCH_CHECK();
-    return PGB_OK;
-  }
-  size_t sm2 = (size_t)((e->n_edges + 31) / 32) * 4;
-  if (sm2 > 48 * 1024) PGB_CUDA(cudaFuncSetAttribute(k_rank, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2));
-  k_rank<<<e->Q, 256, sm2, e->st>>>(e->d_scores, e->n_edges, rk, e->d_qstatus, e->d_rank);
+  const int E = e->n_edges;
+  const size_t keys = (size_t)E * 8;
+  // up to 4 warps (queries) per block with the keys staged, within 96 KB
+  int nw = 4, in_smem = 1;
+  while (nw > 1 && nw * keys > 96 * 1024) nw--;
+  if (nw * keys > e->smem_optin) in_smem = 0;
+  size_t smem = in_smem ? nw * keys : 0;
+  if (smem > 48 * 1024)
+    PGB_CUDA(cudaFuncSetAttribute(k_rank_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  k_rank_warp<<<(e->Q + nw - 1) / nw, 32 * nw, smem, e->st>>>(e->d_scores, E, rk, e->Q, e->d_qstatus, e->d_rank,
+                                                              in_smem);
   PGB_LAUNCH_CHECK();
   return PGB_OK;
 }
@@ -927,7 +932,8 @@ TrialCtx trial_ctx(pgb_engine *e, const pgb_prefs *p, int optimizer, int mode) {
   TrialCtx c{};
   c.darr = e->d_darr; c.parr = e->d_parr; c.dexp = e->d_dexp; c.pexp = e->d_pexp;
   c.S = e->S; c.RP = e->RP; c.K = e->K; c.NM = e->NM; c.ncode = e->ncode; c.gcat = e->gcat;
-  c.bl = e->d_bl; c.reind = e->d_reind; c.mcode = e->d_mcode; c.qlen = e->d_qlen; c.site_cat = e->d_site_cat;
+  c.bl = e->d_bl; c.reind = e->d_reind; c.mcode = e->d_mcode; c.rcode = e->d_rcode; c.qlen = e->d_qlen;
+  c.site_cat = e->d_site_cat;
   c.X = e->d_mf + e->off_X; c.W = e->d_mf + e->off_W; c.Lt = e->d_mf + e->off_Lt; c.lvf = e->d_mf + e->off_lv;
   c.statd = e->d_mf + e->off_statd; c.lam = e->d_mf + e->off_lam; c.rates = e->d_mf + e->off_rates;
   c.log_nrates = e->gcat ? 0.0 : log((double)(float)e->NM);
@@ -968,25 +974,25 @@ bool warp_trials_ok(const pgb_engine *e) {
 }
 
 template <int RP>
-pgb_status launch_trials_warp_rp(pgb_engine *e, cudaStream_t st, TrialCtx c, const int *d_order, int n,
-                                 TrialRes *out) {
+pgb_status launch_trials_warp_rp(pgb_engine *e, cudaStream_t st, TrialCtx c, const WarpSegs &segs, TrialRes *out) {
   size_t smem = warp_trial_smem_bytes(e->NM, e->ncode);
   if (smem > e->smem_optin) { set_error("warp trial shared memory %zu exceeds %zu", smem, e->smem_optin); return PGB_ERR_ARG; }
   PGB_CUDA(cudaFuncSetAttribute(k_trials_warp<RP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  int grid = (n + kWarpTrialWarps - 1) / kWarpTrialWarps;
-  k_trials_warp<RP><<<grid, 32 * kWarpTrialWarps, smem, st>>>(c, e->d_trials, d_order, n, out);
+  int grid = (segs.n + kWarpTrialWarps - 1) / kWarpTrialWarps;
+  k_trials_warp<RP><<<grid, 32 * kWarpTrialWarps, smem, st>>>(c, e->d_trials, segs, out);
   PGB_LAUNCH_CHECK();
   return PGB_OK;
 }
 
-pgb_status launch_trials_warp(pgb_engine *e, cudaStream_t st, TrialCtx c, const int *d_order, int n, TrialRes *out) {
+pgb_status launch_trials_warp(pgb_engine *e, cudaStream_t st, TrialCtx c, const WarpSegs &segs, TrialRes *out) {
+  if (segs.nseg < 1 || segs.n <= 0) return PGB_OK;
   c.smem_win = 0;
   c.cap = 0;
   switch (e->RP) {
-    case 1: return launch_trials_warp_rp<1>(e, st, c, d_order, n, out);
-    case 2: return launch_trials_warp_rp<2>(e, st, c, d_order, n, out);
-    case 4: return launch_trials_warp_rp<4>(e, st, c, d_order, n, out);
-    default: return launch_trials_warp_rp<8>(e, st, c, d_order, n, out);
+    case 1: return launch_trials_warp_rp<1>(e, st, c, segs, out);
+    case 2: return launch_trials_warp_rp<2>(e, st, c, segs, out);
+    case 4: return launch_trials_warp_rp<4>(e, st, c, segs, out);
+    default: return launch_trials_warp_rp<8>(e, st, c, segs, out);
   }
 }
 
@@ -996,7 +1002,15 @@ pgb_status launch_trials(pgb_engine *e, cudaStream_t st, TrialCtx c, const int *
                          TrialRes *out, int threads) {
   if (n <= 0) return PGB_OK;
   if (threads == 32) {
-    if (warp_trials_ok(e)) return launch_trials_warp(e, st, c, d_order, n, out);
+    if (warp_trials_ok(e)) {
+      WarpSegs segs{};
+      segs.list[0] = d_order;
+      segs.start[0] = 0;
+      segs.start[1] = n;
+      segs.nseg = 1;
+      segs.n = n;
+      return launch_trials_warp(e, st, c, segs, out);
+    }
     threads = 256;
   }
   if (e->K == 4)
@@ -1019,6 +1033,23 @@ void bin_shape(const pgb_engine *e, int b, int max_sq, int allow_win, int *cap, 
 // Launch every non-empty bin of the trial lists, concurrently (one stream
 // each, longest windows first), and join them on the engine stream.
 pgb_status run_bins(pgb_engine *e, TrialCtx c, const int *h_bin_count, int max_sq) {
+  bool all_warp = warp_trials_ok(e);
+  for (int b = 0; b < kBins; b++)
+    if (h_bin_count[b] > 0 && e->tune_threads[b] != 32) all_warp = false;
+  if (all_warp) {  // one launch over every bin, longest bin first
+    WarpSegs segs{};
+    int tot = 0;
+    for (int b = kBins - 1; b >= 0; b--) {
+      if (h_bin_count[b] == 0) continue;
+      segs.list[segs.nseg] = e->d_bin_list + (long)b * e->trials_cap;
+      segs.start[segs.nseg] = tot;
+      tot += h_bin_count[b];
+      segs.nseg++;
+    }
+    segs.start[segs.nseg] = tot;
+    segs.n = tot;
+    return launch_trials_warp(e, e->st, c, segs, e->d_tres);
+  }
   PGB_CUDA(cudaEventRecord(e->bin_ev[8], e->st));
   int used[kBins], nu = 0;
   for (int b = kBins - 1; b >= 0; b--) {
@@ -1233,8 +1264,8 @@ pgb_status pgb_engine_destroy(pgb_engine *e) {
                   e->d_mf, e->d_site_cat, e->d_char_code, e->d_informative, e->d_edge_nodes, e->d_parent,
                   e->d_ch_start, e->d_ch_list, e->d_darr, e->d_parr, e->d_snode, e->d_dexp, e->d_pexp, e->d_sexp,
                   e->d_qe, e->d_B3, e->d_BX, e->d_A, e->d_M, e->d_C, e->d_Xhi, e->d_Xlo, e->d_qamb,
-                  e->d_amb_list, e->d_seqs, e->d_qcode, e->d_mcode, e->d_reind, e->d_qlen, e->d_qstatus,
-                  e->d_scores, e->d_rank, e->d_bb, e->d_res, e->d_tbase, e->d_tcount, e->d_keep_idx, e->d_keep_n,
+                  e->d_amb_list, e->d_seqs, e->d_qcode, e->d_mcode, e->d_reind, e->d_rcode, e->d_qlen,
+                  e->d_qstatus, e->d_scores, e->d_rank, e->d_bb, e->d_res, e->d_tbase, e->d_tcount, e->d_keep_idx, e->d_keep_n,
                   e->d_trials, e->d_tres, e->d_bin_list, e->d_small, e->d_out, e->d_nout, e->d_stats};
   for (void *p : ptrs)
     if (p) cudaFree(p);
@@ -1416,8 +1447,8 @@ pgb_status pgb_queries_load(pgb_engine *e, int n_queries, const char *seqs) {
   if (!n_queries) return PGB_OK;
   PGB_CUDA(cudaMemcpyAsync(e->d_seqs, seqs, (size_t)n_queries * e->S, cudaMemcpyHostToDevice, e->st));
   k_query_prep<<<n_queries, 256, 0, e->st>>>(e->d_seqs, e->S, e->prim, e->d_char_code, e->d_informative,
-                                             e->d_qcode, e->d_reind, e->d_mcode, e->d_qlen, e->d_qstatus,
-                                             e->d_qamb);
+                                             e->d_qcode, e->d_reind, e->d_mcode, e->d_rcode, e->d_qlen,
+                                             e->d_qstatus, e->d_qamb);
   PGB_LAUNCH_CHECK();
   e->h_qlen.resize(n_queries);
   PGB_CUDA(cudaMemcpyAsync(e->h_qlen.data(), e->d_qlen, (size_t)n_queries * 4, cudaMemcpyDeviceToHost, e->st));
@@ -1442,6 +1473,20 @@ pgb_status pgb_queries_stage1(pgb_engine *e, const pgb_prefs *p, double *scores)
   pgb_status s;
   if ((s = check_prefs(p)) || (s = build_stage1_table(e, p->start_pend)) || (s = run_stage1(e))) return s;
   PGB_CUDA(cudaMemcpyAsync(scores, e->d_scores, (size_t)e->Q * e->n_edges * 8, cudaMemcpyDeviceToHost, e->st));
+  PGB_CUDA(cudaStreamSynchronize(e->st));
+  return PGB_OK;
+}
+
+pgb_status pgb_queries_rank(pgb_engine *e, const pgb_prefs *p, int rk, int *rank) {
+  if (!e || !e->glvs_ready || e->Q < 1) { set_error("rank: no GLVs or no queries"); return PGB_ERR_STATE; }
+  if (rk < 1 || rk > e->n_edges || !rank) { set_error("rank: rk %d outside 1..%d", rk, e->n_edges); return PGB_ERR_ARG; }
+  pgb_status s;
+  if ((s = check_prefs(p))) return s;
+  size_t rn = (size_t)e->Q * rk;
+  if (rn > e->rank_cap) { if ((s = dalloc(&e->d_rank, rn))) return s; e->rank_cap = rn; }
+  PGB_CUDA(cudaMemsetAsync(e->d_rank, 0xff, rn * sizeof(int), e->st));
+  if ((s = build_stage1_table(e, p->start_pend)) || (s = run_stage1(e)) || (s = run_rank(e, rk))) return s;
+  PGB_CUDA(cudaMemcpyAsync(rank, e->d_rank, rn * sizeof(int), cudaMemcpyDeviceToHost, e->st));
   PGB_CUDA(cudaStreamSynchronize(e->st));
   return PGB_OK;
 }

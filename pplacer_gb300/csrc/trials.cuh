@@ -36,6 +36,7 @@ struct TrialCtx {
   const double *bl;
   const uint16_t *reind;
   const uint8_t *mcode;
+  const uint32_t *rcode;  // (column << 8) | code
   const int *qlen;
   const uint8_t *site_cat;
   const float *X, *W, *Lt, *lvf, *statd, *lam, *rates;

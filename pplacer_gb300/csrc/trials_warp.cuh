@@ -34,9 +34,20 @@ __host__ __device__ inline size_t warp_trial_const_floats(int NM, int ncode) {
 __host__ __device__ inline size_t warp_trial_table_floats(int NM, int ncode) {
   return 6 * (size_t)NM * 16 + 3 * (size_t)NM * ncode * 4 + 2 * 3 * (size_t)NM * 4;
 }
-// per warp: its tables, then the ring of D / P float4s [2][kWarpRing][32]
+static_assert((kWarpRing & (kWarpRing - 1)) == 0 && kWarpRing >= 8, "ring depth: a power of two, >= 8");
+
+// The trials of one launch: the concatenation of up to 8 index lists (the
+// query-length bins, longest first, so the longest trials start first);
+// list[k] == nullptr stands for the identity start[k], start[k] + 1, ...
+struct WarpSegs {
+  const int *list[8];
+  int start[9];
+  int nseg, n;  // n = start[nseg]
+};
+// per warp: its tables, the ring of D / P float4s [2][kWarpRing][32], and
+// the ring of the sites' character codes [kWarpRing][32]
 __host__ __device__ inline size_t warp_trial_warp_bytes(int NM, int ncode) {
-  return align16(4 * warp_trial_table_floats(NM, ncode)) + 2 * kWarpRing * 32 * 16;
+  return align16(4 * warp_trial_table_floats(NM, ncode)) + 2 * kWarpRing * 32 * 16 + kWarpRing * 32;
 }
 __host__ __device__ inline size_t warp_trial_smem_bytes(int NM, int ncode) {
   return align16(4 * warp_trial_const_floats(NM, ncode)) + kWarpTrialWarps * warp_trial_warp_bytes(NM, ncode);
@@ -79,136 +90,130 @@ __device__ __forceinline__ void sites_warp(const TrialCtx &c, const TrialSmem &s
   }
   const float *gd = c.darr + (long)node * c.S * RP * K + r * K;
   const float *gp = c.parr + (long)node * c.S * RP * K + r * K;
-  const uint16_t *ri = c.reind + (long)q * c.S;
-  const uint8_t *mc = c.mcode + (long)q * c.S;
+  const uint32_t *rc = c.rcode + (long)q * c.S;
+  uint8_t *cring = reinterpret_cast<uint8_t *>(ring + 2 * kWarpRing * 32);
   const float *Zr = sm.Z + r * nc * K, *Z1r = sm.Z1 + r * nc * K, *Z2r = sm.Z2 + r * nc * K;
   const int last = Sq - 1;
-  // Ring stage of iteration it: it % kWarpRing; iteration it covers the
-  // sites it * SPW + slot.  Iterations past the end copy the last site and
-  // are not accumulated.  Copies run kWarpRing - 1 iterations ahead; the
-  // column of the next copy is loaded one iteration before it is issued.
-  // A lane reads back only the ring entries it copied itself, so the
-  // per-thread wait_group is the only synchronisation the ring needs.
+  // Iterations come in groups of G; in iteration k of a group the lane
+  // evaluates position k ^ r of the group (for 2 and 4 rates), so that the
+  // reduce-scatter below needs no selects.  Site of iteration j:
+  // (j / G) * G * SPW + off[j % G].
+  constexpr int G = (RP == 2 || RP == 4) ? RP : 1;
+  int off[G];
 #pragma unroll
-  for (int k = 0; k < kWarpRing - 1; k++) {
-    int s0 = ri[min(k * SPW + slot, last)];
-    cp_async16(ring + (k * 32 + lane), gd + (long)s0 * RP * K);
-    cp_async16(ring + ((kWarpRing + k) * 32 + lane), gp + (long)s0 * RP * K);
+  for (int k = 0; k < G; k++) off[k] = (G > 1 ? (k ^ r) : 0) * SPW + slot;
+  // Ring stage of iteration j: j % kWarpRing.  Iteration j issues the copy of
+  // iteration j + kWarpRing - 1 into the stage iteration j - 1 consumed, and
+  // loads the (column, code) word of iteration j + kWarpRing + 1, two
+  // iterations before its copy is issued; the site of iteration
+  // j + kWarpRing is the site of j plus kWarpRing * SPW.
+  // Sites past the end read the last site and are not accumulated.  A lane
+  // reads back only ring entries it copied itself, so the per-thread
+  // wait_group is the only synchronisation the ring needs.
+  auto issue = [&](int stage, uint32_t pk) {
+    const long col = (long)(pk >> 8);
+    cring[stage * 32 + lane] = (uint8_t)(pk & 255u);
+    cp_async16(ring + (stage * 32 + lane), gd + col * RP * K);
+    cp_async16(ring + ((kWarpRing + stage) * 32 + lane), gp + col * RP * K);
     cp_async_commit();
-  }
-  int col = ri[min((kWarpRing - 1) * SPW + slot, last)];
-  int code = mc[min(slot, last)];
-  int st_w = kWarpRing - 1, st_r = 0;
-  // one ring iteration: copy ahead, wait for this iteration's window entry,
-  // and the lane's six rate terms of its site
-  auto iteration = [&](int i, bool live, float *v) {
-    cp_async16(ring + (st_w * 32 + lane), gd + (long)col * RP * K);
-    cp_async16(ring + ((kWarpRing + st_w) * 32 + lane), gp + (long)col * RP * K);
-    cp_async_commit();
-    col = ri[min(i + kWarpRing * SPW, last)];
-    const int coden = mc[min(i + SPW, last)];
+  };
+#pragma unroll
+  for (int j = 0; j < kWarpRing - 1; j++) issue(j, rc[min((j / G) * G * SPW + off[j % G], last)]);
+  uint32_t pk_next = rc[min(((kWarpRing - 1) / G) * G * SPW + off[(kWarpRing - 1) % G], last)];
+  uint32_t pk_next2 = rc[min(off[0] + kWarpRing * SPW, last)];
+  int st = 0;
+  // i: the lane's site in this iteration; inext: in the next one
+  auto iteration = [&](int i, int inext, float (&v)[6]) {
+    issue((st + kWarpRing - 1) & (kWarpRing - 1), pk_next);
+    pk_next = pk_next2;
+    pk_next2 = rc[min(inext + kWarpRing * SPW, last)];
     cp_async_wait<kWarpRing - 1>();  // this iteration's copies have landed
-    const float4 dcur = ring[st_r * 32 + lane];
-    const float4 pcur = ring[(kWarpRing + st_r) * 32 + lane];
-    st_w = st_w + 1 == kWarpRing ? 0 : st_w + 1;
-    st_r = st_r + 1 == kWarpRing ? 0 : st_r + 1;
+    const float4 dcur = ring[st * 32 + lane];
+    const float4 pcur = ring[(kWarpRing + st) * 32 + lane];
+    const int code = cring[st * 32 + lane];
+    st = (st + 1) & (kWarpRing - 1);
+    const float dv[4] = {dcur.x, dcur.y, dcur.z, dcur.w}, pv[4] = {pcur.x, pcur.y, pcur.z, pcur.w};
+    const float4 Z4 = *reinterpret_cast<const float4 *>(Zr + code * K);
+    const float z[4] = {Z4.x, Z4.y, Z4.z, Z4.w};
+    float z1[4], z2[4];
+    if (DER) {
+      float4 a = *reinterpret_cast<const float4 *>(Z1r + code * K);
+      float4 b = *reinterpret_cast<const float4 *>(Z2r + code * K);
+      z1[0] = a.x; z1[1] = a.y; z1[2] = a.z; z1[3] = a.w;
+      z2[0] = b.x; z2[1] = b.y; z2[2] = b.z; z2[3] = b.w;
+    }
 #pragma unroll
     for (int k = 0; k < 6; k++) v[k] = 0.f;
-    if (live) {  // uniform over the warp
-      const float dv[4] = {dcur.x, dcur.y, dcur.z, dcur.w}, pv[4] = {pcur.x, pcur.y, pcur.z, pcur.w};
-      const float4 Z4 = *reinterpret_cast<const float4 *>(Zr + code * K);
-      const float z[4] = {Z4.x, Z4.y, Z4.z, Z4.w};
-      float z1[4], z2[4];
-      if (DER) {
-        float4 a = *reinterpret_cast<const float4 *>(Z1r + code * K);
-        float4 b = *reinterpret_cast<const float4 *>(Z2r + code * K);
-        z1[0] = a.x; z1[1] = a.y; z1[2] = a.z; z1[3] = a.w;
-        z2[0] = b.x; z2[1] = b.y; z2[2] = b.z; z2[3] = b.w;
-      }
 #pragma unroll
-      for (int ii = 0; ii < 4; ii++) {
-        float x = 0.f, y = 0.f;
+    for (int ii = 0; ii < 4; ii++) {
+      float x = 0.f, y = 0.f;
+#pragma unroll
+      for (int jj = 0; jj < 4; jj++) {
+        x = fmaf(md[ii * 4 + jj], dv[jj], x);
+        y = fmaf(mp[ii * 4 + jj], pv[jj], y);
+      }
+      float xy = x * y;
+      v[0] = fmaf(z[ii], xy, v[0]);
+      if (DER) {
+        float x1 = 0.f, x2 = 0.f, y1 = 0.f, y2 = 0.f;
 #pragma unroll
         for (int jj = 0; jj < 4; jj++) {
-          x = fmaf(md[ii * 4 + jj], dv[jj], x);
-          y = fmaf(mp[ii * 4 + jj], pv[jj], y);
+          x1 = fmaf(md1[ii * 4 + jj], dv[jj], x1);
+          x2 = fmaf(md2[ii * 4 + jj], dv[jj], x2);
+          y1 = fmaf(mp1[ii * 4 + jj], pv[jj], y1);
+          y2 = fmaf(mp2[ii * 4 + jj], pv[jj], y2);
         }
-        float xy = x * y;
-        v[0] = fmaf(z[ii], xy, v[0]);
-        if (DER) {
-          float x1 = 0.f, x2 = 0.f, y1 = 0.f, y2 = 0.f;
-#pragma unroll
-          for (int jj = 0; jj < 4; jj++) {
-            x1 = fmaf(md1[ii * 4 + jj], dv[jj], x1);
-            x2 = fmaf(md2[ii * 4 + jj], dv[jj], x2);
-            y1 = fmaf(mp1[ii * 4 + jj], pv[jj], y1);
-            y2 = fmaf(mp2[ii * 4 + jj], pv[jj], y2);
-          }
-          float aa = x1 * y - x * y1;
-          float bb = x2 * y - 2.f * x1 * y1 + x * y2;
-          v[1] = fmaf(z[ii], aa, v[1]);
-          v[2] = fmaf(z[ii], bb, v[2]);
-          v[3] = fmaf(z1[ii], xy, v[3]);
-          v[4] = fmaf(z2[ii], xy, v[4]);
-          v[5] = fmaf(z1[ii], aa, v[5]);
-        }
+        float aa = x1 * y - x * y1;
+        float bb = x2 * y - 2.f * x1 * y1 + x * y2;
+        v[1] = fmaf(z[ii], aa, v[1]);
+        v[2] = fmaf(z[ii], bb, v[2]);
+        v[3] = fmaf(z1[ii], xy, v[3]);
+        v[4] = fmaf(z2[ii], xy, v[4]);
+        v[5] = fmaf(z1[ii], aa, v[5]);
       }
     }
-    code = coden;
   };
   constexpr int NV = DER ? 6 : 1;
-  if (RP == 2 || RP == 4) {
-    // Reduce-scatter over groups of RP iterations: after the exchange lane r
-    // holds the rate sum of its slot's site in iteration r of the group, so
-    // every lane accumulates one site per group.  Stage xor 1 pairs
-    // iterations (0, 1) and (2, 3); stage xor 2 pairs the two halves.
-    const bool b0 = r & 1, b1 = (r >> 1) & 1;
-    for (int base = 0; base < Sq; base += RP * SPW) {
-      float h[2][6];
+  for (int gbase = 0; gbase < Sq; gbase += G * SPW) {
+    float f[6];
+    if (G == 4) {
+      // v_k holds position k ^ r.  Stage xor 1: the partner's v1 (v3) is at
+      // the position of this lane's v0 (v2); stage xor 2: the partner's h1
+      // is at this lane's position r.
+      float v0[6], v1[6], h0[6], h1[6];
+      iteration(gbase + off[0], gbase + off[1], v0);
+      iteration(gbase + off[1], gbase + off[2], v1);
 #pragma unroll
-      for (int half = 0; half < RP / 2; half++) {
-        float v0[6], v1[6];
-        const int i0 = base + (2 * half) * SPW + slot;
-        iteration(i0, i0 - slot < Sq, v0);
-        iteration(i0 + SPW, i0 + SPW - slot < Sq, v1);
+      for (int k = 0; k < NV; k++) h0[k] = v0[k] + __shfl_xor_sync(0xffffffffu, v1[k], 1);
+      iteration(gbase + off[2], gbase + off[3], v0);
+      iteration(gbase + off[3], gbase + G * SPW + off[0], v1);
 #pragma unroll
-        for (int k = 0; k < NV; k++) {
-          float keep = b0 ? v1[k] : v0[k], send = b0 ? v0[k] : v1[k];
-          h[half][k] = keep + __shfl_xor_sync(0xffffffffu, send, 1);
-        }
-      }
-      float f[6];
+      for (int k = 0; k < NV; k++) h1[k] = v0[k] + __shfl_xor_sync(0xffffffffu, v1[k], 1);
 #pragma unroll
-      for (int k = 0; k < NV; k++) {
-        if (RP == 4) {
-          float keep = b1 ? h[1][k] : h[0][k], send = b1 ? h[0][k] : h[1][k];
-          f[k] = keep + __shfl_xor_sync(0xffffffffu, send, 2);
-        } else {
-          f[k] = h[0][k];
-        }
-      }
-      if (base + r * SPW + slot < Sq) acc.add(f[0], f[1], f[2], f[3], f[4], f[5], DER);
-    }
-  } else {
-    // RP = 1: a lane's site needs no exchange; RP = 8: xor all-reduce of
-    // the site's rate terms, lane r == 0 accumulates
-    for (int base = 0; base < Sq; base += SPW) {
-      float v[6];
-      iteration(base + slot, true, v);
+      for (int k = 0; k < NV; k++) f[k] = h0[k] + __shfl_xor_sync(0xffffffffu, h1[k], 2);
+    } else if (G == 2) {
+      float v0[6], v1[6];
+      iteration(gbase + off[0], gbase + off[1], v0);
+      iteration(gbase + off[1], gbase + G * SPW + off[0], v1);
+#pragma unroll
+      for (int k = 0; k < NV; k++) f[k] = v0[k] + __shfl_xor_sync(0xffffffffu, v1[k], 1);
+    } else {
+      // one rate: the lane's own site; eight rates: xor all-reduce
+      iteration(gbase + off[0], gbase + SPW + off[0], f);
 #pragma unroll
       for (int o = 1; o < RP; o <<= 1)
 #pragma unroll
-        for (int k = 0; k < NV; k++) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
-      if (r == 0 && base + slot < Sq) acc.add(v[0], v[1], v[2], v[3], v[4], v[5], DER);
+        for (int k = 0; k < NV; k++) f[k] += __shfl_xor_sync(0xffffffffu, f[k], o);
     }
+    const bool mine = G > 1 ? gbase + r * SPW + slot < Sq : (r == 0 && gbase + slot < Sq);
+    if (mine) acc.add(f[0], f[1], f[2], f[3], f[4], f[5], DER);
   }
   cp_async_wait<0>();  // drain the copies issued past the end
 }
 
 template <int RP>
 __global__ void __launch_bounds__(32 * kWarpTrialWarps, kWarpTrialMinCtas)
-    k_trials_warp(TrialCtx c, const TrialIn *__restrict__ trials, const int *__restrict__ order, int n,
-                  TrialRes *out) {
+    k_trials_warp(TrialCtx c, const TrialIn *__restrict__ trials, WarpSegs segs, TrialRes *out) {
   constexpr int K = 4;
   extern __shared__ __align__(16) char t_smem[];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -240,8 +245,14 @@ __global__ void __launch_bounds__(32 * kWarpTrialWarps, kWarpTrialMinCtas)
   }
   __syncthreads();
   const int t = blockIdx.x * kWarpTrialWarps + warp;
-  if (t >= n) return;
-  const int ti = order ? order[t] : t;
+  if (t >= segs.n) return;
+  // segment of t (constant indices keep segs in the parameter bank)
+  const int *lst = segs.list[0];
+  int s0 = 0;
+#pragma unroll
+  for (int k = 1; k < 8; k++)
+    if (k < segs.nseg && t >= segs.start[k]) { lst = segs.list[k]; s0 = segs.start[k]; }
+  const int ti = lst ? lst[t - s0] : t - s0;
   const TrialIn tr = trials[ti];
   const int q = tr.q, node = tr.node;
   const int Sq = c.qlen[q];

@@ -119,6 +119,13 @@ class Engine:
         _L.check(_L.load().pgb_queries_stage1(self.h, C.byref(prefs), sc.ctypes.data), "pgb_queries_stage1")
         return sc
 
+    def rank(self, rk, prefs=None):
+        """Stage-1 ranking: the rk best edge columns per query (-1 for a query without placement)."""
+        prefs = prefs or default_prefs()
+        out = np.zeros((self.Q, rk), dtype=np.int32)
+        _L.check(_L.load().pgb_queries_rank(self.h, C.byref(prefs), rk, out.ctypes.data), "pgb_queries_rank")
+        return out
+
     def trials(self, trials, optimizer=NEWTON, mode=0, prefs=None):
         """trials: list of (query, edge_node, pend0, dist0, tol)."""
         prefs = prefs or default_prefs()

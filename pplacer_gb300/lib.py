@@ -98,6 +98,7 @@ def load(build_if_missing=True):
     L.pgb_queries_run.argtypes = [vp, C.POINTER(Prefs)]
     L.pgb_queries_fetch.argtypes = [vp, vp, vp, vp]
     L.pgb_queries_stage1.argtypes = [vp, C.POINTER(Prefs), vp]
+    L.pgb_queries_rank.argtypes = [vp, C.POINTER(Prefs), i, vp]
     L.pgb_queries_trials.argtypes = [vp, C.POINTER(Prefs), i, i, i, vp, vp]
     L.pgb_engine_timings.argtypes = [vp, vp, vp]
     L.pgb_engine_autotune.argtypes = [vp, C.POINTER(Prefs)]
@@ -105,7 +106,7 @@ def load(build_if_missing=True):
     L.pgb_engine_set_tuning.argtypes = [vp, vp, vp]
     for name in ["pgb_engine_create", "pgb_engine_destroy", "pgb_engine_precompute", "pgb_engine_set_glvs",
                  "pgb_engine_get_glv", "pgb_place", "pgb_queries_load", "pgb_queries_run", "pgb_queries_fetch",
-                 "pgb_queries_stage1", "pgb_queries_trials", "pgb_engine_timings", "pgb_engine_autotune",
+                 "pgb_queries_stage1", "pgb_queries_rank", "pgb_queries_trials", "pgb_engine_timings", "pgb_engine_autotune",
                  "pgb_engine_get_tuning", "pgb_engine_set_tuning"]:
         getattr(L, name).restype = i
     _lib = L

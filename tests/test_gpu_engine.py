@@ -65,6 +65,19 @@ def test_stage1_scores_match_oracle(small, oracle_lib):
         np.testing.assert_allclose(got, ref, rtol=1e-6)
 
 
+def test_stage1_ranking(small):
+    """The rk best edges per query: scores descending, equal scores by
+    increasing edge index, NaN last (fig.ml:143-147)."""
+    w, oref, eng = small
+    sc = eng.stage1()
+    E = sc.shape[1]
+    rk = min(E, 65)
+    got = eng.rank(rk)
+    for q in range(sc.shape[0]):
+        want = sorted(range(E), key=lambda i: (math.isnan(sc[q, i]), -sc[q, i] if not math.isnan(sc[q, i]) else 0.0, i))
+        assert list(got[q]) == want[:rk], q
+
+
 def _trial_list(w, n, seed):
     rng = np.random.default_rng(seed)
     edges = np.where(w.parent >= 0)[0]
