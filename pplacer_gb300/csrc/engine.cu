@@ -933,7 +933,7 @@ TrialCtx trial_ctx(pgb_engine *e, const pgb_prefs *p, int optimizer, int mode) {
   c.darr = e->d_darr; c.parr = e->d_parr; c.dexp = e->d_dexp; c.pexp = e->d_pexp;
   c.S = e->S; c.RP = e->RP; c.K = e->K; c.NM = e->NM; c.ncode = e->ncode; c.gcat = e->gcat;
   c.bl = e->d_bl; c.reind = e->d_reind; c.mcode = e->d_mcode; c.rcode = e->d_rcode; c.qlen = e->d_qlen;
-  c.site_cat = e->d_site_cat;
+  c.site_cat = e->d_site_cat; c.qamb = e->d_qamb; c.prim = e->prim;
   c.X = e->d_mf + e->off_X; c.W = e->d_mf + e->off_W; c.Lt = e->d_mf + e->off_Lt; c.lvf = e->d_mf + e->off_lv;
   c.statd = e->d_mf + e->off_statd; c.lam = e->d_mf + e->off_lam; c.rates = e->d_mf + e->off_rates;
   c.log_nrates = e->gcat ? 0.0 : log((double)(float)e->NM);

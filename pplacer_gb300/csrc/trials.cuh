@@ -37,6 +37,8 @@ struct TrialCtx {
   const uint16_t *reind;
   const uint8_t *mcode;
   const uint32_t *rcode;  // (column << 8) | code
+  const int *qamb;        // informative ambiguity characters per query
+  int prim;               // primary (one-hot) character codes: 0 .. prim - 1
   const int *qlen;
   const uint8_t *site_cat;
   const float *X, *W, *Lt, *lvf, *statd, *lam, *rates;
@@ -187,9 +189,11 @@ struct Optimiser {
     }
   }
 
+  // The Newton form needs the FP64 logL only at its start and end (it
+  // compares evaluations by exact exponent differences), so it skips it here.
   __device__ void record(const EvalOut *res) {
     last = *res;
-    L_last = full(*res);
+    if (optimizer != 1 || mode == 1) L_last = full(*res);
     n_evals++;
   }
 
@@ -346,6 +350,7 @@ struct Optimiser {
         request(p, d, (float)cut - d, true);
         PGB_YIELD(20);
         cur = last;
+        L_last = full(cur);
         if (!isfinite(cur.lm)) {
           if (attempt == 0) {
             attempt = 1;
@@ -451,8 +456,8 @@ __device__ __forceinline__ void trial_exps(const TrialSmem &sm, int NM, int K, c
 // P(t) = I + X diag(expm1(r lambda t)) X^-T for the distal and proximal
 // lengths, its first and second derivatives, and the statd-weighted evolved
 // query vectors Z (and d/dpend, d2/dpend2) of every character code.
-__device__ __forceinline__ void trial_tables(const TrialSmem &sm, const float *W, int NM, int nc, int K, bool derivs,
-                                             int i0, int stride) {
+__device__ __forceinline__ void trial_tables(const TrialSmem &sm, const float *W, int NM, int nc, int ncz, int K,
+                                             bool derivs, int i0, int stride) {
   const int nmat = NM * K * K;
   for (int i = i0; i < 2 * nmat; i += stride) {
     int wh = i / nmat, r = i - wh * nmat;
@@ -478,10 +483,13 @@ __device__ __forceinline__ void trial_tables(const TrialSmem &sm, const float *W
       (wh == 0 ? sm.Md2 : sm.Mp2)[r] = a2;
     }
   }
-  const int nz = NM * nc * K;
-  for (int i = i0; i < nz; i += stride) {
-    int m = i / (nc * K), ck = i - m * nc * K;
+  // Z rows of codes 0 .. ncz - 1 only (ncz = the primary states when the
+  // query has no ambiguity character); the table keeps its nc-row stride
+  const int nz = NM * ncz * K;
+  for (int j = i0; j < nz; j += stride) {
+    int m = j / (ncz * K), ck = j - m * ncz * K;
     int code = ck / K, ii = ck - code * K;
+    const int i = (m * nc + code) * K + ii;
     const float *x = sm.X + ii * K;
     const float *lt = sm.Lt + code * K;
     const float *em = sm.Em1 + (2 * NM + m) * K;
@@ -789,7 +797,7 @@ __global__ void __launch_bounds__(T, 1) k_trials(TrialCtx c, const TrialIn *__re
     const bool derivs = ctl.cmd == 2;
     trial_exps(sm, NM, K, ctl, tid, T);
     __syncthreads();  // A2: exp factors
-    trial_tables(sm, K == 4 ? sm.W : c.W, NM, nc, K, derivs, tid, T);
+    trial_tables(sm, K == 4 ? sm.W : c.W, NM, nc, c.qamb[q] > 0 ? nc : c.prim, K, derivs, tid, T);
     __syncthreads();  // B
     // ---- sites ----
     SiteAcc acc;

@@ -25,7 +25,7 @@
 // uniform by construction.
 
 constexpr int kWarpTrialWarps = 1;  // warps (trials) per CTA
-constexpr int kWarpTrialMinCtas = 11;  // resident CTAs per SM: at most 186 registers
+constexpr int kWarpTrialMinCtas = 10;  // register cap 204; the kernel uses ~168, so 12 fit
 constexpr int kWarpRing = 8;        // site iterations in flight per warp
 
 __host__ __device__ inline size_t warp_trial_const_floats(int NM, int ncode) {
@@ -256,6 +256,7 @@ __global__ void __launch_bounds__(32 * kWarpTrialWarps, kWarpTrialMinCtas)
   const TrialIn tr = trials[ti];
   const int q = tr.q, node = tr.node;
   const int Sq = c.qlen[q];
+  const int ncz = c.qamb[q] > 0 ? nc : c.prim;  // Z rows the query's codes use
   // exponent sum of the query's sites of darr / parr[node]
   long long esum = 0;
   const long qo = (long)q * c.S;
@@ -300,7 +301,7 @@ __global__ void __launch_bounds__(32 * kWarpTrialWarps, kWarpTrialMinCtas)
     __syncwarp();  // the previous evaluation's sites have read the tables
     trial_exps(sm, NM, K, ctl, lane, 32);
     __syncwarp();
-    trial_tables(sm, sm.W, NM, nc, K, derivs, lane, 32);
+    trial_tables(sm, sm.W, NM, nc, ncz, K, derivs, lane, 32);
     __syncwarp();
     SiteAcc acc;
     acc.init();
