@@ -34,7 +34,7 @@ __host__ __device__ inline size_t warp_trial_const_floats(int NM, int ncode) {
 __host__ __device__ inline size_t warp_trial_table_floats(int NM, int ncode) {
   return 6 * (size_t)NM * 16 + 3 * (size_t)NM * ncode * 4 + 2 * 3 * (size_t)NM * 4;
 }
-static_assert((kWarpRing & (kWarpRing - 1)) == 0 && kWarpRing >= 8, "ring depth: a power of two, >= 8");
+static_assert(kWarpRing == 8, "ring depth 8: the codes in flight fill one 64-bit register");
 
 // The trials of one launch: the concatenation of up to 8 index lists (the
 // query-length bins, longest first, so the longest trials start first);
@@ -44,10 +44,9 @@ struct WarpSegs {
   int start[9];
   int nseg, n;  // n = start[nseg]
 };
-// per warp: its tables, the ring of D / P float4s [2][kWarpRing][32], and
-// the ring of the sites' character codes [kWarpRing][32]
+// per warp: its tables and the ring of D / P float4s [2][kWarpRing][32]
 __host__ __device__ inline size_t warp_trial_warp_bytes(int NM, int ncode) {
-  return align16(4 * warp_trial_table_floats(NM, ncode)) + 2 * kWarpRing * 32 * 16 + kWarpRing * 32;
+  return align16(4 * warp_trial_table_floats(NM, ncode)) + 2 * kWarpRing * 32 * 16;
 }
 __host__ __device__ inline size_t warp_trial_smem_bytes(int NM, int ncode) {
   return align16(4 * warp_trial_const_floats(NM, ncode)) + kWarpTrialWarps * warp_trial_warp_bytes(NM, ncode);
@@ -91,7 +90,6 @@ __device__ __forceinline__ void sites_warp(const TrialCtx &c, const TrialSmem &s
   const float *gd = c.darr + (long)node * c.S * RP * K + r * K;
   const float *gp = c.parr + (long)node * c.S * RP * K + r * K;
   const uint32_t *rc = c.rcode + (long)q * c.S;
-  uint8_t *cring = reinterpret_cast<uint8_t *>(ring + 2 * kWarpRing * 32);
   const float *Zr = sm.Z + r * nc * K, *Z1r = sm.Z1 + r * nc * K, *Z2r = sm.Z2 + r * nc * K;
   const int last = Sq - 1;
   // Iterations come in groups of G; in iteration k of a group the lane
@@ -109,28 +107,37 @@ __device__ __forceinline__ void sites_warp(const TrialCtx &c, const TrialSmem &s
   // j + kWarpRing is the site of j plus kWarpRing * SPW.
   // Sites past the end read the last site and are not accumulated.  A lane
   // reads back only ring entries it copied itself, so the per-thread
-  // wait_group is the only synchronisation the ring needs.
+  // wait_group is the only synchronisation the ring needs.  The character
+  // codes of the iterations in flight travel in a register, byte k holding
+  // the code of the k-th next iteration, so the evolved-query loads of an
+  // iteration need no shared-memory round trip first.
+  unsigned long long cq = 0ull;
   auto issue = [&](int stage, uint32_t pk) {
     const long col = (long)(pk >> 8);
-    cring[stage * 32 + lane] = (uint8_t)(pk & 255u);
     cp_async16(ring + (stage * 32 + lane), gd + col * RP * K);
     cp_async16(ring + ((kWarpRing + stage) * 32 + lane), gp + col * RP * K);
     cp_async_commit();
   };
 #pragma unroll
-  for (int j = 0; j < kWarpRing - 1; j++) issue(j, rc[min((j / G) * G * SPW + off[j % G], last)]);
+  for (int j = 0; j < kWarpRing - 1; j++) {
+    const uint32_t pk = rc[min((j / G) * G * SPW + off[j % G], last)];
+    issue(j, pk);
+    cq |= (unsigned long long)(pk & 255u) << (8 * j);
+  }
   uint32_t pk_next = rc[min(((kWarpRing - 1) / G) * G * SPW + off[(kWarpRing - 1) % G], last)];
   uint32_t pk_next2 = rc[min(off[0] + kWarpRing * SPW, last)];
   int st = 0;
   // i: the lane's site in this iteration; inext: in the next one
   auto iteration = [&](int i, int inext, float (&v)[6]) {
     issue((st + kWarpRing - 1) & (kWarpRing - 1), pk_next);
+    cq |= (unsigned long long)(pk_next & 255u) << (8 * (kWarpRing - 1));
+    const int code = (int)(cq & 255ull);
+    cq >>= 8;
     pk_next = pk_next2;
     pk_next2 = rc[min(inext + kWarpRing * SPW, last)];
     cp_async_wait<kWarpRing - 1>();  // this iteration's copies have landed
     const float4 dcur = ring[st * 32 + lane];
     const float4 pcur = ring[(kWarpRing + st) * 32 + lane];
-    const int code = cring[st * 32 + lane];
     st = (st + 1) & (kWarpRing - 1);
     const float dv[4] = {dcur.x, dcur.y, dcur.z, dcur.w}, pv[4] = {pcur.x, pcur.y, pcur.z, pcur.w};
     const float4 Z4 = *reinterpret_cast<const float4 *>(Zr + code * K);
