@@ -687,6 +687,159 @@ __global__ void k_finalize(BBCtx c, int keep_at_most, const int *__restrict__ ke
   n_out[q] = m;
 }
 
+// ---------------------------------------------------------------------------
+// Whole queries, one per warp (nucleotide Gamma mixtures): the baseball
+// search over the stage-1 ranking (core.ml:429-464), keep (core.ml:482-496),
+// refinement from the kept optima (core.ml:497-523) and like_weight_ratio
+// (pquery.ml:8-9).  A query's trials run in rank order inside its warp, each
+// decided before the next starts, so nothing is evaluated speculatively and
+// no host round trip separates the trials; queries come from a counter,
+// longest first.  The decisions are those of k_bb_update / k_keep_emit /
+// k_finalize for one result at a time.
+// ---------------------------------------------------------------------------
+struct PlaceCtx {
+  BBCtx bb;
+  const int *qorder;  // queries, longest first
+  int *qnext;         // next position in qorder
+  int keep_at_most;
+  double log_keep_factor;
+  pgb_placement *out;  // [Q][keep_at_most]
+  int *n_out;
+  unsigned long long *tstats;  // [0] baseball trials, [1] refinement trials
+};
+
+template <int RP>
+__global__ void __launch_bounds__(32, kWarpTrialMinCtas) k_place_warp(TrialCtx c, PlaceCtx p) {
+  extern __shared__ __align__(16) char t_smem[];
+  const int lane = threadIdx.x & 31;
+  TrialSmem sm;
+  float4 *ring;
+  warp_trial_setup(c, t_smem, sm, ring);
+  const BBCtx &b = p.bb;
+  // One trial call site (the trial code is inlined once): a query moves from
+  // its baseball trials (refine < 0) to the refinement of its kept
+  // locations (refine = index of the next one).
+  int q = -1, next = 0, nres = 0, nk = 0, refine = -1;
+  long strikes = 0;
+  double record = -INFINITY;
+  unsigned long long n_bb = 0;
+  for (;;) {
+    if (q < 0) {  // take the next query
+      int qi = 0;
+      if (lane == 0) qi = atomicAdd(p.qnext, 1);
+      qi = __shfl_sync(0xffffffffu, qi, 0);
+      if (qi >= b.Q) break;
+      q = p.qorder[qi];
+      if (lane == 0) p.n_out[q] = 0;
+      if (b.qstatus[q] != PGB_Q_OK || b.rk < 1) { q = -1; continue; }
+      next = 0; nres = 0; nk = 0; refine = -1; strikes = 0; record = -INFINITY; n_bb = 0;
+    }
+    ResEntry *r = b.res + (long)q * b.maxr;
+    TrialIn t;
+    t.q = q;
+    int ei = -1;
+    if (refine < 0) {
+      ei = b.rank[(long)q * b.rk + next];
+      t.node = b.edge_nodes[ei];
+      t.pend0 = b.start_pend;
+      t.dist0 = b.bl[t.node] / 2.;
+      t.tol = b.tol;
+    } else {
+      const ResEntry e = r[refine];
+      t.node = b.edge_nodes[e.edge];
+      t.pend0 = e.pend;
+      t.dist0 = e.dist;
+      t.tol = 1e-5;  // final_tolerance (core.ml:160)
+    }
+    const TrialRes tr = trial_warp<RP>(c, sm, ring, lane, t);
+    if (refine >= 0) {  // ---- a refined location ----
+      pgb_placement *o = p.out + (long)q * p.keep_at_most;
+      if (lane == 0) {
+        const ResEntry e = r[refine];
+        pgb_placement pl;
+        pl.edge = t.node;
+        pl.pad = 0;
+        pl.lwr = 0;
+        if (tr.status == ST_FAILED || tr.status == ST_STARTFAIL) { pl.like = e.like; pl.pend = e.pend; pl.dist = e.dist; }
+        else { pl.like = tr.like; pl.pend = tr.pend; pl.dist = tr.dist; }
+        o[refine] = pl;
+      }
+      if (++refine < nk) continue;
+      // like_weight_ratio, then stable sort by it, descending
+      if (lane == 0) {
+        atomicAdd(&p.tstats[1], (unsigned long long)nk);
+        const int m = min(nk, 64);
+        for (int j = 0; j < m; j++) {
+          double tot = 0;
+          for (int k = 0; k < m; k++) tot += exp(o[k].like - o[j].like);
+          o[j].lwr = 1. / tot;
+        }
+        for (int i = 1; i < m; i++) {
+          pgb_placement x = o[i];
+          int j = i - 1;
+          while (j >= 0 && x.lwr > o[j].lwr) { o[j + 1] = o[j]; j--; }
+          o[j + 1] = x;
+        }
+        p.n_out[q] = m;
+      }
+      __syncwarp();
+      q = -1;
+      continue;
+    }
+    // ---- a baseball result (k_bb_update's rules for one trial) ----
+    n_bb++;
+    next++;
+    bool stop = false;
+    int qst = PGB_Q_OK;
+    if (tr.status == ST_STARTFAIL) {
+      qst = PGB_Q_START_FAILURE;
+      stop = true;
+    } else if (tr.status != ST_FAILED) {  // ST_FAILED: skipped location (core.ml:435-443)
+      const long before = nres;
+      if (nres < b.maxr) {
+        if (lane == 0) {
+          ResEntry e;
+          e.edge = ei; e.status = tr.status; e.like = tr.like; e.pend = tr.pend; e.dist = tr.dist;
+          r[nres] = e;
+        }
+        nres++;
+      }
+      if (before >= b.max_pitches) stop = true;
+      else if (tr.like > record) record = tr.like;
+      else if (tr.like < record - b.strike_box) {
+        if (strikes + 1 >= b.max_strikes) stop = true;
+        else strikes++;
+      }
+    }
+    if (!stop && next < b.rk) continue;
+    if (lane == 0) atomicAdd(&p.tstats[0], n_bb);
+    if (qst != PGB_Q_OK || nres == 0) {
+      if (lane == 0) b.qstatus[q] = qst != PGB_Q_OK ? qst : PGB_Q_EMPTY;
+      __syncwarp();
+      q = -1;
+      continue;
+    }
+    // ---- keep: stable sort by like, descending, NaN last ----
+    __syncwarp();
+    if (lane == 0)
+      for (int i = 1; i < nres; i++) {
+        ResEntry x = r[i];
+        int j = i - 1;
+        while (j >= 0 && (isnan(r[j].like) ? !isnan(x.like) : (!isnan(x.like) && x.like > r[j].like))) {
+          r[j + 1] = r[j];
+          j--;
+        }
+        r[j + 1] = x;
+      }
+    __syncwarp();
+    const double best = r[0].like;
+    nk = 0;
+    while (nk < nres && nk < p.keep_at_most && r[nk].like >= p.log_keep_factor + best) nk++;
+    if (nk == 0) { q = -1; continue; }
+    refine = 0;
+  }
+}
+
 }  // namespace
 }  // namespace pgb
 
@@ -751,6 +904,8 @@ struct pgb_engine {
   unsigned long long *d_stats = nullptr;  // trial-kernel evaluation counters
   int *d_small = nullptr;  // counters: [0] trial counter, [1] n_active, [2..2+bins) bin counts, then bin limits
   pgb_placement *d_out = nullptr;
+  int *d_qorder = nullptr;  // queries longest first (whole-query warp kernel)
+  size_t qorder_cap = 0;
   int *d_nout = nullptr;
   int out_keep = 0;
   // trial-kernel shape per length bin: threads per CTA, shared-memory windows
@@ -1090,6 +1245,68 @@ pgb_status ensure_run_buffers(pgb_engine *e, const pgb_prefs *p, int rk, int max
   return PGB_OK;
 }
 
+template <int RP>
+pgb_status launch_place_warp_rp(pgb_engine *e, TrialCtx c, const PlaceCtx &pc) {
+  size_t smem = warp_trial_smem_bytes(e->NM, e->ncode);
+  PGB_CUDA(cudaFuncSetAttribute(k_place_warp<RP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int per_sm = 0;
+  PGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_place_warp<RP>, 32, smem));
+  int grid = std::max(1, std::min(e->Q, e->n_sm * std::max(1, per_sm)));
+  k_place_warp<RP><<<grid, 32, smem, e->st>>>(c, pc);
+  PGB_LAUNCH_CHECK();
+  return PGB_OK;
+}
+
+// Stage 2 and refinement as one persistent launch of whole-query warps.
+pgb_status run_whole_queries(pgb_engine *e, const pgb_prefs *p, const BBCtx &c, TrialCtx tc) {
+  pgb_status s;
+  if ((size_t)e->Q > e->qorder_cap) {
+    if ((s = dalloc(&e->d_qorder, e->Q))) return s;
+    e->qorder_cap = e->Q;
+  }
+  std::vector<int> ord(e->Q);
+  for (int i = 0; i < e->Q; i++) ord[i] = i;
+  std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return e->h_qlen[a] > e->h_qlen[b]; });
+  PGB_CUDA(cudaMemcpyAsync(e->d_qorder, ord.data(), ord.size() * sizeof(int), cudaMemcpyHostToDevice, e->st));
+  PGB_CUDA(cudaMemsetAsync(e->d_small, 0, sizeof(int), e->st));
+  tc.smem_win = 0;
+  tc.cap = 0;
+  PlaceCtx pc{};
+  pc.bb = c;
+  pc.qorder = e->d_qorder;
+  pc.qnext = e->d_small;
+  pc.keep_at_most = p->keep_at_most;
+  pc.log_keep_factor = log(p->keep_factor);
+  pc.out = e->d_out;
+  pc.n_out = e->d_nout;
+  pc.tstats = e->d_stats + 2;
+  switch (e->RP) {
+    case 1: s = launch_place_warp_rp<1>(e, tc, pc); break;
+    case 2: s = launch_place_warp_rp<2>(e, tc, pc); break;
+    case 4: s = launch_place_warp_rp<4>(e, tc, pc); break;
+    default: s = launch_place_warp_rp<8>(e, tc, pc); break;
+  }
+  if (s) return s;
+  PGB_CUDA(cudaEventRecord(e->ev[3], e->st));
+  PGB_CUDA(cudaEventRecord(e->ev[4], e->st));
+  PGB_CUDA(cudaEventSynchronize(e->ev[4]));
+  float ms;
+  cudaEventElapsedTime(&ms, e->ev[0], e->ev[1]); e->t_ms[1] = ms;
+  cudaEventElapsedTime(&ms, e->ev[1], e->ev[2]); e->t_ms[2] = ms;
+  cudaEventElapsedTime(&ms, e->ev[2], e->ev[3]); e->t_ms[3] = ms;
+  e->t_ms[4] = 0;
+  cudaEventElapsedTime(&ms, e->ev[0], e->ev[4]); e->t_ms[5] = ms;
+  unsigned long long st_h[4] = {0, 0, 0, 0};
+  PGB_CUDA(cudaMemcpy(st_h, e->d_stats, sizeof st_h, cudaMemcpyDeviceToHost));
+  e->counts[1] = (double)(st_h[2] + st_h[3]);
+  e->counts[2] = (double)st_h[0];
+  e->counts[3] = (double)st_h[1];
+  e->counts[4] = e->counts[5] = (double)st_h[2];
+  e->counts[6] = (double)st_h[3];
+  e->counts[7] = 1;
+  return PGB_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -1266,7 +1483,8 @@ pgb_status pgb_engine_destroy(pgb_engine *e) {
                   e->d_qe, e->d_B3, e->d_BX, e->d_A, e->d_M, e->d_C, e->d_Xhi, e->d_Xlo, e->d_qamb,
                   e->d_amb_list, e->d_seqs, e->d_qcode, e->d_mcode, e->d_reind, e->d_rcode, e->d_qlen,
                   e->d_qstatus, e->d_scores, e->d_rank, e->d_bb, e->d_res, e->d_tbase, e->d_tcount, e->d_keep_idx, e->d_keep_n,
-                  e->d_trials, e->d_tres, e->d_bin_list, e->d_small, e->d_out, e->d_nout, e->d_stats};
+                  e->d_trials, e->d_tres, e->d_bin_list, e->d_small, e->d_out, e->d_nout, e->d_stats,
+                  e->d_qorder};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   for (int i = 0; i < 8; i++)
@@ -1529,6 +1747,10 @@ pgb_status pgb_queries_run(pgb_engine *e, const pgb_prefs *p) {
   for (int b = 0; b < kBins; b++) h_small[2 + kBins + b] = lim[b];
   TrialCtx tc = trial_ctx(e, p, p->optimizer, 0);
   int n = e->Q;
+  bool whole_query = warp_trials_ok(e);
+  for (int b = 0; b < kBins; b++)
+    if (e->tune_threads[b] != 32) whole_query = false;
+  if (whole_query) return run_whole_queries(e, p, c, tc);
   k_bb_init<<<(n + 255) / 256, 256, 0, e->st>>>(c);
   PGB_LAUNCH_CHECK();
   double n_trials_total = 0;

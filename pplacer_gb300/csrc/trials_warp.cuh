@@ -218,16 +218,14 @@ __device__ __forceinline__ void sites_warp(const TrialCtx &c, const TrialSmem &s
   cp_async_wait<0>();  // drain the copies issued past the end
 }
 
-template <int RP>
-__global__ void __launch_bounds__(32 * kWarpTrialWarps, kWarpTrialMinCtas)
-    k_trials_warp(TrialCtx c, const TrialIn *__restrict__ trials, WarpSegs segs, TrialRes *out) {
+// Per-CTA constants and this warp's tables and ring; returns after a block
+// barrier, the only one the warp kernels take.
+__device__ __forceinline__ void warp_trial_setup(const TrialCtx &c, char *t_smem, TrialSmem &sm, float4 *&ring) {
   constexpr int K = 4;
-  extern __shared__ __align__(16) char t_smem[];
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int tid = threadIdx.x, warp = tid >> 5;
   const int NM = c.NM, nc = c.ncode;
-  // ---- CTA constants, then one barrier; the warps are independent after it ----
   float *cst = reinterpret_cast<float *>(t_smem);
-  TrialSmem sm{};
+  sm = TrialSmem{};
   sm.X = cst;
   sm.W = cst + 16;
   sm.Lt = cst + 80;
@@ -239,28 +237,24 @@ __global__ void __launch_bounds__(32 * kWarpTrialWarps, kWarpTrialMinCtas)
   for (int i = tid; i < nc * K; i += blockDim.x) { sm.Lt[i] = c.Lt[i]; sm.lv[i] = c.lvf[i]; }
   for (int i = tid; i < NM * K; i += blockDim.x) sm.Lr[i] = c.rates[i / K] * c.lam[i % K];
   if (tid < K) sm.statd[tid] = c.statd[tid];
-  float4 *ring;
-  {
-    char *wb = t_smem + align16(4 * warp_trial_const_floats(NM, nc)) + warp * warp_trial_warp_bytes(NM, nc);
-    float *tb = reinterpret_cast<float *>(wb);
-    ring = reinterpret_cast<float4 *>(wb + align16(4 * warp_trial_table_floats(NM, nc)));
-    const int mb = NM * 16, zb = NM * nc * K;
-    sm.Md = tb; sm.Mp = tb + mb; sm.Md1 = tb + 2 * mb; sm.Md2 = tb + 3 * mb; sm.Mp1 = tb + 4 * mb;
-    sm.Mp2 = tb + 5 * mb;
-    sm.Z = tb + 6 * mb; sm.Z1 = sm.Z + zb; sm.Z2 = sm.Z1 + zb;
-    sm.E = sm.Z2 + zb; sm.Em1 = sm.E + 3 * NM * K;
-  }
+  char *wb = t_smem + align16(4 * warp_trial_const_floats(NM, nc)) + warp * warp_trial_warp_bytes(NM, nc);
+  float *tb = reinterpret_cast<float *>(wb);
+  ring = reinterpret_cast<float4 *>(wb + align16(4 * warp_trial_table_floats(NM, nc)));
+  const int mb = NM * 16, zb = NM * nc * K;
+  sm.Md = tb; sm.Mp = tb + mb; sm.Md1 = tb + 2 * mb; sm.Md2 = tb + 3 * mb; sm.Mp1 = tb + 4 * mb;
+  sm.Mp2 = tb + 5 * mb;
+  sm.Z = tb + 6 * mb; sm.Z1 = sm.Z + zb; sm.Z2 = sm.Z1 + zb;
+  sm.E = sm.Z2 + zb; sm.Em1 = sm.E + 3 * NM * K;
   __syncthreads();
-  const int t = blockIdx.x * kWarpTrialWarps + warp;
-  if (t >= segs.n) return;
-  // segment of t (constant indices keep segs in the parameter bank)
-  const int *lst = segs.list[0];
-  int s0 = 0;
-#pragma unroll
-  for (int k = 1; k < 8; k++)
-    if (k < segs.nseg && t >= segs.start[k]) { lst = segs.list[k]; s0 = segs.start[k]; }
-  const int ti = lst ? lst[t - s0] : t - s0;
-  const TrialIn tr = trials[ti];
+}
+
+// One trial (Three_tax.optimize at one location) by the calling warp.  Every
+// lane runs the same optimiser on the same all-reduced values and returns
+// the same result.
+template <int RP>
+__device__ TrialRes trial_warp(const TrialCtx &c, const TrialSmem &sm, float4 *ring, int lane, const TrialIn &tr) {
+  constexpr int K = 4;
+  const int NM = c.NM, nc = c.ncode;
   const int q = tr.q, node = tr.node;
   const int Sq = c.qlen[q];
   const int ncz = c.qamb[q] > 0 ? nc : c.prim;  // Z rows the query's codes use
@@ -339,20 +333,41 @@ __global__ void __launch_bounds__(32 * kWarpTrialWarps, kWarpTrialMinCtas)
     res.g[0] = acc.gp; res.g[1] = acc.gd;
     res.h[0] = acc.hpp; res.h[1] = acc.hdd; res.h[2] = acc.hpd;
   }
-  if (lane == 0) {
-    TrialRes rr;
-    rr.like = opt.L_last;
-    rr.pend = opt.pend;
-    rr.dist = opt.dist;
-    rr.der[0] = opt.last.g[0]; rr.der[1] = opt.last.g[1];
-    rr.der[2] = opt.last.h[0]; rr.der[3] = opt.last.h[1]; rr.der[4] = opt.last.h[2];
-    rr.der[5] = 0;
-    rr.status = opt.status;
-    rr.n_evals = opt.n_evals;
-    out[ti] = rr;
-    if (c.stats) {
-      atomicAdd(&c.stats[0], (unsigned long long)opt.n_evals);
-      atomicAdd(&c.stats[1], (unsigned long long)opt.n_evals * (unsigned long long)Sq);
-    }
+  __syncwarp();
+  TrialRes rr;
+  rr.like = opt.L_last;
+  rr.pend = opt.pend;
+  rr.dist = opt.dist;
+  rr.der[0] = opt.last.g[0]; rr.der[1] = opt.last.g[1];
+  rr.der[2] = opt.last.h[0]; rr.der[3] = opt.last.h[1]; rr.der[4] = opt.last.h[2];
+  rr.der[5] = 0;
+  rr.status = opt.status;
+  rr.n_evals = opt.n_evals;
+  if (lane == 0 && c.stats) {
+    atomicAdd(&c.stats[0], (unsigned long long)opt.n_evals);
+    atomicAdd(&c.stats[1], (unsigned long long)opt.n_evals * (unsigned long long)Sq);
   }
+  return rr;
+}
+
+// A batch of independent trials, one per warp.
+template <int RP>
+__global__ void __launch_bounds__(32 * kWarpTrialWarps, kWarpTrialMinCtas)
+    k_trials_warp(TrialCtx c, const TrialIn *__restrict__ trials, WarpSegs segs, TrialRes *out) {
+  extern __shared__ __align__(16) char t_smem[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  TrialSmem sm;
+  float4 *ring;
+  warp_trial_setup(c, t_smem, sm, ring);
+  const int t = blockIdx.x * kWarpTrialWarps + warp;
+  if (t >= segs.n) return;
+  // segment of t (constant indices keep segs in the parameter bank)
+  const int *lst = segs.list[0];
+  int s0 = 0;
+#pragma unroll
+  for (int k = 1; k < 8; k++)
+    if (k < segs.nseg && t >= segs.start[k]) { lst = segs.list[k]; s0 = segs.start[k]; }
+  const int ti = lst ? lst[t - s0] : t - s0;
+  const TrialRes rr = trial_warp<RP>(c, sm, ring, lane, trials[ti]);
+  if (lane == 0) out[ti] = rr;
 }
