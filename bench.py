@@ -34,6 +34,13 @@ sys.path.insert(0, ROOT)
 MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 
 
+# measured constants of the stage-2 roofline (see the roofline block below)
+DRAM_BYTES_PER_SITE_EVAL = None  # filled from the ncu capture of k_place_warp on dna_1k
+FMA_OPS_PER_SITE_RATE = 148      # FFMA + FMUL per site and rate with derivatives (the kernel's arithmetic)
+N_SM = 152
+SM_MAX_HZ = 2.07e9
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -233,16 +240,28 @@ def run_ours(args):
     e2e = Q * world * args.steps / t_e2e
     if rank != 0:
         return
-    # ---- roofline of the dominant kernel (stage-2 trials) ----
-    # algorithmic bytes per objective evaluation: the distal and proximal GLV
-    # windows of the query's informative sites (FP32 + int32 exponent per site)
-    # and one query code byte per site: S_q * (2 * (4*R*K + 4) + 1).
+    # ---- roofline of the dominant kernel ----
+    # Stage 2 + refinement run as one launch of the whole-query warp kernel
+    # (k_place_warp) per step; its duration is the engine's stage-2 event
+    # interval.  Algorithmic bytes per site evaluation: the distal and
+    # proximal FP32 window entries of every rate (2 * 4 * R * K) and the
+    # packed (column, code) word of the site (4); the exponent sums are read
+    # once per trial, not per evaluation, and are left out.
     R, K = len(w.rates) if w.site_cats is None else 1, w.K
-    bytes_per_site_eval = 2 * (4 * R * K + 4) + 1
+    bytes_per_site_eval = 2 * 4 * R * K + 4
     site_evals = counts[3]
     t_trials = phase[3] / 1e3 / args.steps
     peak, peak_kind = load_peaks()
     achieved = bytes_per_site_eval * site_evals / args.steps / t_trials / 1e9 if t_trials > 0 else 0.0
+    # DRAM traffic per site evaluation from one ncu capture of k_place_warp on
+    # this workload (dram__bytes_read.sum + dram__bytes_write.sum over the
+    # launch's site evaluations; profiles/k_place_warp_dna_1k.md)
+    traffic = (DRAM_BYTES_PER_SITE_EVAL * site_evals / args.steps
+               if args.workload == "dna_1k" and DRAM_BYTES_PER_SITE_EVAL else None)
+    # the binding unit is the FP32 pipe: FMA-pipe lane operations per site
+    # evaluation (148 per rate with derivatives), against 128 lanes per SM
+    fp32_ops = FMA_OPS_PER_SITE_RATE * R * site_evals / args.steps / t_trials if t_trials > 0 else 0.0
+    fp32_peak = 128 * N_SM * SM_MAX_HZ
     cpu_v, cpu_threads, cpu_n, cpu_dt = cpu_baseline(w, args.cpu_sample, dict(w.prefs))
     line = {
         "metric": "query placements/s", "value": value, "unit": "placements/s", "n_gpus": world,
@@ -264,8 +283,12 @@ def run_ours(args):
                        "refine_trials": counts[6] / args.steps, "rounds": counts[7] / args.steps,
                        "phase_ms": {"stage1_table": phase[1] / args.steps, "stage1_rank": phase[2] / args.steps,
                                     "stage2": phase[3] / args.steps, "refine_out": phase[4] / args.steps}},
-        "roofline": {"kernel": "k_trials (stage 2)", "bound": "hbm", "achieved": achieved, "peak": peak,
-                     "unit": "GB/s", "frac": achieved / peak, "traffic": None, "peak_source": peak_kind},
+        "roofline": {"kernel": "k_place_warp (stage 2 + refinement)", "bound": "hbm", "achieved": achieved,
+                     "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                     "traffic_unit": "bytes per launch", "algorithmic_bytes_per_site_eval": bytes_per_site_eval,
+                     "peak_source": peak_kind,
+                     "fp32_pipe": {"achieved": fp32_ops, "peak": fp32_peak, "unit": "FMA-pipe lane ops/s",
+                                   "frac": fp32_ops / fp32_peak, "peak_source": "nominal: 128 lanes x 152 SMs x 2070 MHz"}},
         "cpu_baseline": {"value": cpu_v, "unit": "placements/s", "cores": cpu_threads, "kind": "port",
                          "sample": "%d queries of %s (%.1f s)" % (cpu_n, args.workload, cpu_dt)},
         "e2e": {"value": e2e, "unit": "placements/s", "h2d_bytes_per_step": Q * S,

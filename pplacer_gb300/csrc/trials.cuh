@@ -79,6 +79,7 @@ struct TrialSmem {
   float *red;                // [warps][8]
   int *redi;                 // [warps]
   Ctrl *ctrl;
+  void *opt;  // the warp kernels' optimiser state (one per warp)
 };
 
 __host__ __device__ inline size_t trial_smem_bytes(int cap, int win, int RP, int K, int NM, int ncode) {

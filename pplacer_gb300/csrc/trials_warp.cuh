@@ -44,9 +44,10 @@ struct WarpSegs {
   int start[9];
   int nseg, n;  // n = start[nseg]
 };
-// per warp: its tables and the ring of D / P float4s [2][kWarpRing][32]
+// per warp: its tables, the ring of D / P float4s [2][kWarpRing][32], and
+// the optimiser state
 __host__ __device__ inline size_t warp_trial_warp_bytes(int NM, int ncode) {
-  return align16(4 * warp_trial_table_floats(NM, ncode)) + 2 * kWarpRing * 32 * 16;
+  return align16(4 * warp_trial_table_floats(NM, ncode)) + 2 * kWarpRing * 32 * 16 + align16(sizeof(Optimiser));
 }
 __host__ __device__ inline size_t warp_trial_smem_bytes(int NM, int ncode) {
   return align16(4 * warp_trial_const_floats(NM, ncode)) + kWarpTrialWarps * warp_trial_warp_bytes(NM, ncode);
@@ -240,6 +241,7 @@ __device__ __forceinline__ void warp_trial_setup(const TrialCtx &c, char *t_smem
   char *wb = t_smem + align16(4 * warp_trial_const_floats(NM, nc)) + warp * warp_trial_warp_bytes(NM, nc);
   float *tb = reinterpret_cast<float *>(wb);
   ring = reinterpret_cast<float4 *>(wb + align16(4 * warp_trial_table_floats(NM, nc)));
+  sm.opt = wb + align16(4 * warp_trial_table_floats(NM, nc)) + 2 * kWarpRing * 32 * 16;
   const int mb = NM * 16, zb = NM * nc * K;
   sm.Md = tb; sm.Mp = tb + mb; sm.Md1 = tb + 2 * mb; sm.Md2 = tb + 3 * mb; sm.Mp1 = tb + 4 * mb;
   sm.Mp2 = tb + 5 * mb;
@@ -274,30 +276,40 @@ __device__ TrialRes trial_warp(const TrialCtx &c, const TrialSmem &sm, float4 *r
   }
   for (int o = 16; o > 0; o >>= 1) esum += __shfl_xor_sync(0xffffffffu, esum, o);
 
-  Optimiser opt;
-  opt.optimizer = c.optimizer;
-  opt.mode = c.mode;
-  opt.cut = c.bl[node];
-  opt.tol = tr.tol;
-  opt.max_pend = c.max_pend;
-  opt.start_pend = c.start_pend;
-  opt.pend0 = tr.pend0;
-  opt.dist0 = tr.dist0;
-  opt.cst = kLn2 * (double)esum - (double)(float)Sq * c.log_nrates;
-  opt.n_evals = 0;
-  opt.pc = 0;
-  opt.L_last = NAN;
-  opt.last.ex = 0; opt.last.lm = 0.f;
-  opt.last.g[0] = opt.last.g[1] = opt.last.h[0] = opt.last.h[1] = opt.last.h[2] = 0.f;
+  // The optimiser state lives in shared memory, one copy per warp, and only
+  // lane 0 runs it; the other lanes receive each request by shuffle.
+  Optimiser &opt = *static_cast<Optimiser *>(sm.opt);
+  if (lane == 0) {
+    opt.optimizer = c.optimizer;
+    opt.mode = c.mode;
+    opt.cut = c.bl[node];
+    opt.tol = tr.tol;
+    opt.max_pend = c.max_pend;
+    opt.start_pend = c.start_pend;
+    opt.pend0 = tr.pend0;
+    opt.dist0 = tr.dist0;
+    opt.cst = kLn2 * (double)esum - (double)(float)Sq * c.log_nrates;
+    opt.n_evals = 0;
+    opt.pc = 0;
+    opt.L_last = NAN;
+    opt.last.ex = 0; opt.last.lm = 0.f;
+    opt.last.g[0] = opt.last.g[1] = opt.last.h[0] = opt.last.h[1] = opt.last.h[2] = 0.f;
+  }
   EvalOut res;
   for (int ev = 0; ev < kMaxTrialEvals; ev++) {
-    bool more = opt.next(ev == 0 ? nullptr : &res);
+    int cmd = 0;
+    float rp = 0.f, rd = 0.f, rx = 0.f;
+    if (lane == 0) {
+      bool more = opt.next(ev == 0 ? nullptr : &res);
+      cmd = more ? (opt.req_derivs ? 2 : 1) : 0;
+      rp = opt.req_p; rd = opt.req_d; rx = opt.req_x;
+    }
     Ctrl ctl;
-    ctl.cmd = __shfl_sync(0xffffffffu, more ? (opt.req_derivs ? 2 : 1) : 0, 0);
+    ctl.cmd = __shfl_sync(0xffffffffu, cmd, 0);
     if (ctl.cmd == 0) break;
-    ctl.pend = __shfl_sync(0xffffffffu, opt.req_p, 0);
-    ctl.dist = __shfl_sync(0xffffffffu, opt.req_d, 0);
-    ctl.prox = __shfl_sync(0xffffffffu, opt.req_x, 0);
+    ctl.pend = __shfl_sync(0xffffffffu, rp, 0);
+    ctl.dist = __shfl_sync(0xffffffffu, rd, 0);
+    ctl.prox = __shfl_sync(0xffffffffu, rx, 0);
     const bool derivs = ctl.cmd == 2;
     __syncwarp();  // the previous evaluation's sites have read the tables
     trial_exps(sm, NM, K, ctl, lane, 32);
@@ -333,7 +345,7 @@ __device__ TrialRes trial_warp(const TrialCtx &c, const TrialSmem &sm, float4 *r
     res.g[0] = acc.gp; res.g[1] = acc.gd;
     res.h[0] = acc.hpp; res.h[1] = acc.hdd; res.h[2] = acc.hpd;
   }
-  __syncwarp();
+  __syncwarp();  // lane 0's final optimiser state is visible to the warp
   TrialRes rr;
   rr.like = opt.L_last;
   rr.pend = opt.pend;
@@ -343,6 +355,7 @@ __device__ TrialRes trial_warp(const TrialCtx &c, const TrialSmem &sm, float4 *r
   rr.der[5] = 0;
   rr.status = opt.status;
   rr.n_evals = opt.n_evals;
+  __syncwarp();  // every lane has read the state before the next trial resets it
   if (lane == 0 && c.stats) {
     atomicAdd(&c.stats[0], (unsigned long long)opt.n_evals);
     atomicAdd(&c.stats[1], (unsigned long long)opt.n_evals * (unsigned long long)Sq);
