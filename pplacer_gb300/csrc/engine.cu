@@ -1830,6 +1830,10 @@ pgb_status pgb_engine_autotune(pgb_engine *e, const pgb_prefs *p) {
   if (!e || !e->glvs_ready || e->Q < 1) { set_error("autotune: no GLVs or no queries"); return PGB_ERR_STATE; }
   pgb_status s;
   if ((s = check_prefs(p))) return s;
+  if (warp_trials_ok(e)) {  // the whole-query warp kernel: nothing to tune
+    for (int b = 0; b < kBins; b++) { e->tune_threads[b] = 32; e->tune_win[b] = 0; }
+    return PGB_OK;
+  }
   bool all_edges = p->max_strikes == 0;
   int rk = all_edges ? e->n_edges : std::min(e->n_edges, p->max_pitches + 1 + 24);
   int maxr = all_edges ? e->n_edges : std::min(e->n_edges, p->max_pitches + 1);
