@@ -721,7 +721,7 @@ __global__ void __launch_bounds__(32, kWarpTrialMinCtas) k_place_warp(TrialCtx c
   // locations (refine = index of the next one).
   int q = -1, next = 0, nres = 0, nk = 0, refine = -1;
   long strikes = 0;
-  double record = -INFINITY;
+  double record = -INFINITY, pend_hint = b.start_pend;
   unsigned long long n_bb = 0;
   for (;;) {
     if (q < 0) {  // take the next query
@@ -733,6 +733,7 @@ __global__ void __launch_bounds__(32, kWarpTrialMinCtas) k_place_warp(TrialCtx c
       if (lane == 0) p.n_out[q] = 0;
       if (b.qstatus[q] != PGB_Q_OK || b.rk < 1) { q = -1; continue; }
       next = 0; nres = 0; nk = 0; refine = -1; strikes = 0; record = -INFINITY; n_bb = 0;
+      pend_hint = b.start_pend;
     }
     ResEntry *r = b.res + (long)q * b.maxr;
     TrialIn t;
@@ -741,7 +742,10 @@ __global__ void __launch_bounds__(32, kWarpTrialMinCtas) k_place_warp(TrialCtx c
     if (refine < 0) {
       ei = b.rank[(long)q * b.rk + next];
       t.node = b.edge_nodes[ei];
-      t.pend0 = b.start_pend;
+      // The Newton form starts the pendant length at the query's best
+      // optimum so far (the optimum, not the path, is its result); the
+      // Brent replica keeps the reference's start.
+      t.pend0 = c.optimizer == 1 ? pend_hint : b.start_pend;
       t.dist0 = b.bl[t.node] / 2.;
       t.tol = b.tol;
     } else {
@@ -805,7 +809,10 @@ __global__ void __launch_bounds__(32, kWarpTrialMinCtas) k_place_warp(TrialCtx c
         nres++;
       }
       if (before >= b.max_pitches) stop = true;
-      else if (tr.like > record) record = tr.like;
+      else if (tr.like > record) {
+        record = tr.like;
+        if (tr.pend > 1e-6 && tr.pend < c.max_pend) pend_hint = tr.pend;
+      }
       else if (tr.like < record - b.strike_box) {
         if (strikes + 1 >= b.max_strikes) stop = true;
         else strikes++;
