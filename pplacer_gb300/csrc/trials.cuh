@@ -375,13 +375,20 @@ struct Optimiser {
             sp = 0.f;
             sd = 0.f;
             float det = hpp * hdd - hpd * hpd;
+            bool model = false;  // the step is a Newton step of a concave quadratic model
             if (free_p && free_d && hpp < 0.f && hdd < 0.f && det > 0.f) {
               sp = -(hdd * gp - hpd * gd) / det;
               sd = -(hpp * gd - hpd * gp) / det;
+              model = true;
             } else {
               if (free_p) sp = hpp < 0.f ? -gp / hpp : copysignf(fmaxf(0.5f * p, 0.01f), gp);
               if (free_d) sd = hdd < 0.f ? -gd / hdd : copysignf(0.25f * dmax, gd);
+              model = !(free_p && free_d) && (free_p ? hpp < 0.f : hdd < 0.f);
             }
+            // Converged before stepping: the full Newton step would gain less
+            // than the tolerance (g . s is twice the model's gain), so the
+            // current point -- already evaluated -- is the result.
+            if (model && gp * sp + gd * sd < newton_gain_tol() + allow) break;
             // Trust region: one factor for both coordinates, so the step
             // keeps the direction of the Newton (or diagonal) step, which is
             // an ascent direction.  Clipping each coordinate on its own can
