@@ -510,6 +510,7 @@ struct BBState {
 struct ResEntry {
   int edge, status;
   double like, pend, dist;
+  EvalOut ev;  // the trial's evaluation at (pend, dist): seeds the Newton refinement
 };
 struct BBCtx {
   int Q, rk, maxr, n_edges, bins;
@@ -564,7 +565,7 @@ __global__ void k_bb_emit(BBCtx c, int B, int *counter) {
   for (int j = 0; j < n; j++) {
     int ei = c.rank[(long)q * c.rk + s.next + j];
     int node = c.edge_nodes[ei];
-    TrialIn t;
+    TrialIn t{};
     t.q = q;
     t.node = node;
     t.pend0 = c.start_pend;
@@ -591,7 +592,7 @@ __global__ void k_bb_update(BBCtx c, const TrialRes *__restrict__ tres) {
     long before = s.nres;
     if (s.nres < c.maxr) {
       ResEntry e;
-      e.edge = ei; e.status = r.status; e.like = r.like; e.pend = r.pend; e.dist = r.dist;
+      e.edge = ei; e.status = r.status; e.like = r.like; e.pend = r.pend; e.dist = r.dist; e.ev = r.last;
       c.res[(long)q * c.maxr + s.nres] = e;
       s.nres++;
     }
@@ -640,12 +641,14 @@ __global__ void k_keep_emit(BBCtx c, int keep_at_most, double log_keep_factor, i
   int bpos = atomicAdd(&c.bin_count[bin], nk);
   for (int j = 0; j < nk; j++) {
     ResEntry e = r[keep_idx[(long)q * keep_at_most + j]];
-    TrialIn t;
+    TrialIn t{};
     t.q = q;
     t.node = c.edge_nodes[e.edge];
     t.pend0 = e.pend;
     t.dist0 = e.dist;
     t.tol = 1e-5;  // final_tolerance (core.ml:160)
+    t.seeded = 1;  // used by the Newton form only
+    t.seed = e.ev;
     c.trials[base + j] = t;
     c.bin_list[(long)bin * c.cap_trials + bpos + j] = base + j;
   }
@@ -736,7 +739,7 @@ __global__ void __launch_bounds__(32, kWarpTrialMinCtas) k_place_warp(TrialCtx c
       pend_hint = b.start_pend;
     }
     ResEntry *r = b.res + (long)q * b.maxr;
-    TrialIn t;
+    TrialIn t{};
     t.q = q;
     int ei = -1;
     if (refine < 0) {
@@ -754,6 +757,8 @@ __global__ void __launch_bounds__(32, kWarpTrialMinCtas) k_place_warp(TrialCtx c
       t.pend0 = e.pend;
       t.dist0 = e.dist;
       t.tol = 1e-5;  // final_tolerance (core.ml:160)
+      t.seeded = 1;  // the stage-2 evaluation at (pend0, dist0); Newton form only
+      t.seed = e.ev;
     }
     const TrialRes tr = trial_warp<RP>(c, sm, ring, lane, t);
     if (refine >= 0) {  // ---- a refined location ----
@@ -803,7 +808,7 @@ __global__ void __launch_bounds__(32, kWarpTrialMinCtas) k_place_warp(TrialCtx c
       if (nres < b.maxr) {
         if (lane == 0) {
           ResEntry e;
-          e.edge = ei; e.status = tr.status; e.like = tr.like; e.pend = tr.pend; e.dist = tr.dist;
+          e.edge = ei; e.status = tr.status; e.like = tr.like; e.pend = tr.pend; e.dist = tr.dist; e.ev = tr.last;
           r[nres] = e;
         }
         nres++;

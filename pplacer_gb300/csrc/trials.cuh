@@ -19,14 +19,24 @@
 constexpr int kTrialMaxWarps = 8;  // CTAs of 128 or 256 threads (autotuned per bin)
 constexpr int kMaxTrialEvals = 200000;
 
+// One evaluation: logL = ex * ln2 + lm + (trial constant); derivatives FP32.
+struct EvalOut {
+  int ex;
+  float lm;
+  float g[2], h[3];
+};
+
 struct TrialIn {
   int q, node;
   double pend0, dist0, tol;
+  int seeded;    // the Newton form: seed is the evaluation at (pend0, dist0)
+  EvalOut seed;  //   (derivatives included), which it then does not redo
 };
 struct TrialRes {
   double like, pend, dist;
   double der[6];
   int status, n_evals;
+  EvalOut last;  // the evaluation at (pend, dist)
 };
 
 struct TrialCtx {
@@ -54,12 +64,6 @@ struct Ctrl {
   int cmd;  // 0 stop, 1 value, 2 value + derivatives
 };
 
-// One evaluation: logL = ex * ln2 + lm + (trial constant); derivatives FP32.
-struct EvalOut {
-  int ex;
-  float lm;
-  float g[2], h[3];
-};
 
 // logL difference a - b without FP64 (exact exponent difference)
 __device__ __forceinline__ float dlogl(const EvalOut &a, const EvalOut &b) {
@@ -157,6 +161,8 @@ struct Optimiser {
   double xl, xu, xm, fl, fu, fm, v, w, fv, fw, bd, be, u, fz, z, probe_dx, fval, fx;
   bool probe;
   // Newton state
+  bool seeded;
+  EvalOut seed;
   int it, ls, stall;
   float p, d, sp, sd, np, nd, allow, pred;
   bool accepted;
@@ -348,8 +354,13 @@ struct Optimiser {
       NEWTON:
         p = fminf(fmaxf((float)pend, 1e-8f), (float)max_pend);
         d = fminf(fmaxf((float)dist, 0.f), (float)cut);
-        request(p, d, (float)cut - d, true);
-        PGB_YIELD(20);
+        if (seeded) {  // the start point's evaluation is known (a refinement)
+          seeded = false;
+          last = seed;
+        } else {
+          request(p, d, (float)cut - d, true);
+          PGB_YIELD(20);
+        }
         cur = last;
         L_last = full(cur);
         if (!isfinite(cur.lm)) {
@@ -782,6 +793,8 @@ __global__ void __launch_bounds__(T, 1) k_trials(TrialCtx c, const TrialIn *__re
     opt.dist0 = tr.dist0;
     opt.cst = kLn2 * (double)etot - (double)(float)Sq * c.log_nrates;
     opt.n_evals = 0;
+    opt.seeded = tr.seeded != 0;
+    opt.seed = tr.seed;
     opt.pc = 0;
     opt.L_last = NAN;
     opt.last.ex = 0; opt.last.lm = 0.f;
@@ -876,6 +889,7 @@ __global__ void __launch_bounds__(T, 1) k_trials(TrialCtx c, const TrialIn *__re
     r.der[2] = opt.last.h[0]; r.der[3] = opt.last.h[1]; r.der[4] = opt.last.h[2];
     r.der[5] = 0;
     r.status = opt.status;
+    r.last = opt.last;
     r.n_evals = opt.n_evals;
     out[ti] = r;
     if (c.stats) {

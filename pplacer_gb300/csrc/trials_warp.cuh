@@ -290,6 +290,8 @@ __device__ TrialRes trial_warp(const TrialCtx &c, const TrialSmem &sm, float4 *r
     opt.dist0 = tr.dist0;
     opt.cst = kLn2 * (double)esum - (double)(float)Sq * c.log_nrates;
     opt.n_evals = 0;
+    opt.seeded = tr.seeded != 0;
+    opt.seed = tr.seed;
     opt.pc = 0;
     opt.L_last = NAN;
     opt.last.ex = 0; opt.last.lm = 0.f;
@@ -354,6 +356,7 @@ __device__ TrialRes trial_warp(const TrialCtx &c, const TrialSmem &sm, float4 *r
   rr.der[2] = opt.last.h[0]; rr.der[3] = opt.last.h[1]; rr.der[4] = opt.last.h[2];
   rr.der[5] = 0;
   rr.status = opt.status;
+  rr.last = opt.last;
   rr.n_evals = opt.n_evals;
   __syncwarp();  // every lane has read the state before the next trial resets it
   if (lane == 0 && c.stats) {
