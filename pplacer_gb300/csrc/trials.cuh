@@ -170,13 +170,13 @@ struct Optimiser {
 
   __device__ double full(const EvalOut &o) const { return (double)o.ex * kLn2 + (double)o.lm + cst; }
 
-  // Newton stops when the first-order gain of its last step, g . s, is below
-  // this (logL units): 1e-3 in the stage-2 pass (pplacer's tolerance 0.01,
-  // whose Brent stops within about 0.05 logL of the optimum), 1e-7 in the
-  // final 1e-5 pass -- plus the evaluation's rounding allowance.  A step-size
-  // rule alone is unsound here: near a zero pendant the curvature is huge and
-  // Newton steps are tiny while the gradient is not.
-  __device__ float newton_gain_tol() const { return tol >= 1e-3 ? 1e-3f : 1e-7f; }
+  // Newton stops when the first-order gain g . s of its next (or last) step
+  // is below this (logL units): 1e-2 in the stage-2 pass (pplacer's
+  // tolerance 0.01, whose Brent stops within about 0.05 logL of the
+  // optimum), 1e-7 in the final 1e-5 pass -- plus the evaluation's rounding
+  // allowance.  A step-size rule alone is unsound here: near a zero pendant
+  // the curvature is huge and Newton steps are tiny while the gradient is not.
+  __device__ float newton_gain_tol() const { return tol >= 1e-3 ? 1e-2f : 1e-7f; }
 
   __device__ void request(double pp, double dd, double xx, bool derivs) {
     req_p = (float)pp;
