@@ -48,6 +48,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--optimizer", default="newton", choices=["newton", "brent"])
+    ap.add_argument("--brent-steps", type=int, default=2,
+                    help="untimed-region comparison: placement steps with the Brent replica")
     ap.add_argument("--queries", type=int, default=None)
     ap.add_argument("--workload", default="dna_1k")
     ap.add_argument("--cpu-sample", type=int, default=512, help="queries in the CPU-baseline sample")
@@ -224,6 +226,20 @@ def run_ours(args):
     clocks = sampler.stop() if sampler else None
     t_dev = max_over_ranks(dist, sum(ms_steps) / 1e3)
     value = Q * world * args.steps / t_dev
+    # ---- the reference's optimiser (GSL Brent replica) on the same kernel path ----
+    brent = None
+    if args.optimizer == "newton" and args.brent_steps > 0:
+        bprefs = E.default_prefs(optimizer=0, **w.prefs)
+        eng.run(bprefs)
+        bms, bev, btr = 0.0, 0.0, 0.0
+        for _ in range(args.brent_steps):
+            eng.run(bprefs)
+            ms, cnt = eng.timings()
+            bms += ms[5]
+            bev += cnt[2]
+            btr += cnt[1]
+        brent = {"value": Q * args.brent_steps / (bms / 1e3), "unit": "placements/s",
+                 "evals_per_trial": bev / btr, "steps": args.brent_steps}
     # ---- end to end through pgb_place, host buffers ----
     seqs = "".join(w.query_seqs).encode()
     kam = prefs.keep_at_most
@@ -293,6 +309,8 @@ def run_ours(args):
                          "sample": "%d queries of %s (%.1f s)" % (cpu_n, args.workload, cpu_dt)},
         "e2e": {"value": e2e, "unit": "placements/s", "h2d_bytes_per_step": Q * S,
                 "d2h_bytes_per_step": Q * kam * C.sizeof(L.Placement) + 8 * Q},
+        "brent_replica": brent,
+        "newton_evals_per_trial": counts[2] / counts[1] if counts[1] else None,
         "gpu_launches": int(launches),
         "clocks": clocks,
     }

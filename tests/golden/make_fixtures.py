@@ -14,6 +14,10 @@ Outputs (committed; the GPU machine never reads the reference):
       the masked-logdot known answers of tests/pplacer/test_linear.ml:4-28.
   gamma_kat.json
       discrete_gamma 4 0.5 from the doc comment at pplacer_src/gamma.ml:345-352.
+  jplace_trees.json
+      the numbered reference trees of tests/data/simple/test1.jplace and
+      tests/data/trim/trim_out.jplace, with the trees parsed to post-order
+      arrays (the jplace writer must reproduce the numbered strings).
 """
 import json
 import math
@@ -163,10 +167,33 @@ def main(ref_root):
     }
     with open(os.path.join(HERE, "linear_kat.json"), "w") as f:
         json.dump(kat, f, indent=1)
+    write_jplace_fixture(ref_root)
     with open(os.path.join(HERE, "gamma_kat.json"), "w") as f:
         json.dump({"n_cat": 4, "alpha": 0.5,
                    "rates": [0.0333877533835995541, 0.251915917593438454, 0.820268481973647878,
                              2.89442784704931411]}, f, indent=1)
+
+
+def jplace_tree_fixture(ref_root, rel):
+    """The numbered reference tree of one of the reference's jplace test
+    files: the tree without its edge numbers (parsed to post-order arrays)
+    and the numbered string pplacer wrote, in version-3 braces."""
+    with open(os.path.join(ref_root, rel)) as f:
+        tree = json.load(f)["tree"]
+    numbered = re.sub(r"\[(\d+)\]", r"{\1}", tree)  # version 1 wrote [n]
+    plain = re.sub(r"\{\d+\}", "", numbered)
+    parent, bl, label = parse_newick(plain)
+    ids = [int(m) for m in re.findall(r"\{(\d+)\}", numbered)]
+    assert sorted(ids) == list(range(len(parent)))
+    return {"source": rel, "parent": parent, "bl": bl, "label": label, "numbered": numbered}
+
+
+def write_jplace_fixture(ref_root):
+    # tests/data/simple/test1.jplace (version 1) and tests/data/trim/trim_out.jplace (version 3)
+    fx = [jplace_tree_fixture(ref_root, "tests/data/simple/test1.jplace"),
+          jplace_tree_fixture(ref_root, "tests/data/trim/trim_out.jplace")]
+    with open(os.path.join(HERE, "jplace_trees.json"), "w") as f:
+        json.dump(fx, f, indent=1)
 
 
 if __name__ == "__main__":

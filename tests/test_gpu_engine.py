@@ -312,3 +312,19 @@ def test_edge_cases(small, oracle_lib):
     got = eng2.trials([(0, 3, 0.1, 0.0, 1e-5)], optimizer=0)
     st, ref = oref2.optimize_location(w2.query_seqs[0], 3, 0.1, 0.0, 1e-5)
     assert got[0]["dist"] == 0.0 and abs(got[0]["like"] - ref[0]) <= LOGL_RTOL * abs(ref[0])
+
+
+def test_jplace_of_engine_results(small):
+    """Engine results through the jplace writer (placerun_io.ml:58-90)."""
+    import json
+    from pplacer_gb300 import engine as E
+    from pplacer_gb300 import jplace
+    w, oref, eng = small
+    qs = w.query_seqs[:12]
+    res, st = eng.place(qs, E.default_prefs())
+    doc = json.loads(jplace.to_jplace(res, ["q%d" % i for i in range(len(qs))], w.parent, w.bl))
+    assert len(doc["placements"]) == sum(1 for r in res if r)
+    f = doc["fields"]
+    for row, r in zip(doc["placements"], [r for r in res if r]):
+        assert [p[f.index("edge_num")] for p in row["p"]] == [p[0] for p in r]
+        assert abs(sum(p[f.index("like_weight_ratio")] for p in row["p"]) - 1.0) < 1e-9

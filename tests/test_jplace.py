@@ -1,0 +1,40 @@
+"""jplace writer (placerun_io.ml:58-90): numbered tree strings against the
+reference's own jplace test files, field order, number formatting."""
+import json
+import os
+
+from pplacer_gb300 import jplace
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden", "jplace_trees.json")
+
+
+def test_numbered_tree_matches_reference_files():
+    for fx in json.load(open(GOLD)):
+        got = jplace.numbered_newick(fx["parent"], fx["bl"], fx["label"])
+        assert got == fx["numbered"], fx["source"]
+
+
+def test_quote_label():
+    assert jplace.quote_label("taxon_1") == "taxon_1"
+    assert jplace.quote_label("a b") == "'a b'"
+    assert jplace.quote_label("x(1)") == "'x(1)'"
+    assert jplace.quote_label("it's") == "'it\\'s'"
+    assert jplace.quote_label("a\\b") == "'a\\\\b'"
+
+
+def test_document_layout():
+    parent, bl = [2, 2, -1], [0.1, 0.25, 0.0]
+    results = [[(0, -1309.83, 0.710949502625, 0.5, 0.9), (1, -1310.1, 0.289050497375, 1.0, 2.4)], [],
+               [(1, -20.0, 1.0, 0.125, 1e-08)]]
+    text = jplace.to_jplace(results, ["q1", "q2", "q3"], parent, bl, ["A", "B", ""], invocation="test run")
+    doc = json.loads(text)
+    assert list(doc) == ["tree", "placements", "metadata", "version", "fields"]
+    assert doc["version"] == 3
+    assert doc["fields"] == ["distal_length", "edge_num", "like_weight_ratio", "likelihood", "pendant_length"]
+    assert doc["tree"] == "(A:0.1{0},B:0.25{1}):0{2};"
+    assert doc["metadata"] == {"invocation": "test run"}
+    # the query without placements is left out; rows follow the field order
+    assert [r["nm"] for r in doc["placements"]] == [[["q1", 1]], [["q3", 1]]]
+    assert doc["placements"][0]["p"][0] == [0.5, 0, 0.710949502625, -1309.83, 0.9]
+    assert "-1309.83," in text and "1e-08" in text  # %.12g numbers, %d edge numbers
+    assert "0.710949502625" in text
