@@ -195,6 +195,13 @@ typedef struct {
   double keep_factor;        /* [0.01] */
   int optimizer;             /* 0: Brent as the reference (minimization.ml:83-101);
                                 1: batched safeguarded Newton on the adjoint */
+  int calc_pp;               /* [0] posterior probabilities (-p, core.ml:378-401); Newton form,
+                                nucleotide Gamma models */
+  int prior;                 /* [0] pendant prior: 0 exponential with mean = tree length / edges,
+                                1 uniform (--unif-prior), 2 informative exponential
+                                (--inform-prior, core.ml:34-51) */
+  double pp_rel_err;         /* [0.01] accepted; the quadrature is fixed (see marginal_like) */
+  double prior_lower;        /* [0.0] added to the informative prior's means (--prior-lower) */
 } pgb_prefs;
 
 void pgb_prefs_default(pgb_prefs *p);
@@ -207,6 +214,8 @@ typedef struct {
   double lwr;     /* like_weight_ratio */
   double dist;    /* distal_length */
   double pend;    /* pendant_length */
+  double marginal_like;  /* marginal_like (calc_pp), else NaN */
+  double post_prob;      /* post_prob (calc_pp), else NaN */
 } pgb_placement;
 
 /* Per-query status codes. */
@@ -247,7 +256,10 @@ pgb_status pgb_queries_rank(pgb_engine *e, const pgb_prefs *prefs, int rk, int *
  * loaded queries (Three_tax.optimize from the given start, core.ml:401-425 with
  * the retry from default lengths).  optimizer: 0 Brent, 1 Newton;
  * mode 0 optimises, mode 1 only evaluates logL and its derivatives at the
- * start point (the forward/backward pair).  Outputs per trial:
+ * start point (the forward/backward pair), mode 2 computes the marginal
+ * likelihood around the start point, which must be the location's optimum
+ * (Three_tax.calc_marg_prob, three_tax.ml:169-215; prefs.prior selects the
+ * pendant prior; the result is in like).  Outputs per trial:
  * like, pend, dist, status (0 ok, 1 max-iter, 2 failed), n_evals, and
  * derivs[6] = dL/dpend, dL/ddist, d2L/dpend2, d2L/ddist2, d2L/dpend ddist,
  * (unused) at the final point. */

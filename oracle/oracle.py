@@ -353,3 +353,86 @@ def polish(ref, seq, loc, pend, dist, max_pend=2.0, iters=100):
         if step < 1e-10:
             break
     return v[0], p, d
+
+
+def prior_means(parent, bl, prior, prior_lower=0.0):
+    """Pendant prior mean per node (pplacer_run.ml:379-389): prior 0 (the
+    default) the flat exponential with mean tree length / edge count,
+    2 the informative exponential of core.ml:34-51 (average distance from the
+    node to the leaves below it, plus its branch length and prior_lower);
+    prior 1 (uniform) has no mean (None)."""
+    n = len(parent)
+    if prior == 1:
+        return None
+    if prior == 0:
+        edges = [i for i in range(n) if parent[i] >= 0]
+        return [sum(bl[i] for i in edges) / len(edges)] * n
+    children = [[] for _ in range(n)]
+    for i, p in enumerate(parent):
+        if p >= 0:
+            children[p].append(i)
+
+    def dists(i):  # leaf distances below node i, measured from node i
+        if not children[i]:
+            return [0.0]
+        out = []
+        for c in children[i]:
+            out += [x + bl[c] for x in dists(c)]
+        return out
+    return [float(np.mean(dists(i))) + bl[i] + prior_lower for i in range(n)]
+
+
+def marginal_like(ref, seq, loc, pend, dist, prior, mu=None, max_pend=2.0, rel=1e-9):
+    """Three_tax.calc_marg_prob (three_tax.ml:169-215) in FP64:
+    base + log((1/cut) int_0^cut int_0^U exp(L(p, d) - base) prior(p) dp dd),
+    base = L at (pend, dist), the location's optimum; U = where
+    L(., dist) + log prior has dropped 10 below its value at the optimum
+    (find_upper_limit, three_tax.ml:125-160), found here by bisection to
+    1e-10 where the reference runs 10 Brent iterations to 0.02 (the integral
+    beyond either point is below e^-10 of the total); a zero-length edge
+    integrates the pendant only, at the edge midpoint.  The integrals use
+    adaptive Gauss-Kronrod quadrature (scipy.integrate.quad) to relative
+    error `rel`, in place of GSL's QNG to pp_rel_err: both approximate the
+    same integral."""
+    import math
+    from scipy import integrate
+    cut = float(ref.bl[loc])
+
+    def L(p, d):
+        st, v = ref.loglike_derivs(seq, loc, max(p, 1e-12), min(max(d, 0.0), cut))
+        return v[0]
+
+    def lp(x):
+        return 0.0 if prior == 1 else -math.log(mu) - x / mu
+    base = L(pend, dist)
+    target = base + lp(pend) - 10.0
+    lo, hi, step = pend, pend, max(1e-4, 0.01 * pend)
+    while True:
+        q = min(hi + step, max_pend)
+        if q <= hi:
+            break
+        if not (L(q, dist) + lp(q) > target):
+            lo, hi = hi, q
+            while hi - lo > 1e-10:
+                m = 0.5 * (lo + hi)
+                if L(m, dist) + lp(m) > target:
+                    lo = m
+                else:
+                    hi = m
+            break
+        hi = q
+        step *= 2
+    U = hi
+
+    def inner(d):
+        pts = [pend] if 0 < pend < U else None
+        v, _ = integrate.quad(lambda p: math.exp(L(p, d) - base + lp(p)), 0.0, U, epsabs=0.0, epsrel=rel,
+                              points=pts, limit=400)
+        return v
+    if cut <= 1e-10:
+        I = inner(0.5 * cut)
+    else:
+        pts = [dist] if 0 < dist < cut else None
+        v, _ = integrate.quad(inner, 0.0, cut, epsabs=0.0, epsrel=rel, points=pts, limit=400)
+        I = v / cut
+    return base + math.log(I)

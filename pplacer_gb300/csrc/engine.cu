@@ -671,6 +671,8 @@ __global__ void k_finalize(BBCtx c, int keep_at_most, const int *__restrict__ ke
     pgb_placement p;
     p.edge = c.edge_nodes[e.edge];
     p.pad = 0;
+    p.marginal_like = NAN;
+    p.post_prob = NAN;
     if (t.status == ST_FAILED || t.status == ST_STARTFAIL) { p.like = e.like; p.pend = e.pend; p.dist = e.dist; }
     else { p.like = t.like; p.pend = t.pend; p.dist = t.dist; }
     like[j] = p.like;
@@ -702,6 +704,8 @@ __global__ void k_finalize(BBCtx c, int keep_at_most, const int *__restrict__ ke
 // ---------------------------------------------------------------------------
 struct PlaceCtx {
   BBCtx bb;
+  int calc_pp, prior_kind;  // prior_kind: 0 uniform, 1 exponential with per-node mean prior_mu
+  const double *prior_mu;
   const int *qorder;  // queries, longest first
   int *qnext;         // next position in qorder
   int keep_at_most;
@@ -723,6 +727,7 @@ __global__ void __launch_bounds__(32, kWarpTrialMinCtas) k_place_warp(TrialCtx c
   // its baseball trials (refine < 0) to the refinement of its kept
   // locations (refine = index of the next one).
   int q = -1, next = 0, nres = 0, nk = 0, refine = -1;
+  bool marginal = false;  // the next trial is the marginal likelihood of kept location `refine`
   long strikes = 0;
   double record = -INFINITY, pend_hint = b.start_pend;
   unsigned long long n_bb = 0;
@@ -735,7 +740,7 @@ __global__ void __launch_bounds__(32, kWarpTrialMinCtas) k_place_warp(TrialCtx c
       q = p.qorder[qi];
       if (lane == 0) p.n_out[q] = 0;
       if (b.qstatus[q] != PGB_Q_OK || b.rk < 1) { q = -1; continue; }
-      next = 0; nres = 0; nk = 0; refine = -1; strikes = 0; record = -INFINITY; n_bb = 0;
+      next = 0; nres = 0; nk = 0; refine = -1; strikes = 0; record = -INFINITY; n_bb = 0; marginal = false;
       pend_hint = b.start_pend;
     }
     ResEntry *r = b.res + (long)q * b.maxr;
@@ -757,24 +762,47 @@ __global__ void __launch_bounds__(32, kWarpTrialMinCtas) k_place_warp(TrialCtx c
       t.pend0 = e.pend;
       t.dist0 = e.dist;
       t.tol = 1e-5;  // final_tolerance (core.ml:160)
-      t.seeded = 1;  // the stage-2 evaluation at (pend0, dist0); Newton form only
+      t.seeded = 1;  // the evaluation at (pend0, dist0); the Newton form does not redo it
       t.seed = e.ev;
+      if (marginal) {  // after the refinement: e holds the refined optimum
+        t.marginal = 1;
+        t.prior_kind = p.prior_kind;
+        t.prior_mu = p.prior_mu[t.node];
+      }
     }
     const TrialRes tr = trial_warp<RP>(c, sm, ring, lane, t);
-    if (refine >= 0) {  // ---- a refined location ----
+    if (refine >= 0) {  // ---- a refined location, or its marginal likelihood ----
       pgb_placement *o = p.out + (long)q * p.keep_at_most;
-      if (lane == 0) {
-        const ResEntry e = r[refine];
-        pgb_placement pl;
-        pl.edge = t.node;
-        pl.pad = 0;
-        pl.lwr = 0;
-        if (tr.status == ST_FAILED || tr.status == ST_STARTFAIL) { pl.like = e.like; pl.pend = e.pend; pl.dist = e.dist; }
-        else { pl.like = tr.like; pl.pend = tr.pend; pl.dist = tr.dist; }
-        o[refine] = pl;
+      if (marginal) {
+        if (lane == 0) o[refine].marginal_like = tr.like;
+        marginal = false;
+      } else {
+        const bool ok = !(tr.status == ST_FAILED || tr.status == ST_STARTFAIL);
+        if (lane == 0) {
+          ResEntry e = r[refine];
+          pgb_placement pl;
+          pl.edge = t.node;
+          pl.pad = 0;
+          pl.lwr = 0;
+          pl.marginal_like = NAN;
+          pl.post_prob = NAN;
+          if (!ok) { pl.like = e.like; pl.pend = e.pend; pl.dist = e.dist; }
+          else { pl.like = tr.like; pl.pend = tr.pend; pl.dist = tr.dist; }
+          o[refine] = pl;
+          if (ok && p.calc_pp) {  // the marginal likelihood integrates around the refined optimum
+            e.pend = tr.pend; e.dist = tr.dist; e.ev = tr.last;
+            r[refine] = e;
+          }
+        }
+        __syncwarp();
+        if (p.calc_pp) {
+          marginal = true;
+          continue;
+        }
       }
       if (++refine < nk) continue;
-      // like_weight_ratio, then stable sort by it, descending
+      // like_weight_ratio (and with calc_pp the posterior probabilities,
+      // core.ml:396-401), then stable sort by like_weight_ratio, descending
       if (lane == 0) {
         atomicAdd(&p.tstats[1], (unsigned long long)nk);
         const int m = min(nk, 64);
@@ -783,6 +811,12 @@ __global__ void __launch_bounds__(32, kWarpTrialMinCtas) k_place_warp(TrialCtx c
           for (int k = 0; k < m; k++) tot += exp(o[k].like - o[j].like);
           o[j].lwr = 1. / tot;
         }
+        if (p.calc_pp)
+          for (int j = 0; j < m; j++) {
+            double tot = 0;
+            for (int k = 0; k < m; k++) tot += exp(o[k].marginal_like - o[j].marginal_like);
+            o[j].post_prob = 1. / tot;
+          }
         for (int i = 1; i < m; i++) {
           pgb_placement x = o[i];
           int j = i - 1;
@@ -918,6 +952,11 @@ struct pgb_engine {
   pgb_placement *d_out = nullptr;
   int *d_qorder = nullptr;  // queries longest first (whole-query warp kernel)
   size_t qorder_cap = 0;
+  double *d_gl = nullptr;        // Gauss-Legendre rule of the marginal likelihood
+  double *d_prior_mu = nullptr;  // pendant prior mean per node, for (mu_prior, mu_lower)
+  std::vector<double> h_prior_mu;
+  int mu_prior = -1;
+  double mu_lower = 0;
   int *d_nout = nullptr;
   int out_keep = 0;
   // trial-kernel shape per length bin: threads per CTA, shared-memory windows
@@ -1109,6 +1148,7 @@ TrialCtx trial_ctx(pgb_engine *e, const pgb_prefs *p, int optimizer, int mode) {
   c.optimizer = optimizer;
   c.mode = mode;
   c.stats = e->d_stats;
+  c.gl = e->d_gl;
   return c;
 }
 
@@ -1257,6 +1297,58 @@ pgb_status ensure_run_buffers(pgb_engine *e, const pgb_prefs *p, int rk, int max
   return PGB_OK;
 }
 
+// Gauss-Legendre rule on [-1, 1]: the roots of P_n by Newton's method from
+// the Chebyshev-like guess cos(pi (i + 3/4) / (n + 1/2)), P_n and P_n' by the
+// three-term recurrence; weights 2 / ((1 - x^2) P_n'(x)^2).
+void gauss_legendre(int n, double *x, double *w) {
+  for (int i = 0; i < n; i++) {
+    double z = std::cos(M_PI * (i + 0.75) / (n + 0.5)), dp = 1;
+    for (int it = 0; it < 100; it++) {
+      double p0 = 1, p1 = z;
+      for (int k = 2; k <= n; k++) {
+        double pk = ((2 * k - 1) * z * p1 - (k - 1) * p0) / k;
+        p0 = p1;
+        p1 = pk;
+      }
+      dp = n * (z * p1 - p0) / (z * z - 1);
+      double dz = p1 / dp;
+      z -= dz;
+      if (std::fabs(dz) < 1e-16) break;
+    }
+    x[i] = -z;  // ascending
+    w[i] = 2 / ((1 - z * z) * dp * dp);
+  }
+}
+
+// Pendant prior means per node (pplacer_run.ml:379-389): the flat
+// exponential's mean is the tree length over the edge count; the informative
+// prior's mean at node i is the average over the leaves below i of their
+// distance to i, plus bl(i) + prior_lower (core.ml:34-51, top_segment_f =
+// (+) prior_lower).
+pgb_status ensure_prior_means(pgb_engine *e, int prior, double prior_lower) {
+  if (e->d_prior_mu && e->mu_prior == prior && e->mu_lower == prior_lower) return PGB_OK;
+  std::vector<double> mu(e->n_nodes, 0.0);
+  if (prior == 2) {
+    std::vector<double> cnt(e->n_nodes, 0.0), sum(e->n_nodes, 0.0);
+    for (int i = 0; i < e->n_nodes; i++) {  // post-order: children before parents
+      if (e->ch_start[i + 1] == e->ch_start[i]) cnt[i] = 1;
+      mu[i] = sum[i] / cnt[i] + e->bl[i] + prior_lower;
+      int p = e->parent[i];
+      if (p >= 0) { cnt[p] += cnt[i]; sum[p] += sum[i] + cnt[i] * e->bl[i]; }
+    }
+  } else {
+    double len = 0;
+    for (int i : e->edge_nodes) len += e->bl[i];
+    for (double &m : mu) m = len / e->n_edges;
+  }
+  pgb_status s;
+  if ((s = upload(&e->d_prior_mu, mu.data(), mu.size(), e->st))) return s;
+  e->h_prior_mu = mu;
+  e->mu_prior = prior;
+  e->mu_lower = prior_lower;
+  return PGB_OK;
+}
+
 template <int RP>
 pgb_status launch_place_warp_rp(pgb_engine *e, TrialCtx c, const PlaceCtx &pc) {
   size_t smem = warp_trial_smem_bytes(e->NM, e->ncode);
@@ -1292,6 +1384,10 @@ pgb_status run_whole_queries(pgb_engine *e, const pgb_prefs *p, const BBCtx &c, 
   pc.out = e->d_out;
   pc.n_out = e->d_nout;
   pc.tstats = e->d_stats + 2;
+  pc.calc_pp = p->calc_pp;
+  pc.prior_kind = p->prior == 1 ? 0 : 1;
+  if ((s = ensure_prior_means(e, p->prior, p->prior_lower))) return s;
+  pc.prior_mu = e->d_prior_mu;
   switch (e->RP) {
     case 1: s = launch_place_warp_rp<1>(e, tc, pc); break;
     case 2: s = launch_place_warp_rp<2>(e, tc, pc); break;
@@ -1333,6 +1429,10 @@ void pgb_prefs_default(pgb_prefs *p) {
   p->keep_at_most = 7;
   p->keep_factor = 0.01;
   p->optimizer = 1;
+  p->calc_pp = 0;
+  p->prior = 0;
+  p->pp_rel_err = 0.01;
+  p->prior_lower = 0.0;
 }
 
 pgb_status pgb_engine_create(const pgb_model_desc *m, const pgb_tree_desc *t, pgb_engine **out) {
@@ -1449,6 +1549,8 @@ pgb_status pgb_engine_create(const pgb_model_desc *m, const pgb_tree_desc *t, pg
   std::vector<uint8_t> scat(e->S, 0);
   if (e->gcat)
     for (int s = 0; s < e->S; s++) scat[s] = (uint8_t)e->site_cats[s];
+  std::vector<double> glr(2 * kGlPoints);
+  gauss_legendre(kGlPoints, glr.data(), glr.data() + kGlPoints);
   pgb_status s;
   if ((s = upload(&e->d_mf, mf.data(), mf.size(), e->st)) || (s = upload(&e->d_bl, e->bl.data(), e->bl.size(), e->st)) ||
       (s = upload(&e->d_Xd, e->X.data(), e->X.size(), e->st)) ||
@@ -1457,6 +1559,7 @@ pgb_status pgb_engine_create(const pgb_model_desc *m, const pgb_tree_desc *t, pg
       (s = upload(&e->d_ratesd, e->rates.data(), e->rates.size(), e->st)) ||
       (s = upload(&e->d_statdd, e->statd.data(), e->statd.size(), e->st)) ||
       (s = upload(&e->d_lvd, lvd.data(), lvd.size(), e->st)) ||
+      (s = upload(&e->d_gl, glr.data(), glr.size(), e->st)) ||
       (s = upload(&e->d_site_cat, scat.data(), scat.size(), e->st)) ||
       (s = upload(&e->d_char_code, cc.data(), cc.size(), e->st)) ||
       (s = upload(&e->d_informative, inf.data(), inf.size(), e->st)) ||
@@ -1496,7 +1599,7 @@ pgb_status pgb_engine_destroy(pgb_engine *e) {
                   e->d_amb_list, e->d_seqs, e->d_qcode, e->d_mcode, e->d_reind, e->d_rcode, e->d_qlen,
                   e->d_qstatus, e->d_scores, e->d_rank, e->d_bb, e->d_res, e->d_tbase, e->d_tcount, e->d_keep_idx, e->d_keep_n,
                   e->d_trials, e->d_tres, e->d_bin_list, e->d_small, e->d_out, e->d_nout, e->d_stats,
-                  e->d_qorder};
+                  e->d_qorder, e->d_gl, e->d_prior_mu};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   for (int i = 0; i < 8; i++)
@@ -1691,8 +1794,10 @@ pgb_status pgb_queries_load(pgb_engine *e, int n_queries, const char *seqs) {
 static pgb_status check_prefs(const pgb_prefs *p) {
   if (!p || p->keep_at_most < 1 || p->keep_at_most > 64 || p->max_pitches < 0 || p->max_strikes < 0 ||
       !(p->max_pend > 1e-8) || !(p->start_pend > 0) || !(p->initial_tolerance > 0) || p->optimizer < 0 ||
-      p->optimizer > 1) {
-    set_error("invalid prefs (keep_at_most 1..64, max_pend > 1e-8, tolerances > 0, optimizer 0|1)");
+      p->optimizer > 1 || p->calc_pp < 0 || p->calc_pp > 1 || p->prior < 0 || p->prior > 2 ||
+      !(p->pp_rel_err > 0) || !(p->prior_lower >= 0)) {
+    set_error("invalid prefs (keep_at_most 1..64, max_pend > 1e-8, tolerances > 0, optimizer 0|1, calc_pp 0|1, "
+              "prior 0|1|2, pp_rel_err > 0, prior_lower >= 0)");
     return PGB_ERR_ARG;
   }
   return PGB_OK;
@@ -1763,6 +1868,11 @@ pgb_status pgb_queries_run(pgb_engine *e, const pgb_prefs *p) {
   for (int b = 0; b < kBins; b++)
     if (e->tune_threads[b] != 32) whole_query = false;
   if (whole_query) return run_whole_queries(e, p, c, tc);
+  if (p->calc_pp) {
+    set_error("calc_pp: posterior probabilities need the whole-query kernel (nucleotide Gamma models, "
+              "threads 32 in every bin)");
+    return PGB_ERR_ARG;
+  }
   k_bb_init<<<(n + 255) / 256, 256, 0, e->st>>>(c);
   PGB_LAUNCH_CHECK();
   double n_trials_total = 0;
@@ -1985,8 +2095,9 @@ pgb_status pgb_queries_trials(pgb_engine *e, const pgb_prefs *p, int optimizer, 
   if (!e || !e->glvs_ready || e->Q < 1) { set_error("trials: no GLVs or no queries"); return PGB_ERR_STATE; }
   pgb_status s;
   if ((s = check_prefs(p))) return s;
-  if (optimizer < 0 || optimizer > 1 || mode < 0 || mode > 1 || n_trials < 0) { set_error("trials: bad mode"); return PGB_ERR_ARG; }
+  if (optimizer < 0 || optimizer > 1 || mode < 0 || mode > 2 || n_trials < 0) { set_error("trials: bad mode"); return PGB_ERR_ARG; }
   if (!n_trials) return PGB_OK;
+  if (mode == 2 && (s = ensure_prior_means(e, p->prior, p->prior_lower))) return s;
   std::vector<TrialIn> tin(n_trials);
   int max_sq = 1;
   for (int i = 0; i < n_trials; i++) {
@@ -1997,6 +2108,10 @@ pgb_status pgb_queries_trials(pgb_engine *e, const pgb_prefs *p, int optimizer, 
     }
     if (e->h_qlen[t.query] < 1) { set_error("trials: query %d has no informative site", t.query); return PGB_ERR_ARG; }
     tin[i] = TrialIn{t.query, t.edge, t.pend0, t.dist0, t.tol};
+    if (mode == 2) {
+      tin[i].prior_kind = p->prior == 1 ? 0 : 1;
+      tin[i].prior_mu = e->h_prior_mu[t.edge];
+    }
     max_sq = std::max(max_sq, e->h_qlen[t.query]);
   }
   if ((size_t)n_trials > e->trials_cap) {

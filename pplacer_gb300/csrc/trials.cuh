@@ -31,6 +31,9 @@ struct TrialIn {
   double pend0, dist0, tol;
   int seeded;    // the Newton form: seed is the evaluation at (pend0, dist0)
   EvalOut seed;  //   (derivatives included), which it then does not redo
+  int marginal;     // 1: the marginal likelihood (mode 2) around (pend0, dist0)
+  int prior_kind;   //   pendant prior: 0 uniform, 1 exponential
+  double prior_mu;  //   mean of the exponential
 };
 struct TrialRes {
   double like, pend, dist;
@@ -57,7 +60,10 @@ struct TrialCtx {
   int optimizer, mode;
   int smem_win, cap;
   unsigned long long *stats;  // [0] objective evaluations, [1] site evaluations
+  const double *gl;           // Gauss-Legendre rule on [-1, 1]: kGlPoints nodes, then weights
 };
+
+constexpr int kGlPoints = 12;  // nodes per panel of the marginal-likelihood quadrature
 
 struct Ctrl {
   float pend, dist, prox;
@@ -160,6 +166,13 @@ struct Optimiser {
   double raw, left, right, lefty, righty, smaller, miny, prevx, pv;
   double xl, xu, xm, fl, fu, fm, v, w, fv, fw, bd, be, u, fz, z, probe_dx, fval, fx;
   bool probe;
+  // marginal likelihood state (mode 2)
+  int prior_kind;
+  double prior_mu;
+  const double *gl;
+  double base, tgt, lo_b, hi_b, stp, sig_p, sig_d, acc_in, acc_out, qp, qd, wd;
+  double ppan[3], dpan[3];
+  int k_srch, n_ppan, n_dpan, ipan, jpan, ip, jd;
   // Newton state
   bool seeded;
   EvalOut seed;
@@ -177,6 +190,11 @@ struct Optimiser {
   // allowance.  A step-size rule alone is unsound here: near a zero pendant
   // the curvature is huge and Newton steps are tiny while the gradient is not.
   __device__ float newton_gain_tol() const { return tol >= 1e-3 ? 1e-2f : 1e-7f; }
+
+  // log of the pendant prior density (core.ml:86-92): uniform 1 or
+  // Gsl.Randist.exponential_pdf with mean mu
+  __device__ double log_prior(double pnd) const { return prior_kind == 0 ? 0.0 : -log(prior_mu) - pnd / prior_mu; }
+  __device__ double value_of(const EvalOut &o, double pnd) const { return full(o) + log_prior(pnd); }
 
   __device__ void request(double pp, double dd, double xx, bool derivs) {
     req_p = (float)pp;
@@ -218,6 +236,7 @@ struct Optimiser {
           PGB_YIELD(1);
           return false;
         }
+        if (mode == 2) goto MARGINAL;
         if (optimizer == 1) goto NEWTON;
         // ---------------- Brent replica (three_tax.ml:285-320) ----------------
       BRENT_ATTEMPT:
@@ -447,6 +466,128 @@ struct Optimiser {
         prox = (double)((float)cut - d);
         last = cur;
         L_last = full(cur);
+        return false;
+        // ---------------- marginal likelihood (three_tax.ml:169-215) ----------------
+        // log of (1/cut) int_0^cut int exp(L(p, d)) prior(p) dp dd, for the
+        // posterior probabilities of core.ml:378-401.  The pendant range
+        // ends where L + log prior has dropped 10 below its value at the
+        // optimum (find_upper_limit, three_tax.ml:125-160; searched upward
+        // and downward here), the distal range is the optimum +- 6 marginal
+        // standard deviations of the Hessian's Gaussian (all of [0, cut]
+        // when the Hessian is not negative definite); both are split at
+        // the optimum and integrated by tensor Gauss-Legendre, kGlPoints
+        // nodes per panel, in place of GSL's QNG.  A zero-length edge
+        // integrates the pendant only, at the edge midpoint.
+      MARGINAL:
+        p = fminf(fmaxf((float)pend, 1e-8f), (float)max_pend);
+        d = fminf(fmaxf((float)dist, 0.f), (float)cut);
+        if (seeded) {
+          seeded = false;
+          last = seed;
+        } else {
+          request(p, d, (float)cut - d, true);
+          PGB_YIELD(30);
+        }
+        cur = last;
+        base = full(cur);
+        pend = p;
+        dist = d;
+        prox = (double)((float)cut - d);
+        if (!isfinite(base)) { status = ST_FAILED; L_last = base; return false; }
+        tgt = value_of(cur, p) - 10.0;
+        {
+          const double hpp = cur.h[0], hdd = cur.h[1], hpd = cur.h[2];
+          const double det = hpp * hdd - hpd * hpd;
+          const bool nd = hpp < 0.0 && hdd < 0.0 && det > 0.0;
+          sig_p = nd ? sqrt(-hdd / det) : 0.05;
+          sig_d = nd ? sqrt(-hpp / det) : 1e30;
+        }
+        // upper pendant limit
+        stp = fmax(sig_p, 1e-4);
+        lo_b = p;
+        hi_b = p;
+        for (k_srch = 0; k_srch < 60; k_srch++) {
+          qp = fmin(hi_b + stp, max_pend);
+          if (qp <= hi_b) break;  // at max_pend
+          request(qp, d, (float)cut - d, false);
+          PGB_YIELD(31);
+          if (!(value_of(last, qp) > tgt)) { lo_b = hi_b; hi_b = qp; break; }
+          hi_b = qp;
+          lo_b = qp;
+          stp *= 2.0;
+        }
+        for (k_srch = 0; k_srch < 6 && hi_b > lo_b; k_srch++) {  // refine the crossing
+          qp = 0.5 * (lo_b + hi_b);
+          request(qp, d, (float)cut - d, false);
+          PGB_YIELD(32);
+          if (!(value_of(last, qp) > tgt)) hi_b = qp;
+          else lo_b = qp;
+        }
+        ppan[2] = hi_b;
+        // lower pendant limit
+        stp = fmax(sig_p, 1e-4);
+        lo_b = p;
+        hi_b = p;
+        for (k_srch = 0; k_srch < 60; k_srch++) {
+          qp = fmax(lo_b - stp, 0.0);
+          if (qp >= lo_b) break;  // at 0
+          request(fmax(qp, 1e-8), d, (float)cut - d, false);
+          PGB_YIELD(33);
+          if (!(value_of(last, qp) > tgt)) { hi_b = lo_b; lo_b = qp; break; }
+          lo_b = qp;
+          hi_b = qp;
+          stp *= 2.0;
+        }
+        for (k_srch = 0; k_srch < 6 && hi_b > lo_b; k_srch++) {
+          qp = 0.5 * (lo_b + hi_b);
+          request(qp, d, (float)cut - d, false);
+          PGB_YIELD(34);
+          if (!(value_of(last, qp) > tgt)) lo_b = qp;
+          else hi_b = qp;
+        }
+        ppan[0] = lo_b;
+        ppan[1] = p;
+        // distal range
+        if (cut <= 1e-10) {
+          n_dpan = 0;  // zero-length edge: the pendant integral alone, at cut / 2
+        } else {
+          dpan[0] = fmax(0.0, (double)d - 6.0 * sig_d);
+          dpan[1] = d;
+          dpan[2] = fmin(cut, (double)d + 6.0 * sig_d);
+          n_dpan = 2;
+        }
+        acc_out = 0.0;
+        for (jpan = 0; jpan < (n_dpan ? n_dpan : 1); jpan++) {
+          if (n_dpan && !(dpan[jpan + 1] > dpan[jpan])) continue;
+          for (jd = 0; jd < (n_dpan ? kGlPoints : 1); jd++) {
+            if (n_dpan) {
+              const double half = 0.5 * (dpan[jpan + 1] - dpan[jpan]);
+              qd = dpan[jpan] + half * (1.0 + gl[jd]);
+              wd = half * gl[kGlPoints + jd];
+            } else {
+              qd = 0.5 * cut;
+              wd = 1.0;
+            }
+            acc_in = 0.0;
+            for (ipan = 0; ipan < 2; ipan++) {
+              if (!(ppan[ipan + 1] > ppan[ipan])) continue;
+              for (ip = 0; ip < kGlPoints; ip++) {
+                {
+                  const double half = 0.5 * (ppan[ipan + 1] - ppan[ipan]);
+                  qp = ppan[ipan] + half * (1.0 + gl[ip]);
+                }
+                request(fmax(qp, 1e-8), qd, cut - qd, false);
+                PGB_YIELD(35);
+                acc_in += 0.5 * (ppan[ipan + 1] - ppan[ipan]) * gl[kGlPoints + ip] *
+                          exp(full(last) - base + log_prior(qp));
+              }
+            }
+            acc_out += wd * acc_in;
+          }
+        }
+        L_last = base + log(n_dpan ? acc_out / cut : acc_out);
+        status = isfinite(L_last) ? ST_OK : ST_FAILED;
+        last = cur;
         return false;
       default:
         return false;
@@ -795,6 +936,10 @@ __global__ void __launch_bounds__(T, 1) k_trials(TrialCtx c, const TrialIn *__re
     opt.n_evals = 0;
     opt.seeded = tr.seeded != 0;
     opt.seed = tr.seed;
+    if (tr.marginal) opt.mode = 2;
+    opt.prior_kind = tr.prior_kind;
+    opt.prior_mu = tr.prior_mu;
+    opt.gl = c.gl;
     opt.pc = 0;
     opt.L_last = NAN;
     opt.last.ex = 0; opt.last.lm = 0.f;

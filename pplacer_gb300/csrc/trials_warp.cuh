@@ -292,6 +292,10 @@ __device__ TrialRes trial_warp(const TrialCtx &c, const TrialSmem &sm, float4 *r
     opt.n_evals = 0;
     opt.seeded = tr.seeded != 0;
     opt.seed = tr.seed;
+    if (tr.marginal) opt.mode = 2;
+    opt.prior_kind = tr.prior_kind;
+    opt.prior_mu = tr.prior_mu;
+    opt.gl = c.gl;
     opt.pc = 0;
     opt.L_last = NAN;
     opt.last.ex = 0; opt.last.lm = 0.f;

@@ -39,6 +39,7 @@ class Engine:
         self.S = None
         self.RP = 1 if model.gcat else len(model.rates)
         self._keep = {}  # arrays that must outlive the create call
+        self._pp = False
         self.h = None
 
     def _create(self, n_sites):
@@ -92,6 +93,7 @@ class Engine:
 
     def run(self, prefs):
         self._kam = prefs.keep_at_most
+        self._pp = bool(prefs.calc_pp)
         _L.check(_L.load().pgb_queries_run(self.h, C.byref(prefs)), "pgb_queries_run")
 
     def fetch(self):
@@ -101,12 +103,15 @@ class Engine:
         status = np.zeros(max(Q, 1), dtype=np.int32)
         _L.check(_L.load().pgb_queries_fetch(self.h, C.addressof(out), n_out.ctypes.data, status.ctypes.data),
                  "pgb_queries_fetch")
-        res = [[(out[q * kam + i].edge, out[q * kam + i].like, out[q * kam + i].lwr, out[q * kam + i].dist,
-                 out[q * kam + i].pend) for i in range(n_out[q])] for q in range(Q)]
+        def row(o):
+            t = (o.edge, o.like, o.lwr, o.dist, o.pend)
+            return t + (o.post_prob, o.marginal_like) if self._pp else t
+        res = [[row(out[q * kam + i]) for i in range(n_out[q])] for q in range(Q)]
         return res, status[:Q]
 
     def place(self, seqs, prefs=None):
-        """Place query rows; returns ([(edge, like, lwr, dist, pend), ...] per query, status per query)."""
+        """Place query rows; returns ([(edge, like, lwr, dist, pend), ...] per query, status per query);
+        with prefs.calc_pp each tuple adds (post_prob, marginal_like)."""
         prefs = prefs or default_prefs()
         self.load_queries(seqs)
         self.run(prefs)

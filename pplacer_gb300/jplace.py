@@ -114,21 +114,28 @@ def to_jplace(results, names, parent, bl, labels=None, invocation="pplacer_gb300
     """The jplace text of placement results.
 
     results: per query, a list of (edge, like, lwr, distal, pendant) tuples
-    best first (Engine.place / Engine.fetch); queries with no placement are
-    left out, as pplacer leaves out failed queries.  names: one name per
-    query (multiplicity 1)."""
+    best first (Engine.place / Engine.fetch), or (..., post_prob,
+    marginal_like) with posterior probabilities, which adds those two fields
+    (placement.ml:176-180); queries with no placement are left out, as
+    pplacer leaves out failed queries.  names: one name per query
+    (multiplicity 1)."""
     rows = []
+    with_pp = any(len(pl) > 5 for places in results for pl in places)
+    fields = sorted(FIELDS + (["marginal_like", "post_prob"] if with_pp else []))
     for name, places in zip(names, results):
         if not places:
             continue
         p = []
-        for edge, like, lwr, dist, pend in places:
+        for pl in places:
+            edge, like, lwr, dist, pend = pl[:5]
             val = {"edge_num": int(edge), "likelihood": float(like), "like_weight_ratio": float(lwr),
                    "distal_length": float(dist), "pendant_length": float(pend)}
-            p.append([val[f] for f in FIELDS])
+            if with_pp:
+                val["post_prob"], val["marginal_like"] = float(pl[5]), float(pl[6])
+            p.append([val[f] for f in fields])
         rows.append({"p": p, "nm": [[name, 1]]})
     doc = {"tree": numbered_newick(parent, bl, labels), "placements": rows,
-           "metadata": {"invocation": invocation}, "version": 3, "fields": FIELDS}
+           "metadata": {"invocation": invocation}, "version": 3, "fields": fields}
     out = []
     _dump(doc, out)
     return "".join(out) + "\n"

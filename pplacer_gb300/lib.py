@@ -32,12 +32,13 @@ class TreeDesc(C.Structure):
 class Prefs(C.Structure):
     _fields_ = [("start_pend", C.c_double), ("max_pend", C.c_double), ("initial_tolerance", C.c_double),
                 ("max_strikes", C.c_int), ("strike_box", C.c_double), ("max_pitches", C.c_int),
-                ("keep_at_most", C.c_int), ("keep_factor", C.c_double), ("optimizer", C.c_int)]
+                ("keep_at_most", C.c_int), ("keep_factor", C.c_double), ("optimizer", C.c_int),
+                ("calc_pp", C.c_int), ("prior", C.c_int), ("pp_rel_err", C.c_double), ("prior_lower", C.c_double)]
 
 
 class Placement(C.Structure):
     _fields_ = [("edge", C.c_int), ("pad", C.c_int), ("like", C.c_double), ("lwr", C.c_double),
-                ("dist", C.c_double), ("pend", C.c_double)]
+                ("dist", C.c_double), ("pend", C.c_double), ("marginal_like", C.c_double), ("post_prob", C.c_double)]
 
 
 class Trial(C.Structure):

@@ -328,3 +328,60 @@ def test_jplace_of_engine_results(small):
     for row, r in zip(doc["placements"], [r for r in res if r]):
         assert [p[f.index("edge_num")] for p in row["p"]] == [p[0] for p in r]
         assert abs(sum(p[f.index("like_weight_ratio")] for p in row["p"]) - 1.0) < 1e-9
+
+
+@pytest.mark.parametrize("prior", [0, 1, 2])
+def test_posterior_probabilities(oracle_lib, prior):
+    """calc_pp (-p): marginal likelihoods of the kept placements against an
+    FP64 adaptive quadrature of the same integral (three_tax.ml:169-215), and
+    the posterior probabilities they give (core.ml:396-401).  pplacer's own
+    QNG is accurate to pp_rel_err (0.01 relative, 0.01 in log units); the
+    tolerance here is 2e-3."""
+    import math
+    from pplacer_gb300 import engine as E
+    from pplacer_gb300 import synth
+    O = oracle_lib
+    w = synth.make_workload("cpu_small", n_queries=4, taxa=60, sites=400, lo=100, hi=300)
+    oref = O.Reference(O.Model(w.exch, w.statd, w.rates), w.parent, w.bl, w.leaf_row, w.ref_seqs)
+    eng = E.engine_for_workload(w)
+    res, st = eng.place(w.query_seqs, E.default_prefs(calc_pp=1, prior=prior, prior_lower=0.01))
+    mu = O.prior_means(w.parent, w.bl, prior, prior_lower=0.01)
+    checked = 0
+    for q in range(3):
+        places = res[q][:3]
+        assert places and all(len(p) == 7 for p in places)
+        want = []
+        for (e, like, lwr, d, p, pp, m) in places:
+            ref_m = O.marginal_like(oref, w.query_seqs[q], e, p, d, prior, None if mu is None else mu[e], rel=1e-8)
+            assert abs(m - ref_m) <= 2e-3, (q, e, m, ref_m)
+            assert m <= like + 1e-9 or prior == 1  # a proper prior integrates to at most the peak
+            want.append(ref_m)
+            checked += 1
+        if len(res[q]) == len(places):
+            mx = max(want)
+            tot = sum(math.exp(v - mx) for v in want)
+            for (_, _, _, _, _, pp, _), v in zip(places, want):
+                assert abs(pp - math.exp(v - mx) / tot) <= 2e-3
+        assert abs(sum(p[5] for p in res[q]) - 1.0) < 1e-9
+    assert checked >= 3
+
+
+def test_marginal_trials_mode(oracle_lib):
+    """pgb_queries_trials mode 2 at the oracle's polished optimum."""
+    from pplacer_gb300 import engine as E
+    from pplacer_gb300 import synth
+    O = oracle_lib
+    w = synth.make_workload("cpu_small", n_queries=4, taxa=60, sites=400, lo=100, hi=300)
+    oref = O.Reference(O.Model(w.exch, w.statd, w.rates), w.parent, w.bl, w.leaf_row, w.ref_seqs)
+    eng = E.engine_for_workload(w)
+    eng.load_queries(w.query_seqs)
+    mu = O.prior_means(w.parent, w.bl, 0)
+    trials = []
+    edges = np.where(w.parent >= 0)[0]
+    for q, e in ((0, edges[5]), (1, edges[17]), (2, edges[29])):
+        like, p, d = O.polish(oref, w.query_seqs[q], int(e), 0.1, float(w.bl[e]) / 2)
+        trials.append((q, int(e), p, d, 0.01))
+    got = eng.trials(trials, optimizer=E.NEWTON, mode=2, prefs=E.default_prefs(prior=0))
+    for (q, e, p, d, _), g in zip(trials, got):
+        ref_m = O.marginal_like(oref, w.query_seqs[q], e, p, d, 0, mu[e], rel=1e-8)
+        assert g["status"] == 0 and abs(g["like"] - ref_m) <= 2e-3, (q, e, g["like"], ref_m)
