@@ -48,6 +48,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--optimizer", default="newton", choices=["newton", "brent"])
+    ap.add_argument("--pp-steps", type=int, default=1,
+                    help="untimed-region comparison: placement steps with posterior probabilities")
     ap.add_argument("--brent-steps", type=int, default=2,
                     help="untimed-region comparison: placement steps with the Brent replica")
     ap.add_argument("--queries", type=int, default=None)
@@ -240,6 +242,19 @@ def run_ours(args):
             btr += cnt[1]
         brent = {"value": Q * args.brent_steps / (bms / 1e3), "unit": "placements/s",
                  "evals_per_trial": bev / btr, "steps": args.brent_steps}
+    # ---- posterior probabilities (-p, default exponential prior) on the same path ----
+    pp = None
+    if args.optimizer == "newton" and args.pp_steps > 0:
+        pprefs = E.default_prefs(optimizer=1, calc_pp=1, **w.prefs)
+        eng.run(pprefs)
+        pms, pev = 0.0, 0.0
+        for _ in range(args.pp_steps):
+            eng.run(pprefs)
+            ms, cnt = eng.timings()
+            pms += ms[5]
+            pev += cnt[2]
+        pp = {"value": Q * args.pp_steps / (pms / 1e3), "unit": "placements/s",
+              "evals_per_step": pev / args.pp_steps, "steps": args.pp_steps}
     # ---- end to end through pgb_place, host buffers ----
     seqs = "".join(w.query_seqs).encode()
     kam = prefs.keep_at_most
@@ -310,6 +325,7 @@ def run_ours(args):
         "e2e": {"value": e2e, "unit": "placements/s", "h2d_bytes_per_step": Q * S,
                 "d2h_bytes_per_step": Q * kam * C.sizeof(L.Placement) + 8 * Q},
         "brent_replica": brent,
+        "with_posterior_probabilities": pp,
         "newton_evals_per_trial": counts[2] / counts[1] if counts[1] else None,
         "gpu_launches": int(launches),
         "clocks": clocks,

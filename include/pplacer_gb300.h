@@ -172,6 +172,17 @@ pgb_status pgb_engine_destroy(pgb_engine *e);
  * exponents. */
 pgb_status pgb_engine_precompute(pgb_engine *e, const int *leaf_row, const char *seqs, int n_rows);
 
+/* Site-category refinement of a per-site category model (Gcat_model.refine,
+ * gcat_model.ml:387-419; run by pplacer_run.ml:316-317 when the alignment
+ * comes from the input): for every category, the per-site log likelihood of
+ * the whole tree with every site in it, scored ll + 2 log(rate) - 3 rate;
+ * each site takes the first best category.  The engine's categories are
+ * replaced (written to categories[n_sites] when not NULL), and its GLVs must
+ * be computed again (pgb_engine_precompute) before placing.  Arguments as
+ * pgb_engine_precompute. */
+pgb_status pgb_engine_refine_categories(pgb_engine *e, const int *leaf_row, const char *seqs, int n_rows,
+                                        int *categories);
+
 /* Upload darr / parr / snodes that the caller computed (FP64 GLVs
  * [n_nodes][R][n_sites][n_states] with int32 exponents [n_nodes][n_sites]; R
  * is 1 for gcat).  snodes may be NULL, in which case they are rebuilt on the

@@ -1144,6 +1144,20 @@ void orc_ref_glv(void *rp, int which, int node, double *a, int *e) {
   std::copy(g.a.begin(), g.a.end(), a);
   std::copy(g.e.begin(), g.e.end(), e);
 }
+// Per-site log likelihood of the whole tree at the root, from the root's
+// distal GLV (the product of its children's evolved GLVs): the values of
+// Like_stree.site_log_like_arr (like_stree.ml:113-131) for a one-plane model.
+void orc_ref_root_site_loglike(void *rp, double *out) {
+  Ref *r = (Ref *)rp;
+  const Model &m = *r->m;
+  const Glv &g = r->darr[r->root];
+  for (int s = 0; s < r->S; s++) {
+    double u = 0;
+    for (int k = 0; k < m.K; k++) u += m.statd[k] * g.a[(size_t)s * m.K + k];
+    out[s] = std::log(u) + kLog2 * g.e[s];
+  }
+}
+
 // Tree log likelihood seen from edge `node` (tests/pplacer/test_like.ml:57-66):
 // out[0] = slow_log_like3(P(bl/2) d, P(bl/2) p, 1); out[1] = logdot(snode, 1).
 void orc_ref_edge_loglike(void *rp, int node, double *out) {

@@ -71,6 +71,7 @@ def lib():
         L.orc_ref_free.argtypes = [C.c_void_p]
         L.orc_ref_glv.argtypes = [C.c_void_p, i, i, _dp, _ip]
         L.orc_ref_edge_loglike.argtypes = [C.c_void_p, i, _dp]
+        L.orc_ref_root_site_loglike.argtypes = [C.c_void_p, _dp]
         L.orc_place.argtypes = [C.c_void_p, C.c_void_p, i, C.c_char_p, i, C.c_void_p, _ip, _ip]
         L.orc_query_trace.argtypes = [C.c_void_p, C.c_void_p, C.c_char_p, _ip, _dp, C.POINTER(C.c_int), _ip, _dp,
                                       C.POINTER(C.c_int)]
@@ -213,6 +214,12 @@ class Reference:
     def edge_loglike(self, node):
         out = np.zeros(2)
         lib().orc_ref_edge_loglike(self.h, node, out)
+        return out
+
+    def root_site_loglike(self):
+        """Per-site log likelihood of the whole tree (Like_stree.site_log_like_arr)."""
+        out = np.zeros(self.S)
+        lib().orc_ref_root_site_loglike(self.h, out)
         return out
 
     def place(self, seqs, prefs=None, n_threads=1):
@@ -436,3 +443,23 @@ def marginal_like(ref, seq, loc, pend, dist, prior, mu=None, max_pend=2.0, rel=1
         v, _ = integrate.quad(inner, 0.0, cut, epsabs=0.0, epsrel=rel, points=pts, limit=400)
         I = v / cut
     return base + math.log(I)
+
+
+def refine_categories(exch, statd, rates, parent, bl, leaf_row, leaf_seqs):
+    """Gcat_model.refine (gcat_model.ml:387-419): for every category c, the
+    per-site tree log likelihood with every site in c, scored
+    ll + 2 log(rate_c) - 3 rate_c; each site takes the first category with
+    the highest score.  Returns (categories, scores [n_cat][S])."""
+    S = len(leaf_seqs[0])
+    scores = []
+    for c, r in enumerate(rates):
+        ref = Reference(Model(exch, statd, rates, np.full(S, c, dtype=np.int32)), parent, bl, leaf_row, leaf_seqs)
+        scores.append(ref.root_site_loglike() + 2.0 * np.log(r) - 3.0 * r)
+    scores = np.array(scores)
+    best = np.full(S, -np.inf)
+    cats = np.full(S, -1, dtype=np.int32)
+    for c in range(len(rates)):
+        up = scores[c] > best
+        best[up] = scores[c][up]
+        cats[up] = c
+    return cats, scores

@@ -206,6 +206,29 @@ __global__ void k_finish_glvs(PreCtx c, int n_nodes, float *d32, float *p32, flo
   }
 }
 
+// Site-category refinement (gcat_model.ml:387-419), one category pass: the
+// per-site tree log likelihood from the root's distal GLV (the product of
+// its children's evolved GLVs, Like_stree.site_log_like_arr), scored
+// ll + 2 log(rate) - 3 rate; a site keeps the first category with the
+// highest score.
+__global__ void k_refine_site(const double *__restrict__ root_distal, const int *__restrict__ root_e,
+                              const double *__restrict__ statd, int S, int K, int cat, double bonus, double *best,
+                              int *best_cat) {
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < S; s += gridDim.x * blockDim.x) {
+    double u = 0;
+    for (int k = 0; k < K; k++) u += statd[k] * root_distal[(long)s * K + k];
+    double x = log(u) + kLn2 * root_e[s] + bonus;
+    if (x > best[s]) { best[s] = x; best_cat[s] = cat; }
+  }
+}
+
+__global__ void k_refine_init(double *best, int *best_cat, int S) {
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < S; s += gridDim.x * blockDim.x) {
+    best[s] = -INFINITY;
+    best_cat[s] = -1;
+  }
+}
+
 // Caller-provided FP64 GLVs [node][R][S][K] -> FP32 site-major.
 __global__ void k_import_glv(const double *__restrict__ src, const int *__restrict__ se, float *dst, int *de,
                              int n_nodes, int S, int RP, int K) {
@@ -1624,42 +1647,61 @@ static pgb_status alloc_glv_store(pgb_engine *e) {
   return PGB_OK;
 }
 
-pgb_status pgb_engine_precompute(pgb_engine *e, const int *leaf_row, const char *seqs, int n_rows) {
-  if (!e || !leaf_row || !seqs || n_rows < 1) { set_error("precompute: bad argument"); return PGB_ERR_ARG; }
-  int K = e->K, S = e->S;
-  // leaves, their codes, and the post-order / pre-order levels
-  std::vector<int> leaves;
+// Leaves with their character codes, and the post-order (height) and
+// pre-order (depth) levels of the tree passes.
+struct TreeLevels {
+  std::vector<int> leaves, hlist, hstart, dlist, dstart;
   std::vector<uint8_t> codes;
+  int maxh = 0, maxd = 0;
+};
+
+pgb_status tree_levels(const pgb_engine *e, const int *leaf_row, const char *seqs, int n_rows, TreeLevels &t) {
+  int K = e->K, S = e->S;
   const char *alpha = code_alphabet(K);
   for (int i = 0; i < e->n_nodes; i++) {
     if (e->ch_start[i + 1] != e->ch_start[i]) continue;
     int row = leaf_row[i];
     if (row < 0 || row >= n_rows) { set_error("precompute: leaf %d has no alignment row", i); return PGB_ERR_ARG; }
-    leaves.push_back(i);
+    t.leaves.push_back(i);
     for (int s = 0; s < S; s++) {
       const char *p = strchr(alpha, seqs[(size_t)row * S + s]);
       if (!p || !seqs[(size_t)row * S + s]) { set_error("precompute: unknown character in reference row %d", row); return PGB_ERR_ARG; }
-      codes.push_back((uint8_t)(p - alpha));
+      t.codes.push_back((uint8_t)(p - alpha));
     }
   }
   std::vector<int> height(e->n_nodes, 0), depth(e->n_nodes, 0);
-  int maxh = 0, maxd = 0;
   for (int i = 0; i < e->n_nodes; i++)
     for (int c = e->ch_start[i]; c < e->ch_start[i + 1]; c++) height[i] = std::max(height[i], height[e->ch_list[c]] + 1);
   for (int i = e->n_nodes - 1; i >= 0; i--)
     if (e->parent[i] >= 0) depth[i] = depth[e->parent[i]] + 1;
-  for (int i = 0; i < e->n_nodes; i++) { maxh = std::max(maxh, height[i]); maxd = std::max(maxd, depth[i]); }
-  std::vector<int> hlist, hstart(maxh + 2, 0), dlist, dstart(maxd + 2, 0);
-  for (int h = 1; h <= maxh; h++) {
-    hstart[h] = (int)hlist.size();
-    for (int i = 0; i < e->n_nodes; i++) if (height[i] == h) hlist.push_back(i);
+  for (int i = 0; i < e->n_nodes; i++) { t.maxh = std::max(t.maxh, height[i]); t.maxd = std::max(t.maxd, depth[i]); }
+  t.hstart.assign(t.maxh + 2, 0);
+  t.dstart.assign(t.maxd + 2, 0);
+  for (int h = 1; h <= t.maxh; h++) {
+    t.hstart[h] = (int)t.hlist.size();
+    for (int i = 0; i < e->n_nodes; i++) if (height[i] == h) t.hlist.push_back(i);
   }
-  hstart[maxh + 1] = (int)hlist.size();
-  for (int d = 1; d <= maxd; d++) {
-    dstart[d] = (int)dlist.size();
-    for (int i = 0; i < e->n_nodes; i++) if (depth[i] == d) dlist.push_back(i);
+  t.hstart[t.maxh + 1] = (int)t.hlist.size();
+  for (int d = 1; d <= t.maxd; d++) {
+    t.dstart[d] = (int)t.dlist.size();
+    for (int i = 0; i < e->n_nodes; i++) if (depth[i] == d) t.dlist.push_back(i);
   }
-  dstart[maxd + 1] = (int)dlist.size();
+  t.dstart[t.maxd + 1] = (int)t.dlist.size();
+  return PGB_OK;
+}
+
+pgb_status pgb_engine_precompute(pgb_engine *e, const int *leaf_row, const char *seqs, int n_rows) {
+  if (!e || !leaf_row || !seqs || n_rows < 1) { set_error("precompute: bad argument"); return PGB_ERR_ARG; }
+  int K = e->K, S = e->S;
+  TreeLevels tl;
+  {
+    pgb_status st = tree_levels(e, leaf_row, seqs, n_rows, tl);
+    if (st) return st;
+  }
+  const std::vector<int> &leaves = tl.leaves, &hlist = tl.hlist, &hstart = tl.hstart, &dlist = tl.dlist,
+                         &dstart = tl.dstart;
+  const std::vector<uint8_t> &codes = tl.codes;
+  const int maxh = tl.maxh, maxd = tl.maxd;
   size_t n = (size_t)e->n_nodes * S * e->RP * K, ne = (size_t)e->n_nodes * S;
   double *d_distal = nullptr, *d_evd = nullptr, *d_prox = nullptr;
   int *d_de = nullptr, *d_ee = nullptr, *d_pe = nullptr, *d_leaves = nullptr, *d_hlist = nullptr, *d_dlist = nullptr;
@@ -1710,6 +1752,74 @@ pgb_status pgb_engine_precompute(pgb_engine *e, const int *leaf_row, const char 
   cleanup();
   if (ce != cudaSuccess) { set_error("precompute: %s", cudaGetErrorString(ce)); return PGB_ERR_CUDA; }
   e->glvs_ready = true;
+  return PGB_OK;
+}
+
+pgb_status pgb_engine_refine_categories(pgb_engine *e, const int *leaf_row, const char *seqs, int n_rows,
+                                        int *categories) {
+  if (!e || !leaf_row || !seqs || n_rows < 1) { set_error("refine: bad argument"); return PGB_ERR_ARG; }
+  if (!e->gcat) { set_error("refine: only per-site category models have site categories"); return PGB_ERR_STATE; }
+  const int K = e->K, S = e->S;
+  TreeLevels tl;
+  pgb_status s = tree_levels(e, leaf_row, seqs, n_rows, tl);
+  if (s) return s;
+  size_t n = (size_t)e->n_nodes * S * K, ne = (size_t)e->n_nodes * S;
+  double *d_distal = nullptr, *d_evd = nullptr, *d_best = nullptr;
+  int *d_de = nullptr, *d_ee = nullptr, *d_leaves = nullptr, *d_hlist = nullptr, *d_bcat = nullptr;
+  uint8_t *d_codes = nullptr;
+  auto cleanup = [&]() {
+    void *ps[] = {d_distal, d_evd, d_best, d_de, d_ee, d_leaves, d_hlist, d_bcat, d_codes};
+    for (void *p : ps) if (p) cudaFree(p);
+  };
+  if ((s = dalloc(&d_distal, n)) || (s = dalloc(&d_evd, n)) || (s = dalloc(&d_de, ne)) || (s = dalloc(&d_ee, ne)) ||
+      (s = dalloc(&d_best, S)) || (s = dalloc(&d_bcat, S)) ||
+      (s = upload(&d_leaves, tl.leaves.data(), tl.leaves.size(), e->st)) ||
+      (s = upload(&d_codes, tl.codes.data(), tl.codes.size(), e->st)) ||
+      (s = upload(&d_hlist, tl.hlist.data(), tl.hlist.size(), e->st))) {
+    cleanup();
+    return s;
+  }
+  PreCtx c{};
+  c.S = S; c.RP = 1; c.K = K; c.NM = e->NM; c.gcat = 1; c.site_cat = e->d_site_cat; c.lvd = e->d_lvd;
+  c.pm = e->d_pm; c.pmh = e->d_pmh; c.statd = e->d_statdd; c.distal = d_distal; c.evd = d_evd;
+  c.de = d_de; c.ee = d_ee;
+  k_refine_init<<<grid_for(S), 256, 0, e->st>>>(d_best, d_bcat, S);
+  count_launch();
+  for (int cat = 0; cat < e->NM; cat++) {  // every site in category cat
+    cudaError_t ce = cudaMemsetAsync(e->d_site_cat, cat, S, e->st);
+    if (ce != cudaSuccess) { cleanup(); set_error("refine: %s", cudaGetErrorString(ce)); return PGB_ERR_CUDA; }
+    k_leaves<<<grid_for((long)tl.leaves.size() * S), 256, 0, e->st>>>(c, d_leaves, (int)tl.leaves.size(), d_codes);
+    count_launch();
+    for (int h = 1; h <= tl.maxh; h++) {
+      int cnt = tl.hstart[h + 1] - tl.hstart[h];
+      if (!cnt) continue;
+      k_distal_level<<<grid_for((long)cnt * S), 256, 0, e->st>>>(c, d_hlist + tl.hstart[h], cnt, e->d_ch_start,
+                                                                 e->d_ch_list);
+      count_launch();
+    }
+    double r = e->rates[cat];
+    k_refine_site<<<grid_for(S), 256, 0, e->st>>>(d_distal + (size_t)e->root * S * K, d_de + (size_t)e->root * S,
+                                                  e->d_statdd, S, K, cat, 2.0 * log(r) - 3.0 * r, d_best, d_bcat);
+    count_launch();
+  }
+  std::vector<int> best(S);
+  cudaError_t ce = cudaMemcpyAsync(best.data(), d_bcat, S * sizeof(int), cudaMemcpyDeviceToHost, e->st);
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(e->st);
+  cleanup();
+  if (ce != cudaSuccess) { set_error("refine: %s", cudaGetErrorString(ce)); return PGB_ERR_CUDA; }
+  for (int i = 0; i < S; i++)
+    if (best[i] < 0) {  // gcat_model.ml:363-364
+      set_error("refine: site %d has zero likelihood", i);
+      return PGB_ERR_ARG;
+    }
+  e->site_cats = best;
+  std::vector<uint8_t> sc(S);
+  for (int i = 0; i < S; i++) sc[i] = (uint8_t)best[i];
+  PGB_CUDA(cudaMemcpyAsync(e->d_site_cat, sc.data(), S, cudaMemcpyHostToDevice, e->st));
+  PGB_CUDA(cudaStreamSynchronize(e->st));
+  e->glvs_ready = false;  // the placement GLVs follow the categories: precompute again
+  e->lt_pend = -1;
+  if (categories) std::copy(best.begin(), best.end(), categories);
   return PGB_OK;
 }
 

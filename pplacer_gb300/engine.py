@@ -67,6 +67,19 @@ class Engine:
         buf = "".join(ref_seqs).encode()
         _L.check(_L.load().pgb_engine_precompute(self.h, lr.ctypes.data, buf, len(ref_seqs)), "pgb_engine_precompute")
 
+    def refine_categories(self, leaf_row, ref_seqs):
+        """Gcat site-category refinement on the GPU (gcat_model.ml:387-419); returns the
+        new categories.  Run precompute again before placing."""
+        S = len(ref_seqs[0])
+        if self.h is None:
+            self._create(S)
+        lr = np.ascontiguousarray(leaf_row, dtype=np.int32)
+        cats = np.zeros(S, dtype=np.int32)
+        buf = "".join(ref_seqs).encode()
+        _L.check(_L.load().pgb_engine_refine_categories(self.h, lr.ctypes.data, buf, len(ref_seqs), cats.ctypes.data),
+                 "pgb_engine_refine_categories")
+        return cats
+
     def set_glvs(self, darr, darr_e, parr, parr_e, snodes=None, snodes_e=None):
         """Upload caller-computed FP64 GLVs ([n_nodes][R][S][K], exponents [n_nodes][S])."""
         S = darr.shape[2]

@@ -90,6 +90,7 @@ def load(build_if_missing=True):
     L.pgb_engine_create.argtypes = [C.POINTER(ModelDesc), C.POINTER(TreeDesc), C.POINTER(C.c_void_p)]
     L.pgb_engine_destroy.argtypes = [vp]
     L.pgb_engine_precompute.argtypes = [vp, vp, C.c_char_p, i]
+    L.pgb_engine_refine_categories.argtypes = [vp, vp, C.c_char_p, i, vp]
     L.pgb_engine_set_glvs.argtypes = [vp, vp, vp, vp, vp, vp, vp]
     L.pgb_engine_get_glv.argtypes = [vp, i, i, vp, vp]
     L.pgb_prefs_default.argtypes = [C.POINTER(Prefs)]
@@ -105,7 +106,8 @@ def load(build_if_missing=True):
     L.pgb_engine_autotune.argtypes = [vp, C.POINTER(Prefs)]
     L.pgb_engine_get_tuning.argtypes = [vp, vp, vp]
     L.pgb_engine_set_tuning.argtypes = [vp, vp, vp]
-    for name in ["pgb_engine_create", "pgb_engine_destroy", "pgb_engine_precompute", "pgb_engine_set_glvs",
+    for name in ["pgb_engine_create", "pgb_engine_destroy", "pgb_engine_precompute", "pgb_engine_refine_categories",
+                 "pgb_engine_set_glvs",
                  "pgb_engine_get_glv", "pgb_place", "pgb_queries_load", "pgb_queries_run", "pgb_queries_fetch",
                  "pgb_queries_stage1", "pgb_queries_rank", "pgb_queries_trials", "pgb_engine_timings", "pgb_engine_autotune",
                  "pgb_engine_get_tuning", "pgb_engine_set_tuning"]:

@@ -385,3 +385,29 @@ def test_marginal_trials_mode(oracle_lib):
     for (q, e, p, d, _), g in zip(trials, got):
         ref_m = O.marginal_like(oref, w.query_seqs[q], e, p, d, 0, mu[e], rel=1e-8)
         assert g["status"] == 0 and abs(g["like"] - ref_m) <= 2e-3, (q, e, g["like"], ref_m)
+
+
+def test_refine_categories(oracle_lib):
+    """Gcat site-category refinement (gcat_model.ml:387-419) against the
+    oracle, then placement with the refined categories."""
+    from pplacer_gb300 import engine as E
+    from pplacer_gb300 import synth
+    from pplacer_gb300.model import Model
+    O = oracle_lib
+    w = synth.make_workload("cat_5k", n_queries=12, taxa=80, sites=300, lo=60, hi=300)
+    S = w.n_sites
+    want, scores = O.refine_categories(w.exch, w.statd, w.rates, w.parent, w.bl, w.leaf_row, w.ref_seqs)
+    eng = E.Engine(Model.from_exchangeabilities(w.exch, w.statd, w.rates, np.zeros(S, dtype=np.int32)),
+                   w.parent, w.bl)
+    got = eng.refine_categories(w.leaf_row, w.ref_seqs)
+    srt = np.sort(scores, axis=0)
+    gap = srt[-1] - srt[-2]
+    diff = got != want
+    assert np.all(gap[diff] <= 1e-9 * np.abs(srt[-1][diff])), (np.where(diff), gap[diff])
+    assert diff.sum() <= 0.01 * S
+    eng.precompute(w.leaf_row, w.ref_seqs)
+    oref = O.Reference(O.Model(w.exch, w.statd, w.rates, got), w.parent, w.bl, w.leaf_row, w.ref_seqs)
+    ores, ost = oref.place(w.query_seqs, O.make_prefs(), n_threads=8)
+    gres, gst = eng.place(w.query_seqs, E.default_prefs(optimizer=1))
+    assert list(gst) == list(ost)
+    _compare_placements(O, oref, w.query_seqs, gres, ores)
