@@ -192,6 +192,65 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def plain_dropin_brent(eng, w, evals_per_query, reps=40):
+    """pplacer's own per-query flow over the plain drop-in (linear.ml externals
+    replaced one for one), timed call by call: a
+    stage-1 score is one ten_masked_logdot over the full alignment per edge
+    (core.ml:333-343); a Brent evaluation re-evolves the pendant (one
+    evolve) or the distal and proximal edges (two) -- per rate a
+    dediagonalize of the exponentiated eigenvalues and a gemmish
+    (diagd.ml:79-98, gstar_support.ml:70-79) -- then one ten_log_like3
+    (three_tax.ml:30-47).  Placements/s = 1 / (edges x t_score +
+    evals_per_query x t_eval), with evals_per_query measured on the Brent
+    replica (the same algorithm) and t_eval the mean of the pendant and the
+    distal evaluation."""
+    import numpy as np
+    from pplacer_gb300 import linear as Lin
+    m = eng.model
+    R, K = len(m.rates), m.K
+    S = w.n_sites
+    sq = int(np.mean([sum(ch not in "-?." for ch in q) for q in w.query_seqs[:200]]))
+    rng = np.random.default_rng(7)
+    x = [np.ascontiguousarray(rng.random((sq, K)) + 0.1) for _ in range(R)]
+    xt = np.ascontiguousarray(rng.random((R, sq, K)) + 0.1)
+    util = np.zeros(sq)
+    statd = np.ascontiguousarray(m.statd, dtype=np.float64)
+    u, lam, uit = (np.ascontiguousarray(a, dtype=np.float64) for a in (m.x, m.lam, m.xit))
+    P = np.zeros((K, K))
+    dst = np.zeros((sq, K))
+
+    def evolve(t):
+        for r in range(R):
+            Lin.dediagonalize(P, u, np.exp(m.rates[r] * t * lam), uit)
+            Lin.gemmish(dst, P, x[r])
+
+    def pend_eval():
+        evolve(0.1)
+        Lin.ten_log_like3(statd, xt, xt, xt, util)
+
+    def dist_eval():
+        evolve(0.05)
+        evolve(0.02)
+        Lin.ten_log_like3(statd, xt, xt, xt, util)
+    full = np.ascontiguousarray(rng.random((R, S, K)) + 0.1)
+    mask = np.ascontiguousarray((rng.random(S) < sq / S).astype(np.uint16))
+    futil = np.zeros(S)
+
+    def score():
+        Lin.ten_masked_logdot(full, full, mask, futil)
+    out = {}
+    for name, f in (("pendant_eval", pend_eval), ("distal_eval", dist_eval), ("stage1_score", score)):
+        f()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            f()
+        out[name] = (time.perf_counter() - t0) / reps
+    t_eval = 0.5 * (out["pendant_eval"] + out["distal_eval"])
+    t_query = (len(w.parent) - 1) * out["stage1_score"] + evals_per_query * t_eval
+    return {"value": 1.0 / t_query, "unit": "placements/s", "method": "per-call timing x measured Brent counts",
+            "seconds": {k: v for k, v in out.items()}, "query_sites": sq}
+
+
 def run_ours(args):
     rank, world, local, dist = dist_setup(args.gpus)
     import numpy as np
@@ -241,7 +300,9 @@ def run_ours(args):
             bev += cnt[2]
             btr += cnt[1]
         brent = {"value": Q * args.brent_steps / (bms / 1e3), "unit": "placements/s",
-                 "evals_per_trial": bev / btr, "steps": args.brent_steps}
+                 "evals_per_trial": bev / btr, "evals_per_query": bev / (args.brent_steps * Q),
+                 "steps": args.brent_steps}
+        brent["plain_dropin"] = plain_dropin_brent(eng, w, brent["evals_per_query"])
     # ---- posterior probabilities (-p, default exponential prior) on the same path ----
     pp = None
     if args.optimizer == "newton" and args.pp_steps > 0:
