@@ -2193,10 +2193,23 @@ pgb_status pgb_queries_fetch(pgb_engine *e, pgb_placement *out, int *n_out, int 
 
 pgb_status pgb_place(pgb_engine *e, const pgb_prefs *p, int n_queries, const char *seqs, pgb_placement *out,
                      int *n_out, int *qstatus) {
+  if (!e || !p || n_queries < 0 || (n_queries > 0 && (!seqs || !out || !n_out || !qstatus))) {
+    set_error("place: bad argument");
+    return PGB_ERR_ARG;
+  }
+  // Device batches: the stage-1 products take ~24 bytes per (query, edge),
+  // so a batch holds at most 2 GiB of them (8,192 queries for 10,000 edges).
+  const long ep = (e->n_edges + 15) & ~15;
+  int batch = (int)std::max(1024L, std::min(65536L, (2L << 30) / (24 * ep)));
+  if (const char *env = getenv("PGB_PLACE_BATCH")) batch = std::max(1, atoi(env));  // override (tests, tuning)
   pgb_status s;
-  if ((s = pgb_queries_load(e, n_queries, seqs)) || (s = pgb_queries_run(e, p)) ||
-      (s = pgb_queries_fetch(e, out, n_out, qstatus)))
-    return s;
+  if (n_queries == 0) return pgb_queries_load(e, 0, seqs);
+  for (int b0 = 0; b0 < n_queries; b0 += batch) {
+    const int nb = std::min(batch, n_queries - b0);
+    if ((s = pgb_queries_load(e, nb, seqs + (size_t)b0 * e->S)) || (s = pgb_queries_run(e, p)) ||
+        (s = pgb_queries_fetch(e, out + (size_t)b0 * p->keep_at_most, n_out + b0, qstatus + b0)))
+      return s;
+  }
   return PGB_OK;
 }
 

@@ -130,6 +130,20 @@ class Engine:
         self.run(prefs)
         return self.fetch()
 
+    def place_host(self, seqs, prefs=None):
+        """Place through the single C-ABI call pgb_place (host buffers in and out, device batches)."""
+        prefs = prefs or default_prefs()
+        Q, kam = len(seqs), prefs.keep_at_most
+        out = (_L.Placement * max(1, Q * kam))()
+        n_out = np.zeros(max(Q, 1), dtype=np.int32)
+        status = np.zeros(max(Q, 1), dtype=np.int32)
+        buf = "".join(seqs).encode() if Q else b""
+        _L.check(_L.load().pgb_place(self.h, C.byref(prefs), Q, buf, C.addressof(out), n_out.ctypes.data,
+                                     status.ctypes.data), "pgb_place")
+        res = [[(out[q * kam + i].edge, out[q * kam + i].like, out[q * kam + i].lwr, out[q * kam + i].dist,
+                 out[q * kam + i].pend) for i in range(n_out[q])] for q in range(Q)]
+        return res, status[:Q]
+
     def stage1(self, prefs=None):
         prefs = prefs or default_prefs()
         n_edges = self.n_nodes - 1

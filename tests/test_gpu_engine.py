@@ -185,8 +185,14 @@ def _compare_placements(O, oref, seqs, res_gpu, res_orc, min_logl_frac=1.0):
     queries the best edge must be identical (>= 99.9%), and the best logL must
     lie within 1e-6 relative of the oracle's, allowing for the oracle's own
     distance to the optimum (its Brent stops within its tolerance); a logL
-    above the polished optimum would be an error."""
-    mismatch = non_tied = logl_ok = n = 0
+    above the polished optimum would be an error.
+
+    The reference's alternating Brent can stop well below a location's
+    optimum (on long queries by up to ~1 logL), which can change the
+    location it ranks best.  When the GPU's best location has the higher
+    polished optimum -- it found the better placement -- the query counts as
+    agreeing, provided the GPU's logL there is that optimum."""
+    mismatch = non_tied = logl_ok = n = better = 0
     for q, (g, o) in enumerate(zip(res_gpu, res_orc)):
         if not o:
             assert not g
@@ -203,12 +209,16 @@ def _compare_placements(O, oref, seqs, res_gpu, res_orc, min_logl_frac=1.0):
                 logl_ok += abs(gl - g_star) <= tol
                 continue
             non_tied += 1
-            mismatch += 1
+            if g_star > o_star + tol and abs(gl - g_star) <= tol:
+                better += 1
+                logl_ok += 1
+            else:
+                mismatch += 1
             continue
         non_tied += 1
         assert gl <= o_star + tol, (q, gl, o_star)
         logl_ok += abs(gl - ol) <= tol + max(0.0, o_star - ol)
-    assert mismatch <= 0.001 * max(non_tied, 1), (mismatch, non_tied)
+    assert mismatch <= 0.001 * max(non_tied, 1), (mismatch, non_tied, better)
     assert logl_ok >= min_logl_frac * n, (logl_ok, n)
 
 
@@ -407,6 +417,61 @@ def test_refine_categories(oracle_lib):
     assert diff.sum() <= 0.01 * S
     eng.precompute(w.leaf_row, w.ref_seqs)
     oref = O.Reference(O.Model(w.exch, w.statd, w.rates, got), w.parent, w.bl, w.leaf_row, w.ref_seqs)
+    ores, ost = oref.place(w.query_seqs, O.make_prefs(), n_threads=8)
+    gres, gst = eng.place(w.query_seqs, E.default_prefs(optimizer=1))
+    assert list(gst) == list(ost)
+    _compare_placements(O, oref, w.query_seqs, gres, ores)
+
+
+def test_place_host_batches(small, monkeypatch):
+    """pgb_place (host buffers, device batches) gives the load/run/fetch
+    results, with batches of 7 queries."""
+    from pplacer_gb300 import engine as E
+    w, oref, eng = small
+    qs = w.query_seqs[:20]
+    want, wst = eng.place(qs, E.default_prefs())
+    monkeypatch.setenv("PGB_PLACE_BATCH", "7")
+    got, gst = eng.place_host(qs, E.default_prefs())
+    assert list(gst) == list(wst)
+    for g, r in zip(got, want):
+        assert [p[0] for p in g] == [p[0] for p in r]
+        for a, b in zip(g, r):
+            assert a[1] == b[1] and a[3] == b[3] and a[4] == b[4]
+
+
+def test_long_queries_gradients_and_placement(oracle_lib):
+    """dna_2k shapes (3,000 sites, queries up to 3,000 informative sites):
+    1,000 sampled (query, edge, pendant, distal) points, GPU value and adjoint
+    against the FP64 oracle; central differences (h = 1e-6) of the oracle's
+    FP64 value against its analytic gradient on 50 of them; and Newton
+    placements against the oracle."""
+    from pplacer_gb300 import engine as E
+    from pplacer_gb300 import synth
+    O = oracle_lib
+    w = synth.make_workload("dna_2k", n_queries=40, taxa=300, lo=1500, hi=3000)
+    oref = O.Reference(O.Model(w.exch, w.statd, w.rates), w.parent, w.bl, w.leaf_row, w.ref_seqs)
+    eng = E.engine_for_workload(w)
+    eng.load_queries(w.query_seqs)
+    rng = np.random.default_rng(11)
+    edges = np.where(w.parent >= 0)[0]
+    pts = []
+    for _ in range(1000):
+        q = int(rng.integers(len(w.query_seqs)))
+        e = int(rng.choice(edges))
+        pts.append((q, e, float(rng.uniform(1e-3, 0.3)), float(rng.uniform(0, w.bl[e])), 0.01))
+    got = eng.trials(pts, optimizer=E.NEWTON, mode=1)
+    for i, ((q, e, p, d, _), g) in enumerate(zip(pts, got)):
+        st, ref = oref.loglike_derivs(w.query_seqs[q], e, p, d)
+        assert abs(g["like"] - ref[0]) <= 2e-7 * abs(ref[0]), (q, e, g["like"], ref[0])
+        hscale = math.sqrt(abs(ref[3] * ref[4])) + 1.0
+        for k, (gv, rv) in enumerate(zip(g["derivs"][:5], ref[1:6])):
+            tol = 2e-3 * abs(rv) + (1e-5 * abs(ref[3 + k]) + 1e-2 if k < 2 else 1e-3 * hscale + 1.0)
+            assert abs(gv - rv) <= tol, (i, k, gv, rv)
+        if i < 50:
+            h = 1e-6
+            s = w.query_seqs[q]
+            fp = (oref.loglike_derivs(s, e, p + h, d)[1][0] - oref.loglike_derivs(s, e, p - h, d)[1][0]) / (2 * h)
+            assert abs(fp - ref[1]) <= 1e-6 * abs(ref[1]) + 4e-16 * abs(ref[0]) / h
     ores, ost = oref.place(w.query_seqs, O.make_prefs(), n_threads=8)
     gres, gst = eng.place(w.query_seqs, E.default_prefs(optimizer=1))
     assert list(gst) == list(ost)
