@@ -25,7 +25,12 @@
 // uniform by construction.
 
 constexpr int kWarpTrialWarps = 1;  // warps (trials) per CTA
-constexpr int kWarpTrialMinCtas = 10;  // register cap 204; the kernel uses ~168, so 12 fit
+// Resident one-warp CTAs per SM the register allocation aims for.  A warp's
+// registers come from one scheduler's file: 8 warps (2 per scheduler) leave
+// 255 registers each, 12 (3 per scheduler) only 168.  With 255 the compiler
+// interleaves the unrolled site iterations, which measured 6.6% faster than
+// the third warp per scheduler.
+constexpr int kWarpTrialMinCtas = 8;
 constexpr int kWarpRing = 8;        // site iterations in flight per warp
 
 __host__ __device__ inline size_t warp_trial_const_floats(int NM, int ncode) {
