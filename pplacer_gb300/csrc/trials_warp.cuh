@@ -266,18 +266,24 @@ __device__ TrialRes trial_warp(const TrialCtx &c, const TrialSmem &sm, float4 *r
   const int Sq = c.qlen[q];
   const int ncz = c.qamb[q] > 0 ? nc : c.prim;  // Z rows the query's codes use
   // exponent sum of the query's sites of darr / parr[node]
+  // (sixteen unconditional gathers in flight per lane: past the end they
+  // read the last site and add nothing)
   long long esum = 0;
-  const long qo = (long)q * c.S;
-  for (int i0 = lane; i0 < Sq; i0 += 8 * 32) {  // eight gathers in flight per lane
-    int col8[8];
+  {
+    const long qo = (long)q * c.S, nb = (long)node * c.S;
+    const int last = Sq - 1;
+    for (int i0 = lane; i0 < Sq; i0 += 16 * 32) {
+      int col[16];
 #pragma unroll
-    for (int k = 0; k < 8; k++) col8[k] = i0 + 32 * k < Sq ? (int)c.reind[qo + i0 + 32 * k] : -1;
+      for (int k = 0; k < 16; k++) col[k] = c.reind[qo + min(i0 + 32 * k, last)];
+      int part = 0;
 #pragma unroll
-    for (int k = 0; k < 8; k++)
-      if (col8[k] >= 0) {
-        long go = (long)node * c.S + col8[k];
-        esum += (long long)c.dexp[go] + (long long)c.pexp[go];
+      for (int k = 0; k < 16; k++) {
+        const int v = c.dexp[nb + col[k]] + c.pexp[nb + col[k]];
+        part += i0 + 32 * k < Sq ? v : 0;
       }
+      esum += part;
+    }
   }
   for (int o = 16; o > 0; o >>= 1) esum += __shfl_xor_sync(0xffffffffu, esum, o);
 
