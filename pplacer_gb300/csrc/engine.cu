@@ -407,16 +407,23 @@ __global__ void k_s1_query(int S, int Sp, int prim, const uint8_t *__restrict__ 
 }
 
 // scores = T-sum - n log R + ln2 * exponent sum
-__global__ void k_s1_epilogue(int Q, int E, int Ep, const float *__restrict__ C, const float *__restrict__ Xhi,
-                              const float *__restrict__ Xlo, const int *__restrict__ qlen,
-                              const int *__restrict__ qstatus, double log_nrates, double *scores) {
-  long n = (long)Q * E;
+__device__ __forceinline__ double s1_score(const float *__restrict__ C, const float *__restrict__ Xhi,
+                                           const float *__restrict__ Xlo, long tp, int qlen, double log_nrates) {
+  long long ex = 256LL * __float2ll_rn(Xhi[tp]) + __float2ll_rn(Xlo[tp]);
+  return (double)C[tp] - (double)(float)qlen * log_nrates + kLn2 * (double)ex;
+}
+
+// rows: the n_rows queries of qlist, or queries 0 .. n_rows - 1 when qlist is null
+__global__ void k_s1_epilogue(int n_rows, const int *__restrict__ qlist, int E, int Ep, const float *__restrict__ C,
+                              const float *__restrict__ Xhi, const float *__restrict__ Xlo,
+                              const int *__restrict__ qlen, const int *__restrict__ qstatus, double log_nrates,
+                              double *scores) {
+  long n = (long)n_rows * E;
   for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
-    int q = (int)(t / E);
+    int row = (int)(t / E), ei = (int)(t - (long)row * E);
+    int q = qlist ? qlist[row] : row;
     if (qstatus[q] != PGB_Q_OK) continue;
-    long tp = (long)q * Ep + (t - (long)q * E);
-    long long ex = 256LL * __float2ll_rn(Xhi[tp]) + __float2ll_rn(Xlo[tp]);
-    scores[t] = (double)C[tp] - (double)(float)qlen[q] * log_nrates + kLn2 * (double)ex;
+    scores[(long)q * E + ei] = s1_score(C, Xhi, Xlo, (long)q * Ep + ei, qlen[q], log_nrates);
   }
 }
 
@@ -460,16 +467,31 @@ __device__ __forceinline__ bool rank_before(unsigned long long ka, int ia, unsig
   return ka > kb || (ka == kb && ia < ib);
 }
 
-__global__ void __launch_bounds__(128) k_rank_warp(const double *__restrict__ scores, int E, int rk, int Q,
-                                                   const int *__restrict__ qstatus, int *rank, int keys_in_smem) {
+// The GEMM products, when the ranking forms the scores itself (queries
+// without ambiguity characters; the others read their FP64 scores row).
+struct S1Products {
+  const float *C, *Xhi, *Xlo;
+  const int *qlen, *qamb;
+  int Ep, on;
+  double log_nrates;
+};
+
+__global__ void __launch_bounds__(128) k_rank_warp(const double *__restrict__ scores, S1Products pr, int E, int rk,
+                                                   int Q, const int *__restrict__ qstatus, int *rank,
+                                                   int keys_in_smem) {
   extern __shared__ unsigned long long rk_smem[];
   const int nw = blockDim.x >> 5, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int q = blockIdx.x * nw + w;
   if (q >= Q || qstatus[q] != PGB_Q_OK) return;
   unsigned long long *keys = rk_smem + (long)w * E;
   const double *sc = scores + (long)q * E;
+  const bool direct = pr.on && pr.qamb[q] == 0;
+  const int ql = pr.on ? pr.qlen[q] : 0;
+  auto key_of = [&](int i) {
+    return s1_key(direct ? s1_score(pr.C, pr.Xhi, pr.Xlo, (long)q * pr.Ep + i, ql, pr.log_nrates) : sc[i]);
+  };
   if (keys_in_smem)
-    for (int i = lane; i < E; i += 32) keys[i] = s1_key(sc[i]);
+    for (int i = lane; i < E; i += 32) keys[i] = key_of(i);
   __syncwarp();
   unsigned long long ck[kRankCache];
   int ci[kRankCache];
@@ -479,7 +501,7 @@ __global__ void __launch_bounds__(128) k_rank_warp(const double *__restrict__ sc
 #pragma unroll
     for (int c = 0; c < kRankCache; c++) { ck[c] = 0ull; ci[c] = -1; }
     for (int i = lane; i < E; i += 32) {
-      unsigned long long k = keys_in_smem ? keys[i] : s1_key(sc[i]);
+      unsigned long long k = keys_in_smem ? keys[i] : key_of(i);
       if (li >= 0 && !rank_before(lk, li, k, i)) continue;
       if (ci[kRankCache - 1] >= 0 && !rank_before(k, i, ck[kRankCache - 1], ci[kRankCache - 1])) continue;
       // insert into the sorted cache
@@ -1092,7 +1114,10 @@ pgb_status gemm_bf16(pgb_engine *e, const __nv_bfloat16 *B, const __nv_bfloat16 
   return PGB_OK;
 }
 
-pgb_status run_stage1(pgb_engine *e) {
+// all_scores: write every query's FP64 scores; otherwise only the queries
+// with ambiguity characters get them (the ranking forms the others' scores
+// from the GEMM products itself)
+pgb_status run_stage1(pgb_engine *e, bool all_scores = true) {
   pgb_status s;
   size_t K4 = (size_t)e->prim * e->Sp;
   size_t qe_n = (size_t)e->Q * e->n_edges;
@@ -1125,14 +1150,18 @@ pgb_status run_stage1(pgb_engine *e) {
       (s = gemm_bf16(e, e->d_BX + (size_t)Ep * e->Sp, e->d_M, e->d_Xlo, Ep, e->Q, e->Sp, Ep, 0.f)))
     return s;
   double log_nrates = e->gcat ? 0.0 : log((double)(float)e->NM);
-  k_s1_epilogue<<<grid_for((long)qe_n), 256, 0, e->st>>>(e->Q, e->n_edges, Ep, e->d_C, e->d_Xhi, e->d_Xlo, e->d_qlen,
-                                                         e->d_qstatus, log_nrates, e->d_scores);
-  PGB_LAUNCH_CHECK();
   std::vector<int> amb;
   for (int q = 0; q < e->Q; q++)
     if (e->h_qamb[q] > 0) amb.push_back(q);
+  if (!amb.empty()) PGB_CUDA(cudaMemcpyAsync(e->d_amb_list, amb.data(), amb.size() * 4, cudaMemcpyHostToDevice, e->st));
+  if (all_scores || !amb.empty()) {
+    const int rows = all_scores ? e->Q : (int)amb.size();
+    k_s1_epilogue<<<grid_for((long)rows * e->n_edges), 256, 0, e->st>>>(
+        rows, all_scores ? nullptr : e->d_amb_list, e->n_edges, Ep, e->d_C, e->d_Xhi, e->d_Xlo, e->d_qlen,
+        e->d_qstatus, log_nrates, e->d_scores);
+    PGB_LAUNCH_CHECK();
+  }
   if (!amb.empty()) {
-    PGB_CUDA(cudaMemcpyAsync(e->d_amb_list, amb.data(), amb.size() * 4, cudaMemcpyHostToDevice, e->st));
     dim3 grid((unsigned)amb.size(), (unsigned)((e->n_edges + 127) / 128));
     k_s1_ambig<<<grid, 128, 0, e->st>>>(stage1_ctx(e), e->d_amb_list, e->d_reind, e->d_mcode, e->d_qlen,
                                         e->d_scores);
@@ -1141,7 +1170,9 @@ pgb_status run_stage1(pgb_engine *e) {
   return PGB_OK;
 }
 
-pgb_status run_rank(pgb_engine *e, int rk) {
+// fused: the scores of queries without ambiguity characters come from the
+// GEMM products (run_stage1 with all_scores false)
+pgb_status run_rank(pgb_engine *e, int rk, bool fused = false) {
   const int E = e->n_edges;
   const size_t keys = (size_t)E * 8;
   // up to 4 warps (queries) per block with the keys staged, within 96 KB
@@ -1151,8 +1182,13 @@ pgb_status run_rank(pgb_engine *e, int rk) {
   size_t smem = in_smem ? nw * keys : 0;
   if (smem > 48 * 1024)
     PGB_CUDA(cudaFuncSetAttribute(k_rank_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  k_rank_warp<<<(e->Q + nw - 1) / nw, 32 * nw, smem, e->st>>>(e->d_scores, E, rk, e->Q, e->d_qstatus, e->d_rank,
-                                                              in_smem);
+  S1Products pr{};
+  pr.on = fused ? 1 : 0;
+  pr.C = e->d_C; pr.Xhi = e->d_Xhi; pr.Xlo = e->d_Xlo; pr.qlen = e->d_qlen; pr.qamb = e->d_qamb;
+  pr.Ep = (E + 15) & ~15;
+  pr.log_nrates = e->gcat ? 0.0 : log((double)(float)e->NM);
+  k_rank_warp<<<(e->Q + nw - 1) / nw, 32 * nw, smem, e->st>>>(e->d_scores, pr, E, rk, e->Q, e->d_qstatus,
+                                                              e->d_rank, in_smem);
   PGB_LAUNCH_CHECK();
   return PGB_OK;
 }
@@ -1930,7 +1966,8 @@ pgb_status pgb_queries_rank(pgb_engine *e, const pgb_prefs *p, int rk, int *rank
   size_t rn = (size_t)e->Q * rk;
   if (rn > e->rank_cap) { if ((s = dalloc(&e->d_rank, rn))) return s; e->rank_cap = rn; }
   PGB_CUDA(cudaMemsetAsync(e->d_rank, 0xff, rn * sizeof(int), e->st));
-  if ((s = build_stage1_table(e, p->start_pend)) || (s = run_stage1(e)) || (s = run_rank(e, rk))) return s;
+  if ((s = build_stage1_table(e, p->start_pend)) || (s = run_stage1(e, false)) || (s = run_rank(e, rk, true)))
+    return s;
   PGB_CUDA(cudaMemcpyAsync(rank, e->d_rank, rn * sizeof(int), cudaMemcpyDeviceToHost, e->st));
   PGB_CUDA(cudaStreamSynchronize(e->st));
   return PGB_OK;
@@ -1954,8 +1991,8 @@ pgb_status pgb_queries_run(pgb_engine *e, const pgb_prefs *p) {
   PGB_CUDA(cudaEventRecord(e->ev[0], e->st));
   if ((s = build_stage1_table(e, p->start_pend))) return s;
   PGB_CUDA(cudaEventRecord(e->ev[1], e->st));
-  if ((s = run_stage1(e))) return s;
-  if ((s = run_rank(e, rk))) return s;
+  if ((s = run_stage1(e, false))) return s;
+  if ((s = run_rank(e, rk, true))) return s;
   PGB_CUDA(cudaEventRecord(e->ev[2], e->st));
   e->counts[0] = (double)e->Q * e->n_edges;
   // baseball rounds
