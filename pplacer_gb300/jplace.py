@@ -117,8 +117,9 @@ def to_jplace(results, names, parent, bl, labels=None, invocation="pplacer_gb300
     best first (Engine.place / Engine.fetch), or (..., post_prob,
     marginal_like) with posterior probabilities, which adds those two fields
     (placement.ml:176-180); queries with no placement are left out, as
-    pplacer leaves out failed queries.  names: one name per query
-    (multiplicity 1)."""
+    pplacer leaves out failed queries.  names: per query a name, or a list
+    of names (``model.dedup``), each written with multiplicity 1
+    (placerun.ml:95-112)."""
     rows = []
     with_pp = any(len(pl) > 5 for places in results for pl in places)
     fields = sorted(FIELDS + (["marginal_like", "post_prob"] if with_pp else []))
@@ -133,7 +134,8 @@ def to_jplace(results, names, parent, bl, labels=None, invocation="pplacer_gb300
             if with_pp:
                 val["post_prob"], val["marginal_like"] = float(pl[5]), float(pl[6])
             p.append([val[f] for f in fields])
-        rows.append({"p": p, "nm": [[name, 1]]})
+        namel = [name] if isinstance(name, str) else list(name)
+        rows.append({"p": p, "nm": [[n, 1] for n in namel]})
     doc = {"tree": numbered_newick(parent, bl, labels), "placements": rows,
            "metadata": {"invocation": invocation}, "version": 3, "fields": fields}
     out = []

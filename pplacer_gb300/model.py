@@ -7,6 +7,7 @@ hot path and hands to the likelihood engine.
 * ``discrete_gamma`` -- Gamma.discrete_gamma (pplacer_src/gamma.ml:315-371).
 * ``emper_freq`` -- Alignment.emper_freq (common_src/alignment.ml:186-215).
 * ``premask`` -- Pplacer_run.premask (pplacer_src/pplacer_run.ml:59-144).
+* ``dedup`` -- the query deduplication of pplacer_src/pplacer_run.ml:228-253.
 """
 from dataclasses import dataclass
 
@@ -130,3 +131,25 @@ def premask(ref_seqs, query_seqs):
     mask = ref_mask & qry_inf.any(0)
     cut = lambda rows: [r[mask].tobytes().decode() for r in rows]
     return cut(ref), cut(qry), mask
+
+
+def dedup(names, seqs):
+    """Place identical query sequences once (pplacer_run.ml:228-253): returns
+    (unique_seqs, name_lists), name_lists[i] holding every name whose
+    sequence is unique_seqs[i], in input order.  Run it on pre-masked
+    sequences, as the reference does.  Writing one pquery per unique sequence
+    with each of its names at multiplicity 1 is Placerun.redup without
+    ``as_mass`` (placerun.ml:95-112); ``jplace.to_jplace`` takes the name
+    lists directly.  Unique sequences come in order of first appearance (the
+    reference's order is its hash table's)."""
+    if len(names) != len(seqs):
+        raise ValueError("%d names for %d sequences" % (len(names), len(seqs)))
+    index, uniq, namel = {}, [], []
+    for n, s in zip(names, seqs):
+        i = index.get(s)
+        if i is None:
+            index[s] = i = len(uniq)
+            uniq.append(s)
+            namel.append([])
+        namel[i].append(n)
+    return uniq, namel

@@ -38,3 +38,21 @@ def test_document_layout():
     assert doc["placements"][0]["p"][0] == [0.5, 0, 0.710949502625, -1309.83, 0.9]
     assert "-1309.83," in text and "1e-08" in text  # %.12g numbers, %d edge numbers
     assert "0.710949502625" in text
+
+
+def test_dedup_and_redup():
+    from pplacer_gb300.model import dedup
+    names = ["a", "b", "c", "d", "e"]
+    seqs = ["ACGT", "AC-T", "ACGT", "ACGT", "AC-T"]
+    uniq, namel = dedup(names, seqs)
+    assert uniq == ["ACGT", "AC-T"]
+    assert namel == [["a", "c", "d"], ["b", "e"]]
+    results = [[(0, -10.0, 1.0, 0.05, 0.1)], [(1, -12.0, 1.0, 0.025, 0.2)]]
+    doc = json.loads(jplace.to_jplace(results, namel, [2, 2, -1], [0.1, 0.05, 0.0], ["A", "B", ""]))
+    assert [r["nm"] for r in doc["placements"]] == [[["a", 1], ["c", 1], ["d", 1]], [["b", 1], ["e", 1]]]
+    try:
+        dedup(["a"], ["A", "C"])
+    except ValueError:
+        pass
+    else:
+        raise AssertionError("length mismatch accepted")
