@@ -456,12 +456,14 @@ __device__ __forceinline__ unsigned long long s1_key(double v) {
   return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
 }
 
-// keys in shared memory when a warp's row fits (E * 8 bytes), else read
-// from global memory.  Each lane keeps a sorted cache of its kRankCache best
-// remaining edges; a lane that wins pops its cache and, when it runs dry,
-// refills it from its edges ranked after the last one it gave out, so most
-// lanes scan their edges once.
-constexpr int kRankCache = 4;
+// Each lane keeps a sorted cache of its kRankCache best remaining edges; a
+// lane that wins pops its cache and, when it runs dry, refills it from its
+// edges ranked after the last one it gave out.  With rk well below
+// 32 * kRankCache most lanes scan their edges once, reading the scores (or
+// GEMM products) straight from global memory; ranking many edges per query
+// (rk = E when every edge is tried) stages the row's keys in shared memory
+// first, as the refills rescan it.
+constexpr int kRankCache = 8;
 
 __device__ __forceinline__ bool rank_before(unsigned long long ka, int ia, unsigned long long kb, int ib) {
   return ka > kb || (ka == kb && ia < ib);
@@ -1175,10 +1177,13 @@ pgb_status run_stage1(pgb_engine *e, bool all_scores = true) {
 pgb_status run_rank(pgb_engine *e, int rk, bool fused = false) {
   const int E = e->n_edges;
   const size_t keys = (size_t)E * 8;
-  // up to 4 warps (queries) per block with the keys staged, within 96 KB
-  int nw = 4, in_smem = 1;
-  while (nw > 1 && nw * keys > 96 * 1024) nw--;
-  if (nw * keys > e->smem_optin) in_smem = 0;
+  // up to 4 warps (queries) per block; keys staged (within 96 KB) only for
+  // long rankings, where lanes refill their caches often
+  int nw = 4, in_smem = rk > 16 * kRankCache ? 1 : 0;
+  if (in_smem) {
+    while (nw > 1 && nw * keys > 96 * 1024) nw--;
+    if (nw * keys > e->smem_optin) in_smem = 0;
+  }
   size_t smem = in_smem ? nw * keys : 0;
   if (smem > 48 * 1024)
     PGB_CUDA(cudaFuncSetAttribute(k_rank_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));

@@ -65,13 +65,16 @@ def test_stage1_scores_match_oracle(small, oracle_lib):
         np.testing.assert_allclose(got, ref, rtol=1e-6)
 
 
-def test_stage1_ranking(small):
-    """The rk best edges per query: scores descending, equal scores by
-    increasing edge index, NaN last (fig.ml:143-147)."""
+@pytest.mark.parametrize("rk", [1, 65, 130, 0])
+def test_stage1_ranking(small, rk):
+    """The rk best edges per query (0: every edge): scores descending, equal
+    scores by increasing edge index, NaN last (fig.ml:143-147).  Short
+    rankings read the scores from global memory, long ones stage them in
+    shared memory and refill the lanes' caches."""
     w, oref, eng = small
     sc = eng.stage1()
     E = sc.shape[1]
-    rk = min(E, 65)
+    rk = min(E, rk) if rk else E
     got = eng.rank(rk)
     for q in range(sc.shape[0]):
         want = sorted(range(E), key=lambda i: (math.isnan(sc[q, i]), -sc[q, i] if not math.isnan(sc[q, i]) else 0.0, i))
