@@ -128,6 +128,16 @@ pgb_status pgb_float_mat_int_vec_mul(double *dst, const double *mat, const uint1
 pgb_status pgb_ten_log_like3_noalloc(const double *statd, const double *x, const double *y, const double *z,
                                      int n_rates, int n_sites, int n_states, double *result, void *stream);
 
+/* FP32 evolve on the tensor cores: out[s][i] = sum_j b[i][j] a[s][j] for
+ * s < n_rows, i < n_out (<= 64), j < n_states (<= 24) -- the per-site
+ * matrix-vector product of gemmish_c (linear_c.c:29-90) with the sites as
+ * rows, computed as the 20-state trial kernel computes it (tcgen05 MMAs of
+ * 128 sites, operands split into TF32 hi + lo, three products accumulated in
+ * FP32).  Host pointers, row-major; synchronous.  No counterpart in the
+ * reference (which evolves in FP64 on the CPU): it exposes the trial kernel's
+ * arithmetic for checks. */
+pgb_status pgb_tc_evolve(const float *a, const float *b, float *out, int n_rows, int n_states, int n_out);
+
 /* ----------------------------------------------------------------------------
  * 2. Batched placement engine
  * ------------------------------------------------------------------------- */

@@ -16,7 +16,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libpplacer_gb300.so")
-SOURCES = ["dropin.cu", "engine.cu", "noalloc.cu"]
+SOURCES = ["dropin.cu", "engine.cu", "noalloc.cu", "tc.cu"]
 # The drop-in keeps linear_c.c's unfused multiply-add arithmetic so that its
 # FP64 results equal the reference's to the last bit where the summation order
 # is the same.

@@ -1,0 +1,116 @@
+// Stand-alone tensor-core evolve (pgb_tc_evolve): the tcgen05 path of the
+// 20-state trial kernel on caller data, one 128-row tile per CTA.
+#include "pgb_common.cuh"
+#include "tc.cuh"
+
+namespace pgb {
+
+constexpr int kTcEvolveN = 64;  // TMEM columns (and B rows) of one tile
+
+__global__ void __launch_bounds__(128) k_tc_evolve(const float *__restrict__ A, const float *__restrict__ B,
+                                                   float *__restrict__ out, int n, int K, int N, int *err) {
+  extern __shared__ __align__(1024) float tsm[];
+  float *a_hi = tsm, *a_lo = tsm + tc::kTileFloats;
+  float *b_hi = tsm + 2 * tc::kTileFloats, *b_lo = b_hi + kTcEvolveN * tc::kKPad;
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ uint32_t tbase;
+  const int t = threadIdx.x, w = t >> 5;
+  const long row = (long)blockIdx.x * tc::kTileRows + t;
+  // operand tiles, zero past n rows, K states and N matrix rows
+  for (int k = 0; k < tc::kKPad; k += 4) {
+    float h[4], l[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) tc::split_tf32(row < n && k + j < K ? A[row * K + k + j] : 0.f, h[j], l[j]);
+    *reinterpret_cast<float4 *>(a_hi + tc::off(t, k)) = make_float4(h[0], h[1], h[2], h[3]);
+    *reinterpret_cast<float4 *>(a_lo + tc::off(t, k)) = make_float4(l[0], l[1], l[2], l[3]);
+  }
+  for (int i = t; i < kTcEvolveN * (tc::kKPad / 4); i += blockDim.x) {
+    const int r = i / (tc::kKPad / 4), k = (i - r * (tc::kKPad / 4)) * 4;
+    float h[4], l[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) tc::split_tf32(r < N && k + j < K ? B[r * K + k + j] : 0.f, h[j], l[j]);
+    *reinterpret_cast<float4 *>(b_hi + tc::off(r, k)) = make_float4(h[0], h[1], h[2], h[3]);
+    *reinterpret_cast<float4 *>(b_lo + tc::off(r, k)) = make_float4(l[0], l[1], l[2], l[3]);
+  }
+  if (w == 0) tc::tmem_alloc(&tbase, kTcEvolveN);
+  if (t == 0) tc::bar_init(&bar, 1);
+  tc::fence_async_smem();
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
+  const uint32_t d = tbase;
+  const int nm = N <= 32 ? 32 : 64;
+  if (t == 0) {
+    tc::mma_3xtf32(d, tc::smem_addr(a_hi), tc::smem_addr(a_lo), tc::smem_addr(b_hi), tc::smem_addr(b_lo),
+                   tc::idesc_tf32(tc::kTileRows, nm));
+    tc::commit(&bar);
+  }
+  bool ok = tc::bar_wait(&bar, 0);
+  ok = __all_sync(0xffffffffu, ok);
+  if (!ok) {
+    if ((t & 31) == 0) atomicExch(err, 1);
+    tc::bar_wait(&bar, 0);  // once more, bounded, before the columns are freed
+  }
+  tc::fence_after();
+  if (ok) {
+    for (int c0 = 0; c0 < nm; c0 += 16) {
+      float v[16];
+      tc::ld16(d + ((uint32_t)(32 * w) << 16) + (uint32_t)c0, v);
+      tc::ld_wait();
+      tc::pin(v);
+#pragma unroll
+      for (int j = 0; j < 16; j++)
+        if (row < n && c0 + j < N) out[row * N + c0 + j] = v[j];
+    }
+  }
+  tc::fence_before();
+  __syncthreads();
+  if (w == 0) tc::tmem_dealloc(d, kTcEvolveN);
+}
+
+}  // namespace pgb
+
+using namespace pgb;
+
+extern "C" pgb_status pgb_tc_evolve(const float *A, const float *B, float *out, int n_rows, int K, int N) {
+  if (n_rows < 0 || K < 1 || K > tc::kKPad || N < 1 || N > kTcEvolveN || (!A && n_rows) || !B || (!out && n_rows)) {
+    set_error("tc_evolve: n_rows %d, K %d (1..%d), N %d (1..%d)", n_rows, K, tc::kKPad, N, kTcEvolveN);
+    return PGB_ERR_ARG;
+  }
+  if (n_rows == 0) return PGB_OK;
+  float *dA = nullptr, *dB = nullptr, *dO = nullptr;
+  int *derr = nullptr;
+  pgb_status st = PGB_OK;
+  auto fail = [&](cudaError_t e, const char *what) {
+    set_error("tc_evolve %s: %s", what, cudaGetErrorString(e));
+    st = PGB_ERR_CUDA;
+  };
+  cudaError_t e;
+  const size_t smem = (size_t)(2 * tc::kTileFloats + 2 * kTcEvolveN * tc::kKPad) * 4;
+  if ((e = cudaMalloc(&dA, (size_t)n_rows * K * 4)) || (e = cudaMalloc(&dB, (size_t)N * K * 4)) ||
+      (e = cudaMalloc(&dO, (size_t)n_rows * N * 4)) || (e = cudaMalloc(&derr, 4))) {
+    fail(e, "alloc");
+  } else if ((e = cudaMemcpy(dA, A, (size_t)n_rows * K * 4, cudaMemcpyHostToDevice)) ||
+             (e = cudaMemcpy(dB, B, (size_t)N * K * 4, cudaMemcpyHostToDevice)) || (e = cudaMemset(derr, 0, 4)) ||
+             (e = cudaFuncSetAttribute(k_tc_evolve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem))) {
+    fail(e, "upload");
+  } else {
+    k_tc_evolve<<<(n_rows + tc::kTileRows - 1) / tc::kTileRows, 128, smem>>>(dA, dB, dO, n_rows, K, N, derr);
+    count_launch();
+    int herr = 0;
+    if ((e = cudaGetLastError()) || (e = cudaDeviceSynchronize()) ||
+        (e = cudaMemcpy(&herr, derr, 4, cudaMemcpyDeviceToHost))) {
+      fail(e, "launch");
+    } else if (herr) {
+      set_error("tc_evolve: tensor-core completion wait timed out");
+      st = PGB_ERR_CUDA;
+    } else if ((e = cudaMemcpy(out, dO, (size_t)n_rows * N * 4, cudaMemcpyDeviceToHost))) {
+      fail(e, "download");
+    }
+  }
+  cudaFree(dA);
+  cudaFree(dB);
+  cudaFree(dO);
+  cudaFree(derr);
+  return st;
+}

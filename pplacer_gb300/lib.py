@@ -74,7 +74,8 @@ def load(build_if_missing=True):
                        ("pgb_ten_statd_pairwise_prod", [dp, dp, dp, dp, i, i, i]),
                        ("pgb_vec_pairwise_prod", [dp, dp, dp, i]),
                        ("pgb_int_vec_pairwise_prod", [vp, vp, vp, i]),
-                       ("pgb_float_mat_int_vec_mul", [dp, dp, vp, i, i])]:
+                       ("pgb_float_mat_int_vec_mul", [dp, dp, vp, i, i]),
+                       ("pgb_tc_evolve", [vp, vp, vp, i, i, i])]:
         getattr(L, name).argtypes = args
         getattr(L, name).restype = i
     for name, args in [("pgb_mat_log_like3", [dp, dp, dp, dp, i, i]),
