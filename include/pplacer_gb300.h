@@ -308,14 +308,18 @@ pgb_status pgb_queries_trials(pgb_engine *e, const pgb_prefs *prefs, int optimiz
  * mixture has 1, 2, 4 or 8 rates always use the whole-query warp kernel (one
  * warp runs a query's baseball trials, keep and refinement); autotune sets
  * that and returns.  For the other models: for each of the 6 query-length bins
- * (<= 256, 512, 768, 1024, 1536 informative sites, longer), time one CTA of
+ * (<= 256, 512, 768, 1024, 1536 informative sites, longer; 128, 256, 384,
+ * 512, 640 for 20 states and CAT), time one CTA of
  * 128 or 256 threads per trial with the query's sites of darr / parr staged
- * in shared memory or read from L2, on the loaded queries' first baseball
- * round, and keep the fastest for later runs.  get_tuning reports the table
- * (threads[6], smem_windows[6]); set_tuning imposes one (threads 32, 128 or
- * 256; smem_windows 0 or 1).  threads 32 in every bin selects the whole-query
- * warp kernel; where the warp form does not apply it falls back to 256.  No
- * reference counterpart: pplacer has one CPU code path. */
+ * in shared memory or read from L2, and for 20-state Gamma mixtures the
+ * tensor-core CTA (tcgen05 evolves, 128 threads), on the loaded queries'
+ * first baseball round, and keep the fastest for later runs.  get_tuning
+ * reports the table (threads[6], smem_windows[6]); set_tuning imposes one
+ * (threads 1 = tensor-core CTA, 32, 128 or 256; smem_windows 0 or 1).
+ * threads 32 in every bin selects the whole-query warp kernel; where the warp
+ * or tensor-core form does not apply it falls back to 256.  20-state Gamma
+ * mixtures start with the tensor-core form.  No reference counterpart:
+ * pplacer has one CPU code path. */
 pgb_status pgb_engine_autotune(pgb_engine *e, const pgb_prefs *prefs);
 pgb_status pgb_engine_get_tuning(pgb_engine *e, int *threads, int *smem_windows);
 pgb_status pgb_engine_set_tuning(pgb_engine *e, const int *threads, const int *smem_windows);

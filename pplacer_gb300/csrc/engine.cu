@@ -21,6 +21,7 @@
 #include <cuda_bf16.h>
 
 #include "pgb_common.cuh"
+#include "tc.cuh"
 
 namespace pgb {
 namespace {
@@ -545,6 +546,7 @@ __global__ void __launch_bounds__(128) k_rank_warp(const double *__restrict__ sc
 
 #include "trials.cuh"
 #include "trials_warp.cuh"
+#include "trials_tc.cuh"
 
 // ---------------------------------------------------------------------------
 // Baseball (core.ml:429-464) and keep / refine / like_weight_ratio
@@ -956,7 +958,7 @@ struct pgb_engine {
   double *d_bl = nullptr, *d_Xd = nullptr, *d_Xitd = nullptr, *d_lamd = nullptr, *d_ratesd = nullptr,
          *d_statdd = nullptr, *d_lvd = nullptr, *d_pm = nullptr, *d_pmh = nullptr;
   float *d_mf = nullptr;  // X, W, Lt, lvf, statd, lam, rates (float)
-  size_t off_X = 0, off_W = 0, off_Lt = 0, off_lv = 0, off_statd = 0, off_lam = 0, off_rates = 0;
+  size_t off_X = 0, off_W = 0, off_Lt = 0, off_lv = 0, off_statd = 0, off_lam = 0, off_rates = 0, off_Xit = 0;
   uint8_t *d_site_cat = nullptr, *d_char_code = nullptr, *d_informative = nullptr;
   int *d_edge_nodes = nullptr, *d_parent = nullptr, *d_ch_start = nullptr, *d_ch_list = nullptr;
   // GLVs
@@ -995,6 +997,7 @@ struct pgb_engine {
   int *d_bin_list = nullptr;
   size_t trials_cap = 0;
   unsigned long long *d_stats = nullptr;  // trial-kernel evaluation counters
+  int *d_tc_err = nullptr;  // set by the tensor-core trial kernel when a completion wait timed out
   int *d_small = nullptr;  // counters: [0] trial counter, [1] n_active, [2..2+bins) bin counts, then bin limits
   pgb_placement *d_out = nullptr;
   int *d_qorder = nullptr;  // queries longest first (whole-query warp kernel)
@@ -1018,6 +1021,7 @@ struct pgb_engine {
 namespace {
 
 constexpr int kBins = 6;
+constexpr int kTuneTc = 1;  // tuning code of the tensor-core trial kernel
 
 template <class T>
 pgb_status dalloc(T **p, size_t n) {
@@ -1206,6 +1210,8 @@ TrialCtx trial_ctx(pgb_engine *e, const pgb_prefs *p, int optimizer, int mode) {
   c.site_cat = e->d_site_cat; c.qamb = e->d_qamb; c.prim = e->prim;
   c.X = e->d_mf + e->off_X; c.W = e->d_mf + e->off_W; c.Lt = e->d_mf + e->off_Lt; c.lvf = e->d_mf + e->off_lv;
   c.statd = e->d_mf + e->off_statd; c.lam = e->d_mf + e->off_lam; c.rates = e->d_mf + e->off_rates;
+  c.Xit = e->d_mf + e->off_Xit;
+  c.tc_err = e->d_tc_err;
   c.log_nrates = e->gcat ? 0.0 : log((double)(float)e->NM);
   c.start_pend = p->start_pend;
   c.max_pend = p->max_pend;
@@ -1267,11 +1273,45 @@ pgb_status launch_trials_warp(pgb_engine *e, cudaStream_t st, TrialCtx c, const 
   }
 }
 
-// threads: 32 selects the warp-per-trial kernel where it applies, else the
-// CTA-per-trial kernel with 128 or 256 threads
+// the tensor-core trial kernel covers 20-state Gamma mixtures
+bool tc_trials_ok(const pgb_engine *e) { return e->K == kTcK && !e->gcat && e->NM == e->RP; }
+
+pgb_status launch_trials_tc(pgb_engine *e, cudaStream_t st, TrialCtx c, const int *d_order, int n, int cap,
+                            TrialRes *out) {
+  c.smem_win = 0;
+  c.cap = std::max(cap, 1);
+  size_t smem = tc_trial_smem_bytes(c.cap, e->NM, e->ncode);
+  if (smem > e->smem_optin) { set_error("tensor-core trial shared memory %zu exceeds %zu", smem, e->smem_optin); return PGB_ERR_ARG; }
+  PGB_CUDA(cudaFuncSetAttribute(k_trials_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  k_trials_tc<<<n, kTcThreads, smem, st>>>(c, e->d_trials, d_order, n, out);
+  PGB_LAUNCH_CHECK();
+  return PGB_OK;
+}
+
+// the tensor-core kernel's completion-wait flag: an error once set
+pgb_status check_tc_err(pgb_engine *e) {
+  int h[16];
+  PGB_CUDA(cudaMemcpy(h, e->d_tc_err, sizeof h, cudaMemcpyDeviceToHost));
+  if (h[0]) {
+    cudaMemset(e->d_tc_err, 0, sizeof h);
+    set_error("tensor-core trial kernel: an MMA completion wait timed out (cta %d rate %d chunk %d phase %d: "
+              "wait %d test %d/%d; tmem 0x%x, tiles 0x%x, barrier 0x%x; sites %d chunks %d)",
+              h[1], h[2], h[3], h[4], h[5], h[6], h[7], h[8], h[9], h[10], h[11], h[12]);
+    return PGB_ERR_CUDA;
+  }
+  return PGB_OK;
+}
+
+// threads: 32 selects the warp-per-trial kernel where it applies, 1 the
+// tensor-core CTA kernel where it applies, else the CTA-per-trial kernel with
+// 128 or 256 threads
 pgb_status launch_trials(pgb_engine *e, cudaStream_t st, TrialCtx c, const int *d_order, int n, int cap, bool win,
                          TrialRes *out, int threads) {
   if (n <= 0) return PGB_OK;
+  if (threads == kTuneTc) {
+    if (tc_trials_ok(e)) return launch_trials_tc(e, st, c, d_order, n, cap, out);
+    threads = 256;
+  }
   if (threads == 32) {
     if (warp_trials_ok(e)) {
       WarpSegs segs{};
@@ -1575,6 +1615,8 @@ pgb_status pgb_engine_create(const pgb_model_desc *m, const pgb_tree_desc *t, pg
   e->smem_optin = (size_t)optin;
   if (warp_trials_ok(e))  // one warp per trial unless the autotuner finds better
     for (int b = 0; b < kBins; b++) { e->tune_threads[b] = 32; e->tune_win[b] = 0; }
+  if (tc_trials_ok(e))  // tensor-core CTAs unless the autotuner finds better
+    for (int b = 0; b < kBins; b++) { e->tune_threads[b] = kTuneTc; e->tune_win[b] = 0; }
   for (int i = 0; i < 8; i++) cudaEventCreate(&e->ev[i]);
   for (int i = 0; i < 8; i++) cudaStreamCreateWithFlags(&e->bin_st[i], cudaStreamNonBlocking);
   for (int i = 0; i < 9; i++) cudaEventCreateWithFlags(&e->bin_ev[i], cudaEventDisableTiming);
@@ -1582,10 +1624,10 @@ pgb_status pgb_engine_create(const pgb_model_desc *m, const pgb_tree_desc *t, pg
   // model constants
   std::vector<float> mf;
   auto put = [&](const std::vector<float> &v) { size_t o = mf.size(); mf.insert(mf.end(), v.begin(), v.end()); while (mf.size() % 4) mf.push_back(0.f); return o; };
-  std::vector<float> Xf(K * K), W((size_t)K * K * K), Lt((size_t)e->ncode * K), lvf((size_t)e->ncode * K), sf(K), lf(K),
+  std::vector<float> Xf(K * K), Xitf(K * K), W((size_t)K * K * K), Lt((size_t)e->ncode * K), lvf((size_t)e->ncode * K), sf(K), lf(K),
       rf(e->NM);
   std::vector<double> lvd((size_t)e->ncode * K), lv(K);
-  for (int i = 0; i < K * K; i++) Xf[i] = (float)e->X[i];
+  for (int i = 0; i < K * K; i++) { Xf[i] = (float)e->X[i]; Xitf[i] = (float)e->Xit[i]; }
   for (int i = 0; i < K; i++)
     for (int j = 0; j < K; j++)
       for (int k = 0; k < K; k++) W[((size_t)i * K + j) * K + k] = (float)(e->X[i * K + k] * e->Xit[j * K + k]);
@@ -1602,7 +1644,7 @@ pgb_status pgb_engine_create(const pgb_model_desc *m, const pgb_tree_desc *t, pg
   for (int i = 0; i < K; i++) { sf[i] = (float)e->statd[i]; lf[i] = (float)e->lam[i]; }
   for (int i = 0; i < e->NM; i++) rf[i] = (float)e->rates[i];
   e->off_X = put(Xf); e->off_W = put(W); e->off_Lt = put(Lt); e->off_lv = put(lvf);
-  e->off_statd = put(sf); e->off_lam = put(lf); e->off_rates = put(rf);
+  e->off_statd = put(sf); e->off_lam = put(lf); e->off_rates = put(rf); e->off_Xit = put(Xitf);
   // character tables
   std::vector<uint8_t> cc(256, kBadCode), inf(kMaxCodes, 0);
   const char *alpha = code_alphabet(K);
@@ -1631,9 +1673,14 @@ pgb_status pgb_engine_create(const pgb_model_desc *m, const pgb_tree_desc *t, pg
       (s = upload(&e->d_parent, e->parent.data(), e->parent.size(), e->st)) ||
       (s = upload(&e->d_ch_start, e->ch_start.data(), e->ch_start.size(), e->st)) ||
       (s = upload(&e->d_ch_list, e->ch_list.data(), e->ch_list.size(), e->st)) ||
-      (s = dalloc(&e->d_small, 64)) || (s = dalloc(&e->d_stats, 4))) {
+      (s = dalloc(&e->d_small, 64)) || (s = dalloc(&e->d_stats, 4)) || (s = dalloc(&e->d_tc_err, 16))) {
     pgb_engine_destroy(e);
     return s;
+  }
+  if ((ce = cudaMemsetAsync(e->d_tc_err, 0, 16 * sizeof(int), e->st)) != cudaSuccess) {
+    set_error("engine_create: %s", cudaGetErrorString(ce));
+    pgb_engine_destroy(e);
+    return PGB_ERR_CUDA;
   }
   // P matrices of every node at bl and bl/2 (FP64)
   size_t npm = (size_t)e->n_nodes * e->NM * K * K;
@@ -2093,6 +2140,7 @@ pgb_status pgb_queries_run(pgb_engine *e, const pgb_prefs *p) {
   e->counts[1] = n_trials_total;
   unsigned long long st_h[2] = {0, 0};
   PGB_CUDA(cudaMemcpy(st_h, e->d_stats, sizeof st_h, cudaMemcpyDeviceToHost));
+  if ((s = check_tc_err(e))) return s;
   e->counts[2] = (double)st_h[0];
   e->counts[3] = (double)st_h[1];
   return PGB_OK;
@@ -2142,18 +2190,20 @@ pgb_status pgb_engine_autotune(pgb_engine *e, const pgb_prefs *p) {
   PGB_CUDA(cudaStreamSynchronize(e->st));
   TrialCtx tc = trial_ctx(e, p, p->optimizer, 0);
   tc.stats = nullptr;
-  const int cand_threads[3] = {32, 256, 128};
-  const int n_cand = warp_trials_ok(e) ? 3 : 2, c0 = warp_trials_ok(e) ? 0 : 1;
+  const int cand_threads[4] = {32, kTuneTc, 256, 128};
   for (int b = 0; b < kBins; b++) {
     int n = got[2 + b];
     if (n == 0) continue;
     float best = 1e30f;
     int bt = e->tune_threads[b], bw = e->tune_win[b];
-    for (int ti = c0; ti < c0 + n_cand && ti < 3; ti++)
+    for (int ti = 0; ti < 4; ti++)
       for (int w = 1; w >= 0; w--) {
         int cap;
         bool win;
-        if (cand_threads[ti] == 32 && w == 1) continue;  // the warp kernel reads windows from L2
+        if (cand_threads[ti] == 32 && !warp_trials_ok(e)) continue;
+        if (cand_threads[ti] == kTuneTc && !tc_trials_ok(e)) continue;
+        // the warp and tensor-core kernels read the windows from L2
+        if ((cand_threads[ti] == 32 || cand_threads[ti] == kTuneTc) && w == 1) continue;
         bin_shape(e, b, max_sq, w, &cap, &win);
         if (w == 1 && !win) continue;  // window does not fit: same as w == 0
         float ms_best = 1e30f;
@@ -2178,11 +2228,12 @@ pgb_status pgb_engine_autotune(pgb_engine *e, const pgb_prefs *p) {
   // Time the whole round for the per-bin choice and for each uniform form.
   int per_bin_t[kBins], per_bin_w[kBins];
   for (int b = 0; b < kBins; b++) { per_bin_t[b] = e->tune_threads[b]; per_bin_w[b] = e->tune_win[b]; }
-  const int uni_t[3] = {32, 128, 256}, uni_w[3] = {0, 1, 1};
+  const int uni_t[4] = {32, kTuneTc, 128, 256}, uni_w[4] = {0, 0, 1, 1};
   float best = 1e30f;
   int best_cfg = -1;
-  for (int cfg = -1; cfg < 3; cfg++) {
+  for (int cfg = -1; cfg < 4; cfg++) {
     if (cfg == 0 && !warp_trials_ok(e)) continue;
+    if (cfg == 1 && !tc_trials_ok(e)) continue;
     for (int b = 0; b < kBins; b++) {
       e->tune_threads[b] = cfg < 0 ? per_bin_t[b] : uni_t[cfg];
       e->tune_win[b] = cfg < 0 ? per_bin_w[b] : uni_w[cfg];
@@ -2215,8 +2266,9 @@ pgb_status pgb_engine_get_tuning(pgb_engine *e, int *threads, int *smem_windows)
 pgb_status pgb_engine_set_tuning(pgb_engine *e, const int *threads, const int *smem_windows) {
   if (!e || !threads || !smem_windows) { set_error("set_tuning: null argument"); return PGB_ERR_ARG; }
   for (int b = 0; b < kBins; b++)
-    if ((threads[b] != 32 && threads[b] != 128 && threads[b] != 256) || (smem_windows[b] & ~1)) {
-      set_error("set_tuning: bin %d: threads must be 32, 128 or 256 and smem_windows 0 or 1", b);
+    if ((threads[b] != 32 && threads[b] != kTuneTc && threads[b] != 128 && threads[b] != 256) ||
+        (smem_windows[b] & ~1)) {
+      set_error("set_tuning: bin %d: threads must be 1, 32, 128 or 256 and smem_windows 0 or 1", b);
       return PGB_ERR_ARG;
     }
   for (int b = 0; b < kBins; b++) { e->tune_threads[b] = threads[b]; e->tune_win[b] = smem_windows[b]; }
@@ -2307,6 +2359,7 @@ pgb_status pgb_queries_trials(pgb_engine *e, const pgb_prefs *p, int optimizer, 
   std::vector<TrialRes> res(n_trials);
   PGB_CUDA(cudaMemcpyAsync(res.data(), e->d_tres, n_trials * sizeof(TrialRes), cudaMemcpyDeviceToHost, e->st));
   PGB_CUDA(cudaStreamSynchronize(e->st));
+  if ((s = check_tc_err(e))) return s;
   for (int i = 0; i < n_trials; i++) {
     out[i].like = res[i].like;
     out[i].pend = res[i].pend;

@@ -3,6 +3,8 @@
 #include "pgb_common.cuh"
 #include "tc.cuh"
 
+#include <algorithm>
+
 namespace pgb {
 
 constexpr int kTcEvolveN = 64;  // TMEM columns (and B rows) of one tile
@@ -32,7 +34,8 @@ __global__ void __launch_bounds__(128) k_tc_evolve(const float *__restrict__ A, 
     *reinterpret_cast<float4 *>(b_hi + tc::off(r, k)) = make_float4(h[0], h[1], h[2], h[3]);
     *reinterpret_cast<float4 *>(b_lo + tc::off(r, k)) = make_float4(l[0], l[1], l[2], l[3]);
   }
-  if (w == 0) tc::tmem_alloc(&tbase, kTcEvolveN);
+  __syncwarp();
+  if (w == 0) tc::tmem_alloc(&tbase, 2 * kTcEvolveN);
   if (t == 0) tc::bar_init(&bar, 1);
   tc::fence_async_smem();
   tc::fence_before();
@@ -40,32 +43,42 @@ __global__ void __launch_bounds__(128) k_tc_evolve(const float *__restrict__ A, 
   tc::fence_after();
   const uint32_t d = tbase;
   const int nm = N <= 32 ? 32 : 64;
-  if (t == 0) {
-    tc::mma_3xtf32(d, tc::smem_addr(a_hi), tc::smem_addr(a_lo), tc::smem_addr(b_hi), tc::smem_addr(b_lo),
-                   tc::idesc_tf32(tc::kTileRows, nm));
-    tc::commit(&bar);
+  // Two passes, as the trial kernel runs them: the product into columns
+  // [0, 64), then again into [64, 128), each its own barrier phase; the two
+  // must agree bit for bit.
+  bool ok = true;
+  int pass = 0;
+  for (; pass < 2 && ok; pass++) {
+    if (t == 0) {
+      tc::fence_after();
+      tc::mma_3xtf32(d + 64 * pass, tc::smem_addr(a_hi), tc::smem_addr(a_lo), tc::smem_addr(b_hi),
+                     tc::smem_addr(b_lo), tc::idesc_tf32(tc::kTileRows, nm));
+      tc::commit(&bar);
+    }
+    ok = __syncthreads_and(tc::bar_wait(&bar, (uint32_t)pass) ? 1 : 0) != 0;
+    tc::fence_after();
   }
-  bool ok = tc::bar_wait(&bar, 0);
-  ok = __all_sync(0xffffffffu, ok);
   if (!ok) {
-    if ((t & 31) == 0) atomicExch(err, 1);
-    tc::bar_wait(&bar, 0);  // once more, bounded, before the columns are freed
-  }
-  tc::fence_after();
-  if (ok) {
+    if (t == 0) atomicExch(err, 1);
+    tc::bar_wait(&bar, (uint32_t)(pass - 1));  // the timed-out phase, bounded, before the columns are freed
+  } else {
     for (int c0 = 0; c0 < nm; c0 += 16) {
-      float v[16];
+      float v[16], v2[16];
       tc::ld16(d + ((uint32_t)(32 * w) << 16) + (uint32_t)c0, v);
+      tc::ld16(d + ((uint32_t)(32 * w) << 16) + (uint32_t)(64 + c0), v2);
       tc::ld_wait();
       tc::pin(v);
+      tc::pin(v2);
 #pragma unroll
-      for (int j = 0; j < 16; j++)
-        if (row < n && c0 + j < N) out[row * N + c0 + j] = v[j];
+      for (int j = 0; j < 16; j++) {
+        if (row < n && c0 + j < N) out[row * N + c0 + j] = v2[j];
+        if (row < n && c0 + j < N && __float_as_uint(v[j]) != __float_as_uint(v2[j])) atomicExch(err, 2);
+      }
     }
   }
   tc::fence_before();
   __syncthreads();
-  if (w == 0) tc::tmem_dealloc(d, kTcEvolveN);
+  if (w == 0) tc::tmem_dealloc(d, 2 * kTcEvolveN);
 }
 
 }  // namespace pgb
@@ -86,7 +99,9 @@ extern "C" pgb_status pgb_tc_evolve(const float *A, const float *B, float *out, 
     st = PGB_ERR_CUDA;
   };
   cudaError_t e;
-  const size_t smem = (size_t)(2 * tc::kTileFloats + 2 * kTcEvolveN * tc::kKPad) * 4;
+  // at most 4 CTAs per SM (4 x 128 TMEM columns): the shared memory of one
+  // is raised to a quarter of the SM's
+  const size_t smem = std::max((size_t)(2 * tc::kTileFloats + 2 * kTcEvolveN * tc::kKPad) * 4, (size_t)58 * 1024);
   if ((e = cudaMalloc(&dA, (size_t)n_rows * K * 4)) || (e = cudaMalloc(&dB, (size_t)N * K * 4)) ||
       (e = cudaMalloc(&dO, (size_t)n_rows * N * 4)) || (e = cudaMalloc(&derr, 4))) {
     fail(e, "alloc");
@@ -102,7 +117,8 @@ extern "C" pgb_status pgb_tc_evolve(const float *A, const float *B, float *out, 
         (e = cudaMemcpy(&herr, derr, 4, cudaMemcpyDeviceToHost))) {
       fail(e, "launch");
     } else if (herr) {
-      set_error("tc_evolve: tensor-core completion wait timed out");
+      set_error(herr == 1 ? "tc_evolve: tensor-core completion wait timed out"
+                          : "tc_evolve: the two passes of the product differ");
       st = PGB_ERR_CUDA;
     } else if ((e = cudaMemcpy(out, dO, (size_t)n_rows * N * 4, cudaMemcpyDeviceToHost))) {
       fail(e, "download");

@@ -89,6 +89,20 @@ __device__ __forceinline__ bool bar_try_wait(uint64_t *bar, uint32_t parity) {
   return ok != 0;
 }
 
+// Non-blocking: has the phase of the given parity completed?
+__device__ __forceinline__ bool bar_test(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t"
+      "}"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
 // Bounded wait for the phase of the given parity: false when it did not
 // complete within the limit (the caller records an error and stops issuing).
 constexpr int kWaitLimit = 1 << 22;

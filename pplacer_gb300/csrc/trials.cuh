@@ -55,6 +55,8 @@ struct TrialCtx {
   const int *qlen;
   const uint8_t *site_cat;
   const float *X, *W, *Lt, *lvf, *statd, *lam, *rates;
+  const float *Xit;           // X^-T (K x K): the tensor-core kernel's P(t) = I + X diag(.) Xit^T
+  int *tc_err;                // [16]: [0] set when a tensor-core completion wait timed out, then where
   double log_nrates;
   double start_pend, max_pend;
   int optimizer, mode;

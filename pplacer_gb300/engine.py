@@ -182,7 +182,8 @@ class Engine:
         return list(th), list(wi)
 
     def set_tuning(self, threads, smem_windows):
-        """Impose the trial-kernel shape per query-length bin (threads 32 = one warp per trial)."""
+        """Impose the trial-kernel shape per query-length bin (threads 32 = one
+        warp per trial, 1 = the tensor-core CTA of 20-state models)."""
         th = np.ascontiguousarray(np.broadcast_to(threads, 6), dtype=np.int32)
         wi = np.ascontiguousarray(np.broadcast_to(smem_windows, 6), dtype=np.int32)
         _L.check(_L.load().pgb_engine_set_tuning(self.h, th.ctypes.data, wi.ctypes.data), "pgb_engine_set_tuning")

@@ -1,0 +1,74 @@
+"""20-state Gamma-mixture trials against the FP64 oracle, in both kernel
+forms: the tensor-core CTA (tcgen05 3xTF32 evolves, tuning code 1) and the
+CUDA-core CTA (256 threads, windows in shared memory).  Queries up to 300
+sites span three 128-site MMA tiles; some carry ambiguity characters.
+
+Tolerances as in test_gpu_engine: fixed-point logL 2e-7 relative, optimised
+logL 1e-6 relative, best edge identical for non-tied queries."""
+import math
+
+import numpy as np
+import pytest
+
+from test_gpu_engine import _compare_placements
+
+pytestmark = pytest.mark.gpu
+
+FORMS = {"tc": (1, 0), "cta": (256, 1)}
+
+
+@pytest.fixture(scope="module")
+def protein(oracle_lib):
+    from pplacer_gb300 import synth
+    w = synth.make_workload("aa_500", n_queries=40, taxa=60, sites=300, lo=40, hi=300)
+    seqs = list(w.query_seqs)
+    # ambiguity characters (B, Z, X) in every fifth query
+    for q in range(0, len(seqs), 5):
+        s = list(seqs[q])
+        idx = [i for i, c in enumerate(s) if c not in "-?"]
+        for k, i in enumerate(idx[::9]):
+            s[i] = "BZX"[k % 3]
+        seqs[q] = "".join(s)
+    w.query_seqs = seqs
+    O = oracle_lib
+    oref = O.Reference(O.Model(w.exch, w.statd, w.rates), w.parent, w.bl, w.leaf_row, w.ref_seqs)
+    return w, oref
+
+
+@pytest.mark.parametrize("form", sorted(FORMS))
+def test_protein_loglike_and_derivatives(protein, form):
+    from pplacer_gb300 import engine as E
+    w, oref = protein
+    eng = E.engine_for_workload(w)
+    eng.set_tuning(*FORMS[form])
+    eng.load_queries(w.query_seqs)
+    rng = np.random.default_rng(7)
+    edges = np.where(w.parent >= 0)[0]
+    trials = []
+    for _ in range(40):
+        q = int(rng.integers(len(w.query_seqs)))
+        e = int(rng.choice(edges))
+        trials.append((q, e, float(rng.uniform(1e-8, 0.5)), float(rng.uniform(0, w.bl[e])), 0.01))
+    got = eng.trials(trials, optimizer=E.NEWTON, mode=1)
+    for (q, e, p, d, _), g in zip(trials, got):
+        st, ref = oref.loglike_derivs(w.query_seqs[q], e, p, d)
+        assert st == 0
+        assert abs(g["like"] - ref[0]) <= 2e-7 * abs(ref[0]), (q, e, g["like"], ref[0])
+        hscale = math.sqrt(abs(ref[3] * ref[4])) + 1.0
+        for k, (gv, rv) in enumerate(zip(g["derivs"][:5], ref[1:6])):
+            tol = 2e-3 * abs(rv) + (1e-5 * abs(ref[3 + k]) + 1e-2 if k < 2 else 1e-3 * hscale + 1.0)
+            assert abs(gv - rv) <= tol, (k, gv, rv)
+
+
+@pytest.mark.parametrize("form", sorted(FORMS))
+def test_protein_placements(protein, oracle_lib, form):
+    from pplacer_gb300 import engine as E
+    O = oracle_lib
+    w, oref = protein
+    ores, ost = oref.place(w.query_seqs, O.make_prefs(), n_threads=8)
+    eng = E.engine_for_workload(w)
+    eng.set_tuning(*FORMS[form])
+    assert list(eng.get_tuning()[0]) == [FORMS[form][0]] * 6
+    gres, gst = eng.place(w.query_seqs, E.default_prefs(optimizer=1))
+    assert list(gst) == list(ost)
+    _compare_placements(O, oref, w.query_seqs, gres, ores)

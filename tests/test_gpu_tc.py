@@ -1,6 +1,8 @@
 """Tensor-core (tcgen05) evolve of the 20-state trial kernel: 128-site tiles,
-operands split into TF32 hi + lo, three products accumulated in FP32.
-Checked against FP64 products with an FP32-order error bound."""
+operands split into TF32 hi + lo, three products accumulated in FP32, two
+barrier phases into two TMEM column ranges per tile (the largest case puts
+several tiles on each SM).  Checked against FP64 products with an
+FP32-order error bound."""
 import numpy as np
 import pytest
 
@@ -9,7 +11,7 @@ from pplacer_gb300 import lib as L
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("n,K,N", [(1, 20, 60), (128, 20, 60), (300, 20, 20), (257, 4, 12), (130, 24, 64),
-                                   (1000, 20, 32)])
+                                   (1000, 20, 32), (152 * 4 * 128 + 5, 20, 60)])
 def test_tc_evolve_matches_fp64(n, K, N):
     lib = L.load()
     rng = np.random.default_rng(n * 100 + K)
