@@ -963,6 +963,10 @@ struct pgb_engine {
   int *d_edge_nodes = nullptr, *d_parent = nullptr, *d_ch_start = nullptr, *d_ch_list = nullptr;
   // GLVs
   float *d_darr = nullptr, *d_parr = nullptr, *d_snode = nullptr;
+  // darr / parr in the eigenbasis of the rate matrix (rows X^-1 v), for the
+  // tensor-core trial kernel; built on first use after the GLVs change
+  float *d_darr_e = nullptr, *d_parr_e = nullptr;
+  bool eig_ready = false;
   int *d_dexp = nullptr, *d_pexp = nullptr, *d_sexp = nullptr;
   bool glvs_ready = false;
   // stage 1: edge tables (bf16 GEMM operands), query operands, GEMM outputs
@@ -1212,6 +1216,7 @@ TrialCtx trial_ctx(pgb_engine *e, const pgb_prefs *p, int optimizer, int mode) {
   c.statd = e->d_mf + e->off_statd; c.lam = e->d_mf + e->off_lam; c.rates = e->d_mf + e->off_rates;
   c.Xit = e->d_mf + e->off_Xit;
   c.tc_err = e->d_tc_err;
+  c.darr_e = e->d_darr_e; c.parr_e = e->d_parr_e;
   c.log_nrates = e->gcat ? 0.0 : log((double)(float)e->NM);
   c.start_pend = p->start_pend;
   c.max_pend = p->max_pend;
@@ -1273,14 +1278,29 @@ pgb_status launch_trials_warp(pgb_engine *e, cudaStream_t st, TrialCtx c, const 
   }
 }
 
-// the tensor-core trial kernel covers 20-state Gamma mixtures
-bool tc_trials_ok(const pgb_engine *e) { return e->K == kTcK && !e->gcat && e->NM == e->RP; }
+// the tensor-core trial kernel covers 20-state Gamma mixtures of up to 4 rates
+bool tc_trials_ok(const pgb_engine *e) { return e->K == kTcK && !e->gcat && e->NM == e->RP && e->RP <= kTcMaxRates; }
+
+pgb_status ensure_eigen_glvs(pgb_engine *e) {
+  if (e->eig_ready || !tc_trials_ok(e)) return PGB_OK;
+  const long rows = (long)e->n_nodes * e->S * e->RP;
+  pgb_status s;
+  if (!e->d_darr_e && ((s = dalloc(&e->d_darr_e, (size_t)rows * e->K)) || (s = dalloc(&e->d_parr_e, (size_t)rows * e->K))))
+    return s;
+  k_eigen_glvs<<<grid_for(2 * rows), 256, 0, e->st>>>(e->d_darr, e->d_parr, e->d_Xitd, rows, e->d_darr_e, e->d_parr_e);
+  PGB_LAUNCH_CHECK();
+  e->eig_ready = true;
+  return PGB_OK;
+}
 
 pgb_status launch_trials_tc(pgb_engine *e, cudaStream_t st, TrialCtx c, const int *d_order, int n, int cap,
                             TrialRes *out) {
   c.smem_win = 0;
   c.cap = std::max(cap, 1);
-  size_t smem = tc_trial_smem_bytes(c.cap, e->NM, e->ncode);
+  c.zcodes = e->prim;
+  for (int a : e->h_qamb)
+    if (a > 0) { c.zcodes = e->ncode; break; }
+  size_t smem = tc_trial_smem_bytes(c.cap, e->NM, e->ncode, c.zcodes);
   if (smem > e->smem_optin) { set_error("tensor-core trial shared memory %zu exceeds %zu", smem, e->smem_optin); return PGB_ERR_ARG; }
   PGB_CUDA(cudaFuncSetAttribute(k_trials_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   k_trials_tc<<<n, kTcThreads, smem, st>>>(c, e->d_trials, d_order, n, out);
@@ -1710,7 +1730,7 @@ pgb_status pgb_engine_destroy(pgb_engine *e) {
                   e->d_amb_list, e->d_seqs, e->d_qcode, e->d_mcode, e->d_reind, e->d_rcode, e->d_qlen,
                   e->d_qstatus, e->d_scores, e->d_rank, e->d_bb, e->d_res, e->d_tbase, e->d_tcount, e->d_keep_idx, e->d_keep_n,
                   e->d_trials, e->d_tres, e->d_bin_list, e->d_small, e->d_out, e->d_nout, e->d_stats,
-                  e->d_qorder, e->d_gl, e->d_prior_mu};
+                  e->d_qorder, e->d_gl, e->d_prior_mu, e->d_darr_e, e->d_parr_e, e->d_tc_err};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   for (int i = 0; i < 8; i++)
@@ -1840,6 +1860,7 @@ pgb_status pgb_engine_precompute(pgb_engine *e, const int *leaf_row, const char 
   cleanup();
   if (ce != cudaSuccess) { set_error("precompute: %s", cudaGetErrorString(ce)); return PGB_ERR_CUDA; }
   e->glvs_ready = true;
+  e->eig_ready = false;
   return PGB_OK;
 }
 
@@ -1906,6 +1927,7 @@ pgb_status pgb_engine_refine_categories(pgb_engine *e, const int *leaf_row, cons
   PGB_CUDA(cudaMemcpyAsync(e->d_site_cat, sc.data(), S, cudaMemcpyHostToDevice, e->st));
   PGB_CUDA(cudaStreamSynchronize(e->st));
   e->glvs_ready = false;  // the placement GLVs follow the categories: precompute again
+  e->eig_ready = false;
   e->lt_pend = -1;
   if (categories) std::copy(best.begin(), best.end(), categories);
   return PGB_OK;
@@ -1948,6 +1970,7 @@ pgb_status pgb_engine_set_glvs(pgb_engine *e, const double *darr, const int *dar
   cudaFree(dd); cudaFree(dp); cudaFree(ed); cudaFree(ep);
   if (ce != cudaSuccess) { set_error("set_glvs: %s", cudaGetErrorString(ce)); return PGB_ERR_CUDA; }
   e->glvs_ready = true;
+  e->eig_ready = false;
   return PGB_OK;
 }
 
@@ -2061,6 +2084,7 @@ pgb_status pgb_queries_run(pgb_engine *e, const pgb_prefs *p) {
   bin_limits(e, lim);
   int h_small[2 + 2 * kBins] = {0};
   for (int b = 0; b < kBins; b++) h_small[2 + kBins + b] = lim[b];
+  if ((s = ensure_eigen_glvs(e))) return s;
   TrialCtx tc = trial_ctx(e, p, p->optimizer, 0);
   int n = e->Q;
   bool whole_query = warp_trials_ok(e);
@@ -2188,6 +2212,7 @@ pgb_status pgb_engine_autotune(pgb_engine *e, const pgb_prefs *p) {
   int got[2 + kBins];
   PGB_CUDA(cudaMemcpyAsync(got, e->d_small, sizeof(got), cudaMemcpyDeviceToHost, e->st));
   PGB_CUDA(cudaStreamSynchronize(e->st));
+  if ((s = ensure_eigen_glvs(e))) return s;
   TrialCtx tc = trial_ctx(e, p, p->optimizer, 0);
   tc.stats = nullptr;
   const int cand_threads[4] = {32, kTuneTc, 256, 128};
@@ -2354,6 +2379,7 @@ pgb_status pgb_queries_trials(pgb_engine *e, const pgb_prefs *p, int optimizer, 
       PGB_CUDA(cudaMemcpyAsync(e->d_bin_list + (size_t)b * e->trials_cap, bins[b].data(), counts[b] * 4,
                                cudaMemcpyHostToDevice, e->st));
   }
+  if ((s = ensure_eigen_glvs(e))) return s;
   TrialCtx tc = trial_ctx(e, p, optimizer, mode);
   if ((s = run_bins(e, tc, counts, max_sq))) return s;
   std::vector<TrialRes> res(n_trials);

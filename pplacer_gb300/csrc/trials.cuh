@@ -57,6 +57,8 @@ struct TrialCtx {
   const float *X, *W, *Lt, *lvf, *statd, *lam, *rates;
   const float *Xit;           // X^-T (K x K): the tensor-core kernel's P(t) = I + X diag(.) Xit^T
   int *tc_err;                // [16]: [0] set when a tensor-core completion wait timed out, then where
+  const float *darr_e, *parr_e;  // darr / parr rows times X^-1 (the tensor-core kernel's operands)
+  int zcodes;                 // character codes of the tensor-core kernel's query tables
   double log_nrates;
   double start_pend, max_pend;
   int optimizer, mode;

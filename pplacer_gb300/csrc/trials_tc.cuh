@@ -5,15 +5,26 @@
 // MMAs.  Included by engine.cu inside its anonymous namespace, after
 // trials.cuh.
 //
+// The operands are the GLVs in the eigenbasis of the rate matrix: with
+// P(t) = X diag(exp(r lambda t)) X^-1, the evolved distal vector is
+// P(t) D = X diag(e) (X^-1 D), and its t-derivatives put r lambda (or its
+// square) beside e.  The A tiles are the rows X^-1 D (darr_e / parr_e, built
+// once per tree), the B tiles the rows of X scaled by those factors, so a
+// new branch length costs one cheap B-tile rewrite per rate instead of
+// re-forming P.
+//
 // One evaluation at (pend, dist):
 //   thread 0: optimiser -> next point                      | barrier
 //   all: exp factors of the three lengths                  | barrier
+//   query tables: the statd-weighted evolved query vectors of every
+//        character code (and d/dpend, d2/dpend2) for every rate, one MMA group
+//        per 128 rows (X rows scaled by the pendant factors) x Lt (the codes'
+//        vectors in the eigenbasis)                         | barriers
 //   per rate r:
-//     all: B tiles of rate r -- the rows of P, dP, d2P at dist (distal) and
-//          at cut - dist (proximal), TF32 hi / lo -- and the statd-weighted
-//          query vectors per character (and d/dpend, d2/dpend2)   | barrier
+//     all: B tiles of rate r -- X rows scaled by e, r lambda e, (r lambda)^2 e
+//          at dist (distal) and cut - dist (proximal), TF32 hi / lo
 //     per chunk of 128 sites:
-//       all: the chunk's darr / parr rows (loaded during the previous
+//       all: the chunk's darr_e / parr_e rows (loaded during the previous
 //            chunk's MMAs) split into TF32 hi / lo A tiles         | barrier
 //       thread 0: 2 x 9 MMAs (3 K steps x 3 products) into TMEM columns
 //                 [0, 64) (distal) and [64, 128) (proximal); commit
@@ -33,15 +44,17 @@ constexpr int kTcNVal = 32;     // B rows of a value-only evaluation: P (20) + 1
 constexpr int kTcCols = 128;    // TMEM columns per CTA: distal [0, 64), proximal [64, 128)
 constexpr int kTcXs = kTcK + 1;  // padded row stride of X and Xit (bank spread)
 constexpr int kTcZs = kTcK + 1;  // padded row stride of the query-vector tables
+constexpr int kTcMaxRates = 4;   // query-table rows 3 x 4 x 20 fit two 128-row MMA tiles
+static_assert(pgb::kMaxCodes <= 32, "the query-vector table GEMM has N = 32 codes");
 
 struct TcSmem {
   float *a_dh, *a_dl, *a_xh, *a_xl;  // A tiles [128 x 24]: distal / proximal rows, hi / lo
   float *b_dh, *b_dl, *b_xh, *b_xl;  // B tiles [64 x 24]
   float *acc;                         // [6][cap] per-site sums over rates
-  float *Z, *Z1, *Z2;                 // [ncode][kTcZs] of the current rate
-  float *X, *Xit;                     // [K][kTcXs]
+  float *Z;                           // [3][NM][zcodes][kTcZs]: query vectors and d/dpend, d2/dpend2
+  float *X;                           // [K][kTcXs]
   float *E, *Em1, *Lr;                // [3][NM][K], [3][NM][K], [NM][K]
-  float *Lt, *lv, *statd;
+  float *lv, *statd;
   float *red;                         // [4][8]
   int *redi;                          // [4]
   uint16_t *col;                      // [cap] alignment columns of the query's sites
@@ -52,21 +65,23 @@ struct TcSmem {
   uint32_t *tbase;
 };
 
-__host__ __device__ inline size_t tc_trial_smem_bytes(int cap, int NM, int ncode) {
+// zcodes: the character codes the query tables hold (the primary states,
+// or every code when a query has ambiguity characters)
+__host__ __device__ inline size_t tc_trial_smem_bytes(int cap, int NM, int ncode, int zcodes) {
   const int K = kTcK;
   size_t b = 4 * align16((size_t)pgb::tc::kTileFloats * 4) + 4 * align16((size_t)kTcNDer * pgb::tc::kKPad * 4);
   b += align16((size_t)6 * cap * 4);
-  b += 3 * align16((size_t)ncode * kTcZs * 4);
-  b += 2 * align16((size_t)K * kTcXs * 4);
+  b += align16((size_t)3 * NM * zcodes * kTcZs * 4);
+  b += align16((size_t)K * kTcXs * 4);
   b += 2 * align16((size_t)3 * NM * K * 4) + align16((size_t)NM * K * 4);
-  b += 2 * align16((size_t)ncode * K * 4) + align16((size_t)K * 4);
+  b += align16((size_t)ncode * K * 4) + align16((size_t)K * 4);
   b += align16(4 * 8 * 4) + align16(4 * 4);
   b += align16((size_t)cap * 2) + align16((size_t)cap);
   b += align16(sizeof(Ctrl)) + align16(sizeof(Optimiser)) + 16 + 16;
   return b + 1024;  // base alignment of the operand tiles
 }
 
-__device__ inline TcSmem tc_carve(char *base, int cap, int NM, int ncode) {
+__device__ inline TcSmem tc_carve(char *base, int cap, int NM, int ncode, int zcodes) {
   const int K = kTcK;
   TcSmem s;
   char *p = (char *)(((uintptr_t)base + 1023) & ~(uintptr_t)1023);
@@ -75,14 +90,11 @@ __device__ inline TcSmem tc_carve(char *base, int cap, int NM, int ncode) {
   s.a_dh = (float *)take(at); s.a_dl = (float *)take(at); s.a_xh = (float *)take(at); s.a_xl = (float *)take(at);
   s.b_dh = (float *)take(bt); s.b_dl = (float *)take(bt); s.b_xh = (float *)take(bt); s.b_xl = (float *)take(bt);
   s.acc = (float *)take((size_t)6 * cap * 4);
-  const size_t zb = (size_t)ncode * kTcZs * 4;
-  s.Z = (float *)take(zb); s.Z1 = (float *)take(zb); s.Z2 = (float *)take(zb);
+  s.Z = (float *)take((size_t)3 * NM * zcodes * kTcZs * 4);
   s.X = (float *)take((size_t)K * kTcXs * 4);
-  s.Xit = (float *)take((size_t)K * kTcXs * 4);
   s.E = (float *)take((size_t)3 * NM * K * 4);
   s.Em1 = (float *)take((size_t)3 * NM * K * 4);
   s.Lr = (float *)take((size_t)NM * K * 4);
-  s.Lt = (float *)take((size_t)ncode * K * 4);
   s.lv = (float *)take((size_t)ncode * K * 4);
   s.statd = (float *)take((size_t)K * 4);
   s.red = (float *)take(4 * 8 * 4);
@@ -96,68 +108,129 @@ __device__ inline TcSmem tc_carve(char *base, int cap, int NM, int ncode) {
   return s;
 }
 
-// B tiles of rate r: row m * 20 + i, column j = (d^m/dt^m P(t))[i][j] at
-// t = dist (distal tiles) and t = cut - dist (proximal tiles), from
-// P = I + X diag(expm1(r lambda t)) X^-1 and its derivatives; plus the
-// statd-weighted evolved query vectors of codes 0 .. ncz - 1 at pend.
+// float4 of row `row`, columns k .. k + 3, as TF32 hi / lo into two tiles
+__device__ __forceinline__ void tc_store_split(float *hi, float *lo, int row, int k, float4 v) {
+  float4 h, l;
+  pgb::tc::split_tf32(v.x, h.x, l.x);
+  pgb::tc::split_tf32(v.y, h.y, l.y);
+  pgb::tc::split_tf32(v.z, h.z, l.z);
+  pgb::tc::split_tf32(v.w, h.w, l.w);
+  *reinterpret_cast<float4 *>(hi + pgb::tc::off(row, k)) = h;
+  *reinterpret_cast<float4 *>(lo + pgb::tc::off(row, k)) = l;
+}
+
+// Query tables of every rate on the tensor cores: rows rho = (m * NM + r) *
+// 20 + i (m = 0: value, 1, 2: d/dpend, d2/dpend2) of A = X[i][.] * f(.), f
+// = expm1(r lambda pend), r lambda e, (r lambda)^2 e; times Lt^T (the codes'
+// likelihood vectors in the eigenbasis, written into the distal B tiles,
+// which are free until the rate's B tiles) gives sum_k X[i][k] f_k Lt[code][k],
+// so that Z = statd_i * (lv[code][i] + that) for m = 0 (P = I + X diag(expm1)
+// X^-1) and statd_i * that for the derivatives.  Rows 0..127 go through
+// (a_dh, a_dl) into TMEM columns [0, 32), rows 128.. through (a_xh, a_xl)
+// into [32, 64).  Returns false when the completion wait timed out.
 template <bool DER>
-__device__ __forceinline__ void tc_rate_tables(const TcSmem &sm, int NM, int r, int ncz, int tid) {
+__device__ __forceinline__ bool tc_query_tables(const TrialCtx &c, const TcSmem &sm, uint32_t tmem, int NM, int ncz,
+                                                int nc, int zc, int tid, uint32_t &phase) {
+  namespace T = pgb::tc;
   const int K = kTcK;
-  for (int it = tid; it < 2 * K * K; it += kTcThreads) {
-    const int g = it / (K * K), ij = it - g * K * K;
-    const int i = ij / K, j = ij - i * K;
-    const float *xi = sm.X + i * kTcXs, *xj = sm.Xit + j * kTcXs;
-    const float *em = sm.Em1 + (g * NM + r) * K;
-    const float *e = sm.E + (g * NM + r) * K;
-    const float *lr = sm.Lr + r * K;
-    float a = i == j ? 1.f : 0.f, a1 = 0.f, a2 = 0.f;
-#pragma unroll 5
-    for (int k = 0; k < K; k++) {
-      const float w = xi[k] * xj[k];
-      a = fmaf(w, em[k], a);
-      if (DER) {
-        const float t1 = w * lr[k] * e[k];
-        a1 += t1;
-        a2 = fmaf(t1, lr[k], a2);
+  const int rows = (DER ? 3 : 1) * NM * K;  // <= 240
+  // B: the rows of Lt (codes), zero past the codes (rows 32..63 unused)
+  for (int it = tid; it < 32 * (K / 4); it += kTcThreads) {
+    const int row = it / (K / 4), k = (it - row * (K / 4)) * 4;
+    const float4 v = row < nc ? *reinterpret_cast<const float4 *>(c.Lt + row * K + k) : make_float4(0.f, 0.f, 0.f, 0.f);
+    tc_store_split(sm.b_dh, sm.b_dl, row, k, v);
+  }
+#pragma unroll
+  for (int h = 0; h < 2; h++) {
+    const int rho = tid + h * T::kTileRows;
+    if (rho < rows) {
+      const int m = rho / (NM * K), r = (rho / K) % NM, i = rho % K;
+      const float *x = sm.X + i * kTcXs, *lr = sm.Lr + r * K;
+      const float *em = sm.Em1 + (2 * NM + r) * K, *e = sm.E + (2 * NM + r) * K;
+#pragma unroll
+      for (int k = 0; k < K; k += 4) {
+        float v[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++)
+          v[j] = x[k + j] * (m == 0 ? em[k + j] : (m == 1 ? lr[k + j] : lr[k + j] * lr[k + j]) * e[k + j]);
+        tc_store_split(h == 0 ? sm.a_dh : sm.a_xh, h == 0 ? sm.a_dl : sm.a_xl, tid, k,
+                       make_float4(v[0], v[1], v[2], v[3]));
       }
-    }
-    float *bh = g == 0 ? sm.b_dh : sm.b_xh, *bl = g == 0 ? sm.b_dl : sm.b_xl;
-    float h, l;
-    pgb::tc::split_tf32(a, h, l);
-    bh[pgb::tc::off(i, j)] = h;
-    bl[pgb::tc::off(i, j)] = l;
-    if (DER) {
-      pgb::tc::split_tf32(a1, h, l);
-      bh[pgb::tc::off(K + i, j)] = h;
-      bl[pgb::tc::off(K + i, j)] = l;
-      pgb::tc::split_tf32(a2, h, l);
-      bh[pgb::tc::off(2 * K + i, j)] = h;
-      bl[pgb::tc::off(2 * K + i, j)] = l;
     }
   }
-  for (int it = tid; it < ncz * K; it += kTcThreads) {
-    const int code = it / K, i = it - code * K;
-    const float *x = sm.X + i * kTcXs;
-    const float *lt = sm.Lt + code * K;
-    const float *em = sm.Em1 + (2 * NM + r) * K;
-    const float *e = sm.E + (2 * NM + r) * K;
-    const float *lr = sm.Lr + r * K;
-    float a = sm.lv[code * K + i], a1 = 0.f, a2 = 0.f;
-#pragma unroll 5
-    for (int k = 0; k < K; k++) {
-      a = fmaf(x[k] * em[k], lt[k], a);
-      if (DER) {
-        const float t1 = x[k] * lr[k] * e[k] * lt[k];
-        a1 += t1;
-        a2 = fmaf(t1, lr[k], a2);
-      }
+  T::fence_async_smem();
+  __syncthreads();
+  if (tid == 0) {
+    T::fence_after();
+    const uint32_t id = T::idesc_tf32(T::kTileRows, 32);
+    T::mma_3xtf32(tmem, T::smem_addr(sm.a_dh), T::smem_addr(sm.a_dl), T::smem_addr(sm.b_dh), T::smem_addr(sm.b_dl),
+                  id);
+    if (rows > T::kTileRows)
+      T::mma_3xtf32(tmem + 32, T::smem_addr(sm.a_xh), T::smem_addr(sm.a_xl), T::smem_addr(sm.b_dh),
+                    T::smem_addr(sm.b_dl), id);
+    T::commit(sm.bar);
+  }
+  const bool mine = T::bar_wait(sm.bar, phase);
+  const bool ok = __syncthreads_and(mine ? 1 : 0) != 0;
+  if (!ok && tid == 0 && c.tc_err && atomicCAS(c.tc_err, 0, 1) == 0) {
+    int *d = c.tc_err;
+    d[1] = blockIdx.x; d[2] = -1; d[3] = -1; d[4] = (int)phase; d[5] = mine;
+    d[6] = T::bar_test(sm.bar, phase); d[7] = T::bar_test(sm.bar, phase ^ 1u);
+    d[8] = (int)tmem; d[9] = (int)T::smem_addr(sm.a_dh); d[10] = (int)T::smem_addr(sm.bar);
+    __threadfence();
+  }
+  phase ^= 1u;
+  T::fence_after();
+  if (!ok) return false;
+  const uint32_t ta = tmem + ((uint32_t)(32 * (tid >> 5)) << 16);
+#pragma unroll
+  for (int h = 0; h < 2; h++) {
+    const int rho = tid + h * T::kTileRows;
+    if (h == 1 && rows <= T::kTileRows) break;  // uniform
+    float zv[32];
+    {
+      float t16[16];
+      T::ld16(ta + 32 * h, t16);
+#pragma unroll
+      for (int j = 0; j < 16; j++) zv[j] = t16[j];
+      T::ld16(ta + 32 * h + 16, t16);
+#pragma unroll
+      for (int j = 0; j < 16; j++) zv[16 + j] = t16[j];
     }
-    const float pi = sm.statd[i];
-    sm.Z[code * kTcZs + i] = pi * a;
-    if (DER) {
-      sm.Z1[code * kTcZs + i] = pi * a1;
-      sm.Z2[code * kTcZs + i] = pi * a2;
+    T::ld_wait();
+    T::pin(zv);
+    if (rho < rows) {
+      const int m = rho / (NM * K), i = rho % K;
+      const float pi = sm.statd[i];
+      float *z = sm.Z + (size_t)(rho / K) * zc * kTcZs + i;  // table (m, r), column i
+#pragma unroll
+      for (int code = 0; code < 32; code++)
+        if (code < ncz) z[code * kTcZs] = pi * (m == 0 ? zv[code] + sm.lv[code * K + i] : zv[code]);
     }
+  }
+  T::fence_before();  // the next barrier orders these TMEM reads before the chunk MMAs
+  return true;
+}
+
+// B tiles of rate r: row m * 20 + i, column k = X[i][k] * (r lambda_k)^m *
+// exp(r lambda_k t) at t = dist (distal tiles) and t = cut - dist (proximal
+// tiles).  The previous MMAs have completed (their wait and barrier).
+template <bool DER>
+__device__ __forceinline__ void tc_btiles(const TcSmem &sm, int NM, int r, int tid) {
+  const int K = kTcK;
+  const int nrow = DER ? 3 * K : K;
+  for (int it = tid; it < 2 * nrow * (K / 4); it += kTcThreads) {
+    const int g = it / (nrow * (K / 4)), rem = it - g * nrow * (K / 4);
+    const int n = rem / (K / 4), k = (rem - n * (K / 4)) * 4;
+    const int m = n / K, i = n - m * K;
+    const float *x = sm.X + i * kTcXs, *lr = sm.Lr + r * K, *e = sm.E + (g * NM + r) * K;
+    float v[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      const float f = m == 0 ? 1.f : (m == 1 ? lr[k + j] : lr[k + j] * lr[k + j]);
+      v[j] = x[k + j] * f * e[k + j];
+    }
+    tc_store_split(g == 0 ? sm.b_dh : sm.b_xh, g == 0 ? sm.b_dl : sm.b_xl, n, k, make_float4(v[0], v[1], v[2], v[3]));
   }
 }
 
@@ -171,23 +244,14 @@ __device__ __forceinline__ void tc_load_rows(const TrialCtx &c, const TcSmem &sm
   const int i = ch * pgb::tc::kTileRows + tid;
   if (i < Sq) {
     const long o = (((long)node * c.S + sm.col[i]) * c.RP + r) * kTcK;
-    const float4 *dp = reinterpret_cast<const float4 *>(c.darr + o);
-    const float4 *xp = reinterpret_cast<const float4 *>(c.parr + o);
+    const float4 *dp = reinterpret_cast<const float4 *>(c.darr_e + o);
+    const float4 *xp = reinterpret_cast<const float4 *>(c.parr_e + o);
 #pragma unroll
     for (int k = 0; k < 5; k++) { rw.d[k] = __ldg(dp + k); rw.x[k] = __ldg(xp + k); }
   } else {
 #pragma unroll
     for (int k = 0; k < 5; k++) rw.d[k] = rw.x[k] = make_float4(0.f, 0.f, 0.f, 0.f);
   }
-}
-__device__ __forceinline__ void tc_store_split(float *hi, float *lo, int row, int k, float4 v) {
-  float4 h, l;
-  pgb::tc::split_tf32(v.x, h.x, l.x);
-  pgb::tc::split_tf32(v.y, h.y, l.y);
-  pgb::tc::split_tf32(v.z, h.z, l.z);
-  pgb::tc::split_tf32(v.w, h.w, l.w);
-  *reinterpret_cast<float4 *>(hi + pgb::tc::off(row, k)) = h;
-  *reinterpret_cast<float4 *>(lo + pgb::tc::off(row, k)) = l;
 }
 
 // One rate of one chunk: MMAs, then the epilogue adds the rate's site
@@ -240,7 +304,8 @@ __device__ __forceinline__ bool tc_chunk(const TrialCtx &c, const TcSmem &sm, ui
   const uint32_t ta = tmem + ((uint32_t)(32 * w) << 16);
   const int i = ch * T::kTileRows + tid;
   const int code = i < Sq ? sm.code[i] : 0;
-  const float *z = sm.Z + code * kTcZs;
+  const int NM = c.NM, zc = c.zcodes;
+  const float *z = sm.Z + ((size_t)r * zc + code) * kTcZs;
   float u = 0.f, ud = 0.f, udd = 0.f, up = 0.f, upp = 0.f, upd = 0.f;
   if (DER) {
     float dv[64], xv[64];
@@ -257,7 +322,7 @@ __device__ __forceinline__ bool tc_chunk(const TrialCtx &c, const TcSmem &sm, ui
     T::ld_wait();
     T::pin(dv);
     T::pin(xv);
-    const float *z1 = sm.Z1 + code * kTcZs, *z2 = sm.Z2 + code * kTcZs;
+    const float *z1 = z + (size_t)NM * zc * kTcZs, *z2 = z1 + (size_t)NM * zc * kTcZs;
 #pragma unroll
     for (int ii = 0; ii < K; ii++) {
       const float x = dv[ii], x1 = dv[K + ii], x2 = dv[2 * K + ii];
@@ -306,6 +371,27 @@ __device__ __forceinline__ bool tc_chunk(const TrialCtx &c, const TcSmem &sm, ui
   return true;
 }
 
+// rows (node, site, rate) of darr and parr times X^-1 (FP64 accumulation)
+__global__ void k_eigen_glvs(const float *__restrict__ darr, const float *__restrict__ parr,
+                             const double *__restrict__ Xit, long rows, float *darr_e, float *parr_e) {
+  constexpr int K = kTcK;
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < 2 * rows; t += (long)gridDim.x * blockDim.x) {
+    const bool prox = t >= rows;
+    const long row = prox ? t - rows : t;
+    const float *v = (prox ? parr : darr) + row * K;
+    float *o = (prox ? parr_e : darr_e) + row * K;
+    float x[K];
+#pragma unroll
+    for (int j = 0; j < K; j++) x[j] = v[j];
+    for (int k = 0; k < K; k++) {
+      double a = 0.0;
+#pragma unroll
+      for (int j = 0; j < K; j++) a += Xit[j * K + k] * (double)x[j];  // (X^-1)[k][j] = Xit[j][k]
+      o[k] = (float)a;
+    }
+  }
+}
+
 __global__ void __launch_bounds__(kTcThreads, 1) k_trials_tc(TrialCtx c, const TrialIn *__restrict__ trials,
                                                              const int *__restrict__ order, int n, TrialRes *out) {
   namespace T = pgb::tc;
@@ -316,7 +402,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_trials_tc(TrialCtx c, const T
   const TrialIn tr = trials[ti];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int NM = c.NM, nc = c.ncode, cap = c.cap;
-  const TcSmem sm = tc_carve(t_smem, cap, NM, nc);
+  const int zc = c.zcodes;
+  const TcSmem sm = tc_carve(t_smem, cap, NM, nc, zc);
   const int q = tr.q, node = tr.node;
   const int Sq = c.qlen[q];
   const int ncz = c.qamb[q] > 0 ? nc : c.prim;
@@ -325,9 +412,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_trials_tc(TrialCtx c, const T
   for (int it = tid; it < K * K; it += kTcThreads) {
     const int i = it / K, k = it - i * K;
     sm.X[i * kTcXs + k] = c.X[it];
-    sm.Xit[i * kTcXs + k] = c.Xit[it];
   }
-  for (int it = tid; it < nc * K; it += kTcThreads) { sm.Lt[it] = c.Lt[it]; sm.lv[it] = c.lvf[it]; }
+  for (int it = tid; it < nc * K; it += kTcThreads) sm.lv[it] = c.lvf[it];
   for (int it = tid; it < NM * K; it += kTcThreads) sm.Lr[it] = c.rates[it / K] * c.lam[it % K];
   if (tid < K) sm.statd[tid] = c.statd[tid];
   // the padding columns 20..23 of every tile and the rows 60..63 of the B
@@ -404,9 +490,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_trials_tc(TrialCtx c, const T
     __syncthreads();
     TcRows rw;
     if (nch > 0) tc_load_rows(c, sm, node, Sq, 0, 0, tid, rw);
-    for (int r = 0; r < c.RP && !failed; r++) {
-      if (derivs) tc_rate_tables<true>(sm, NM, r, ncz, tid);
-      else tc_rate_tables<false>(sm, NM, r, ncz, tid);
+    if (nch > 0 && !(derivs ? tc_query_tables<true>(c, sm, tmem, NM, ncz, nc, zc, tid, phase)
+                            : tc_query_tables<false>(c, sm, tmem, NM, ncz, nc, zc, tid, phase)))
+      failed = true;
+    for (int r = 0; r < c.RP && nch > 0 && !failed; r++) {
+      if (derivs) tc_btiles<true>(sm, NM, r, tid);
+      else tc_btiles<false>(sm, NM, r, tid);
       // (the barrier at the top of the first chunk publishes the tables)
       for (int ch = 0; ch < nch; ch++) {
         const bool ok = derivs ? tc_chunk<true>(c, sm, tmem, node, Sq, r, ch, nch, cap, tid, phase, rw)
