@@ -137,6 +137,16 @@ class ClockSampler:
         return {"sm_mhz": med, "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def stage2_kernel(w, tune):
+    """The trial kernel that ran stage 2 + refinement for this workload and tuning."""
+    th = set(int(v) for v in tune[0])
+    if w.K == 4 and w.site_cats is None:
+        return "k_place_warp (stage 2 + refinement, whole queries)"
+    if th == {1}:
+        return "k_trials_tc (stage 2 + refinement, tcgen05 evolves)"
+    return "k_trials (stage 2 + refinement, CTA per trial, %s threads)" % "/".join(str(t) for t in sorted(th))
+
+
 def load_peaks():
     try:
         with open(MEASURED_PEAKS) as f:
@@ -361,7 +371,8 @@ def run_ours(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic",
         "config": {"workload": args.workload, "taxa": (w.n_nodes + 1) // 2, "sites": S, "queries": Q,
-                   "model": "GTR+G4" if w.site_cats is None else "GTR+CAT20",
+                   "model": ("GTR+CAT%d" % (int(np.max(w.site_cats)) + 1) if w.site_cats is not None
+                             else ("20-state+G%d" if K == 20 else "GTR+G%d") % len(w.rates)),
                    "optimizer": args.optimizer, "keep_at_most": prefs.keep_at_most,
                    "max_strikes": prefs.max_strikes,
                    "trial_tuning": {"threads": [int(v) for v in tune[0]], "smem_windows": [int(v) for v in tune[1]]},
@@ -375,7 +386,7 @@ def run_ours(args):
                        "refine_trials": counts[6] / args.steps, "rounds": counts[7] / args.steps,
                        "phase_ms": {"stage1_table": phase[1] / args.steps, "stage1_rank": phase[2] / args.steps,
                                     "stage2": phase[3] / args.steps, "refine_out": phase[4] / args.steps}},
-        "roofline": {"kernel": "k_place_warp (stage 2 + refinement)", "bound": "hbm", "achieved": achieved,
+        "roofline": {"kernel": stage2_kernel(w, tune), "bound": "hbm", "achieved": achieved,
                      "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
                      "traffic_unit": "bytes per launch", "algorithmic_bytes_per_site_eval": bytes_per_site_eval,
                      "peak_source": peak_kind,
