@@ -274,9 +274,14 @@ __global__ void k_snodes_from(const double *__restrict__ d, const double *__rest
 // Query preparation: character codes, informative mask, masked site lists
 // (core.ml:267-304).  One CTA per query.
 // ---------------------------------------------------------------------------
+// Columns are visited in the order `order` (null: 0 .. S-1); the CAT models
+// pass the columns grouped by category, so that a query's informative sites
+// come grouped by category and neighbouring trial threads read the same
+// category's matrices (the site order changes only FP32 summation order).
 __global__ void k_query_prep(const char *__restrict__ seqs, int S, int prim, const uint8_t *__restrict__ char_code,
-                             const uint8_t *__restrict__ informative, uint8_t *qcode, uint16_t *reind,
-                             uint8_t *mcode, uint32_t *rcode, int *qlen, int *qstatus, int *qamb) {
+                             const uint8_t *__restrict__ informative, const uint16_t *__restrict__ order,
+                             uint8_t *qcode, uint16_t *reind, uint8_t *mcode, uint32_t *rcode, int *qlen,
+                             int *qstatus, int *qamb) {
   int q = blockIdx.x;
   const char *seq = seqs + (long)q * S;
   __shared__ int s_off;
@@ -288,6 +293,7 @@ __global__ void k_query_prep(const char *__restrict__ seqs, int S, int prim, con
   int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
   for (int base = 0; base < S; base += blockDim.x) {
     int s = base + threadIdx.x;
+    if (order && s < S) s = order[s];
     uint8_t c = kBadCode;
     int inf = 0;
     if (s < S) {
@@ -960,6 +966,7 @@ struct pgb_engine {
   float *d_mf = nullptr;  // X, W, Lt, lvf, statd, lam, rates (float)
   size_t off_X = 0, off_W = 0, off_Lt = 0, off_lv = 0, off_statd = 0, off_lam = 0, off_rates = 0, off_Xit = 0;
   uint8_t *d_site_cat = nullptr, *d_char_code = nullptr, *d_informative = nullptr;
+  uint16_t *d_col_order = nullptr;  // CAT: columns grouped by category (query site order)
   int *d_edge_nodes = nullptr, *d_parent = nullptr, *d_ch_start = nullptr, *d_ch_list = nullptr;
   // GLVs
   float *d_darr = nullptr, *d_parr = nullptr, *d_snode = nullptr;
@@ -1559,6 +1566,23 @@ void pgb_prefs_default(pgb_prefs *p) {
   p->prior_lower = 0.0;
 }
 
+// CAT models: the alignment columns sorted by (category, column) -- the
+// order in which k_query_prep lists a query's sites
+static pgb_status upload_col_order(pgb_engine *e) {
+  if (!e->gcat) return PGB_OK;
+  std::vector<uint16_t> ord(e->S);
+  for (int i = 0; i < e->S; i++) ord[i] = (uint16_t)i;
+  std::stable_sort(ord.begin(), ord.end(), [&](uint16_t a, uint16_t b) { return e->site_cats[a] < e->site_cats[b]; });
+  if (!e->d_col_order) {
+    pgb_status s = dalloc(&e->d_col_order, (size_t)e->S);
+    if (s) return s;
+  }
+  PGB_CUDA(cudaMemcpyAsync(e->d_col_order, ord.data(), (size_t)e->S * sizeof(uint16_t), cudaMemcpyHostToDevice,
+                           e->st));
+  PGB_CUDA(cudaStreamSynchronize(e->st));  // before the host vector goes
+  return PGB_OK;
+}
+
 pgb_status pgb_engine_create(const pgb_model_desc *m, const pgb_tree_desc *t, pgb_engine **out) {
   if (!m || !t || !out) { set_error("engine_create: null argument"); return PGB_ERR_ARG; }
   if ((m->n_states != 4 && m->n_states != 20) || m->n_rates < 1 || m->n_rates > 64 || m->n_sites < 1 ||
@@ -1687,6 +1711,7 @@ pgb_status pgb_engine_create(const pgb_model_desc *m, const pgb_tree_desc *t, pg
       (s = upload(&e->d_lvd, lvd.data(), lvd.size(), e->st)) ||
       (s = upload(&e->d_gl, glr.data(), glr.size(), e->st)) ||
       (s = upload(&e->d_site_cat, scat.data(), scat.size(), e->st)) ||
+      (s = upload_col_order(e)) ||
       (s = upload(&e->d_char_code, cc.data(), cc.size(), e->st)) ||
       (s = upload(&e->d_informative, inf.data(), inf.size(), e->st)) ||
       (s = upload(&e->d_edge_nodes, e->edge_nodes.data(), e->edge_nodes.size(), e->st)) ||
@@ -1730,7 +1755,8 @@ pgb_status pgb_engine_destroy(pgb_engine *e) {
                   e->d_amb_list, e->d_seqs, e->d_qcode, e->d_mcode, e->d_reind, e->d_rcode, e->d_qlen,
                   e->d_qstatus, e->d_scores, e->d_rank, e->d_bb, e->d_res, e->d_tbase, e->d_tcount, e->d_keep_idx, e->d_keep_n,
                   e->d_trials, e->d_tres, e->d_bin_list, e->d_small, e->d_out, e->d_nout, e->d_stats,
-                  e->d_qorder, e->d_gl, e->d_prior_mu, e->d_darr_e, e->d_parr_e, e->d_tc_err};
+                  e->d_qorder, e->d_gl, e->d_prior_mu, e->d_darr_e, e->d_parr_e, e->d_tc_err,
+                  e->d_col_order};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   for (int i = 0; i < 8; i++)
@@ -1925,6 +1951,8 @@ pgb_status pgb_engine_refine_categories(pgb_engine *e, const int *leaf_row, cons
   std::vector<uint8_t> sc(S);
   for (int i = 0; i < S; i++) sc[i] = (uint8_t)best[i];
   PGB_CUDA(cudaMemcpyAsync(e->d_site_cat, sc.data(), S, cudaMemcpyHostToDevice, e->st));
+  pgb_status us = upload_col_order(e);  // queries loaded from now on follow the new grouping
+  if (us) return us;
   PGB_CUDA(cudaStreamSynchronize(e->st));
   e->glvs_ready = false;  // the placement GLVs follow the categories: precompute again
   e->eig_ready = false;
@@ -2001,8 +2029,8 @@ pgb_status pgb_queries_load(pgb_engine *e, int n_queries, const char *seqs) {
   if (!n_queries) return PGB_OK;
   PGB_CUDA(cudaMemcpyAsync(e->d_seqs, seqs, (size_t)n_queries * e->S, cudaMemcpyHostToDevice, e->st));
   k_query_prep<<<n_queries, 256, 0, e->st>>>(e->d_seqs, e->S, e->prim, e->d_char_code, e->d_informative,
-                                             e->d_qcode, e->d_reind, e->d_mcode, e->d_rcode, e->d_qlen,
-                                             e->d_qstatus, e->d_qamb);
+                                             e->gcat ? e->d_col_order : nullptr, e->d_qcode, e->d_reind,
+                                             e->d_mcode, e->d_rcode, e->d_qlen, e->d_qstatus, e->d_qamb);
   PGB_LAUNCH_CHECK();
   e->h_qlen.resize(n_queries);
   PGB_CUDA(cudaMemcpyAsync(e->h_qlen.data(), e->d_qlen, (size_t)n_queries * 4, cudaMemcpyDeviceToHost, e->st));
