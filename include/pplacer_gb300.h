@@ -216,8 +216,9 @@ typedef struct {
   double keep_factor;        /* [0.01] */
   int optimizer;             /* 0: Brent as the reference (minimization.ml:83-101);
                                 1: batched safeguarded Newton on the adjoint */
-  int calc_pp;               /* [0] posterior probabilities (-p, core.ml:378-401); Newton form,
-                                nucleotide Gamma models */
+  int calc_pp;               /* [0] posterior probabilities (-p, core.ml:378-401): one
+                                marginal-likelihood trial per kept location after its
+                                refinement; every model and trial kernel */
   int prior;                 /* [0] pendant prior: 0 exponential with mean = tree length / edges,
                                 1 uniform (--unif-prior), 2 informative exponential
                                 (--inform-prior, core.ml:34-51) */

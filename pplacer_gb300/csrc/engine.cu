@@ -709,8 +709,46 @@ __global__ void k_keep_emit(BBCtx c, int keep_at_most, double log_keep_factor, i
   }
 }
 
+// Posterior probabilities (core.ml:378-401): one marginal-likelihood trial
+// per kept location (Three_tax.calc_marg_prob, three_tax.ml:169-215), around
+// the refined optimum (the stage-2 one where the refinement failed), at trial
+// index off + tbase[q] + j.
+__global__ void k_pp_emit(BBCtx c, int keep_at_most, const int *__restrict__ keep_idx,
+                          const int *__restrict__ keep_n, const TrialRes *__restrict__ tres, int off, int prior_kind,
+                          const double *__restrict__ prior_mu) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= c.Q) return;
+  const int nk = keep_n[q];
+  if (c.qstatus[q] != PGB_Q_OK || nk == 0) return;
+  const ResEntry *r = c.res + (long)q * c.maxr;
+  const int bin = bin_of(c, c.qlen[q]);
+  const int bpos = atomicAdd(&c.bin_count[bin], nk);
+  for (int j = 0; j < nk; j++) {
+    const ResEntry e = r[keep_idx[(long)q * keep_at_most + j]];
+    const TrialRes tr = tres[c.tbase[q] + j];
+    const bool ok = !(tr.status == ST_FAILED || tr.status == ST_STARTFAIL);
+    TrialIn t{};
+    t.q = q;
+    t.node = c.edge_nodes[e.edge];
+    t.pend0 = ok ? tr.pend : e.pend;
+    t.dist0 = ok ? tr.dist : e.dist;
+    t.tol = 1e-5;
+    t.seeded = 1;
+    t.seed = ok ? tr.last : e.ev;
+    t.marginal = 1;
+    t.prior_kind = prior_kind;
+    t.prior_mu = prior_mu[t.node];
+    const int ti = off + c.tbase[q] + j;
+    c.trials[ti] = t;
+    c.bin_list[(long)bin * c.cap_trials + bpos + j] = ti;
+  }
+}
+
+// pp_off >= 0: the marginal likelihoods are the results at pp_off + tbase[q]
+// + j, and give the posterior probabilities (ll_normalized_prob, core.ml:
+// 396-401).
 __global__ void k_finalize(BBCtx c, int keep_at_most, const int *__restrict__ keep_idx, const int *__restrict__ keep_n,
-                           const TrialRes *__restrict__ tres, pgb_placement *out, int *n_out) {
+                           const TrialRes *__restrict__ tres, int pp_off, pgb_placement *out, int *n_out) {
   int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= c.Q) return;
   int nk = keep_n[q];
@@ -730,6 +768,7 @@ __global__ void k_finalize(BBCtx c, int keep_at_most, const int *__restrict__ ke
     p.post_prob = NAN;
     if (t.status == ST_FAILED || t.status == ST_STARTFAIL) { p.like = e.like; p.pend = e.pend; p.dist = e.dist; }
     else { p.like = t.like; p.pend = t.pend; p.dist = t.dist; }
+    if (pp_off >= 0) p.marginal_like = tres[pp_off + c.tbase[q] + j].like;
     like[j] = p.like;
     o[j] = p;
   }
@@ -738,6 +777,12 @@ __global__ void k_finalize(BBCtx c, int keep_at_most, const int *__restrict__ ke
     for (int k = 0; k < m; k++) tot += exp(like[k] - like[j]);
     o[j].lwr = 1. / tot;
   }
+  if (pp_off >= 0)
+    for (int j = 0; j < m; j++) {
+      double tot = 0;
+      for (int k = 0; k < m; k++) tot += exp(o[k].marginal_like - o[j].marginal_like);
+      o[j].post_prob = 1. / tot;
+    }
   for (int i = 1; i < m; i++) {  // stable sort by lwr, descending
     pgb_placement x = o[i];
     int j = i - 1;
@@ -2088,6 +2133,7 @@ pgb_status pgb_queries_run(pgb_engine *e, const pgb_prefs *p) {
   for (int v : e->h_qlen) max_sq = std::max(max_sq, v);
   size_t tcap = (size_t)e->Q * std::max(8, std::min(rk, 16)) + (size_t)e->Q * p->keep_at_most + 64;
   if (all_edges) tcap = std::max(tcap, (size_t)e->Q * e->n_edges + 64);
+  if (p->calc_pp) tcap += (size_t)e->Q * p->keep_at_most;  // marginal trials after the refinements
   if ((s = ensure_run_buffers(e, p, rk, maxr, tcap))) return s;
   for (int i = 0; i < 8; i++) e->counts[i] = 0;
   PGB_CUDA(cudaMemsetAsync(e->d_stats, 0, 4 * sizeof(unsigned long long), e->st));
@@ -2119,11 +2165,7 @@ pgb_status pgb_queries_run(pgb_engine *e, const pgb_prefs *p) {
   for (int b = 0; b < kBins; b++)
     if (e->tune_threads[b] != 32) whole_query = false;
   if (whole_query) return run_whole_queries(e, p, c, tc);
-  if (p->calc_pp) {
-    set_error("calc_pp: posterior probabilities need the whole-query kernel (nucleotide Gamma models, "
-              "threads 32 in every bin)");
-    return PGB_ERR_ARG;
-  }
+  if (p->calc_pp && (s = ensure_prior_means(e, p->prior, p->prior_lower))) return s;
   k_bb_init<<<(n + 255) / 256, 256, 0, e->st>>>(c);
   PGB_LAUNCH_CHECK();
   double n_trials_total = 0;
@@ -2178,7 +2220,20 @@ pgb_status pgb_queries_run(pgb_engine *e, const pgb_prefs *p) {
   n_trials_total += got[0];
   e->counts[6] = got[0];
   if ((s = run_bins(e, tc, got + 2, max_sq))) return s;
-  k_finalize<<<(n + 255) / 256, 256, 0, e->st>>>(c, p->keep_at_most, e->d_keep_idx, e->d_keep_n, e->d_tres,
+  int pp_off = -1;
+  if (p->calc_pp) {  // the marginal likelihood of every kept location, after all refinements
+    pp_off = got[0];
+    PGB_CUDA(cudaMemcpyAsync(e->d_small, h_small, sizeof(h_small), cudaMemcpyHostToDevice, e->st));
+    k_pp_emit<<<(n + 255) / 256, 256, 0, e->st>>>(c, p->keep_at_most, e->d_keep_idx, e->d_keep_n, e->d_tres, pp_off,
+                                                  p->prior == 1 ? 0 : 1, e->d_prior_mu);
+    PGB_LAUNCH_CHECK();
+    int got_pp[2 + kBins];
+    PGB_CUDA(cudaMemcpyAsync(got_pp, e->d_small, sizeof(got_pp), cudaMemcpyDeviceToHost, e->st));
+    PGB_CUDA(cudaStreamSynchronize(e->st));
+    n_trials_total += got[0];
+    if ((s = run_bins(e, tc, got_pp + 2, max_sq))) return s;
+  }
+  k_finalize<<<(n + 255) / 256, 256, 0, e->st>>>(c, p->keep_at_most, e->d_keep_idx, e->d_keep_n, e->d_tres, pp_off,
                                                  e->d_out, e->d_nout);
   PGB_LAUNCH_CHECK();
   PGB_CUDA(cudaEventRecord(e->ev[4], e->st));

@@ -1,7 +1,9 @@
 """20-state Gamma-mixture trials against the FP64 oracle, in both kernel
 forms: the tensor-core CTA (tcgen05 3xTF32 evolves, tuning code 1) and the
 CUDA-core CTA (256 threads, windows in shared memory).  Queries up to 300
-sites span three 128-site MMA tiles; some carry ambiguity characters.
+sites span three 128-site MMA tiles; some carry ambiguity characters.  The
+posterior probabilities of the round-based path (20 states, CAT) against
+the oracle's quadrature.
 
 Tolerances as in test_gpu_engine: fixed-point logL 2e-7 relative, optimised
 logL 1e-6 relative, best edge identical for non-tied queries."""
@@ -72,3 +74,56 @@ def test_protein_placements(protein, oracle_lib, form):
     gres, gst = eng.place(w.query_seqs, E.default_prefs(optimizer=1))
     assert list(gst) == list(ost)
     _compare_placements(O, oref, w.query_seqs, gres, ores)
+
+
+def _check_pp(O, oref, w, res, prior, mu, nq=3):
+    import math
+    checked = 0
+    for q in range(nq):
+        places = res[q][:3]
+        assert places and all(len(p) == 7 for p in places)
+        want = []
+        for (e, like, lwr, d, p, pp, m) in places:
+            ref_m = O.marginal_like(oref, w.query_seqs[q], e, p, d, prior, None if mu is None else mu[e], rel=1e-8)
+            assert abs(m - ref_m) <= 2e-3, (q, e, m, ref_m)
+            want.append(ref_m)
+            checked += 1
+        if len(res[q]) == len(places):
+            mx = max(want)
+            tot = sum(math.exp(v - mx) for v in want)
+            for (_, _, _, _, _, pp, _), v in zip(places, want):
+                assert abs(pp - math.exp(v - mx) / tot) <= 2e-3
+        assert abs(sum(p[5] for p in res[q]) - 1.0) < 1e-9
+    assert checked >= 3
+
+
+@pytest.mark.parametrize("form", sorted(FORMS))
+def test_protein_posterior_probabilities(oracle_lib, form):
+    """calc_pp on the round-based path: one marginal-likelihood trial per
+    kept location after the refinements, in either kernel form, against the
+    FP64 quadrature of the same integral (three_tax.ml:169-215)."""
+    from pplacer_gb300 import engine as E
+    from pplacer_gb300 import synth
+    O = oracle_lib
+    w = synth.make_workload("aa_500", n_queries=3, taxa=30, sites=200, lo=80, hi=200)
+    oref = O.Reference(O.Model(w.exch, w.statd, w.rates), w.parent, w.bl, w.leaf_row, w.ref_seqs)
+    eng = E.engine_for_workload(w)
+    eng.set_tuning(*FORMS[form])
+    prior = 0
+    res, st = eng.place(w.query_seqs, E.default_prefs(calc_pp=1, prior=prior, prior_lower=0.01))
+    assert list(st) == [0, 0, 0]
+    _check_pp(O, oref, w, res, prior, O.prior_means(w.parent, w.bl, prior, prior_lower=0.01))
+
+
+def test_cat_posterior_probabilities(oracle_lib):
+    """calc_pp for a per-site CAT model (Gcat_model) on the CTA kernel."""
+    from pplacer_gb300 import engine as E
+    from pplacer_gb300 import synth
+    O = oracle_lib
+    w = synth.make_workload("cat_5k", n_queries=3, taxa=40, sites=300, lo=100, hi=300)
+    oref = O.Reference(O.Model(w.exch, w.statd, w.rates, w.site_cats), w.parent, w.bl, w.leaf_row, w.ref_seqs)
+    eng = E.engine_for_workload(w)
+    prior = 1
+    res, st = eng.place(w.query_seqs, E.default_prefs(calc_pp=1, prior=prior))
+    assert list(st) == [0, 0, 0]
+    _check_pp(O, oref, w, res, prior, None)
