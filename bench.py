@@ -156,6 +156,16 @@ def load_peaks():
         return 6800.0, "fallback"
 
 
+def load_bf16_peak():
+    """Dense bf16 TFLOP/s of this GPU (burst: the stage-1 GEMMs run for well
+    under a second)."""
+    try:
+        with open(MEASURED_PEAKS) as f:
+            return float(json.load(f)["bf16_tflops"]), "measured"
+    except Exception:
+        return 1900.0, "fallback"
+
+
 def cpu_baseline(w, n_sample, prefs_kw):
     """The oracle (FP64 CPU restatement of pplacer's path, with the reference's
     own linear_c.c arithmetic) on a bounded sample, all host threads."""
@@ -364,6 +374,17 @@ def run_ours(args):
     # evaluation (148 per rate with derivatives), against 128 lanes per SM
     fp32_ops = FMA_OPS_PER_SITE_RATE * R * site_evals / args.steps / t_trials if t_trials > 0 else 0.0
     fp32_peak = 128 * N_SM * SM_MAX_HZ
+    # Stage 1 (the masked_logdot score of every (query, edge) pair): five bf16
+    # GEMMs on the tensor cores, [Ep x Q] by K = 3 x (prim x Sp) for the three
+    # bf16 terms of the log-likelihood tables and 2 x Sp for the exponent
+    # digits (Ep, Sp: edges and sites padded to 16 and 8), then the ranking
+    prim = 4 if K == 4 else 20
+    n_edges = int(np.sum(np.asarray(w.parent) >= 0))
+    Sp, Ep = (S + 7) // 8 * 8, (n_edges + 15) // 16 * 16
+    s1_flops = 2.0 * Ep * Q * (3 * prim * Sp + 2 * Sp)
+    t_s1 = phase[2] / 1e3 / args.steps
+    bf16_peak, bf16_kind = load_bf16_peak()
+    s1_tflops = s1_flops / t_s1 / 1e12 if t_s1 > 0 else 0.0
     cpu_v, cpu_threads, cpu_n, cpu_dt = cpu_baseline(w, args.cpu_sample, dict(w.prefs))
     line = {
         "metric": "query placements/s", "value": value, "unit": "placements/s", "n_gpus": world,
@@ -391,7 +412,11 @@ def run_ours(args):
                      "traffic_unit": "bytes per launch", "algorithmic_bytes_per_site_eval": bytes_per_site_eval,
                      "peak_source": peak_kind,
                      "fp32_pipe": {"achieved": fp32_ops, "peak": fp32_peak, "unit": "FMA-pipe lane ops/s",
-                                   "frac": fp32_ops / fp32_peak, "peak_source": "nominal: 128 lanes x 152 SMs x 2070 MHz"}},
+                                   "frac": fp32_ops / fp32_peak, "peak_source": "nominal: 128 lanes x 152 SMs x 2070 MHz"},
+                     "stage1": {"kernels": "5 bf16 GEMMs (cuBLAS tcgen05) + k_rank_warp", "bound": "tensor",
+                                "achieved": s1_tflops, "peak": bf16_peak, "unit": "TFLOP/s",
+                                "frac": s1_tflops / bf16_peak, "peak_source": bf16_kind,
+                                "gemm_flops_per_step": s1_flops, "note": "time includes the ranking"}},
         "cpu_baseline": {"value": cpu_v, "unit": "placements/s", "cores": cpu_threads, "kind": "port",
                          "sample": "%d queries of %s (%.1f s)" % (cpu_n, args.workload, cpu_dt)},
         "e2e": {"value": e2e, "unit": "placements/s", "h2d_bytes_per_step": Q * S,
