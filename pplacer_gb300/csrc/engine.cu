@@ -986,6 +986,212 @@ __global__ void __launch_bounds__(32, kWarpTrialMinCtas) k_place_warp(TrialCtx c
   }
 }
 
+// The whole-query search of k_place_warp for any team of threads that runs
+// one trial at a time: Team::leader() is the one thread that writes results,
+// Team::sync() orders its writes before the team's reads, Team::bcast(v) is
+// the leader's v in every thread, Team::trial(t) the trial's result
+// (identical in every thread) and Team::aborted() true after a trial the
+// team could not complete (the launch then reports an error).
+template <class Team>
+__device__ __forceinline__ void place_queries(Team &tm, const TrialCtx &c, const PlaceCtx &p) {
+  const BBCtx &b = p.bb;
+  // One trial call site (the trial code is inlined once): a query moves from
+  // its baseball trials (refine < 0) to the refinement of its kept
+  // locations (refine = index of the next one).
+  int q = -1, next = 0, nres = 0, nk = 0, refine = -1;
+  bool marginal = false;  // the next trial is the marginal likelihood of kept location `refine`
+  long strikes = 0;
+  double record = -INFINITY, pend_hint = b.start_pend;
+  unsigned long long n_bb = 0;
+  for (;;) {
+    if (q < 0) {  // take the next query
+      const int qi = tm.bcast(tm.leader() ? atomicAdd(p.qnext, 1) : 0);
+      if (qi >= b.Q) break;
+      q = p.qorder[qi];
+      if (tm.leader()) p.n_out[q] = 0;
+      if (b.qstatus[q] != PGB_Q_OK || b.rk < 1) { q = -1; continue; }
+      next = 0; nres = 0; nk = 0; refine = -1; strikes = 0; record = -INFINITY; n_bb = 0; marginal = false;
+      pend_hint = b.start_pend;
+    }
+    ResEntry *r = b.res + (long)q * b.maxr;
+    TrialIn t{};
+    t.q = q;
+    int ei = -1;
+    if (refine < 0) {
+      ei = b.rank[(long)q * b.rk + next];
+      t.node = b.edge_nodes[ei];
+      // The Newton form starts the pendant length at the query's best
+      // optimum so far (the optimum, not the path, is its result); the
+      // Brent replica keeps the reference's start.
+      t.pend0 = c.optimizer == 1 ? pend_hint : b.start_pend;
+      t.dist0 = b.bl[t.node] / 2.;
+      t.tol = b.tol;
+    } else {
+      const ResEntry e = r[refine];
+      t.node = b.edge_nodes[e.edge];
+      t.pend0 = e.pend;
+      t.dist0 = e.dist;
+      t.tol = 1e-5;  // final_tolerance (core.ml:160)
+      t.seeded = 1;  // the evaluation at (pend0, dist0); the Newton form does not redo it
+      t.seed = e.ev;
+      if (marginal) {  // after the refinement: e holds the refined optimum
+        t.marginal = 1;
+        t.prior_kind = p.prior_kind;
+        t.prior_mu = p.prior_mu[t.node];
+      }
+    }
+    const TrialRes tr = tm.trial(t);
+    if (tm.aborted()) return;
+    if (refine >= 0) {  // ---- a refined location, or its marginal likelihood ----
+      pgb_placement *o = p.out + (long)q * p.keep_at_most;
+      if (marginal) {
+        if (tm.leader()) o[refine].marginal_like = tr.like;
+        marginal = false;
+      } else {
+        const bool ok = !(tr.status == ST_FAILED || tr.status == ST_STARTFAIL);
+        if (tm.leader()) {
+          ResEntry e = r[refine];
+          pgb_placement pl;
+          pl.edge = t.node;
+          pl.pad = 0;
+          pl.lwr = 0;
+          pl.marginal_like = NAN;
+          pl.post_prob = NAN;
+          if (!ok) { pl.like = e.like; pl.pend = e.pend; pl.dist = e.dist; }
+          else { pl.like = tr.like; pl.pend = tr.pend; pl.dist = tr.dist; }
+          o[refine] = pl;
+          if (ok && p.calc_pp) {  // the marginal likelihood integrates around the refined optimum
+            e.pend = tr.pend; e.dist = tr.dist; e.ev = tr.last;
+            r[refine] = e;
+          }
+        }
+        tm.sync();
+        if (p.calc_pp) {
+          marginal = true;
+          continue;
+        }
+      }
+      if (++refine < nk) continue;
+      // like_weight_ratio (and with calc_pp the posterior probabilities,
+      // core.ml:396-401), then stable sort by like_weight_ratio, descending
+      if (tm.leader()) {
+        atomicAdd(&p.tstats[1], (unsigned long long)nk);
+        const int m = min(nk, 64);
+        for (int j = 0; j < m; j++) {
+          double tot = 0;
+          for (int k = 0; k < m; k++) tot += exp(o[k].like - o[j].like);
+          o[j].lwr = 1. / tot;
+        }
+        if (p.calc_pp)
+          for (int j = 0; j < m; j++) {
+            double tot = 0;
+            for (int k = 0; k < m; k++) tot += exp(o[k].marginal_like - o[j].marginal_like);
+            o[j].post_prob = 1. / tot;
+          }
+        for (int i = 1; i < m; i++) {
+          pgb_placement x = o[i];
+          int j = i - 1;
+          while (j >= 0 && x.lwr > o[j].lwr) { o[j + 1] = o[j]; j--; }
+          o[j + 1] = x;
+        }
+        p.n_out[q] = m;
+      }
+      tm.sync();
+      q = -1;
+      continue;
+    }
+    // ---- a baseball result (k_bb_update's rules for one trial) ----
+    n_bb++;
+    next++;
+    bool stop = false;
+    int qst = PGB_Q_OK;
+    if (tr.status == ST_STARTFAIL) {
+      qst = PGB_Q_START_FAILURE;
+      stop = true;
+    } else if (tr.status != ST_FAILED) {  // ST_FAILED: skipped location (core.ml:435-443)
+      const long before = nres;
+      if (nres < b.maxr) {
+        if (tm.leader()) {
+          ResEntry e;
+          e.edge = ei; e.status = tr.status; e.like = tr.like; e.pend = tr.pend; e.dist = tr.dist; e.ev = tr.last;
+          r[nres] = e;
+        }
+        nres++;
+      }
+      if (before >= b.max_pitches) stop = true;
+      else if (tr.like > record) {
+        record = tr.like;
+        if (tr.pend > 1e-6 && tr.pend < c.max_pend) pend_hint = tr.pend;
+      }
+      else if (tr.like < record - b.strike_box) {
+        if (strikes + 1 >= b.max_strikes) stop = true;
+        else strikes++;
+      }
+    }
+    if (!stop && next < b.rk) continue;
+    if (tm.leader()) atomicAdd(&p.tstats[0], n_bb);
+    if (qst != PGB_Q_OK || nres == 0) {
+      if (tm.leader()) b.qstatus[q] = qst != PGB_Q_OK ? qst : PGB_Q_EMPTY;
+      tm.sync();
+      q = -1;
+      continue;
+    }
+    // ---- keep: stable sort by like, descending, NaN last ----
+    tm.sync();
+    if (tm.leader())
+      for (int i = 1; i < nres; i++) {
+        ResEntry x = r[i];
+        int j = i - 1;
+        while (j >= 0 && (isnan(r[j].like) ? !isnan(x.like) : (!isnan(x.like) && x.like > r[j].like))) {
+          r[j + 1] = r[j];
+          j--;
+        }
+        r[j + 1] = x;
+      }
+    tm.sync();
+    const double best = r[0].like;
+    nk = 0;
+    while (nk < nres && nk < p.keep_at_most && r[nk].like >= p.log_keep_factor + best) nk++;
+    if (nk == 0) { q = -1; continue; }
+    refine = 0;
+  }
+}
+
+// The tensor-core CTA as a team: thread 0 leads, the CTA's barriers order,
+// a shared int broadcasts.
+struct TcTeam {
+  const TrialCtx &c;
+  const TcSmem &sm;
+  uint32_t tmem;
+  uint32_t &phase;
+  bool &failed;
+  int tid;
+  __device__ bool leader() const { return tid == 0; }
+  __device__ void sync() const { __syncthreads(); }
+  __device__ int bcast(int v) const {
+    __syncthreads();  // earlier readers of the slot are done
+    if (tid == 0) *sm.redi = v;
+    __syncthreads();
+    return *sm.redi;
+  }
+  __device__ TrialRes trial(const TrialIn &t) { return tc_trial(c, sm, tmem, phase, failed, t, tid); }
+  __device__ bool aborted() const { return failed; }
+};
+
+// Whole queries, one per CTA of the tensor-core trial kernel (20-state
+// Gamma mixtures): the search of k_place_warp with each trial run by the CTA.
+__global__ void __launch_bounds__(kTcThreads, 1) k_place_tc(TrialCtx c, PlaceCtx p) {
+  extern __shared__ __align__(16) char t_smem[];
+  const int tid = threadIdx.x;
+  const TcSmem sm = tc_carve(t_smem, c.cap, c.NM, c.ncode, c.zcodes);
+  const uint32_t tmem = tc_setup(c, sm, tid);
+  uint32_t phase = 0;
+  bool failed = false;
+  TcTeam tm{c, sm, tmem, phase, failed, tid};
+  place_queries(tm, c, p);
+  tc_teardown(sm, tmem, phase, failed, tid);
+}
+
 }  // namespace
 }  // namespace pgb
 
@@ -1078,6 +1284,7 @@ namespace {
 
 constexpr int kBins = 6;
 constexpr int kTuneTc = 1;  // tuning code of the tensor-core trial kernel
+constexpr int kTcMaxInstances = 4;  // concurrent launches of the whole-query tensor-core kernel
 
 template <class T>
 pgb_status dalloc(T **p, size_t n) {
@@ -1345,13 +1552,18 @@ pgb_status ensure_eigen_glvs(pgb_engine *e) {
   return PGB_OK;
 }
 
+// the character codes the tensor-core kernel's query tables hold
+int tc_zcodes(const pgb_engine *e) {
+  for (int a : e->h_qamb)
+    if (a > 0) return e->ncode;
+  return e->prim;
+}
+
 pgb_status launch_trials_tc(pgb_engine *e, cudaStream_t st, TrialCtx c, const int *d_order, int n, int cap,
                             TrialRes *out) {
   c.smem_win = 0;
   c.cap = std::max(cap, 1);
-  c.zcodes = e->prim;
-  for (int a : e->h_qamb)
-    if (a > 0) { c.zcodes = e->ncode; break; }
+  c.zcodes = tc_zcodes(e);
   size_t smem = tc_trial_smem_bytes(c.cap, e->NM, e->ncode, c.zcodes);
   if (smem > e->smem_optin) { set_error("tensor-core trial shared memory %zu exceeds %zu", smem, e->smem_optin); return PGB_ERR_ARG; }
   PGB_CUDA(cudaFuncSetAttribute(k_trials_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -1537,8 +1749,40 @@ pgb_status launch_place_warp_rp(pgb_engine *e, TrialCtx c, const PlaceCtx &pc) {
   return PGB_OK;
 }
 
-// Stage 2 and refinement as one persistent launch of whole-query warps.
-pgb_status run_whole_queries(pgb_engine *e, const pgb_prefs *p, const BBCtx &c, TrialCtx tc) {
+pgb_status launch_place_tc(pgb_engine *e, TrialCtx c, const PlaceCtx &pc, int max_sq) {
+  c.cap = std::max(max_sq, 1);
+  c.zcodes = tc_zcodes(e);
+  size_t smem = tc_trial_smem_bytes(c.cap, e->NM, e->ncode, c.zcodes);
+  if (smem > e->smem_optin) { set_error("tensor-core trial shared memory %zu exceeds %zu", smem, e->smem_optin); return PGB_ERR_ARG; }
+  PGB_CUDA(cudaFuncSetAttribute(k_place_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int per_sm = 0;
+  PGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_place_tc, kTcThreads, smem));
+  // The runtime places one CTA of a tcgen05 kernel per SM per launch (its
+  // occupancy is 1 whatever the registers and shared memory), but CTAs of
+  // concurrent launches share an SM.  So the persistent grid runs as several
+  // launches on separate streams, sharing the query counter: as many as the
+  // SM's shared memory holds, at most 4 (4 x 128 TMEM columns).
+  int sm_smem = 0, rsv = 0;
+  cudaDeviceGetAttribute(&sm_smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor, e->device);
+  cudaDeviceGetAttribute(&rsv, cudaDevAttrReservedSharedMemoryPerBlock, e->device);
+  const int inst = std::max(1, std::min(kTcMaxInstances, (int)((size_t)sm_smem / (smem + (size_t)rsv))));
+  const int grid = std::max(1, std::min(e->Q, e->n_sm * std::max(1, per_sm)));
+  PGB_CUDA(cudaEventRecord(e->bin_ev[8], e->st));
+  for (int k = 1; k < inst; k++) PGB_CUDA(cudaStreamWaitEvent(e->bin_st[k - 1], e->bin_ev[8], 0));
+  for (int k = 0; k < inst; k++) {
+    k_place_tc<<<grid, kTcThreads, smem, k == 0 ? e->st : e->bin_st[k - 1]>>>(c, pc);
+    PGB_LAUNCH_CHECK();
+  }
+  for (int k = 1; k < inst; k++) {
+    PGB_CUDA(cudaEventRecord(e->bin_ev[k - 1], e->bin_st[k - 1]));
+    PGB_CUDA(cudaStreamWaitEvent(e->st, e->bin_ev[k - 1], 0));
+  }
+  return PGB_OK;
+}
+
+// Stage 2 and refinement as one persistent launch of whole-query warps (or
+// whole-query tensor-core CTAs for 20-state models).
+pgb_status run_whole_queries(pgb_engine *e, const pgb_prefs *p, const BBCtx &c, TrialCtx tc, int max_sq) {
   pgb_status s;
   if ((size_t)e->Q > e->qorder_cap) {
     if ((s = dalloc(&e->d_qorder, e->Q))) return s;
@@ -1564,12 +1808,14 @@ pgb_status run_whole_queries(pgb_engine *e, const pgb_prefs *p, const BBCtx &c, 
   pc.prior_kind = p->prior == 1 ? 0 : 1;
   if ((s = ensure_prior_means(e, p->prior, p->prior_lower))) return s;
   pc.prior_mu = e->d_prior_mu;
-  switch (e->RP) {
-    case 1: s = launch_place_warp_rp<1>(e, tc, pc); break;
-    case 2: s = launch_place_warp_rp<2>(e, tc, pc); break;
-    case 4: s = launch_place_warp_rp<4>(e, tc, pc); break;
-    default: s = launch_place_warp_rp<8>(e, tc, pc); break;
-  }
+  if (!warp_trials_ok(e)) s = launch_place_tc(e, tc, pc, max_sq);
+  else
+    switch (e->RP) {
+      case 1: s = launch_place_warp_rp<1>(e, tc, pc); break;
+      case 2: s = launch_place_warp_rp<2>(e, tc, pc); break;
+      case 4: s = launch_place_warp_rp<4>(e, tc, pc); break;
+      default: s = launch_place_warp_rp<8>(e, tc, pc); break;
+    }
   if (s) return s;
   PGB_CUDA(cudaEventRecord(e->ev[3], e->st));
   PGB_CUDA(cudaEventRecord(e->ev[4], e->st));
@@ -1582,6 +1828,7 @@ pgb_status run_whole_queries(pgb_engine *e, const pgb_prefs *p, const BBCtx &c, 
   cudaEventElapsedTime(&ms, e->ev[0], e->ev[4]); e->t_ms[5] = ms;
   unsigned long long st_h[4] = {0, 0, 0, 0};
   PGB_CUDA(cudaMemcpy(st_h, e->d_stats, sizeof st_h, cudaMemcpyDeviceToHost));
+  if ((s = check_tc_err(e))) return s;
   e->counts[1] = (double)(st_h[2] + st_h[3]);
   e->counts[2] = (double)st_h[0];
   e->counts[3] = (double)st_h[1];
@@ -2161,10 +2408,12 @@ pgb_status pgb_queries_run(pgb_engine *e, const pgb_prefs *p) {
   if ((s = ensure_eigen_glvs(e))) return s;
   TrialCtx tc = trial_ctx(e, p, p->optimizer, 0);
   int n = e->Q;
-  bool whole_query = warp_trials_ok(e);
+  // whole queries: every bin tuned to the warp form, or (20 states) to the
+  // tensor-core form
+  bool whole_query = warp_trials_ok(e) || tc_trials_ok(e);
   for (int b = 0; b < kBins; b++)
-    if (e->tune_threads[b] != 32) whole_query = false;
-  if (whole_query) return run_whole_queries(e, p, c, tc);
+    if (e->tune_threads[b] != (warp_trials_ok(e) ? 32 : kTuneTc)) whole_query = false;
+  if (whole_query) return run_whole_queries(e, p, c, tc, max_sq);
   if (p->calc_pp && (s = ensure_prior_means(e, p->prior, p->prior_lower))) return s;
   k_bb_init<<<(n + 255) / 256, 256, 0, e->st>>>(c);
   PGB_LAUNCH_CHECK();

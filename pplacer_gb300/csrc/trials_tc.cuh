@@ -61,6 +61,7 @@ struct TcSmem {
   uint8_t *code;                      // [cap]
   Ctrl *ctrl;
   Optimiser *opt;
+  TrialRes *res;  // a finished trial's result, read by every thread
   uint64_t *bar;
   uint32_t *tbase;
 };
@@ -77,7 +78,7 @@ __host__ __device__ inline size_t tc_trial_smem_bytes(int cap, int NM, int ncode
   b += align16((size_t)ncode * K * 4) + align16((size_t)K * 4);
   b += align16(4 * 8 * 4) + align16(4 * 4);
   b += align16((size_t)cap * 2) + align16((size_t)cap);
-  b += align16(sizeof(Ctrl)) + align16(sizeof(Optimiser)) + 16 + 16;
+  b += align16(sizeof(Ctrl)) + align16(sizeof(Optimiser)) + align16(sizeof(TrialRes)) + 16 + 16;
   return b + 1024;  // base alignment of the operand tiles
 }
 
@@ -103,6 +104,7 @@ __device__ inline TcSmem tc_carve(char *base, int cap, int NM, int ncode, int zc
   s.code = (uint8_t *)take((size_t)cap);
   s.ctrl = (Ctrl *)take(sizeof(Ctrl));
   s.opt = (Optimiser *)take(sizeof(Optimiser));
+  s.res = (TrialRes *)take(sizeof(TrialRes));
   s.bar = (uint64_t *)take(16);
   s.tbase = (uint32_t *)take(16);
   return s;
@@ -392,23 +394,13 @@ __global__ void k_eigen_glvs(const float *__restrict__ darr, const float *__rest
   }
 }
 
-__global__ void __launch_bounds__(kTcThreads, 1) k_trials_tc(TrialCtx c, const TrialIn *__restrict__ trials,
-                                                             const int *__restrict__ order, int n, TrialRes *out) {
+// Per-CTA setup of the tensor-core trial kernels: model constants, the
+// zero padding of the operand tiles (columns 20..23 of every tile, rows
+// 60..63 of the B tiles, never written afterwards), TMEM columns and the
+// mbarrier.  Returns the TMEM base.
+__device__ __forceinline__ uint32_t tc_setup(const TrialCtx &c, const TcSmem &sm, int tid) {
   namespace T = pgb::tc;
-  extern __shared__ __align__(16) char t_smem[];
-  if (blockIdx.x >= n) return;
-  const int K = kTcK;
-  const int ti = order ? order[blockIdx.x] : blockIdx.x;
-  const TrialIn tr = trials[ti];
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int NM = c.NM, nc = c.ncode, cap = c.cap;
-  const int zc = c.zcodes;
-  const TcSmem sm = tc_carve(t_smem, cap, NM, nc, zc);
-  const int q = tr.q, node = tr.node;
-  const int Sq = c.qlen[q];
-  const int ncz = c.qamb[q] > 0 ? nc : c.prim;
-  const int nch = (Sq + T::kTileRows - 1) / T::kTileRows;
-  // ---- prologue: model constants, the query's sites, TMEM, mbarrier ----
+  const int K = kTcK, NM = c.NM, nc = c.ncode;
   for (int it = tid; it < K * K; it += kTcThreads) {
     const int i = it / K, k = it - i * K;
     sm.X[i * kTcXs + k] = c.X[it];
@@ -416,14 +408,46 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_trials_tc(TrialCtx c, const T
   for (int it = tid; it < nc * K; it += kTcThreads) sm.lv[it] = c.lvf[it];
   for (int it = tid; it < NM * K; it += kTcThreads) sm.Lr[it] = c.rates[it / K] * c.lam[it % K];
   if (tid < K) sm.statd[tid] = c.statd[tid];
-  // the padding columns 20..23 of every tile and the rows 60..63 of the B
-  // tiles stay zero; the rest is rewritten before each use
   for (int it = tid; it < T::kTileFloats; it += kTcThreads) {
     sm.a_dh[it] = 0.f; sm.a_dl[it] = 0.f; sm.a_xh[it] = 0.f; sm.a_xl[it] = 0.f;
   }
   for (int it = tid; it < kTcNDer * T::kKPad; it += kTcThreads) {
     sm.b_dh[it] = 0.f; sm.b_dl[it] = 0.f; sm.b_xh[it] = 0.f; sm.b_xl[it] = 0.f;
   }
+  __syncwarp();
+  if ((tid >> 5) == 0) T::tmem_alloc(sm.tbase, kTcCols);
+  if (tid == 0) T::bar_init(sm.bar, 1);
+  T::fence_before();
+  __syncthreads();
+  T::fence_after();
+  return *sm.tbase;
+}
+
+// After the last trial: a timed-out MMA group is waited for once more
+// (bounded) and the TMEM columns are freed.
+__device__ __forceinline__ void tc_teardown(const TcSmem &sm, uint32_t tmem, uint32_t phase, bool failed, int tid) {
+  namespace T = pgb::tc;
+  if (failed) T::bar_wait(sm.bar, phase ^ 1u);
+  T::fence_before();
+  __syncthreads();
+  if ((tid >> 5) == 0) T::tmem_dealloc(tmem, kTcCols);
+}
+
+// One trial (Three_tax.optimize at one location, or its marginal
+// likelihood) by the CTA; every thread returns the same result.  failed is
+// set (in every thread) when an MMA completion wait timed out; the trial then
+// reports status 1 and NaN.
+__device__ TrialRes tc_trial(const TrialCtx &c, const TcSmem &sm, uint32_t tmem, uint32_t &phase, bool &failed,
+                             const TrialIn &tr, int tid) {
+  namespace T = pgb::tc;
+  const int K = kTcK;
+  const int lane = tid & 31, warp = tid >> 5;
+  const int NM = c.NM, nc = c.ncode, cap = c.cap, zc = c.zcodes;
+  const int q = tr.q, node = tr.node;
+  const int Sq = c.qlen[q];
+  const int ncz = c.qamb[q] > 0 ? nc : c.prim;
+  const int nch = (Sq + T::kTileRows - 1) / T::kTileRows;
+  // ---- the query's sites and their exponent sum ----
   long long esum = 0;
   const long qo = (long)q * c.S;
   for (int i = tid; i < Sq; i += kTcThreads) {
@@ -434,14 +458,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_trials_tc(TrialCtx c, const T
     esum += (long long)c.dexp[go] + (long long)c.pexp[go];
   }
   esum = warp_sum_ll(esum);
+  __syncthreads();  // the previous trial's readers of red / res are done
   if (lane == 0) reinterpret_cast<long long *>(sm.red)[warp] = esum;
-  __syncwarp();
-  if (warp == 0) T::tmem_alloc(sm.tbase, kTcCols);
-  if (tid == 0) T::bar_init(sm.bar, 1);
-  T::fence_before();
   __syncthreads();
-  T::fence_after();
-  const uint32_t tmem = *sm.tbase;
   Optimiser &opt = *sm.opt;
   if (tid == 0) {
     long long etot = 0;
@@ -467,8 +486,6 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_trials_tc(TrialCtx c, const T
     opt.last.ex = 0; opt.last.lm = 0.f;
     opt.last.g[0] = opt.last.g[1] = opt.last.h[0] = opt.last.h[1] = opt.last.h[2] = 0.f;
   }
-  uint32_t phase = 0;
-  bool failed = false;
   EvalOut res;
   for (int ev = 0; ev < kMaxTrialEvals; ev++) {
     if (tid == 0) {
@@ -549,10 +566,6 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_trials_tc(TrialCtx c, const T
       res.h[0] = sg[2]; res.h[1] = sg[3]; res.h[2] = sg[4];
     }
   }
-  if (failed) T::bar_wait(sm.bar, phase ^ 1u);  // the timed-out MMAs, bounded, before the columns are freed
-  T::fence_before();
-  __syncthreads();
-  if (warp == 0) T::tmem_dealloc(tmem, kTcCols);
   if (tid == 0) {
     TrialRes rr;
     rr.like = failed ? NAN : opt.L_last;
@@ -564,10 +577,28 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_trials_tc(TrialCtx c, const T
     rr.status = failed ? 1 : opt.status;
     rr.last = opt.last;
     rr.n_evals = opt.n_evals;
-    out[ti] = rr;
+    *sm.res = rr;
     if (c.stats) {
       atomicAdd(&c.stats[0], (unsigned long long)opt.n_evals);
       atomicAdd(&c.stats[1], (unsigned long long)opt.n_evals * (unsigned long long)Sq);
     }
   }
+  __syncthreads();
+  return *sm.res;
+}
+
+// A batch of independent trials, one CTA each.
+__global__ void __launch_bounds__(kTcThreads, 1) k_trials_tc(TrialCtx c, const TrialIn *__restrict__ trials,
+                                                             const int *__restrict__ order, int n, TrialRes *out) {
+  extern __shared__ __align__(16) char t_smem[];
+  if (blockIdx.x >= n) return;
+  const int tid = threadIdx.x;
+  const int ti = order ? order[blockIdx.x] : blockIdx.x;
+  const TcSmem sm = tc_carve(t_smem, c.cap, c.NM, c.ncode, c.zcodes);
+  const uint32_t tmem = tc_setup(c, sm, tid);
+  uint32_t phase = 0;
+  bool failed = false;
+  const TrialRes rr = tc_trial(c, sm, tmem, phase, failed, trials[ti], tid);
+  if (tid == 0) out[ti] = rr;
+  tc_teardown(sm, tmem, phase, failed, tid);
 }
