@@ -140,11 +140,14 @@ class ClockSampler:
 def stage2_kernel(w, tune):
     """The trial kernel that ran stage 2 + refinement for this workload and tuning."""
     th = set(int(v) for v in tune[0])
-    if w.K == 4 and w.site_cats is None:
-        return "k_place_warp (stage 2 + refinement, whole queries)"
+    if w.K == 4 and w.site_cats is None and th == {32}:
+        return "k_place_warp (stage 2 + refinement, whole queries, one warp each)"
     if th == {1}:
-        return "k_trials_tc (stage 2 + refinement, tcgen05 evolves)"
-    return "k_trials (stage 2 + refinement, CTA per trial, %s threads)" % "/".join(str(t) for t in sorted(th))
+        return "k_place_tc (stage 2 + refinement, whole queries, one CTA each, tcgen05 evolves)"
+    if len(th) == 1:
+        return "k_place_cta (stage 2 + refinement, whole queries, one CTA of %d threads each)" % th.pop()
+    return "k_trials (stage 2 + refinement in baseball rounds, CTA per trial, %s threads)" % "/".join(
+        str(t) for t in sorted(th))
 
 
 def load_peaks():

@@ -1178,6 +1178,33 @@ struct TcTeam {
   __device__ bool aborted() const { return failed; }
 };
 
+// The CTA of the CUDA-core trial kernel as a team (CAT models and the
+// other CTA-tuned cases).
+template <int K, int T>
+struct CtaTeam {
+  const TrialCtx &c;
+  const TrialSmem &sm;
+  __device__ bool leader() const { return threadIdx.x == 0; }
+  __device__ void sync() const { __syncthreads(); }
+  __device__ int bcast(int v) const {
+    __syncthreads();  // earlier readers of the slot are done
+    if (threadIdx.x == 0) *sm.redi = v;
+    __syncthreads();
+    return *sm.redi;
+  }
+  __device__ TrialRes trial(const TrialIn &t) { return trial_cta<K, T>(c, sm, t); }
+  __device__ bool aborted() const { return false; }
+};
+
+template <int K, int T>
+__global__ void __launch_bounds__(T, 1) k_place_cta(TrialCtx c, PlaceCtx p) {
+  extern __shared__ __align__(16) char t_smem[];
+  const TrialSmem sm = carve(t_smem, c.cap, c.smem_win, c.RP, K, c.NM, c.ncode);
+  trial_cta_setup<K, T>(c, sm);
+  CtaTeam<K, T> tm{c, sm};
+  place_queries(tm, c, p);
+}
+
 // Whole queries, one per CTA of the tensor-core trial kernel (20-state
 // Gamma mixtures): the search of k_place_warp with each trial run by the CTA.
 __global__ void __launch_bounds__(kTcThreads, 1) k_place_tc(TrialCtx c, PlaceCtx p) {
@@ -1780,8 +1807,51 @@ pgb_status launch_place_tc(pgb_engine *e, TrialCtx c, const PlaceCtx &pc, int ma
   return PGB_OK;
 }
 
+template <int K, int T>
+pgb_status launch_place_cta_kt(pgb_engine *e, TrialCtx c, const PlaceCtx &pc, int max_sq, int win) {
+  int cap = std::max(max_sq, 1);
+  size_t smem = trial_smem_bytes(cap, win, e->RP, K, e->NM, e->ncode);
+  if (win && smem > e->smem_optin) {  // the windows do not fit: read them from L2
+    win = 0;
+    smem = trial_smem_bytes(cap, 0, e->RP, K, e->NM, e->ncode);
+  }
+  if (smem > e->smem_optin) { set_error("trial shared memory %zu exceeds %zu", smem, e->smem_optin); return PGB_ERR_ARG; }
+  c.cap = cap;
+  c.smem_win = win;
+  PGB_CUDA(cudaFuncSetAttribute(k_place_cta<K, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int per_sm = 0;
+  PGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_place_cta<K, T>, T, smem));
+  int grid = std::max(1, std::min(e->Q, e->n_sm * std::max(1, per_sm)));
+  k_place_cta<K, T><<<grid, T, smem, e->st>>>(c, pc);
+  PGB_LAUNCH_CHECK();
+  return PGB_OK;
+}
+
+// the CTA form of whole queries, with the bins' common tuning
+pgb_status launch_place_cta(pgb_engine *e, TrialCtx c, const PlaceCtx &pc, int max_sq) {
+  const int T = e->tune_threads[0], win = e->tune_win[0];
+  if (e->K == 4)
+    return T == 128 ? launch_place_cta_kt<4, 128>(e, c, pc, max_sq, win)
+                    : launch_place_cta_kt<4, 256>(e, c, pc, max_sq, win);
+  return T == 128 ? launch_place_cta_kt<20, 128>(e, c, pc, max_sq, win)
+                  : launch_place_cta_kt<20, 256>(e, c, pc, max_sq, win);
+}
+
+// whole queries in one persistent launch: every bin tuned to the same form
+// (the warp form for nucleotide Gamma mixtures, the tensor-core form for 20
+// states, or one CTA size; the CTA form stages the windows when the first
+// bin does and the longest query's fit)
+bool whole_query_form(const pgb_engine *e) {
+  for (int b = 1; b < kBins; b++)
+    if (e->tune_threads[b] != e->tune_threads[0]) return false;
+  const int t = e->tune_threads[0];
+  if (t == 32) return warp_trials_ok(e);
+  if (t == kTuneTc) return tc_trials_ok(e);
+  return t == 128 || t == 256;
+}
+
 // Stage 2 and refinement as one persistent launch of whole-query warps (or
-// whole-query tensor-core CTAs for 20-state models).
+// whole-query CTAs: tensor-core for 20-state models, CUDA-core otherwise).
 pgb_status run_whole_queries(pgb_engine *e, const pgb_prefs *p, const BBCtx &c, TrialCtx tc, int max_sq) {
   pgb_status s;
   if ((size_t)e->Q > e->qorder_cap) {
@@ -1808,7 +1878,8 @@ pgb_status run_whole_queries(pgb_engine *e, const pgb_prefs *p, const BBCtx &c, 
   pc.prior_kind = p->prior == 1 ? 0 : 1;
   if ((s = ensure_prior_means(e, p->prior, p->prior_lower))) return s;
   pc.prior_mu = e->d_prior_mu;
-  if (!warp_trials_ok(e)) s = launch_place_tc(e, tc, pc, max_sq);
+  if (e->tune_threads[0] == kTuneTc && tc_trials_ok(e)) s = launch_place_tc(e, tc, pc, max_sq);
+  else if (e->tune_threads[0] != 32 || !warp_trials_ok(e)) s = launch_place_cta(e, tc, pc, max_sq);
   else
     switch (e->RP) {
       case 1: s = launch_place_warp_rp<1>(e, tc, pc); break;
@@ -2408,12 +2479,7 @@ pgb_status pgb_queries_run(pgb_engine *e, const pgb_prefs *p) {
   if ((s = ensure_eigen_glvs(e))) return s;
   TrialCtx tc = trial_ctx(e, p, p->optimizer, 0);
   int n = e->Q;
-  // whole queries: every bin tuned to the warp form, or (20 states) to the
-  // tensor-core form
-  bool whole_query = warp_trials_ok(e) || tc_trials_ok(e);
-  for (int b = 0; b < kBins; b++)
-    if (e->tune_threads[b] != (warp_trials_ok(e) ? 32 : kTuneTc)) whole_query = false;
-  if (whole_query) return run_whole_queries(e, p, c, tc, max_sq);
+  if (whole_query_form(e)) return run_whole_queries(e, p, c, tc, max_sq);
   if (p->calc_pp && (s = ensure_prior_means(e, p->prior, p->prior_lower))) return s;
   k_bb_init<<<(n + 255) / 256, 256, 0, e->st>>>(c);
   PGB_LAUNCH_CHECK();

@@ -94,6 +94,7 @@ struct TrialSmem {
   int *redi;                 // [warps]
   Ctrl *ctrl;
   void *opt;  // the warp kernels' optimiser state (one per warp)
+  TrialRes *res;  // the CTA form's finished trial, read by every thread
 };
 
 __host__ __device__ inline size_t trial_smem_bytes(int cap, int win, int RP, int K, int NM, int ncode) {
@@ -106,7 +107,7 @@ __host__ __device__ inline size_t trial_smem_bytes(int cap, int win, int RP, int
   b += align16((size_t)K * K * 4) + (K == 4 ? align16((size_t)K * K * K * 4) : 0) +
        2 * align16((size_t)ncode * K * 4) + align16((size_t)K * 4);
   b += align16(kTrialMaxWarps * 8 * 4) + align16(kTrialMaxWarps * 4);
-  b += align16(sizeof(Ctrl));
+  b += align16(sizeof(Ctrl)) + align16(sizeof(TrialRes));
   return b;
 }
 
@@ -134,6 +135,7 @@ __device__ inline TrialSmem carve(char *base, int cap, int win, int RP, int K, i
   s.red = (float *)take(kTrialMaxWarps * 8 * 4);
   s.redi = (int *)take(kTrialMaxWarps * 4);
   s.ctrl = (Ctrl *)take(sizeof(Ctrl));
+  s.res = (TrialRes *)take(sizeof(TrialRes));
   return s;
 }
 
@@ -878,25 +880,28 @@ __device__ __forceinline__ void sites_generic(const TrialCtx &c, const TrialSmem
   }
 }
 
+// Model constants of the CTA form, once per CTA.
 template <int K, int T>
-__global__ void __launch_bounds__(T, 1) k_trials(TrialCtx c, const TrialIn *__restrict__ trials,
-                                                             const int *__restrict__ order, int n, TrialRes *out) {
-  extern __shared__ __align__(16) char t_smem[];
-  if (blockIdx.x >= n) return;
-  const int ti = order ? order[blockIdx.x] : blockIdx.x;
-  const TrialIn tr = trials[ti];
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const TrialSmem sm = carve(t_smem, c.cap, c.smem_win, c.RP, K, c.NM, c.ncode);
-  const int q = tr.q, node = tr.node;
-  const int Sq = c.qlen[q];
-  const int NM = c.NM, nc = c.ncode;
-  // ---- prologue: model constants and the query's sites of darr / parr ----
+__device__ __forceinline__ void trial_cta_setup(const TrialCtx &c, const TrialSmem &sm) {
+  const int tid = threadIdx.x, NM = c.NM, nc = c.ncode;
   for (int i = tid; i < K * K; i += T) sm.X[i] = c.X[i];
   if (K == 4)
     for (int i = tid; i < K * K * K; i += T) sm.W[i] = c.W[i];
   for (int i = tid; i < nc * K; i += T) { sm.Lt[i] = c.Lt[i]; sm.lv[i] = c.lvf[i]; }
   for (int i = tid; i < NM * K; i += T) sm.Lr[i] = c.rates[i / K] * c.lam[i % K];
   if (tid < K) sm.statd[tid] = c.statd[tid];
+}
+
+// One trial by the CTA (after trial_cta_setup); every thread returns the
+// same result.
+template <int K, int T>
+__device__ TrialRes trial_cta(const TrialCtx &c, const TrialSmem &sm, const TrialIn &tr) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int q = tr.q, node = tr.node;
+  const int Sq = c.qlen[q];
+  const int NM = c.NM, nc = c.ncode;
+  __syncthreads();  // the previous trial's readers of the shared state are done
+  // ---- prologue: the query's sites of darr / parr ----
   long long esum = 0;
   const long qo = (long)q * c.S;
   for (int i = tid; i < Sq; i += T) {
@@ -1040,10 +1045,24 @@ __global__ void __launch_bounds__(T, 1) k_trials(TrialCtx c, const TrialIn *__re
     r.status = opt.status;
     r.last = opt.last;
     r.n_evals = opt.n_evals;
-    out[ti] = r;
+    *sm.res = r;
     if (c.stats) {
       atomicAdd(&c.stats[0], (unsigned long long)opt.n_evals);
       atomicAdd(&c.stats[1], (unsigned long long)opt.n_evals * (unsigned long long)Sq);
     }
   }
+  __syncthreads();
+  return *sm.res;
+}
+
+template <int K, int T>
+__global__ void __launch_bounds__(T, 1) k_trials(TrialCtx c, const TrialIn *__restrict__ trials,
+                                                 const int *__restrict__ order, int n, TrialRes *out) {
+  extern __shared__ __align__(16) char t_smem[];
+  if (blockIdx.x >= n) return;
+  const int ti = order ? order[blockIdx.x] : blockIdx.x;
+  const TrialSmem sm = carve(t_smem, c.cap, c.smem_win, c.RP, K, c.NM, c.ncode);
+  trial_cta_setup<K, T>(c, sm);
+  const TrialRes r = trial_cta<K, T>(c, sm, trials[ti]);
+  if (threadIdx.x == 0) out[ti] = r;
 }
