@@ -127,3 +127,26 @@ def test_cat_posterior_probabilities(oracle_lib):
     res, st = eng.place(w.query_seqs, E.default_prefs(calc_pp=1, prior=prior))
     assert list(st) == [0, 0, 0]
     _check_pp(O, oref, w, res, prior, None)
+
+
+def test_round_based_path(oracle_lib):
+    """Bins tuned to different CTA sizes take the round-based path (baseball
+    rounds, k_keep_emit, k_pp_emit, k_finalize) instead of whole queries:
+    placements and posterior probabilities against the oracle."""
+    from pplacer_gb300 import engine as E
+    from pplacer_gb300 import synth
+    O = oracle_lib
+    w = synth.make_workload("cat_5k", n_queries=12, taxa=40, sites=300, lo=100, hi=300)
+    oref = O.Reference(O.Model(w.exch, w.statd, w.rates, w.site_cats), w.parent, w.bl, w.leaf_row, w.ref_seqs)
+    eng = E.engine_for_workload(w)
+    eng.set_tuning([256, 128, 256, 128, 256, 128], [1, 0, 1, 0, 1, 0])
+    ores, ost = oref.place(w.query_seqs, O.make_prefs(), n_threads=8)
+    gres, gst = eng.place(w.query_seqs, E.default_prefs(optimizer=1))
+    assert list(gst) == list(ost)
+    assert eng.timings()[1][7] > 1  # more than one baseball round
+    _compare_placements(O, oref, w.query_seqs, gres, ores)
+    prior = 1
+    res, st = eng.place(w.query_seqs[:3], E.default_prefs(calc_pp=1, prior=prior))
+    assert list(st) == [0, 0, 0]
+    w.query_seqs = w.query_seqs[:3]
+    _check_pp(O, oref, w, res, prior, None)
