@@ -815,178 +815,7 @@ struct PlaceCtx {
   unsigned long long *tstats;  // [0] baseball trials, [1] refinement trials
 };
 
-template <int RP>
-__global__ void __launch_bounds__(32, kWarpTrialMinCtas) k_place_warp(TrialCtx c, PlaceCtx p) {
-  extern __shared__ __align__(16) char t_smem[];
-  const int lane = threadIdx.x & 31;
-  TrialSmem sm;
-  float4 *ring;
-  warp_trial_setup(c, t_smem, sm, ring);
-  const BBCtx &b = p.bb;
-  // One trial call site (the trial code is inlined once): a query moves from
-  // its baseball trials (refine < 0) to the refinement of its kept
-  // locations (refine = index of the next one).
-  int q = -1, next = 0, nres = 0, nk = 0, refine = -1;
-  bool marginal = false;  // the next trial is the marginal likelihood of kept location `refine`
-  long strikes = 0;
-  double record = -INFINITY, pend_hint = b.start_pend;
-  unsigned long long n_bb = 0;
-  for (;;) {
-    if (q < 0) {  // take the next query
-      int qi = 0;
-      if (lane == 0) qi = atomicAdd(p.qnext, 1);
-      qi = __shfl_sync(0xffffffffu, qi, 0);
-      if (qi >= b.Q) break;
-      q = p.qorder[qi];
-      if (lane == 0) p.n_out[q] = 0;
-      if (b.qstatus[q] != PGB_Q_OK || b.rk < 1) { q = -1; continue; }
-      next = 0; nres = 0; nk = 0; refine = -1; strikes = 0; record = -INFINITY; n_bb = 0; marginal = false;
-      pend_hint = b.start_pend;
-    }
-    ResEntry *r = b.res + (long)q * b.maxr;
-    TrialIn t{};
-    t.q = q;
-    int ei = -1;
-    if (refine < 0) {
-      ei = b.rank[(long)q * b.rk + next];
-      t.node = b.edge_nodes[ei];
-      // The Newton form starts the pendant length at the query's best
-      // optimum so far (the optimum, not the path, is its result); the
-      // Brent replica keeps the reference's start.
-      t.pend0 = c.optimizer == 1 ? pend_hint : b.start_pend;
-      t.dist0 = b.bl[t.node] / 2.;
-      t.tol = b.tol;
-    } else {
-      const ResEntry e = r[refine];
-      t.node = b.edge_nodes[e.edge];
-      t.pend0 = e.pend;
-      t.dist0 = e.dist;
-      t.tol = 1e-5;  // final_tolerance (core.ml:160)
-      t.seeded = 1;  // the evaluation at (pend0, dist0); the Newton form does not redo it
-      t.seed = e.ev;
-      if (marginal) {  // after the refinement: e holds the refined optimum
-        t.marginal = 1;
-        t.prior_kind = p.prior_kind;
-        t.prior_mu = p.prior_mu[t.node];
-      }
-    }
-    const TrialRes tr = trial_warp<RP>(c, sm, ring, lane, t);
-    if (refine >= 0) {  // ---- a refined location, or its marginal likelihood ----
-      pgb_placement *o = p.out + (long)q * p.keep_at_most;
-      if (marginal) {
-        if (lane == 0) o[refine].marginal_like = tr.like;
-        marginal = false;
-      } else {
-        const bool ok = !(tr.status == ST_FAILED || tr.status == ST_STARTFAIL);
-        if (lane == 0) {
-          ResEntry e = r[refine];
-          pgb_placement pl;
-          pl.edge = t.node;
-          pl.pad = 0;
-          pl.lwr = 0;
-          pl.marginal_like = NAN;
-          pl.post_prob = NAN;
-          if (!ok) { pl.like = e.like; pl.pend = e.pend; pl.dist = e.dist; }
-          else { pl.like = tr.like; pl.pend = tr.pend; pl.dist = tr.dist; }
-          o[refine] = pl;
-          if (ok && p.calc_pp) {  // the marginal likelihood integrates around the refined optimum
-            e.pend = tr.pend; e.dist = tr.dist; e.ev = tr.last;
-            r[refine] = e;
-          }
-        }
-        __syncwarp();
-        if (p.calc_pp) {
-          marginal = true;
-          continue;
-        }
-      }
-      if (++refine < nk) continue;
-      // like_weight_ratio (and with calc_pp the posterior probabilities,
-      // core.ml:396-401), then stable sort by like_weight_ratio, descending
-      if (lane == 0) {
-        atomicAdd(&p.tstats[1], (unsigned long long)nk);
-        const int m = min(nk, 64);
-        for (int j = 0; j < m; j++) {
-          double tot = 0;
-          for (int k = 0; k < m; k++) tot += exp(o[k].like - o[j].like);
-          o[j].lwr = 1. / tot;
-        }
-        if (p.calc_pp)
-          for (int j = 0; j < m; j++) {
-            double tot = 0;
-            for (int k = 0; k < m; k++) tot += exp(o[k].marginal_like - o[j].marginal_like);
-            o[j].post_prob = 1. / tot;
-          }
-        for (int i = 1; i < m; i++) {
-          pgb_placement x = o[i];
-          int j = i - 1;
-          while (j >= 0 && x.lwr > o[j].lwr) { o[j + 1] = o[j]; j--; }
-          o[j + 1] = x;
-        }
-        p.n_out[q] = m;
-      }
-      __syncwarp();
-      q = -1;
-      continue;
-    }
-    // ---- a baseball result (k_bb_update's rules for one trial) ----
-    n_bb++;
-    next++;
-    bool stop = false;
-    int qst = PGB_Q_OK;
-    if (tr.status == ST_STARTFAIL) {
-      qst = PGB_Q_START_FAILURE;
-      stop = true;
-    } else if (tr.status != ST_FAILED) {  // ST_FAILED: skipped location (core.ml:435-443)
-      const long before = nres;
-      if (nres < b.maxr) {
-        if (lane == 0) {
-          ResEntry e;
-          e.edge = ei; e.status = tr.status; e.like = tr.like; e.pend = tr.pend; e.dist = tr.dist; e.ev = tr.last;
-          r[nres] = e;
-        }
-        nres++;
-      }
-      if (before >= b.max_pitches) stop = true;
-      else if (tr.like > record) {
-        record = tr.like;
-        if (tr.pend > 1e-6 && tr.pend < c.max_pend) pend_hint = tr.pend;
-      }
-      else if (tr.like < record - b.strike_box) {
-        if (strikes + 1 >= b.max_strikes) stop = true;
-        else strikes++;
-      }
-    }
-    if (!stop && next < b.rk) continue;
-    if (lane == 0) atomicAdd(&p.tstats[0], n_bb);
-    if (qst != PGB_Q_OK || nres == 0) {
-      if (lane == 0) b.qstatus[q] = qst != PGB_Q_OK ? qst : PGB_Q_EMPTY;
-      __syncwarp();
-      q = -1;
-      continue;
-    }
-    // ---- keep: stable sort by like, descending, NaN last ----
-    __syncwarp();
-    if (lane == 0)
-      for (int i = 1; i < nres; i++) {
-        ResEntry x = r[i];
-        int j = i - 1;
-        while (j >= 0 && (isnan(r[j].like) ? !isnan(x.like) : (!isnan(x.like) && x.like > r[j].like))) {
-          r[j + 1] = r[j];
-          j--;
-        }
-        r[j + 1] = x;
-      }
-    __syncwarp();
-    const double best = r[0].like;
-    nk = 0;
-    while (nk < nres && nk < p.keep_at_most && r[nk].like >= p.log_keep_factor + best) nk++;
-    if (nk == 0) { q = -1; continue; }
-    refine = 0;
-  }
-}
-
-// The whole-query search of k_place_warp for any team of threads that runs
+// The whole-query search for any team of threads that runs
 // one trial at a time: Team::leader() is the one thread that writes results,
 // Team::sync() orders its writes before the team's reads, Team::bcast(v) is
 // the leader's v in every thread, Team::trial(t) the trial's result
@@ -1155,6 +984,30 @@ __device__ __forceinline__ void place_queries(Team &tm, const TrialCtx &c, const
     if (nk == 0) { q = -1; continue; }
     refine = 0;
   }
+}
+
+// A warp as a team (nucleotide Gamma mixtures): lane 0 leads.
+template <int RP>
+struct WarpTeam {
+  const TrialCtx &c;
+  const TrialSmem &sm;
+  float4 *ring;
+  int lane;
+  __device__ bool leader() const { return lane == 0; }
+  __device__ void sync() const { __syncwarp(); }
+  __device__ int bcast(int v) const { return __shfl_sync(0xffffffffu, v, 0); }
+  __device__ TrialRes trial(const TrialIn &t) { return trial_warp<RP>(c, sm, ring, lane, t); }
+  __device__ bool aborted() const { return false; }
+};
+
+template <int RP>
+__global__ void __launch_bounds__(32, kWarpTrialMinCtas) k_place_warp(TrialCtx c, PlaceCtx p) {
+  extern __shared__ __align__(16) char t_smem[];
+  TrialSmem sm;
+  float4 *ring;
+  warp_trial_setup(c, t_smem, sm, ring);
+  WarpTeam<RP> tm{c, sm, ring, (int)(threadIdx.x & 31)};
+  place_queries(tm, c, p);
 }
 
 // The tensor-core CTA as a team: thread 0 leads, the CTA's barriers order,
