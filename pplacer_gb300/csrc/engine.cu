@@ -793,14 +793,15 @@ __global__ void k_finalize(BBCtx c, int keep_at_most, const int *__restrict__ ke
 }
 
 // ---------------------------------------------------------------------------
-// Whole queries, one per warp (nucleotide Gamma mixtures): the baseball
-// search over the stage-1 ranking (core.ml:429-464), keep (core.ml:482-496),
-// refinement from the kept optima (core.ml:497-523) and like_weight_ratio
-// (pquery.ml:8-9).  A query's trials run in rank order inside its warp, each
-// decided before the next starts, so nothing is evaluated speculatively and
-// no host round trip separates the trials; queries come from a counter,
-// longest first.  The decisions are those of k_bb_update / k_keep_emit /
-// k_finalize for one result at a time.
+// Whole queries, one per team -- a warp (nucleotide Gamma mixtures), a
+// tensor-core CTA (20 states) or a CUDA-core CTA: the baseball search over
+// the stage-1 ranking (core.ml:429-464), keep (core.ml:482-496), refinement
+// from the kept optima (core.ml:497-523), the marginal likelihoods with
+// calc_pp and like_weight_ratio (pquery.ml:8-9).  A query's trials run in
+// rank order inside its team, each decided before the next starts, so
+// nothing is evaluated speculatively and no host round trip separates the
+// trials; queries come from a counter, longest first.  The decisions are
+// those of k_bb_update / k_keep_emit / k_finalize for one result at a time.
 // ---------------------------------------------------------------------------
 struct PlaceCtx {
   BBCtx bb;
@@ -1059,7 +1060,7 @@ __global__ void __launch_bounds__(T, 1) k_place_cta(TrialCtx c, PlaceCtx p) {
 }
 
 // Whole queries, one per CTA of the tensor-core trial kernel (20-state
-// Gamma mixtures): the search of k_place_warp with each trial run by the CTA.
+// Gamma mixtures): the shared search with each trial run by the CTA.
 __global__ void __launch_bounds__(kTcThreads, 1) k_place_tc(TrialCtx c, PlaceCtx p) {
   extern __shared__ __align__(16) char t_smem[];
   const int tid = threadIdx.x;
