@@ -314,10 +314,14 @@ pgb_status pgb_queries_trials(pgb_engine *e, const pgb_prefs *prefs, int optimiz
  * 128 or 256 threads per trial with the query's sites of darr / parr staged
  * in shared memory or read from L2, and for 20-state Gamma mixtures the
  * tensor-core CTA (tcgen05 evolves, 128 threads), on the loaded queries'
- * first baseball round, and keep the fastest for later runs.  get_tuning
- * reports the table (threads[6], smem_windows[6]); set_tuning imposes one
- * (threads 1 = tensor-core CTA, 32, 128 or 256; smem_windows 0 or 1).
- * threads 32 in every bin selects the whole-query warp kernel; where the warp
+ * first baseball round; then time the whole round for that choice and for
+ * each uniform form, and keep the fastest one with a single CTA size in every
+ * bin for later runs.  get_tuning reports the table (threads[6],
+ * smem_windows[6]); set_tuning imposes one (threads 1 = tensor-core CTA, 32,
+ * 128 or 256; smem_windows 0 or 1).  When every bin has the same threads,
+ * pgb_queries_run places whole queries in one persistent launch (a warp, a
+ * tensor-core CTA or a CTA per query, windows as bin 0 says); otherwise it
+ * runs the baseball in speculative rounds of per-trial CTAs.  Where the warp
  * or tensor-core form does not apply it falls back to 256.  20-state Gamma
  * mixtures start with the tensor-core form.  No reference counterpart:
  * pplacer has one CPU code path. */

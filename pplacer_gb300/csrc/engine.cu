@@ -2503,12 +2503,20 @@ pgb_status pgb_engine_autotune(pgb_engine *e, const pgb_prefs *p) {
   // In a run the bins execute concurrently, so a form that loses on a bin
   // alone can win on the whole round (its tail overlaps the other bins).
   // Time the whole round for the per-bin choice and for each uniform form.
+  // Only forms with one CTA size in every bin are kept: those run as whole
+  // queries (no speculative rounds), which the round timing understates.
   int per_bin_t[kBins], per_bin_w[kBins];
-  for (int b = 0; b < kBins; b++) { per_bin_t[b] = e->tune_threads[b]; per_bin_w[b] = e->tune_win[b]; }
+  bool per_bin_uniform = true;
+  for (int b = 0; b < kBins; b++) {
+    per_bin_t[b] = e->tune_threads[b];
+    per_bin_w[b] = e->tune_win[b];
+    if (per_bin_t[b] != per_bin_t[0]) per_bin_uniform = false;
+  }
   const int uni_t[4] = {32, kTuneTc, 128, 256}, uni_w[4] = {0, 0, 1, 1};
   float best = 1e30f;
-  int best_cfg = -1;
+  int best_cfg = -2;
   for (int cfg = -1; cfg < 4; cfg++) {
+    if (cfg == -1 && !per_bin_uniform) continue;
     if (cfg == 0 && !warp_trials_ok(e)) continue;
     if (cfg == 1 && !tc_trials_ok(e)) continue;
     for (int b = 0; b < kBins; b++) {
@@ -2531,7 +2539,7 @@ pgb_status pgb_engine_autotune(pgb_engine *e, const pgb_prefs *p) {
     e->tune_threads[b] = best_cfg < 0 ? per_bin_t[b] : uni_t[best_cfg];
     e->tune_win[b] = best_cfg < 0 ? per_bin_w[b] : uni_w[best_cfg];
   }
-  return PGB_OK;
+  return check_tc_err(e);
 }
 
 pgb_status pgb_engine_get_tuning(pgb_engine *e, int *threads, int *smem_windows) {
