@@ -140,8 +140,9 @@ class ClockSampler:
 def stage2_kernel(w, tune):
     """The trial kernel that ran stage 2 + refinement for this workload and tuning."""
     th = set(int(v) for v in tune[0])
-    if w.K == 4 and w.site_cats is None and th == {32}:
-        return "k_place_warp (stage 2 + refinement, whole queries, one warp each)"
+    if th == {32}:
+        return "k_place_warp (stage 2 + refinement, whole queries, one warp each%s)" % (
+            ", per-site categories" if w.site_cats is not None else "")
     if th == {1}:
         return "k_place_tc (stage 2 + refinement, whole queries, one CTA each, tcgen05 evolves)"
     if len(th) == 1:

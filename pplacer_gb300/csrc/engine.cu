@@ -278,10 +278,12 @@ __global__ void k_snodes_from(const double *__restrict__ d, const double *__rest
 // pass the columns grouped by category, so that a query's informative sites
 // come grouped by category and neighbouring trial threads read the same
 // category's matrices (the site order changes only FP32 summation order).
+// The packed word of a site is (category << 24) | (column << 8) | code, the
+// category byte from site_cat (CAT models) or 0.
 __global__ void k_query_prep(const char *__restrict__ seqs, int S, int prim, const uint8_t *__restrict__ char_code,
                              const uint8_t *__restrict__ informative, const uint16_t *__restrict__ order,
-                             uint8_t *qcode, uint16_t *reind, uint8_t *mcode, uint32_t *rcode, int *qlen,
-                             int *qstatus, int *qamb) {
+                             const uint8_t *__restrict__ site_cat, uint8_t *qcode, uint16_t *reind, uint8_t *mcode,
+                             uint32_t *rcode, int *qlen, int *qstatus, int *qamb) {
   int q = blockIdx.x;
   const char *seq = seqs + (long)q * S;
   __shared__ int s_off;
@@ -315,7 +317,7 @@ __global__ void k_query_prep(const char *__restrict__ seqs, int S, int prim, con
       int pos = s_off + before + __popc(bal & ((1u << lane) - 1u));
       reind[(long)q * S + pos] = (uint16_t)s;
       mcode[(long)q * S + pos] = c;
-      rcode[(long)q * S + pos] = ((uint32_t)s << 8) | c;
+      rcode[(long)q * S + pos] = (site_cat ? (uint32_t)site_cat[s] << 24 : 0u) | ((uint32_t)s << 8) | c;
     }
     __syncthreads();
     if (threadIdx.x == 0) s_off += tot;
@@ -987,8 +989,8 @@ __device__ __forceinline__ void place_queries(Team &tm, const TrialCtx &c, const
   }
 }
 
-// A warp as a team (nucleotide Gamma mixtures): lane 0 leads.
-template <int RP>
+// A warp as a team (nucleotide Gamma mixtures, CAT): lane 0 leads.
+template <int RP, bool CAT>
 struct WarpTeam {
   const TrialCtx &c;
   const TrialSmem &sm;
@@ -997,17 +999,17 @@ struct WarpTeam {
   __device__ bool leader() const { return lane == 0; }
   __device__ void sync() const { __syncwarp(); }
   __device__ int bcast(int v) const { return __shfl_sync(0xffffffffu, v, 0); }
-  __device__ TrialRes trial(const TrialIn &t) { return trial_warp<RP>(c, sm, ring, lane, t); }
+  __device__ TrialRes trial(const TrialIn &t) { return trial_warp<RP, CAT>(c, sm, ring, lane, t); }
   __device__ bool aborted() const { return false; }
 };
 
-template <int RP>
+template <int RP, bool CAT = false>
 __global__ void __launch_bounds__(32, kWarpTrialMinCtas) k_place_warp(TrialCtx c, PlaceCtx p) {
   extern __shared__ __align__(16) char t_smem[];
   TrialSmem sm;
   float4 *ring;
   warp_trial_setup(c, t_smem, sm, ring);
-  WarpTeam<RP> tm{c, sm, ring, (int)(threadIdx.x & 31)};
+  WarpTeam<RP, CAT> tm{c, sm, ring, (int)(threadIdx.x & 31)};
   place_queries(tm, c, p);
 }
 
@@ -1391,17 +1393,27 @@ pgb_status launch_trials_kt(pgb_engine *e, cudaStream_t st, TrialCtx c, const in
 }
 
 // the warp-per-trial kernel covers nucleotide Gamma mixtures of 1, 2, 4 or 8 rates
+// the warp-per-trial kernel for per-site CAT models (one GLV plane), when
+// the categories' tables fit the shared memory of a one-warp CTA
+bool warp_cat_ok(const pgb_engine *e) {
+  return e->K == 4 && e->gcat && e->RP == 1 && e->NM <= 255 &&
+         warp_trial_smem_bytes(e->NM, e->ncode) <= e->smem_optin;
+}
+
 bool warp_trials_ok(const pgb_engine *e) {
   return e->K == 4 && !e->gcat && e->NM == e->RP && (e->RP == 1 || e->RP == 2 || e->RP == 4 || e->RP == 8);
 }
 
-template <int RP>
+// one warp per trial applies (Gamma mixtures or CAT)
+bool warp_form_ok(const pgb_engine *e) { return warp_trials_ok(e) || warp_cat_ok(e); }
+
+template <int RP, bool CAT = false>
 pgb_status launch_trials_warp_rp(pgb_engine *e, cudaStream_t st, TrialCtx c, const WarpSegs &segs, TrialRes *out) {
   size_t smem = warp_trial_smem_bytes(e->NM, e->ncode);
   if (smem > e->smem_optin) { set_error("warp trial shared memory %zu exceeds %zu", smem, e->smem_optin); return PGB_ERR_ARG; }
-  PGB_CUDA(cudaFuncSetAttribute(k_trials_warp<RP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  PGB_CUDA(cudaFuncSetAttribute(k_trials_warp<RP, CAT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int grid = (segs.n + kWarpTrialWarps - 1) / kWarpTrialWarps;
-  k_trials_warp<RP><<<grid, 32 * kWarpTrialWarps, smem, st>>>(c, e->d_trials, segs, out);
+  k_trials_warp<RP, CAT><<<grid, 32 * kWarpTrialWarps, smem, st>>>(c, e->d_trials, segs, out);
   PGB_LAUNCH_CHECK();
   return PGB_OK;
 }
@@ -1410,6 +1422,7 @@ pgb_status launch_trials_warp(pgb_engine *e, cudaStream_t st, TrialCtx c, const 
   if (segs.nseg < 1 || segs.n <= 0) return PGB_OK;
   c.smem_win = 0;
   c.cap = 0;
+  if (e->gcat) return launch_trials_warp_rp<1, true>(e, st, c, segs, out);
   switch (e->RP) {
     case 1: return launch_trials_warp_rp<1>(e, st, c, segs, out);
     case 2: return launch_trials_warp_rp<2>(e, st, c, segs, out);
@@ -1478,7 +1491,7 @@ pgb_status launch_trials(pgb_engine *e, cudaStream_t st, TrialCtx c, const int *
     threads = 256;
   }
   if (threads == 32) {
-    if (warp_trials_ok(e)) {
+    if (warp_form_ok(e)) {
       WarpSegs segs{};
       segs.list[0] = d_order;
       segs.start[0] = 0;
@@ -1509,7 +1522,7 @@ void bin_shape(const pgb_engine *e, int b, int max_sq, int allow_win, int *cap, 
 // Launch every non-empty bin of the trial lists, concurrently (one stream
 // each, longest windows first), and join them on the engine stream.
 pgb_status run_bins(pgb_engine *e, TrialCtx c, const int *h_bin_count, int max_sq) {
-  bool all_warp = warp_trials_ok(e);
+  bool all_warp = warp_form_ok(e);
   for (int b = 0; b < kBins; b++)
     if (h_bin_count[b] > 0 && e->tune_threads[b] != 32) all_warp = false;
   if (all_warp) {  // one launch over every bin, longest bin first
@@ -1618,14 +1631,14 @@ pgb_status ensure_prior_means(pgb_engine *e, int prior, double prior_lower) {
   return PGB_OK;
 }
 
-template <int RP>
+template <int RP, bool CAT = false>
 pgb_status launch_place_warp_rp(pgb_engine *e, TrialCtx c, const PlaceCtx &pc) {
   size_t smem = warp_trial_smem_bytes(e->NM, e->ncode);
-  PGB_CUDA(cudaFuncSetAttribute(k_place_warp<RP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  PGB_CUDA(cudaFuncSetAttribute(k_place_warp<RP, CAT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int per_sm = 0;
-  PGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_place_warp<RP>, 32, smem));
+  PGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_place_warp<RP, CAT>, 32, smem));
   int grid = std::max(1, std::min(e->Q, e->n_sm * std::max(1, per_sm)));
-  k_place_warp<RP><<<grid, 32, smem, e->st>>>(c, pc);
+  k_place_warp<RP, CAT><<<grid, 32, smem, e->st>>>(c, pc);
   PGB_LAUNCH_CHECK();
   return PGB_OK;
 }
@@ -1699,7 +1712,7 @@ bool whole_query_form(const pgb_engine *e) {
   for (int b = 1; b < kBins; b++)
     if (e->tune_threads[b] != e->tune_threads[0]) return false;
   const int t = e->tune_threads[0];
-  if (t == 32) return warp_trials_ok(e);
+  if (t == 32) return warp_form_ok(e);
   if (t == kTuneTc) return tc_trials_ok(e);
   return t == 128 || t == 256;
 }
@@ -1733,7 +1746,8 @@ pgb_status run_whole_queries(pgb_engine *e, const pgb_prefs *p, const BBCtx &c, 
   if ((s = ensure_prior_means(e, p->prior, p->prior_lower))) return s;
   pc.prior_mu = e->d_prior_mu;
   if (e->tune_threads[0] == kTuneTc && tc_trials_ok(e)) s = launch_place_tc(e, tc, pc, max_sq);
-  else if (e->tune_threads[0] != 32 || !warp_trials_ok(e)) s = launch_place_cta(e, tc, pc, max_sq);
+  else if (e->tune_threads[0] != 32 || !warp_form_ok(e)) s = launch_place_cta(e, tc, pc, max_sq);
+  else if (e->gcat) s = launch_place_warp_rp<1, true>(e, tc, pc);
   else
     switch (e->RP) {
       case 1: s = launch_place_warp_rp<1>(e, tc, pc); break;
@@ -1782,6 +1796,8 @@ void pgb_prefs_default(pgb_prefs *p) {
   p->pp_rel_err = 0.01;
   p->prior_lower = 0.0;
 }
+
+static pgb_status prep_queries(pgb_engine *e);
 
 // CAT models: the alignment columns sorted by (category, column) -- the
 // order in which k_query_prep lists a query's sites
@@ -1874,7 +1890,7 @@ pgb_status pgb_engine_create(const pgb_model_desc *m, const pgb_tree_desc *t, pg
   cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, e->device);
   cudaDeviceGetAttribute(&e->n_sm, cudaDevAttrMultiProcessorCount, e->device);
   e->smem_optin = (size_t)optin;
-  if (warp_trials_ok(e))  // one warp per trial unless the autotuner finds better
+  if (warp_form_ok(e))  // one warp per trial unless the autotuner finds better
     for (int b = 0; b < kBins; b++) { e->tune_threads[b] = 32; e->tune_win[b] = 0; }
   if (tc_trials_ok(e))  // tensor-core CTAs unless the autotuner finds better
     for (int b = 0; b < kBins; b++) { e->tune_threads[b] = kTuneTc; e->tune_win[b] = 0; }
@@ -2168,7 +2184,8 @@ pgb_status pgb_engine_refine_categories(pgb_engine *e, const int *leaf_row, cons
   std::vector<uint8_t> sc(S);
   for (int i = 0; i < S; i++) sc[i] = (uint8_t)best[i];
   PGB_CUDA(cudaMemcpyAsync(e->d_site_cat, sc.data(), S, cudaMemcpyHostToDevice, e->st));
-  pgb_status us = upload_col_order(e);  // queries loaded from now on follow the new grouping
+  pgb_status us = upload_col_order(e);  // the site lists follow the new categories
+  if (!us) us = prep_queries(e);
   if (us) return us;
   PGB_CUDA(cudaStreamSynchronize(e->st));
   e->glvs_ready = false;  // the placement GLVs follow the categories: precompute again
@@ -2238,6 +2255,18 @@ pgb_status pgb_engine_get_glv(pgb_engine *e, int which, int node, double *a, int
   return PGB_OK;
 }
 
+// the per-query site lists of the loaded sequences (d_seqs), in the order and
+// with the categories of the current model
+static pgb_status prep_queries(pgb_engine *e) {
+  if (e->Q < 1) return PGB_OK;
+  k_query_prep<<<e->Q, 256, 0, e->st>>>(e->d_seqs, e->S, e->prim, e->d_char_code, e->d_informative,
+                                        e->gcat ? e->d_col_order : nullptr, e->gcat ? e->d_site_cat : nullptr,
+                                        e->d_qcode, e->d_reind, e->d_mcode, e->d_rcode, e->d_qlen, e->d_qstatus,
+                                        e->d_qamb);
+  PGB_LAUNCH_CHECK();
+  return PGB_OK;
+}
+
 pgb_status pgb_queries_load(pgb_engine *e, int n_queries, const char *seqs) {
   if (!e || n_queries < 0 || (n_queries > 0 && !seqs)) { set_error("queries_load: bad argument"); return PGB_ERR_ARG; }
   pgb_status s = ensure_queries(e, std::max(n_queries, 1));
@@ -2245,10 +2274,7 @@ pgb_status pgb_queries_load(pgb_engine *e, int n_queries, const char *seqs) {
   e->Q = n_queries;
   if (!n_queries) return PGB_OK;
   PGB_CUDA(cudaMemcpyAsync(e->d_seqs, seqs, (size_t)n_queries * e->S, cudaMemcpyHostToDevice, e->st));
-  k_query_prep<<<n_queries, 256, 0, e->st>>>(e->d_seqs, e->S, e->prim, e->d_char_code, e->d_informative,
-                                             e->gcat ? e->d_col_order : nullptr, e->d_qcode, e->d_reind,
-                                             e->d_mcode, e->d_rcode, e->d_qlen, e->d_qstatus, e->d_qamb);
-  PGB_LAUNCH_CHECK();
+  if ((s = prep_queries(e))) return s;
   e->h_qlen.resize(n_queries);
   PGB_CUDA(cudaMemcpyAsync(e->h_qlen.data(), e->d_qlen, (size_t)n_queries * 4, cudaMemcpyDeviceToHost, e->st));
   e->h_qamb.resize(n_queries);
@@ -2477,7 +2503,7 @@ pgb_status pgb_engine_autotune(pgb_engine *e, const pgb_prefs *p) {
       for (int w = 1; w >= 0; w--) {
         int cap;
         bool win;
-        if (cand_threads[ti] == 32 && !warp_trials_ok(e)) continue;
+        if (cand_threads[ti] == 32 && !warp_form_ok(e)) continue;
         if (cand_threads[ti] == kTuneTc && !tc_trials_ok(e)) continue;
         // the warp and tensor-core kernels read the windows from L2
         if ((cand_threads[ti] == 32 || cand_threads[ti] == kTuneTc) && w == 1) continue;
@@ -2517,7 +2543,7 @@ pgb_status pgb_engine_autotune(pgb_engine *e, const pgb_prefs *p) {
   int best_cfg = -2;
   for (int cfg = -1; cfg < 4; cfg++) {
     if (cfg == -1 && !per_bin_uniform) continue;
-    if (cfg == 0 && !warp_trials_ok(e)) continue;
+    if (cfg == 0 && !warp_form_ok(e)) continue;
     if (cfg == 1 && !tc_trials_ok(e)) continue;
     for (int b = 0; b < kBins; b++) {
       e->tune_threads[b] = cfg < 0 ? per_bin_t[b] : uni_t[cfg];

@@ -49,7 +49,7 @@ struct TrialCtx {
   const double *bl;
   const uint16_t *reind;
   const uint8_t *mcode;
-  const uint32_t *rcode;  // (column << 8) | code
+  const uint32_t *rcode;  // (category << 24) | (column << 8) | code; category 0 but for CAT
   const int *qamb;        // informative ambiguity characters per query
   int prim;               // primary (one-hot) character codes: 0 .. prim - 1
   const int *qlen;

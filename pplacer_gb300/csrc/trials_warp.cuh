@@ -1,5 +1,6 @@
 // Stage-2 trials, one WARP per (query, location) optimisation: the form for
-// nucleotide models with Gamma rate mixtures (K = 4, RP = 1, 2, 4 or 8 rates).
+// nucleotide models with Gamma rate mixtures (K = 4, RP = 1, 2, 4 or 8 rates)
+// and with per-site CAT categories (sites_warp_cat).
 // Included by engine.cu after trials.cuh, inside its anonymous namespace.
 //
 // The CTA-per-trial kernel (trials.cuh) stages the query's sites in shared
@@ -224,6 +225,95 @@ __device__ __forceinline__ void sites_warp(const TrialCtx &c, const TrialSmem &s
   cp_async_wait<0>();  // drain the copies issued past the end
 }
 
+// Sites of a per-site CAT model (Gcat_model, one GLV plane): lane = site,
+// 32 sites per iteration, the windows streamed through the same cp.async
+// ring.  A site's matrices are those of its category (the packed word's top
+// byte) and are read from the shared tables in every iteration: a query's
+// sites come grouped by category (k_query_prep), so the lanes of an
+// iteration mostly read one category's matrices as a broadcast.
+template <bool DER>
+__device__ __forceinline__ void sites_warp_cat(const TrialCtx &c, const TrialSmem &sm, float4 *ring, int q, int node,
+                                               int Sq, int lane, SiteAcc &acc) {
+  constexpr int K = 4;
+  const int nc = c.ncode;
+  const float *gd = c.darr + (long)node * c.S * K;
+  const float *gp = c.parr + (long)node * c.S * K;
+  const uint32_t *rc = c.rcode + (long)q * c.S;
+  const int last = Sq - 1;
+  // byte k of cq / kq: the character / category of the k-th next iteration
+  unsigned long long cq = 0ull, kq = 0ull;
+  auto issue = [&](int stage, uint32_t pk) {
+    const long col = (long)((pk >> 8) & 0xffffu);
+    cp_async16(ring + (stage * 32 + lane), gd + col * K);
+    cp_async16(ring + ((kWarpRing + stage) * 32 + lane), gp + col * K);
+    cp_async_commit();
+  };
+#pragma unroll
+  for (int j = 0; j < kWarpRing - 1; j++) {
+    const uint32_t pk = rc[min(j * 32 + lane, last)];
+    issue(j, pk);
+    cq |= (unsigned long long)(pk & 255u) << (8 * j);
+    kq |= (unsigned long long)(pk >> 24) << (8 * j);
+  }
+  uint32_t pk_next = rc[min((kWarpRing - 1) * 32 + lane, last)];
+  uint32_t pk_next2 = rc[min(kWarpRing * 32 + lane, last)];
+  int st = 0;
+  for (int base = 0; base < Sq; base += 32) {
+    issue((st + kWarpRing - 1) & (kWarpRing - 1), pk_next);
+    cq |= (unsigned long long)(pk_next & 255u) << (8 * (kWarpRing - 1));
+    kq |= (unsigned long long)(pk_next >> 24) << (8 * (kWarpRing - 1));
+    const int code = (int)(cq & 255ull), cat = (int)(kq & 255ull);
+    cq >>= 8;
+    kq >>= 8;
+    pk_next = pk_next2;
+    pk_next2 = rc[min(base + 32 + kWarpRing * 32 + lane, last)];
+    cp_async_wait<kWarpRing - 1>();  // this iteration's copies have landed
+    const float4 dcur = ring[st * 32 + lane];
+    const float4 pcur = ring[(kWarpRing + st) * 32 + lane];
+    st = (st + 1) & (kWarpRing - 1);
+    const float dv[4] = {dcur.x, dcur.y, dcur.z, dcur.w}, pv[4] = {pcur.x, pcur.y, pcur.z, pcur.w};
+    const float *Md = sm.Md + cat * 16, *Mp = sm.Mp + cat * 16;
+    const float4 Z4 = *reinterpret_cast<const float4 *>(sm.Z + (cat * nc + code) * K);
+    const float z[4] = {Z4.x, Z4.y, Z4.z, Z4.w};
+    float z1[4], z2[4];
+    if (DER) {
+      const float4 a = *reinterpret_cast<const float4 *>(sm.Z1 + (cat * nc + code) * K);
+      const float4 b = *reinterpret_cast<const float4 *>(sm.Z2 + (cat * nc + code) * K);
+      z1[0] = a.x; z1[1] = a.y; z1[2] = a.z; z1[3] = a.w;
+      z2[0] = b.x; z2[1] = b.y; z2[2] = b.z; z2[3] = b.w;
+    }
+    float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+    for (int ii = 0; ii < 4; ii++) {
+      const float4 a = *reinterpret_cast<const float4 *>(Md + ii * 4);
+      const float4 b = *reinterpret_cast<const float4 *>(Mp + ii * 4);
+      const float x = a.x * dv[0] + a.y * dv[1] + a.z * dv[2] + a.w * dv[3];
+      const float y = b.x * pv[0] + b.y * pv[1] + b.z * pv[2] + b.w * pv[3];
+      const float xy = x * y;
+      v[0] = fmaf(z[ii], xy, v[0]);
+      if (DER) {
+        const float4 a1 = *reinterpret_cast<const float4 *>(sm.Md1 + cat * 16 + ii * 4);
+        const float4 a2 = *reinterpret_cast<const float4 *>(sm.Md2 + cat * 16 + ii * 4);
+        const float4 b1 = *reinterpret_cast<const float4 *>(sm.Mp1 + cat * 16 + ii * 4);
+        const float4 b2 = *reinterpret_cast<const float4 *>(sm.Mp2 + cat * 16 + ii * 4);
+        const float x1 = a1.x * dv[0] + a1.y * dv[1] + a1.z * dv[2] + a1.w * dv[3];
+        const float x2 = a2.x * dv[0] + a2.y * dv[1] + a2.z * dv[2] + a2.w * dv[3];
+        const float y1 = b1.x * pv[0] + b1.y * pv[1] + b1.z * pv[2] + b1.w * pv[3];
+        const float y2 = b2.x * pv[0] + b2.y * pv[1] + b2.z * pv[2] + b2.w * pv[3];
+        const float aa = x1 * y - x * y1;
+        const float bb = x2 * y - 2.f * x1 * y1 + x * y2;
+        v[1] = fmaf(z[ii], aa, v[1]);
+        v[2] = fmaf(z[ii], bb, v[2]);
+        v[3] = fmaf(z1[ii], xy, v[3]);
+        v[4] = fmaf(z2[ii], xy, v[4]);
+        v[5] = fmaf(z1[ii], aa, v[5]);
+      }
+    }
+    if (base + lane < Sq) acc.add(v[0], v[1], v[2], v[3], v[4], v[5], DER);
+  }
+  cp_async_wait<0>();  // drain the copies issued past the end
+}
+
 // Per-CTA constants and this warp's tables and ring; returns after a block
 // barrier, the only one the warp kernels take.
 __device__ __forceinline__ void warp_trial_setup(const TrialCtx &c, char *t_smem, TrialSmem &sm, float4 *&ring) {
@@ -258,7 +348,7 @@ __device__ __forceinline__ void warp_trial_setup(const TrialCtx &c, char *t_smem
 // One trial (Three_tax.optimize at one location) by the calling warp.  Every
 // lane runs the same optimiser on the same all-reduced values and returns
 // the same result.
-template <int RP>
+template <int RP, bool CAT = false>
 __device__ TrialRes trial_warp(const TrialCtx &c, const TrialSmem &sm, float4 *ring, int lane, const TrialIn &tr) {
   constexpr int K = 4;
   const int NM = c.NM, nc = c.ncode;
@@ -336,8 +426,13 @@ __device__ TrialRes trial_warp(const TrialCtx &c, const TrialSmem &sm, float4 *r
     SiteAcc acc;
     acc.init();
     if (Sq > 0) {
-      if (derivs) sites_warp<RP, true>(c, sm, ring, q, node, Sq, lane, acc);
-      else sites_warp<RP, false>(c, sm, ring, q, node, Sq, lane, acc);
+      if (CAT) {
+        if (derivs) sites_warp_cat<true>(c, sm, ring, q, node, Sq, lane, acc);
+        else sites_warp_cat<false>(c, sm, ring, q, node, Sq, lane, acc);
+      } else {
+        if (derivs) sites_warp<RP, true>(c, sm, ring, q, node, Sq, lane, acc);
+        else sites_warp<RP, false>(c, sm, ring, q, node, Sq, lane, acc);
+      }
     }
     // xor all-reduce: every lane ends with the same bits
 #pragma unroll
@@ -382,7 +477,7 @@ __device__ TrialRes trial_warp(const TrialCtx &c, const TrialSmem &sm, float4 *r
 }
 
 // A batch of independent trials, one per warp.
-template <int RP>
+template <int RP, bool CAT = false>
 __global__ void __launch_bounds__(32 * kWarpTrialWarps, kWarpTrialMinCtas)
     k_trials_warp(TrialCtx c, const TrialIn *__restrict__ trials, WarpSegs segs, TrialRes *out) {
   extern __shared__ __align__(16) char t_smem[];
@@ -399,6 +494,6 @@ __global__ void __launch_bounds__(32 * kWarpTrialWarps, kWarpTrialMinCtas)
   for (int k = 1; k < 8; k++)
     if (k < segs.nseg && t >= segs.start[k]) { lst = segs.list[k]; s0 = segs.start[k]; }
   const int ti = lst ? lst[t - s0] : t - s0;
-  const TrialRes rr = trial_warp<RP>(c, sm, ring, lane, trials[ti]);
+  const TrialRes rr = trial_warp<RP, CAT>(c, sm, ring, lane, trials[ti]);
   if (lane == 0) out[ti] = rr;
 }

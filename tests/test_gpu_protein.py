@@ -150,3 +150,38 @@ def test_round_based_path(oracle_lib):
     assert list(st) == [0, 0, 0]
     w.query_seqs = w.query_seqs[:3]
     _check_pp(O, oref, w, res, prior, None)
+
+
+@pytest.mark.parametrize("form", [(32, 0), (128, 1)], ids=["warp", "cta"])
+def test_cat_forms(oracle_lib, form):
+    """Per-site CAT placements in the whole-query warp form (sites_warp_cat:
+    each lane's site reads its category's matrices) and the whole-query CTA
+    form, against the oracle; queries long enough to span many categories."""
+    from pplacer_gb300 import engine as E
+    from pplacer_gb300 import synth
+    O = oracle_lib
+    w = synth.make_workload("cat_5k", n_queries=30, taxa=120, sites=600, lo=100, hi=600)
+    oref = O.Reference(O.Model(w.exch, w.statd, w.rates, w.site_cats), w.parent, w.bl, w.leaf_row, w.ref_seqs)
+    ores, ost = oref.place(w.query_seqs, O.make_prefs(), n_threads=8)
+    eng = E.engine_for_workload(w)
+    eng.set_tuning(*form)
+    gres, gst = eng.place(w.query_seqs, E.default_prefs(optimizer=1))
+    assert list(gst) == list(ost)
+    _compare_placements(O, oref, w.query_seqs, gres, ores)
+    # the fixed-point likelihood and derivatives of the warp trials
+    eng.load_queries(w.query_seqs)
+    rng = np.random.default_rng(3)
+    edges = np.where(w.parent >= 0)[0]
+    trials = []
+    for _ in range(30):
+        q = int(rng.integers(len(w.query_seqs)))
+        e = int(rng.choice(edges))
+        trials.append((q, e, float(rng.uniform(1e-8, 0.5)), float(rng.uniform(0, w.bl[e])), 0.01))
+    got = eng.trials(trials, optimizer=E.NEWTON, mode=1)
+    for (q, e, p, d, _), g in zip(trials, got):
+        st, ref = oref.loglike_derivs(w.query_seqs[q], e, p, d)
+        assert abs(g["like"] - ref[0]) <= 2e-7 * abs(ref[0]), (q, e, g["like"], ref[0])
+        hscale = math.sqrt(abs(ref[3] * ref[4])) + 1.0
+        for k, (gv, rv) in enumerate(zip(g["derivs"][:5], ref[1:6])):
+            tol = 2e-3 * abs(rv) + (1e-5 * abs(ref[3 + k]) + 1e-2 if k < 2 else 1e-3 * hscale + 1.0)
+            assert abs(gv - rv) <= tol, (k, gv, rv)
