@@ -308,7 +308,8 @@ pgb_status pgb_queries_trials(pgb_engine *e, const pgb_prefs *prefs, int optimiz
 /* Autotuner of the stage-2 trial kernel.  Nucleotide models whose Gamma
  * mixture has 1, 2, 4 or 8 rates always use the whole-query warp kernel (one
  * warp runs a query's baseball trials, keep and refinement); autotune sets
- * that and returns.  For the other models: for each of the 6 query-length bins
+ * that and returns.  For the other models (CAT, which also has a warp form,
+ * and 20 states): for each of the 6 query-length bins
  * (<= 256, 512, 768, 1024, 1536 informative sites, longer; 128, 256, 384,
  * 512, 640 for 20 states and CAT), time one CTA of
  * 128 or 256 threads per trial with the query's sites of darr / parr staged
