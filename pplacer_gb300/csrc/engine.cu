@@ -1348,6 +1348,15 @@ pgb_status run_rank(pgb_engine *e, int rk, bool fused = false) {
   return PGB_OK;
 }
 
+// the character codes the query-vector tables of the warp and tensor-core
+// kernels hold: the primary states, or every code when a loaded query has an
+// ambiguity character
+int tc_zcodes(const pgb_engine *e) {
+  for (int a : e->h_qamb)
+    if (a > 0) return e->ncode;
+  return e->prim;
+}
+
 TrialCtx trial_ctx(pgb_engine *e, const pgb_prefs *p, int optimizer, int mode) {
   TrialCtx c{};
   c.darr = e->d_darr; c.parr = e->d_parr; c.dexp = e->d_dexp; c.pexp = e->d_pexp;
@@ -1359,6 +1368,7 @@ TrialCtx trial_ctx(pgb_engine *e, const pgb_prefs *p, int optimizer, int mode) {
   c.Xit = e->d_mf + e->off_Xit;
   c.tc_err = e->d_tc_err;
   c.darr_e = e->d_darr_e; c.parr_e = e->d_parr_e;
+  c.zcodes = tc_zcodes(e);
   c.log_nrates = e->gcat ? 0.0 : log((double)(float)e->NM);
   c.start_pend = p->start_pend;
   c.max_pend = p->max_pend;
@@ -1397,7 +1407,7 @@ pgb_status launch_trials_kt(pgb_engine *e, cudaStream_t st, TrialCtx c, const in
 // the categories' tables fit the shared memory of a one-warp CTA
 bool warp_cat_ok(const pgb_engine *e) {
   return e->K == 4 && e->gcat && e->RP == 1 && e->NM <= 255 &&
-         warp_trial_smem_bytes(e->NM, e->ncode) <= e->smem_optin;
+         warp_trial_smem_bytes(e->NM, e->ncode, e->ncode) <= e->smem_optin;
 }
 
 bool warp_trials_ok(const pgb_engine *e) {
@@ -1409,7 +1419,7 @@ bool warp_form_ok(const pgb_engine *e) { return warp_trials_ok(e) || warp_cat_ok
 
 template <int RP, bool CAT = false>
 pgb_status launch_trials_warp_rp(pgb_engine *e, cudaStream_t st, TrialCtx c, const WarpSegs &segs, TrialRes *out) {
-  size_t smem = warp_trial_smem_bytes(e->NM, e->ncode);
+  size_t smem = warp_trial_smem_bytes(e->NM, e->ncode, c.zcodes);
   if (smem > e->smem_optin) { set_error("warp trial shared memory %zu exceeds %zu", smem, e->smem_optin); return PGB_ERR_ARG; }
   PGB_CUDA(cudaFuncSetAttribute(k_trials_warp<RP, CAT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int grid = (segs.n + kWarpTrialWarps - 1) / kWarpTrialWarps;
@@ -1444,13 +1454,6 @@ pgb_status ensure_eigen_glvs(pgb_engine *e) {
   PGB_LAUNCH_CHECK();
   e->eig_ready = true;
   return PGB_OK;
-}
-
-// the character codes the tensor-core kernel's query tables hold
-int tc_zcodes(const pgb_engine *e) {
-  for (int a : e->h_qamb)
-    if (a > 0) return e->ncode;
-  return e->prim;
 }
 
 pgb_status launch_trials_tc(pgb_engine *e, cudaStream_t st, TrialCtx c, const int *d_order, int n, int cap,
@@ -1633,7 +1636,7 @@ pgb_status ensure_prior_means(pgb_engine *e, int prior, double prior_lower) {
 
 template <int RP, bool CAT = false>
 pgb_status launch_place_warp_rp(pgb_engine *e, TrialCtx c, const PlaceCtx &pc) {
-  size_t smem = warp_trial_smem_bytes(e->NM, e->ncode);
+  size_t smem = warp_trial_smem_bytes(e->NM, e->ncode, c.zcodes);
   PGB_CUDA(cudaFuncSetAttribute(k_place_warp<RP, CAT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int per_sm = 0;
   PGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_place_warp<RP, CAT>, 32, smem));

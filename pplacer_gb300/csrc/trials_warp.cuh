@@ -37,8 +37,9 @@ constexpr int kWarpRing = 8;        // site iterations in flight per warp
 __host__ __device__ inline size_t warp_trial_const_floats(int NM, int ncode) {
   return 16 + 64 + 2 * (size_t)ncode * 4 + 4 + (size_t)NM * 4;
 }
-__host__ __device__ inline size_t warp_trial_table_floats(int NM, int ncode) {
-  return 6 * (size_t)NM * 16 + 3 * (size_t)NM * ncode * 4 + 2 * 3 * (size_t)NM * 4;
+// zc: the character codes the query-vector tables hold (c.zcodes)
+__host__ __device__ inline size_t warp_trial_table_floats(int NM, int zc) {
+  return 6 * (size_t)NM * 16 + 3 * (size_t)NM * zc * 4 + 2 * 3 * (size_t)NM * 4;
 }
 static_assert(kWarpRing == 8, "ring depth 8: the codes in flight fill one 64-bit register");
 
@@ -52,11 +53,11 @@ struct WarpSegs {
 };
 // per warp: its tables, the ring of D / P float4s [2][kWarpRing][32], and
 // the optimiser state
-__host__ __device__ inline size_t warp_trial_warp_bytes(int NM, int ncode) {
-  return align16(4 * warp_trial_table_floats(NM, ncode)) + 2 * kWarpRing * 32 * 16 + align16(sizeof(Optimiser));
+__host__ __device__ inline size_t warp_trial_warp_bytes(int NM, int zc) {
+  return align16(4 * warp_trial_table_floats(NM, zc)) + 2 * kWarpRing * 32 * 16 + align16(sizeof(Optimiser));
 }
-__host__ __device__ inline size_t warp_trial_smem_bytes(int NM, int ncode) {
-  return align16(4 * warp_trial_const_floats(NM, ncode)) + kWarpTrialWarps * warp_trial_warp_bytes(NM, ncode);
+__host__ __device__ inline size_t warp_trial_smem_bytes(int NM, int ncode, int zc) {
+  return align16(4 * warp_trial_const_floats(NM, ncode)) + kWarpTrialWarps * warp_trial_warp_bytes(NM, zc);
 }
 
 __device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
@@ -75,7 +76,7 @@ template <int RP, bool DER>
 __device__ __forceinline__ void sites_warp(const TrialCtx &c, const TrialSmem &sm, float4 *ring, int q, int node,
                                            int Sq, int lane, SiteAcc &acc) {
   constexpr int K = 4, SPW = 32 / RP;
-  const int r = lane & (RP - 1), slot = lane / RP, nc = c.ncode;
+  const int r = lane & (RP - 1), slot = lane / RP, zc = c.zcodes;
   float md[16], mp[16], md1[DER ? 16 : 1], md2[DER ? 16 : 1], mp1[DER ? 16 : 1], mp2[DER ? 16 : 1];
 #pragma unroll
   for (int t = 0; t < 16; t += 4) {
@@ -97,7 +98,7 @@ __device__ __forceinline__ void sites_warp(const TrialCtx &c, const TrialSmem &s
   const float *gd = c.darr + (long)node * c.S * RP * K + r * K;
   const float *gp = c.parr + (long)node * c.S * RP * K + r * K;
   const uint32_t *rc = c.rcode + (long)q * c.S;
-  const float *Zr = sm.Z + r * nc * K, *Z1r = sm.Z1 + r * nc * K, *Z2r = sm.Z2 + r * nc * K;
+  const float *Zr = sm.Z + r * zc * K, *Z1r = sm.Z1 + r * zc * K, *Z2r = sm.Z2 + r * zc * K;
   const int last = Sq - 1;
   // Iterations come in groups of G; in iteration k of a group the lane
   // evaluates position k ^ r of the group (for 2 and 4 rates), so that the
@@ -235,7 +236,7 @@ template <bool DER>
 __device__ __forceinline__ void sites_warp_cat(const TrialCtx &c, const TrialSmem &sm, float4 *ring, int q, int node,
                                                int Sq, int lane, SiteAcc &acc) {
   constexpr int K = 4;
-  const int nc = c.ncode;
+  const int zc = c.zcodes;
   const float *gd = c.darr + (long)node * c.S * K;
   const float *gp = c.parr + (long)node * c.S * K;
   const uint32_t *rc = c.rcode + (long)q * c.S;
@@ -273,12 +274,12 @@ __device__ __forceinline__ void sites_warp_cat(const TrialCtx &c, const TrialSme
     st = (st + 1) & (kWarpRing - 1);
     const float dv[4] = {dcur.x, dcur.y, dcur.z, dcur.w}, pv[4] = {pcur.x, pcur.y, pcur.z, pcur.w};
     const float *Md = sm.Md + cat * 16, *Mp = sm.Mp + cat * 16;
-    const float4 Z4 = *reinterpret_cast<const float4 *>(sm.Z + (cat * nc + code) * K);
+    const float4 Z4 = *reinterpret_cast<const float4 *>(sm.Z + (cat * zc + code) * K);
     const float z[4] = {Z4.x, Z4.y, Z4.z, Z4.w};
     float z1[4], z2[4];
     if (DER) {
-      const float4 a = *reinterpret_cast<const float4 *>(sm.Z1 + (cat * nc + code) * K);
-      const float4 b = *reinterpret_cast<const float4 *>(sm.Z2 + (cat * nc + code) * K);
+      const float4 a = *reinterpret_cast<const float4 *>(sm.Z1 + (cat * zc + code) * K);
+      const float4 b = *reinterpret_cast<const float4 *>(sm.Z2 + (cat * zc + code) * K);
       z1[0] = a.x; z1[1] = a.y; z1[2] = a.z; z1[3] = a.w;
       z2[0] = b.x; z2[1] = b.y; z2[2] = b.z; z2[3] = b.w;
     }
@@ -333,11 +334,12 @@ __device__ __forceinline__ void warp_trial_setup(const TrialCtx &c, char *t_smem
   for (int i = tid; i < nc * K; i += blockDim.x) { sm.Lt[i] = c.Lt[i]; sm.lv[i] = c.lvf[i]; }
   for (int i = tid; i < NM * K; i += blockDim.x) sm.Lr[i] = c.rates[i / K] * c.lam[i % K];
   if (tid < K) sm.statd[tid] = c.statd[tid];
-  char *wb = t_smem + align16(4 * warp_trial_const_floats(NM, nc)) + warp * warp_trial_warp_bytes(NM, nc);
+  const int zc = c.zcodes;
+  char *wb = t_smem + align16(4 * warp_trial_const_floats(NM, nc)) + warp * warp_trial_warp_bytes(NM, zc);
   float *tb = reinterpret_cast<float *>(wb);
-  ring = reinterpret_cast<float4 *>(wb + align16(4 * warp_trial_table_floats(NM, nc)));
-  sm.opt = wb + align16(4 * warp_trial_table_floats(NM, nc)) + 2 * kWarpRing * 32 * 16;
-  const int mb = NM * 16, zb = NM * nc * K;
+  ring = reinterpret_cast<float4 *>(wb + align16(4 * warp_trial_table_floats(NM, zc)));
+  sm.opt = wb + align16(4 * warp_trial_table_floats(NM, zc)) + 2 * kWarpRing * 32 * 16;
+  const int mb = NM * 16, zb = NM * zc * K;
   sm.Md = tb; sm.Mp = tb + mb; sm.Md1 = tb + 2 * mb; sm.Md2 = tb + 3 * mb; sm.Mp1 = tb + 4 * mb;
   sm.Mp2 = tb + 5 * mb;
   sm.Z = tb + 6 * mb; sm.Z1 = sm.Z + zb; sm.Z2 = sm.Z1 + zb;
@@ -421,7 +423,7 @@ __device__ TrialRes trial_warp(const TrialCtx &c, const TrialSmem &sm, float4 *r
     __syncwarp();  // the previous evaluation's sites have read the tables
     trial_exps(sm, NM, K, ctl, lane, 32);
     __syncwarp();
-    trial_tables(sm, sm.W, NM, nc, ncz, K, derivs, lane, 32);
+    trial_tables(sm, sm.W, NM, c.zcodes, ncz, K, derivs, lane, 32);  // Z rows of stride zcodes
     __syncwarp();
     SiteAcc acc;
     acc.init();
