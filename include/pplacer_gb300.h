@@ -254,7 +254,7 @@ enum {
  * as Pquery.make_ml_sorted (pquery.ml:86-92); n_out[q] placements written;
  * qstatus[q] a PGB_Q_* code.  Host buffers in, host buffers out.  Large
  * query sets run in device batches (1,024 to 65,536 queries, sized so the
- * stage-1 products of a batch stay within 2 GiB; the environment variable
+ * stage-1 products of a batch stay within 8 GiB; the environment variable
  * PGB_PLACE_BATCH overrides the size). */
 pgb_status pgb_place(pgb_engine *e, const pgb_prefs *prefs, int n_queries, const char *seqs, pgb_placement *out,
                      int *n_out, int *qstatus);

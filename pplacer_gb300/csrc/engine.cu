@@ -2606,9 +2606,11 @@ pgb_status pgb_place(pgb_engine *e, const pgb_prefs *p, int n_queries, const cha
     return PGB_ERR_ARG;
   }
   // Device batches: the stage-1 products take ~24 bytes per (query, edge),
-  // so a batch holds at most 2 GiB of them (8,192 queries for 10,000 edges).
+  // so a batch holds at most 8 GiB of them (35,791 queries for 10,000 edges),
+  // a small part of the GPU's memory; fewer batches mean fewer stage-1
+  // launches and fewer whole-query tails.
   const long ep = (e->n_edges + 15) & ~15;
-  int batch = (int)std::max(1024L, std::min(65536L, (2L << 30) / (24 * ep)));
+  int batch = (int)std::max(1024L, std::min(65536L, (8L << 30) / (24 * ep)));
   if (const char *env = getenv("PGB_PLACE_BATCH")) batch = std::max(1, atoi(env));  // override (tests, tuning)
   pgb_status s;
   if (n_queries == 0) return pgb_queries_load(e, 0, seqs);
