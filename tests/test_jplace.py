@@ -56,3 +56,14 @@ def test_dedup_and_redup():
         pass
     else:
         raise AssertionError("length mismatch accepted")
+
+
+def test_posterior_fields():
+    """Placements with posterior probabilities add marginal_like and
+    post_prob to the sorted field list (placement.ml:176-180)."""
+    parent, bl = [2, 2, -1], [0.1, 0.25, 0.0]
+    results = [[(0, -10.0, 0.75, 0.05, 0.1, 0.8, -12.5), (1, -11.1, 0.25, 0.1, 0.2, 0.2, -13.9)]]
+    doc = json.loads(jplace.to_jplace(results, ["q"], parent, bl))
+    assert doc["fields"] == ["distal_length", "edge_num", "like_weight_ratio", "likelihood", "marginal_like",
+                             "pendant_length", "post_prob"]
+    assert doc["placements"][0]["p"][0] == [0.05, 0, 0.75, -10.0, -12.5, 0.1, 0.8]
