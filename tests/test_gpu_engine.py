@@ -3,7 +3,7 @@
 Tolerances (FP32 GLVs with exact int32 exponents, FP64 per-site log sums and
 scalar optimiser state):
   * logL of a fixed (query, edge, pendant, distal) point: 2e-7 relative
-  * optimised logL: 1e-6 relative (the benchmark spec's bound)
+  * optimised logL: 1e-6 relative (the accuracy target of the placement path)
   * best edge identical for >= 99.9% of queries whose top two oracle
     placements are not tied (tie: within 1e-6 relative)
 """
