@@ -18,6 +18,9 @@ Outputs (committed; the GPU machine never reads the reference):
       the numbered reference trees of tests/data/simple/test1.jplace and
       tests/data/trim/trim_out.jplace, with the trees parsed to post-order
       arrays (the jplace writer must reproduce the numbered strings).
+  jplace_rows.json
+      the placement rows of three version-3 jplace files as number tokens
+      (the writer's number formatting must reproduce them).
 """
 import json
 import math
@@ -194,6 +197,20 @@ def write_jplace_fixture(ref_root):
           jplace_tree_fixture(ref_root, "tests/data/trim/trim_out.jplace")]
     with open(os.path.join(HERE, "jplace_trees.json"), "w") as f:
         json.dump(fx, f, indent=1)
+    # the placement rows of version-3 files written by pplacer's tools, as the
+    # number tokens they hold (tests/data/misc/test_rarefy.jplace is left out:
+    # its rows were written by hand, "1.0" / "0.0")
+    rows = []
+    for rel in ("tests/data/trim/trim_out.jplace", "tests/data/misc/test_indep_contrasts.jplace",
+                "tests/data/misc/indep_scaled.jplace"):
+        with open(os.path.join(ref_root, rel)) as f:
+            txt = f.read()
+        fields = json.loads(txt)["fields"]
+        sec = txt[txt.index('"placements"'):txt.index('"metadata"')]
+        toks = [[t.strip() for t in m.split(",")] for m in re.findall(r"\[([-0-9.eE+,\s]+)\]", sec)]
+        rows.append({"source": rel, "fields": fields, "rows": toks})
+    with open(os.path.join(HERE, "jplace_rows.json"), "w") as f:
+        json.dump(rows, f, indent=1)
 
 
 if __name__ == "__main__":

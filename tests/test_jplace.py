@@ -67,3 +67,29 @@ def test_posterior_fields():
     assert doc["fields"] == ["distal_length", "edge_num", "like_weight_ratio", "likelihood", "marginal_like",
                              "pendant_length", "post_prob"]
     assert doc["placements"][0]["p"][0] == [0.05, 0, 0.75, -10.0, -12.5, 0.1, 0.8]
+
+
+def test_numbers_as_pplacer_writes_them():
+    """The placement rows of version-3 files written by pplacer's tools: each
+    number the writer emits for the parsed values is the token in the file
+    (%d edge numbers, %.12g floats, json.ml:40-43)."""
+    import re
+    rows = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "jplace_rows.json")))
+    n = 0
+    for fx in rows:
+        fields = fx["fields"]
+        results = []
+        for toks in fx["rows"]:
+            vals = dict(zip(fields, toks))
+            results.append([(int(vals["edge_num"]), float(vals["likelihood"]), float(vals["like_weight_ratio"]),
+                             float(vals["distal_length"]), float(vals["pendant_length"]))])
+        text = jplace.to_jplace(results, ["q%d" % i for i in range(len(results))], [1, -1], [0.5, 0.0])
+        emitted = [[t.strip() for t in m.split(",")]
+                   for m in re.findall(r"\[([-0-9.eE+,\s]+)\]", text[text.index('"placements"'):text.index('"metadata"')])]
+        assert len(emitted) == len(fx["rows"]), fx["source"]
+        for toks, out in zip(fx["rows"], emitted):
+            want = dict(zip(fields, toks))
+            got = dict(zip(jplace.FIELDS, out))
+            assert got == want, (fx["source"], got, want)
+            n += 1
+    assert n >= 25
