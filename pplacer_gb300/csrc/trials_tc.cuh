@@ -54,6 +54,7 @@ struct TcSmem {
   float *Z;                           // [3][NM][zcodes][kTcZs]: query vectors and d/dpend, d2/dpend2
   float *X;                           // [K][kTcXs]
   float *E, *Em1, *Lr;                // [3][NM][K], [3][NM][K], [NM][K]
+  float *F;                           // [2][3][NM][K]: (r lambda)^m exp(r lambda t_g), the B-tile scales
   float *lv, *statd;
   float *red;                         // [4][8]
   int *redi;                          // [4]
@@ -74,7 +75,7 @@ __host__ __device__ inline size_t tc_trial_smem_bytes(int cap, int NM, int ncode
   b += align16((size_t)6 * cap * 4);
   b += align16((size_t)3 * NM * zcodes * kTcZs * 4);
   b += align16((size_t)K * kTcXs * 4);
-  b += 2 * align16((size_t)3 * NM * K * 4) + align16((size_t)NM * K * 4);
+  b += 2 * align16((size_t)3 * NM * K * 4) + align16((size_t)NM * K * 4) + align16((size_t)6 * NM * K * 4);
   b += align16((size_t)ncode * K * 4) + align16((size_t)K * 4);
   b += align16(4 * 8 * 4) + align16(4 * 4);
   b += align16((size_t)cap * 2) + align16((size_t)cap);
@@ -96,6 +97,7 @@ __device__ inline TcSmem tc_carve(char *base, int cap, int NM, int ncode, int zc
   s.E = (float *)take((size_t)3 * NM * K * 4);
   s.Em1 = (float *)take((size_t)3 * NM * K * 4);
   s.Lr = (float *)take((size_t)NM * K * 4);
+  s.F = (float *)take((size_t)6 * NM * K * 4);
   s.lv = (float *)take((size_t)ncode * K * 4);
   s.statd = (float *)take((size_t)K * 4);
   s.red = (float *)take(4 * 8 * 4);
@@ -214,9 +216,22 @@ __device__ __forceinline__ bool tc_query_tables(const TrialCtx &c, const TcSmem 
   return true;
 }
 
-// B tiles of rate r: row m * 20 + i, column k = X[i][k] * (r lambda_k)^m *
-// exp(r lambda_k t) at t = dist (distal tiles) and t = cut - dist (proximal
-// tiles).  The previous MMAs have completed (their wait and barrier).
+// The B-tile scales of every rate, with the exp factors of the evaluation
+// (published by the same barrier): F[g][m][r][k] = (r lambda_k)^m *
+// exp(r lambda_k t_g), t_0 = dist, t_1 = cut - dist.
+__device__ __forceinline__ void tc_scales(const TcSmem &sm, int NM, const Ctrl &ctl, int tid) {
+  const int K = kTcK;
+  for (int it = tid; it < 6 * NM * K; it += kTcThreads) {
+    const int g = it / (3 * NM * K), m = (it / (NM * K)) % 3, rk = it % (NM * K);
+    const float lr = sm.Lr[rk];
+    const float e = expf(lr * (g == 0 ? ctl.dist : ctl.prox));
+    sm.F[it] = (m == 0 ? 1.f : (m == 1 ? lr : lr * lr)) * e;
+  }
+}
+
+// B tiles of rate r: row m * 20 + i, column k = X[i][k] * F[g][m][r][k]
+// (distal tiles g = 0, proximal g = 1).  The previous MMAs have completed
+// (their wait and barrier).
 template <bool DER>
 __device__ __forceinline__ void tc_btiles(const TcSmem &sm, int NM, int r, int tid) {
   const int K = kTcK;
@@ -225,14 +240,10 @@ __device__ __forceinline__ void tc_btiles(const TcSmem &sm, int NM, int r, int t
     const int g = it / (nrow * (K / 4)), rem = it - g * nrow * (K / 4);
     const int n = rem / (K / 4), k = (rem - n * (K / 4)) * 4;
     const int m = n / K, i = n - m * K;
-    const float *x = sm.X + i * kTcXs, *lr = sm.Lr + r * K, *e = sm.E + (g * NM + r) * K;
-    float v[4];
-#pragma unroll
-    for (int j = 0; j < 4; j++) {
-      const float f = m == 0 ? 1.f : (m == 1 ? lr[k + j] : lr[k + j] * lr[k + j]);
-      v[j] = x[k + j] * f * e[k + j];
-    }
-    tc_store_split(g == 0 ? sm.b_dh : sm.b_xh, g == 0 ? sm.b_dl : sm.b_xl, n, k, make_float4(v[0], v[1], v[2], v[3]));
+    const float *x = sm.X + i * kTcXs;
+    const float4 f = *reinterpret_cast<const float4 *>(sm.F + ((g * 3 + m) * NM + r) * K + k);
+    tc_store_split(g == 0 ? sm.b_dh : sm.b_xh, g == 0 ? sm.b_dl : sm.b_xl, n, k,
+                   make_float4(x[k] * f.x, x[k + 1] * f.y, x[k + 2] * f.z, x[k + 3] * f.w));
   }
 }
 
@@ -504,6 +515,7 @@ __device__ TrialRes tc_trial(const TrialCtx &c, const TcSmem &sm, uint32_t tmem,
       ts.E = sm.E; ts.Em1 = sm.Em1; ts.Lr = sm.Lr;
       trial_exps(ts, NM, K, ctl, tid, kTcThreads);
     }
+    tc_scales(sm, NM, ctl, tid);
     __syncthreads();
     TcRows rw;
     if (nch > 0) tc_load_rows(c, sm, node, Sq, 0, 0, tid, rw);
