@@ -46,3 +46,12 @@ def test_argument_errors_before_any_device_work(so):
     td = L.TreeDesc(3, None, None)
     assert lib.pgb_engine_create(C.byref(md), C.byref(td), C.byref(h)) == 1
     assert b"unsupported" in lib.pgb_last_error()
+    # the tensor-core evolve checks its shapes before touching a device
+    import numpy as np
+    a = np.zeros((4, 20), np.float32)
+    b = np.zeros((70, 20), np.float32)
+    o = np.zeros((4, 70), np.float32)
+    assert lib.pgb_tc_evolve(a.ctypes.data, b.ctypes.data, o.ctypes.data, 4, 20, 70) == 1
+    assert b"tc_evolve" in lib.pgb_last_error()
+    assert lib.pgb_tc_evolve(a.ctypes.data, b.ctypes.data, o.ctypes.data, 4, 25, 8) == 1
+    assert lib.pgb_tc_evolve(a.ctypes.data, b.ctypes.data, o.ctypes.data, 0, 20, 8) == 0  # nothing to do
