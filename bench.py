@@ -18,6 +18,11 @@ value: placements/s with queries and GLVs already resident in HBM, timed with
        the 129 MB L2, so no L2 flush is needed between steps.
 e2e:   placements/s through pgb_place (the C ABI call a caller makes) with the
        query rows in host memory and the placements copied back every step.
+
+--workload aa_500 | cat_5k | dna_2k runs the other configurations through the
+same line (20-state + G4 on the tensor-core kernel, GTR + CAT 20 and the long
+nucleotide queries on the warp kernel); the roofline block names the kernel
+that ran.
 """
 import argparse
 import ctypes as C
