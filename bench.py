@@ -223,13 +223,13 @@ def run_reference(args):
 
 def plain_dropin_brent(eng, w, evals_per_query, reps=40):
     """pplacer's own per-query flow over the plain drop-in (linear.ml externals
-    replaced one for one), timed call by call: a
+    replaced one for one through the pgb_* C ABI), timed call by call: a
     stage-1 score is one ten_masked_logdot over the full alignment per edge
-    (core.ml:333-343); a Brent evaluation re-evolves the pendant (one
+    (core.ml:187-197); a Brent evaluation re-evolves the pendant (one
     evolve) or the distal and proximal edges (two) -- per rate a
     dediagonalize of the exponentiated eigenvalues and a gemmish
     (diagd.ml:79-98, gstar_support.ml:70-79) -- then one ten_log_like3
-    (three_tax.ml:30-47).  Placements/s = 1 / (edges x t_score +
+    (three_tax.ml:30-58).  Placements/s = 1 / (edges x t_score +
     evals_per_query x t_eval), with evals_per_query measured on the Brent
     replica (the same algorithm) and t_eval the mean of the pendant and the
     distal evaluation."""
@@ -376,7 +376,7 @@ def run_ours(args):
     achieved = bytes_per_site_eval * site_evals / args.steps / t_trials / 1e9 if t_trials > 0 else 0.0
     # DRAM traffic per site evaluation from one ncu capture of k_place_warp on
     # this workload (dram__bytes_read.sum + dram__bytes_write.sum over the
-    # launch's site evaluations; profiles/k_place_warp_dna_1k.md)
+    # launch's site evaluations, full-size dna_1k capture)
     traffic = (DRAM_BYTES_PER_SITE_EVAL * site_evals / args.steps
                if args.workload == "dna_1k" and DRAM_BYTES_PER_SITE_EVAL else None)
     # the binding unit is the FP32 pipe: FMA-pipe lane operations per site

@@ -18,7 +18,7 @@
  *    worker processes, pplacer_src/multiprocessing.ml:120-152).
  *
  * 2. The batched engine (pgb_engine_*): device-resident reference GLVs and
- *    whole-query placement (pplacer_src/core.ml:222-557) in FP32 with exact
+ *    whole-query placement (pplacer_src/core.ml:113-409) in FP32 with exact
  *    int32 per-site scaling exponents, stage-1 ranking, the baseball
  *    heuristic, Brent or safeguarded-Newton branch-length optimisation and
  *    the final refinement, for the Gamma-mixture (pplacer_src/gmix_model.ml)
@@ -122,8 +122,9 @@ pgb_status pgb_float_mat_int_vec_mul(double *dst, const double *mat, const uint1
  * asynchronous on it.  The reduction's scratch is a fixed array inside the
  * library, held by every GPU that loads it: n_sites <= 65,536, larger sizes
  * return PGB_ERR_ARG.  All calls on a device share that array, so calls that
- * overlap on the GPU race.  The first call on a device looks up the array's
- * address; make it before any stream capture.  Calls no cudaMalloc or
+ * overlap on the GPU race.  The first call on a device, and the first call
+ * after that device's context was reset (cudaDeviceReset), looks up the
+ * array's address; make it before any stream capture.  Calls no cudaMalloc or
  * cudaFree. */
 pgb_status pgb_ten_log_like3_noalloc(const double *statd, const double *x, const double *y, const double *z,
                                      int n_rates, int n_sites, int n_states, double *result, void *stream);
@@ -146,7 +147,7 @@ typedef struct pgb_engine pgb_engine;
 
 /* Model (the fields of Gmix_model.Model.t / Gcat_model.Model.t,
  * gmix_model.ml:10-16, gcat_model.ml:33-41): Diagd x, lambda, xit
- * (diagd.ml:155-161) with x diag(lambda) x^-1 the rate matrix; statd; the
+ * (diagd.ml:33-39) with x diag(lambda) x^-1 the rate matrix; statd; the
  * Gamma category rates (Gmix) or the CAT category rates (Gcat). */
 typedef struct {
   int n_states;               /* 4 (nucleotide) or 20 (amino acid) */
@@ -208,7 +209,7 @@ pgb_status pgb_engine_get_glv(pgb_engine *e, int which, int node, double *a, int
 typedef struct {
   double start_pend;         /* [0.1] */
   double max_pend;           /* [2.0] */
-  double initial_tolerance;  /* [0.01] stage-2 tolerance; the final pass uses 1e-5 (core.ml:160) */
+  double initial_tolerance;  /* [0.01] stage-2 tolerance; the final pass uses 1e-5 (core.ml:14) */
   int max_strikes;           /* [6]; 0 evaluates every edge */
   double strike_box;         /* [3.0] */
   int max_pitches;           /* [40] */
@@ -243,8 +244,8 @@ typedef struct {
 /* Per-query status codes. */
 enum {
   PGB_Q_OK = 0,
-  PGB_Q_NO_INFORMATIVE = 1, /* no informative site (core.ml:303-304) */
-  PGB_Q_EMPTY = 2,          /* every location failed (core.ml:465-467) */
+  PGB_Q_NO_INFORMATIVE = 1, /* no informative site (core.ml:157-158) */
+  PGB_Q_EMPTY = 2,          /* every location failed (core.ml:319-321) */
   PGB_Q_BAD_CHAR = 3,       /* unknown character (pplacer_run.ml:63-69) */
   PGB_Q_START_FAILURE = 4   /* Brent start finder failure (minimization.ml:11-13,35-36) */
 };
@@ -267,18 +268,18 @@ pgb_status pgb_queries_run(pgb_engine *e, const pgb_prefs *prefs);
 pgb_status pgb_queries_fetch(pgb_engine *e, pgb_placement *out, int *n_out, int *qstatus);
 
 /* Stage 1 alone on the loaded queries (Glv.masked_logdot against every
- * supernode, core.ml:333-343): scores[q][i] for the i-th non-root node in
+ * supernode, core.ml:187-197): scores[q][i] for the i-th non-root node in
  * increasing id order. */
 pgb_status pgb_queries_stage1(pgb_engine *e, const pgb_prefs *prefs, double *scores);
 
-/* Stage 1 and its ranking (core.ml:341-343, fig.ml:143-147): rank[q][r] for
+/* Stage 1 and its ranking (core.ml:195-197, fig.ml:143-147): rank[q][r] for
  * r < rk (rk <= the number of edges) is the index, in the order of
  * pgb_queries_stage1's columns, of the query's r-th best edge: scores
  * descending, equal scores by increasing index, NaN below every number. */
 pgb_status pgb_queries_rank(pgb_engine *e, const pgb_prefs *prefs, int rk, int *rank);
 
 /* Branch-length optimisation of explicit (query, location) trials on the
- * loaded queries (Three_tax.optimize from the given start, core.ml:401-425 with
+ * loaded queries (Three_tax.optimize from the given start, core.ml:255-279 with
  * the retry from default lengths).  optimizer: 0 Brent, 1 Newton;
  * mode 0 optimises, mode 1 only evaluates logL and its derivatives at the
  * start point (the forward/backward pair), mode 2 computes the marginal

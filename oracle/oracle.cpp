@@ -228,9 +228,9 @@ struct Diagd {
   std::vector<double> x, l, xit;  // x diag(l) x^-1 = B D ; xit = x^-T
 };
 
-static double safe_invert(double v) { return v == 0. ? 1. : 1. / v; }  // diagd.ml:240
+static double safe_invert(double v) { return v == 0. ? 1. : 1. / v; }  // diagd.ml:118
 
-// of_d_b: X = D^-1/2 U, Xit = D^1/2 U with U L U^T = D^1/2 B D^1/2  (diagd.ml:245-254)
+// of_d_b: X = D^-1/2 U, Xit = D^1/2 U with U L U^T = D^1/2 B D^1/2  (diagd.ml:123-132)
 static Diagd of_d_b(const std::vector<double> &d, const std::vector<double> &b, int n) {
   for (int i = 0; i < n; i++)
     if (!(d[i] >= 0)) throw std::runtime_error("negative element in the diagonal of a DB matrix!");
@@ -255,7 +255,7 @@ static Diagd of_d_b(const std::vector<double> &d, const std::vector<double> &b, 
   return dd;
 }
 
-// b_ii = -(1/pi_i) sum_{k != i} r_ki pi_k              (diagd.ml:262-274)
+// b_ii = -(1/pi_i) sum_{k != i} r_ki pi_k              (diagd.ml:140-152)
 static std::vector<double> b_of_exchangeable_pair(const std::vector<double> &r, const std::vector<double> &pi,
                                                   int n) {
   std::vector<double> b((size_t)n * n);
@@ -272,7 +272,7 @@ static std::vector<double> b_of_exchangeable_pair(const std::vector<double> &r, 
   return b;
 }
 
-// normed_of_exchangeable_pair: scale lambda so the mean rate is one (diagd.ml:280-294)
+// normed_of_exchangeable_pair: scale lambda so the mean rate is one (diagd.ml:156-172)
 static Diagd normed_of_exchangeable_pair(const std::vector<double> &r, const std::vector<double> &pi, int n) {
   Diagd dd = of_d_b(pi, b_of_exchangeable_pair(r, pi, n), n);
   std::vector<double> q((size_t)n * n);
@@ -284,7 +284,7 @@ static Diagd normed_of_exchangeable_pair(const std::vector<double> &r, const std
   return dd;
 }
 
-// multi_exp: dst[r] = X diag(exp(rate_r * bl * l)) X^-1 (diagd.ml:201-220)
+// multi_exp: dst[r] = X diag(exp(rate_r * bl * l)) X^-1 (diagd.ml:79-98)
 static void multi_exp(std::vector<double> &dst, const Diagd &dd, const std::vector<double> &rates, double bl,
                       const std::vector<char> *mask) {
   int n = dd.n;
@@ -298,7 +298,7 @@ static void multi_exp(std::vector<double> &dst, const Diagd &dd, const std::vect
 }
 
 // ---------------------------------------------------------------------------
-// Discrete gamma rates (pplacer_src/gamma.ml:315-371, Yang 1994).
+// Discrete gamma rates (pplacer_src/gamma.ml:14-70, Yang 1994).
 // ---------------------------------------------------------------------------
 // Regularised lower incomplete gamma P(a, x): power series for x < a + 1,
 // modified-Lentz continued fraction for Q = 1 - P otherwise.
@@ -348,7 +348,7 @@ static double gamma_p_inv(double a, double p) {
   return x;
 }
 
-// discrete_gamma n_cat alpha: category means, normalised to mean 1 (gamma.ml:353-371)
+// discrete_gamma n_cat alpha: category means, normalised to mean 1 (gamma.ml:52-70)
 static std::vector<double> discrete_gamma(int n_cat, double alpha) {
   std::vector<double> freq(n_cat + 1);
   for (int i = 0; i <= n_cat; i++) {
@@ -356,7 +356,7 @@ static std::vector<double> discrete_gamma(int n_cat, double alpha) {
     else if (i == n_cat) freq[i] = 1.;
     else {
       double y = (double)i / (double)n_cat;
-      // inverse_gamma_cdf ~alpha ~beta:1 with epsilon 1e-7 (gamma.ml:315-326)
+      // inverse_gamma_cdf ~alpha ~beta:1 with epsilon 1e-7 (gamma.ml:14-25)
       double cut = (y < gamma_p(alpha, 1e-7)) ? 0. : gamma_p_inv(alpha, y);
       freq[i] = gamma_p(alpha + 1., cut);
     }
@@ -364,7 +364,7 @@ static std::vector<double> discrete_gamma(int n_cat, double alpha) {
   std::vector<double> v(n_cat);
   double tot = 0;
   for (int i = 0; i < n_cat; i++) { v[i] = freq[i + 1] - freq[i]; tot += v[i]; }
-  for (int i = 0; i < n_cat; i++) v[i] = (double)n_cat * v[i] / tot;  // make_mean_one, gamma.ml:328-331
+  for (int i = 0; i < n_cat; i++) v[i] = (double)n_cat * v[i] / tot;  // make_mean_one, gamma.ml:27-30
   return v;
 }
 
@@ -543,7 +543,7 @@ static double slow_log_like3(const Model &m, const Glv &x, const Glv &y, const G
 
 // ---------------------------------------------------------------------------
 // Reference tree: darr / parr / snodes (pplacer_src/like_stree.ml:43-110,
-// pplacer_src/pplacer_run.ml:322-340, pplacer_src/glv_arr.ml:92-102).
+// pplacer_src/pplacer_run.ml:322-340, pplacer_src/glv_arr.ml:46-57).
 // Nodes are numbered post-order (newick_parser.mly:50-59); children of a node
 // in increasing id order reproduce the Newick child order.
 // ---------------------------------------------------------------------------
@@ -733,7 +733,7 @@ static double brent(F &f, double raw_start, double left, double right, double to
 }
 
 // ---------------------------------------------------------------------------
-// Placement core (pplacer_src/core.ml:222-557, three_tax.ml:252-322,
+// Placement core (pplacer_src/core.ml:113-409, three_tax.ml:15-85,
 // glv_edge.ml:29-44).
 // ---------------------------------------------------------------------------
 struct Prefs {
@@ -853,7 +853,7 @@ struct Placer {
     QueryOut out;
     int S = ref.S, K = m.K, R = m.R();
     std::vector<double> lv(K);
-    // full-length query GLV evolved by start_pend (core.ml:277-287)
+    // full-length query GLV evolved by start_pend (core.ml:107-141)
     Glv fq, fqe;
     fq.make(R, S, K);
     fqe.make(R, S, K);
@@ -871,7 +871,7 @@ struct Placer {
     evolve_into(m, fqe, fq, prefs.start_pend, nullptr, tensor);
     int Sq = (int)reind.size();
     if (Sq == 0) { out.status = 1; return out; }
-    const std::vector<int> *rp = m.gcat ? &reind : nullptr;  // core.ml:323-326
+    const std::vector<int> *rp = m.gcat ? &reind : nullptr;  // core.ml:175-179
     GlvEdge pend, dist, prox;
     pend.orig.make(R, Sq, K);
     for (int i = 0; i < Sq; i++) {
@@ -885,7 +885,7 @@ struct Placer {
     prox.orig = dist.orig;
     prox.evolv = dist.orig;
     set_bl(pend, prefs.start_pend, rp);
-    // stage 1: rank every non-root edge (core.ml:333-343, fig.ml:101-105,143-147)
+    // stage 1: rank every non-root edge (core.ml:187-197, fig.ml:101-105,143-147)
     std::vector<std::pair<double, int>> scored;
     for (int loc = 0; loc < ref.n_nodes; loc++) {
       if (loc == ref.root) continue;
@@ -903,7 +903,7 @@ struct Placer {
           std::memcpy(&dst.a[((size_t)r * Sq + i) * K], &src.a[((size_t)r * S + reind[i]) * K], K * sizeof(double));
       }
     };
-    auto set_tt_edges = [&](int loc, double pendant, double distal) {  // core.ml:371-385
+    auto set_tt_edges = [&](int loc, double pendant, double distal) {  // core.ml:225-239
       double cut = ref.bl[loc];
       set_bl(pend, pendant, rp);
       mask_into(ref.darr[loc], dist.orig);
@@ -912,21 +912,21 @@ struct Placer {
       set_bl(prox, cut - distal, rp);
     };
     auto tt_default = [&](int loc) { set_tt_edges(loc, prefs.start_pend, ref.bl[loc] / 2.); };
-    auto log_like = [&]() { return log_like3(m, util, prox.evolv, dist.evolv, pend.evolv); };  // three_tax.ml:267-273
-    auto set_dist_bl = [&](double d) {  // three_tax.ml:278-282
+    auto log_like = [&]() { return log_like3(m, util, prox.evolv, dist.evolv, pend.evolv); };  // three_tax.ml:30-36
+    auto set_dist_bl = [&](double d) {  // three_tax.ml:41-45
       double prox_bl = (dist.bl + prox.bl) - d;
       set_bl(dist, d, rp);
       set_bl(prox, prox_bl, rp);
     };
     auto optimize_something = [&](double tol, int which, double start_v, double min_v, double max_v) {
-      if (min_v == max_v) return start_v;  // three_tax.ml:285-295
+      if (min_v == max_v) return start_v;  // three_tax.ml:48-58
       auto f = [&](double v) {
         if (which == 0) set_bl(pend, v, rp); else set_dist_bl(v);
         return -log_like();
       };
       return brent(f, start_v, min_v, max_v, tol);
     };
-    auto optimize = [&](double tol) {  // three_tax.ml:307-320, core.ml:156
+    auto optimize = [&](double tol) {  // three_tax.ml:70-83, core.ml:10
       double prev_pend = pend.bl, prev_dist = dist.bl;
       for (int step = 1;; step++) {
         if (step > 200) throw ExceededMaxIter{};
@@ -937,16 +937,16 @@ struct Placer {
       }
     };
     struct Res { double like, pend, dist; };
-    auto ml_optimize_location = [&](double tol) {  // core.ml:401-417
+    auto ml_optimize_location = [&](double tol) {  // core.ml:255-271
       try { optimize(tol); } catch (ExceededMaxIter &) {}
       return Res{log_like(), pend.bl, dist.bl};
     };
-    auto safe_ml_optimize_location = [&](double tol, int loc) {  // core.ml:418-425
+    auto safe_ml_optimize_location = [&](double tol, int loc) {  // core.ml:272-279
       try { return ml_optimize_location(tol); }
       catch (GslError &) { tt_default(loc); return ml_optimize_location(tol); }
     };
 
-    if (trial_loc >= 0) {  // one location from a given start (core.ml:401-425 after set_tt_edges)
+    if (trial_loc >= 0) {  // one location from a given start (core.ml:255-279 after set_tt_edges)
       set_tt_edges(trial_loc, trial_pend, trial_dist);
       try {
         Res r = safe_ml_optimize_location(trial_tol, trial_loc);
@@ -955,10 +955,10 @@ struct Placer {
       catch (StartFailure &) { out.status = 4; }
       return out;
     }
-    long t_max_pitches, t_max_strikes;  // core.ml:242-252
+    long t_max_pitches, t_max_strikes;  // core.ml:96-106
     if (prefs.max_strikes == 0) { t_max_pitches = 1L << 60; t_max_strikes = 1L << 60; }
     else { t_max_pitches = prefs.max_pitches; t_max_strikes = prefs.max_strikes; }
-    // stage 2: baseball (core.ml:429-464)
+    // stage 2: baseball (core.ml:283-318)
     std::vector<std::pair<int, Res>> results;
     double like_record = -INFINITY;
     long n_strikes = 0;
@@ -981,7 +981,7 @@ struct Placer {
       }
     } catch (StartFailure &) { out.status = 4; return out; }
     if (results.empty()) { out.status = 2; return out; }
-    // sort, keep, refine (core.ml:482-523)
+    // sort, keep, refine (core.ml:336-377)
     std::vector<std::pair<int, Res>> sorted = results;
     std::stable_sort(sorted.begin(), sorted.end(),
                      [](const std::pair<int, Res> &a, const std::pair<int, Res> &b) { return a.second.like > b.second.like; });
@@ -1060,8 +1060,8 @@ void orc_discrete_gamma(int n_cat, double alpha, double *out) {
 }
 double orc_gamma_p(double a, double x) { return gamma_p(a, x); }
 
-// Diagd of (d, b) without normalisation (diagd.ml:245) and the normalised
-// exchangeable-pair form (diagd.ml:291).
+// Diagd of (d, b) without normalisation (diagd.ml:123) and the normalised
+// exchangeable-pair form (diagd.ml:169-172).
 void orc_diagd_of_d_b(int n, const double *d, const double *b, double *x, double *l, double *xit) {
   Diagd dd = of_d_b(std::vector<double>(d, d + n), std::vector<double>(b, b + n * n), n);
   std::copy(dd.x.begin(), dd.x.end(), x);
@@ -1074,7 +1074,7 @@ void orc_diagd_normed(int n, const double *exch, const double *statd, double *x,
   std::copy(dd.l.begin(), dd.l.end(), l);
   std::copy(dd.xit.begin(), dd.xit.end(), xit);
 }
-// to_exp (diagd.ml:187-193)
+// to_exp (diagd.ml:65-71)
 void orc_diagd_to_exp(int n, const double *x, const double *l, const double *xit, double bl, double *dst) {
   std::vector<double> u(n);
   for (int i = 0; i < n; i++) u[i] = std::exp(bl * l[i]);
@@ -1222,7 +1222,7 @@ void orc_place(void *rp, const OrcPrefs *pp, int n_queries, const char *seqs, in
   }
 }
 
-// Stage-1 ranking and stage-2 trace of one query (core.ml:333-464): edges in
+// Stage-1 ranking and stage-2 trace of one query (core.ml:187-318): edges in
 // rank order with scores, then the stage-2 edges tried with their like.
 int orc_query_trace(void *rp, const OrcPrefs *pp, const char *seq, int *rank_edges, double *rank_scores,
                     int *n_rank, int *s2_edges, double *s2_likes, int *n_s2) {

@@ -394,7 +394,7 @@ def marginal_like(ref, seq, loc, pend, dist, prior, mu=None, max_pend=2.0, rel=1
     base + log((1/cut) int_0^cut int_0^U exp(L(p, d) - base) prior(p) dp dd),
     base = L at (pend, dist), the location's optimum; U = where
     L(., dist) + log prior has dropped 10 below its value at the optimum
-    (find_upper_limit, three_tax.ml:125-160), found here by bisection to
+    (find_upper_limit, three_tax.ml:124-159), found here by bisection to
     1e-10 where the reference runs 10 Brent iterations to 0.02 (the integral
     beyond either point is below e^-10 of the total); a zero-length edge
     integrates the pendant only, at the edge midpoint.  The integrals use

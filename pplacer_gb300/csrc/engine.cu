@@ -7,7 +7,7 @@
 //   lt                : float [n_edges][prim][n_sites] stage-1 log table
 //   queries           : codes, masked-site index lists (reind) and codes, lengths
 //
-// Pipeline of one placement call (pplacer_src/core.ml:222-557):
+// Pipeline of one placement call (pplacer_src/core.ml:113-409):
 //   query prep -> stage-1 log table (once per start_pend) -> stage-1 scores
 //   -> per-query ranking -> baseball rounds of speculative stage-2 trials ->
 //   keep / refine trials -> like_weight_ratio and output.
@@ -35,7 +35,7 @@ enum { BR_OK = 0, BR_GSLERR = 1, BR_MAXITER = 2, BR_STARTFAIL = 3 };
 // Precompute kernels (FP64): like_stree.ml:43-110, pplacer_run.ml:332-340
 // ---------------------------------------------------------------------------
 
-// P_m(t) = X diag(exp(rate_m t lambda)) Xit^T for every node (diagd.ml:201-220,
+// P_m(t) = X diag(exp(rate_m t lambda)) Xit^T for every node (diagd.ml:79-98,
 // exp((rate * bl) * l_k) then dediagonalize's (l_k X_ik) Xit_jk order).
 __global__ void k_node_pmats(double *pm, const double *__restrict__ bl, double scale, int n_nodes, int NM, int K,
                              const double *__restrict__ X, const double *__restrict__ Xit,
@@ -111,7 +111,7 @@ __global__ void k_leaves(PreCtx c, const int *__restrict__ leaves, int n_leaves,
 }
 
 // One post-order level: distal = product of children's evd in child order,
-// pull at -50, evd = P(bl) distal (like_stree.ml:148-174).
+// pull at -50, evd = P(bl) distal (like_stree.ml:43-69).
 __global__ void k_distal_level(PreCtx c, const int *__restrict__ nodes, int n_nodes_lvl,
                                const int *__restrict__ ch_start, const int *__restrict__ ch_list) {
   long n = (long)n_nodes_lvl * c.S;
@@ -139,7 +139,7 @@ __global__ void k_distal_level(PreCtx c, const int *__restrict__ nodes, int n_no
 }
 
 // One pre-order level: prox[child] = P(bl_parent) prox[parent] times the
-// siblings' evd in child order, pull at -50 (like_stree.ml:179-205).
+// siblings' evd in child order, pull at -50 (like_stree.ml:74-100).
 __global__ void k_prox_level(PreCtx c, const int *__restrict__ nodes, int n_nodes_lvl, const int *__restrict__ parent,
                              const int *__restrict__ ch_start, const int *__restrict__ ch_list) {
   long n = (long)n_nodes_lvl * c.S;
@@ -173,7 +173,7 @@ __global__ void k_set_unit(double *g, int *e, long n_vals, long n_exps) {
 }
 
 // Pull at -10, supernode = statd (P(bl/2) d) (P(bl/2) p), FP32 copies
-// (pplacer_run.ml:332-340, glv_arr.ml:92-102).
+// (pplacer_run.ml:332-340, glv_arr.ml:46-57).
 __global__ void k_finish_glvs(PreCtx c, int n_nodes, float *d32, float *p32, float *s32, int *dexp, int *pexp,
                               int *sexp) {
   long n = (long)n_nodes * c.S;
@@ -272,7 +272,7 @@ __global__ void k_snodes_from(const double *__restrict__ d, const double *__rest
 
 // ---------------------------------------------------------------------------
 // Query preparation: character codes, informative mask, masked site lists
-// (core.ml:267-304).  One CTA per query.
+// (core.ml:121-170).  One CTA per query.
 // ---------------------------------------------------------------------------
 // Columns are visited in the order `order` (null: 0 .. S-1); the CAT models
 // pass the columns grouped by category, so that a query's informative sites
@@ -331,7 +331,7 @@ __global__ void k_query_prep(const char *__restrict__ seqs, int S, int prim, con
 }
 
 // ---------------------------------------------------------------------------
-// Stage 1 (core.ml:333-343, Glv.masked_logdot against every supernode).
+// Stage 1 (core.ml:187-197, Glv.masked_logdot against every supernode).
 // The query side is the full query evolved by start_pend, so its value at a
 // site depends only on the site's character.  With
 //   T[e][c][s] = log(sum_r sum_k qe_c[r][k] snode_e[s][r][k])
@@ -557,8 +557,8 @@ __global__ void __launch_bounds__(128) k_rank_warp(const double *__restrict__ sc
 #include "trials_tc.cuh"
 
 // ---------------------------------------------------------------------------
-// Baseball (core.ml:429-464) and keep / refine / like_weight_ratio
-// (core.ml:482-523, ppatteries.ml:175-183, pquery.ml:8-9,92).
+// Baseball (core.ml:283-318) and keep / refine / like_weight_ratio
+// (core.ml:336-377, ppatteries.ml:175-183, pquery.ml:8-9,92).
 // ---------------------------------------------------------------------------
 struct BBState {
   int next, strikes, nres, done;
@@ -645,7 +645,7 @@ __global__ void k_bb_update(BBCtx c, const TrialRes *__restrict__ tres) {
     int ei = c.rank[(long)q * c.rk + s.next];
     s.next++;
     if (r.status == ST_STARTFAIL) { s.done = 1; c.qstatus[q] = PGB_Q_START_FAILURE; break; }
-    if (r.status == ST_FAILED) continue;  // skipped location (core.ml:435-443)
+    if (r.status == ST_FAILED) continue;  // skipped location (core.ml:286-297)
     long before = s.nres;
     if (s.nres < c.maxr) {
       ResEntry e;
@@ -703,7 +703,7 @@ __global__ void k_keep_emit(BBCtx c, int keep_at_most, double log_keep_factor, i
     t.node = c.edge_nodes[e.edge];
     t.pend0 = e.pend;
     t.dist0 = e.dist;
-    t.tol = 1e-5;  // final_tolerance (core.ml:160)
+    t.tol = 1e-5;  // final_tolerance (core.ml:14)
     t.seeded = 1;  // used by the Newton form only
     t.seed = e.ev;
     c.trials[base + j] = t;
@@ -797,8 +797,8 @@ __global__ void k_finalize(BBCtx c, int keep_at_most, const int *__restrict__ ke
 // ---------------------------------------------------------------------------
 // Whole queries, one per team -- a warp (nucleotide Gamma mixtures), a
 // tensor-core CTA (20 states) or a CUDA-core CTA: the baseball search over
-// the stage-1 ranking (core.ml:429-464), keep (core.ml:482-496), refinement
-// from the kept optima (core.ml:497-523), the marginal likelihoods with
+// the stage-1 ranking (core.ml:283-318), keep (core.ml:336-352), refinement
+// from the kept optima (core.ml:353-377), the marginal likelihoods with
 // calc_pp and like_weight_ratio (pquery.ml:8-9).  A query's trials run in
 // rank order inside its team, each decided before the next starts, so
 // nothing is evaluated speculatively and no host round trip separates the
@@ -863,7 +863,7 @@ __device__ __forceinline__ void place_queries(Team &tm, const TrialCtx &c, const
       t.node = b.edge_nodes[e.edge];
       t.pend0 = e.pend;
       t.dist0 = e.dist;
-      t.tol = 1e-5;  // final_tolerance (core.ml:160)
+      t.tol = 1e-5;  // final_tolerance (core.ml:14)
       t.seeded = 1;  // the evaluation at (pend0, dist0); the Newton form does not redo it
       t.seed = e.ev;
       if (marginal) {  // after the refinement: e holds the refined optimum
@@ -940,7 +940,7 @@ __device__ __forceinline__ void place_queries(Team &tm, const TrialCtx &c, const
     if (tr.status == ST_STARTFAIL) {
       qst = PGB_Q_START_FAILURE;
       stop = true;
-    } else if (tr.status != ST_FAILED) {  // ST_FAILED: skipped location (core.ml:435-443)
+    } else if (tr.status != ST_FAILED) {  // ST_FAILED: skipped location (core.ml:286-297)
       const long before = nres;
       if (nres < b.maxr) {
         if (tm.leader()) {
@@ -1188,7 +1188,7 @@ int grid_for(long n, int threads = 256) {
   return (int)std::max(1L, std::min(b, 152L * 32));
 }
 
-// Host P(t) for each matrix index (diagd.ml:201-220) in FP64.
+// Host P(t) for each matrix index (diagd.ml:79-98) in FP64.
 void host_pmats(const pgb_engine *e, double t, std::vector<double> &pm) {
   int K = e->K;
   pm.assign((size_t)e->NM * K * K, 0.0);
@@ -1474,7 +1474,7 @@ pgb_status check_tc_err(pgb_engine *e) {
   int h[16];
   PGB_CUDA(cudaMemcpy(h, e->d_tc_err, sizeof h, cudaMemcpyDeviceToHost));
   if (h[0]) {
-    cudaMemset(e->d_tc_err, 0, sizeof h);
+    PGB_CUDA(cudaMemsetAsync(e->d_tc_err, 0, sizeof h, e->st));
     set_error("tensor-core trial kernel: an MMA completion wait timed out (cta %d rate %d chunk %d phase %d: "
               "wait %d test %d/%d; tmem 0x%x, tiles 0x%x, barrier 0x%x; sites %d chunks %d)",
               h[1], h[2], h[3], h[4], h[5], h[6], h[7], h[8], h[9], h[10], h[11], h[12]);
@@ -1724,14 +1724,6 @@ bool whole_query_form(const pgb_engine *e) {
 // whole-query CTAs: tensor-core for 20-state models, CUDA-core otherwise).
 pgb_status run_whole_queries(pgb_engine *e, const pgb_prefs *p, const BBCtx &c, TrialCtx tc, int max_sq) {
   pgb_status s;
-  if ((size_t)e->Q > e->qorder_cap) {
-    if ((s = dalloc(&e->d_qorder, e->Q))) return s;
-    e->qorder_cap = e->Q;
-  }
-  std::vector<int> ord(e->Q);
-  for (int i = 0; i < e->Q; i++) ord[i] = i;
-  std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return e->h_qlen[a] > e->h_qlen[b]; });
-  PGB_CUDA(cudaMemcpyAsync(e->d_qorder, ord.data(), ord.size() * sizeof(int), cudaMemcpyHostToDevice, e->st));
   PGB_CUDA(cudaMemsetAsync(e->d_small, 0, sizeof(int), e->st));
   tc.smem_win = 0;
   tc.cap = 0;
@@ -2282,6 +2274,16 @@ pgb_status pgb_queries_load(pgb_engine *e, int n_queries, const char *seqs) {
   PGB_CUDA(cudaMemcpyAsync(e->h_qlen.data(), e->d_qlen, (size_t)n_queries * 4, cudaMemcpyDeviceToHost, e->st));
   e->h_qamb.resize(n_queries);
   PGB_CUDA(cudaMemcpyAsync(e->h_qamb.data(), e->d_qamb, (size_t)n_queries * 4, cudaMemcpyDeviceToHost, e->st));
+  PGB_CUDA(cudaStreamSynchronize(e->st));
+  // the whole-query kernels take queries longest first from this order
+  if ((size_t)n_queries > e->qorder_cap) {
+    if ((s = dalloc(&e->d_qorder, n_queries))) return s;
+    e->qorder_cap = n_queries;
+  }
+  std::vector<int> ord(n_queries);
+  for (int i = 0; i < n_queries; i++) ord[i] = i;
+  std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return e->h_qlen[a] > e->h_qlen[b]; });
+  PGB_CUDA(cudaMemcpyAsync(e->d_qorder, ord.data(), ord.size() * sizeof(int), cudaMemcpyHostToDevice, e->st));
   PGB_CUDA(cudaStreamSynchronize(e->st));
   return PGB_OK;
 }

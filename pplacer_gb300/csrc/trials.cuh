@@ -1,6 +1,6 @@
 // Stage-2 trials: one CTA per (query, location) branch-length optimisation
-// (Three_tax.optimize, pplacer_src/three_tax.ml:285-320, with the retry from
-// default lengths of core.ml:418-425).  Included by engine.cu inside its
+// (Three_tax.optimize, pplacer_src/three_tax.ml:48-83, with the retry from
+// default lengths of core.ml:272-279).  Included by engine.cu inside its
 // anonymous namespace.
 //
 // Structure of the kernel: the query's informative sites of darr / parr[node]
@@ -157,7 +157,7 @@ struct Optimiser {
   double cut, tol, max_pend, start_pend, pend0, dist0, cst;
   // outputs
   int status, n_evals;
-  double pend, dist, prox;  // three-taxon state (three_tax.ml:252-258)
+  double pend, dist, prox;  // three-taxon state (three_tax.ml:15-21)
   double L_last;
   EvalOut last;
   // request
@@ -209,7 +209,7 @@ struct Optimiser {
     req_derivs = derivs;
   }
 
-  // set_pend_bl / set_dist_bl (three_tax.ml:275-282)
+  // set_pend_bl / set_dist_bl (three_tax.ml:38-45)
   __device__ void set_coord(int wh, double val) {
     if (wh == 0) {
       pend = val;
@@ -236,7 +236,7 @@ struct Optimiser {
         attempt = 0;
         pend = pend0;
         dist = dist0;
-        prox = cut - dist0;  // set_tt_edges (core.ml:371-385)
+        prox = cut - dist0;  // set_tt_edges (core.ml:225-239)
         if (mode == 1) {
           request(pend, dist, prox, true);
           PGB_YIELD(1);
@@ -244,7 +244,7 @@ struct Optimiser {
         }
         if (mode == 2) goto MARGINAL;
         if (optimizer == 1) goto NEWTON;
-        // ---------------- Brent replica (three_tax.ml:285-320) ----------------
+        // ---------------- Brent replica (three_tax.ml:48-83) ----------------
       BRENT_ATTEMPT:
         prev_pend = pend;
         prev_dist = dist;
@@ -361,7 +361,7 @@ struct Optimiser {
         }
         goto BRENT_DONE;
       BRENT_ERR:
-        if (attempt == 0) {  // retry from the default branch lengths (core.ml:418-425)
+        if (attempt == 0) {  // retry from the default branch lengths (core.ml:272-279)
           attempt = 1;
           pend = start_pend;
           dist = cut / 2.;
@@ -477,7 +477,7 @@ struct Optimiser {
         // log of (1/cut) int_0^cut int exp(L(p, d)) prior(p) dp dd, for the
         // posterior probabilities of core.ml:378-401.  The pendant range
         // ends where L + log prior has dropped 10 below its value at the
-        // optimum (find_upper_limit, three_tax.ml:125-160; searched upward
+        // optimum (find_upper_limit, three_tax.ml:124-159; searched upward
         // and downward here), the distal range is the optimum +- 6 marginal
         // standard deviations of the Hessian's Gaussian (all of [0, cut]
         // when the Hessian is not negative definite); both are split at

@@ -1,6 +1,6 @@
 // Stage-2 trials of 20-state Gamma-mixture models on the tensor cores: one
 // CTA of 128 threads per (query, location) optimisation (Three_tax.optimize,
-// pplacer_src/three_tax.ml:285-320), the per-site evolves of the distal and
+// pplacer_src/three_tax.ml:48-83), the per-site evolves of the distal and
 // proximal GLVs (Gmix_model.evolve_into, gmix_model.ml:308-315) as tcgen05
 // MMAs.  Included by engine.cu inside its anonymous namespace, after
 // trials.cuh.

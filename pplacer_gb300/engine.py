@@ -2,7 +2,7 @@
 
 Mirrors the reference's per-run flow (pplacer_src/pplacer_run.ml:167-783):
 build the model, precompute darr / parr / snodes on the reference tree, then
-place queries with ``Core.pplacer_core`` semantics (pplacer_src/core.ml:222-557).
+place queries with ``Core.pplacer_core`` semantics (pplacer_src/core.ml:113-409).
 All computation happens in the CUDA library; this module only marshals
 arguments and results.
 """

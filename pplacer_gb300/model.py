@@ -1,10 +1,10 @@
 """Host-side model construction (FP64): what pplacer computes once before the
 hot path and hands to the likelihood engine.
 
-* ``diagd_normed`` -- Diagd.normed_of_exchangeable_pair (pplacer_src/diagd.ml:245-294):
+* ``diagd_normed`` -- Diagd.normed_of_exchangeable_pair (pplacer_src/diagd.ml:123-172):
   X diag(lambda) X^-1 = B D with B from the exchangeabilities and D = diag(pi),
   eigenvalues scaled to a mean rate of one.
-* ``discrete_gamma`` -- Gamma.discrete_gamma (pplacer_src/gamma.ml:315-371).
+* ``discrete_gamma`` -- Gamma.discrete_gamma (pplacer_src/gamma.ml:14-70).
 * ``emper_freq`` -- Alignment.emper_freq (common_src/alignment.ml:186-215).
 * ``premask`` -- Pplacer_run.premask (pplacer_src/pplacer_run.ml:59-144).
 * ``dedup`` -- the query deduplication of pplacer_src/pplacer_run.ml:228-253.
@@ -62,7 +62,7 @@ def diagd_normed(exch, statd):
     pi = np.asarray(statd, dtype=np.float64)
     n = len(pi)
     b = r.copy()
-    for i in range(n):  # b_ii = -(1/pi_i) sum_{k != i} r_ki pi_k  (diagd.ml:262-274)
+    for i in range(n):  # b_ii = -(1/pi_i) sum_{k != i} r_ki pi_k  (diagd.ml:140-152)
         tot = sum(r[k, i] * pi[k] for k in range(n) if k != i)
         b[i, i] = -(tot * _safe_invert(pi[i]))
     if np.any(pi < 0):

@@ -98,7 +98,7 @@ def random_gtr(rng, K, sigma, dir_alpha):
 
 
 def rate_matrix(ex, statd):
-    """Q_ij = r_ij pi_j, rows sum to zero, mean rate one (pplacer_src/diagd.ml:256-294)."""
+    """Q_ij = r_ij pi_j, rows sum to zero, mean rate one (pplacer_src/diagd.ml:140-172)."""
     Q = ex * statd[None, :]
     np.fill_diagonal(Q, 0.0)
     np.fill_diagonal(Q, -Q.sum(1))

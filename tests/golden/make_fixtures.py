@@ -13,7 +13,7 @@ Outputs (committed; the GPU machine never reads the reference):
   linear_kat.json
       the masked-logdot known answers of tests/pplacer/test_linear.ml:4-28.
   gamma_kat.json
-      discrete_gamma 4 0.5 from the doc comment at pplacer_src/gamma.ml:345-352.
+      discrete_gamma 4 0.5 from the doc comment at pplacer_src/gamma.ml:44-51.
   jplace_trees.json
       the numbered reference trees of tests/data/simple/test1.jplace and
       tests/data/trim/trim_out.jplace, with the trees parsed to post-order

@@ -159,7 +159,7 @@ def test_gpu_forward_vs_fd(small):
 @pytest.mark.parametrize("tol", [0.01, 1e-5])
 def test_single_location_optimisation(small, oracle_lib, optimizer, tol):
     """Three_tax.optimize from the default start at one location
-    (core.ml:386-425).  Newton reaches the FP64-polished optimum; the Brent
+    (core.ml:240-279).  Newton reaches the FP64-polished optimum; the Brent
     replica stops, like the reference, within its tolerance of it."""
     w, oref, eng = small
     O = oracle_lib

@@ -48,14 +48,14 @@ def test_masked_logdot_kat(oracle_lib):
 
 
 def test_discrete_gamma_kat(oracle_lib):
-    """Doc value of pplacer_src/gamma.ml:345-352."""
+    """Doc value of pplacer_src/gamma.ml:44-51."""
     k = load("gamma_kat.json")
     got = oracle_lib.discrete_gamma(k["n_cat"], k["alpha"])
     np.testing.assert_allclose(got, k["rates"], rtol=1e-12)
 
 
 def test_diagd_exp_kat(oracle_lib):
-    """tests/pplacer/test_diagd.ml:138-171 values.  diagd.ml builds
+    """tests/pplacer/test_diagd.ml:7-40 values.  diagd.ml builds
     x diag(l) x^-1 = B D (so exp rows sum to one), while that (disabled)
     reference test states expm(D B); the stated matrices are the transposes
     of what the reference code computes, and match them to the printed 8
