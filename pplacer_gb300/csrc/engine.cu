@@ -4,23 +4,25 @@
 //   darr, parr, snode : float [n_nodes][n_sites][planes][n_states]   site-major,
 //                       one site of all rate planes is contiguous (64 B for DNA G4)
 //   dexp, pexp, sexp  : int32 [n_nodes][n_sites] exact per-site scaling exponents
-//   lt                : float [n_edges][prim][n_sites] stage-1 log table
+//   B3, BX            : bf16 [3][prim][n_edges][Sp], [2][n_edges][Sp] stage-1 tables
+//                       (log-likelihood terms, rebased exponent digits)
 //   queries           : codes, masked-site index lists (reind) and codes, lengths
 //
 // Pipeline of one placement call (pplacer_src/core.ml:113-409):
 //   query prep -> stage-1 log table (once per start_pend) -> stage-1 scores
-//   -> per-query ranking -> baseball rounds of speculative stage-2 trials ->
-//   keep / refine trials -> like_weight_ratio and output.
+//   on the tensor cores -> per-query ranking -> whole-query stage 2, keep,
+//   refinement and like_weight_ratio (or baseball rounds of per-trial
+//   launches) -> output.
 #include <math.h>
 
 #include <algorithm>
 #include <cstring>
 #include <vector>
 
-#include <cublas_v2.h>
 #include <cuda_bf16.h>
 
 #include "pgb_common.cuh"
+#include "stage1_tc.cuh"
 #include "tc.cuh"
 
 namespace pgb {
@@ -331,22 +333,12 @@ __global__ void k_query_prep(const char *__restrict__ seqs, int S, int prim, con
 }
 
 // ---------------------------------------------------------------------------
-// Stage 1 (core.ml:187-197, Glv.masked_logdot against every supernode).
-// The query side is the full query evolved by start_pend, so its value at a
-// site depends only on the site's character.  With
-//   T[e][c][s] = log(sum_r sum_k qe_c[r][k] snode_e[s][r][k])
-// the score of (query q, edge e) is sum over q's informative sites of
-// T[e][code(q, s)][s]: a dense product of the one-hot query matrix
-// A[q][c*Sp + s] with T, done as a bf16 tensor-core GEMM with FP32
-// accumulation on T split into three bf16 terms (hi + mid + lo carry 24
-// mantissa bits).  The exact integer exponent sums come from two more GEMMs
-// of the informative-site mask with the supernode exponents split into
-// base-256 digits (exact in bf16, exact FP32 sums).  Sites with ambiguity
-// characters (outside the one-hot primary set) are added by k_s1_ambig.
+// Stage 1 (core.ml:187-197, Glv.masked_logdot against every supernode): the
+// edge-side tables here, the contraction on the tensor cores in
+// stage1_tc.cuh (k_s1_mma), ambiguity characters in k_s1_ambig.
 // ---------------------------------------------------------------------------
 struct S1Ctx {
   int S, Sp, RP, K, NM, gcat, ncode, prim, n_edges;
-  int Ep;  // edge rows of the tables: n_edges rounded up to 16 (zero rows past n_edges)
   const float *snode;        // [n_nodes][S][RP][K]
   const int *sexp;           // [n_nodes][S]
   const int *edge_nodes;     // [n_edges]
@@ -365,74 +357,57 @@ __device__ __forceinline__ float s1_util(const S1Ctx &c, int node, int s, int co
   return u;
 }
 
-// Edge-side tables, once per start_pend: B3 = hi/mid/lo bf16 of T,
-// [3][Ep][prim * Sp]; BX = base-256 digits of the exponents, [2][Ep][Sp].
-__global__ void k_s1_tables(S1Ctx c, __nv_bfloat16 *B3, __nv_bfloat16 *BX) {
-  long n = (long)c.n_edges * c.Sp;
-  long K4 = (long)c.prim * c.Sp;
-  long plane = (long)c.Ep * K4;
-  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
-    int ei = (int)(t / c.Sp), s = (int)(t - (long)ei * c.Sp);
-    int node = c.edge_nodes[ei];
+// Edge-side tables, once per start_pend, one block per edge:
+//   B3[plane][code][edge][s]: T split into bf16 hi / mid / lo (plane 0..2);
+//   BX[digit][edge][s]: the exponents rebased by the edge's mean,
+//     ex - base = 256 hi + lo with lo in [0, 255], as 256 hi and lo (exact in
+//     bf16 while |ex - base| < 2^15);
+//   ebase[edge] = base.
+// err is set when an edge breaks the exactness bounds of the exponent sums
+// (a per-site deviation of 2^15 or more, or digit sums reaching 2^24).
+__global__ void __launch_bounds__(256) k_s1_tables(S1Ctx c, __nv_bfloat16 *B3, __nv_bfloat16 *BX, int *ebase,
+                                                   int *err) {
+  __shared__ long long sh[8];
+  const int ei = blockIdx.x;
+  const int node = c.edge_nodes[ei];
+  const int *ex = c.sexp + (long)node * c.S;
+  long long sum = 0;
+  for (int s = threadIdx.x; s < c.S; s += blockDim.x) sum += ex[s];
+  sum = s1::block_sum_ll(sum, sh);
+  long long b = sum / c.S;
+  if (b * c.S > sum) b--;  // floor of the mean
+  const int base = (int)b;
+  const size_t plane = (size_t)c.prim * c.n_edges * c.Sp;
+  long long digits = 0;
+  int bad = 0;
+  for (int s = threadIdx.x; s < c.S; s += blockDim.x) {
     for (int code = 0; code < c.prim; code++) {
-      float v = 0.f;
-      if (s < c.S) {
-        double lg = log((double)s1_util(c, node, s, code));
-        if (!(lg > -1e30)) lg = -1e30;  // log 0 (and NaN) -> a finite -1e30: 0 * inf would poison the GEMM
-        if (lg > 1e30) lg = 1e30;
-        v = (float)lg;
-      }
-      __nv_bfloat16 hi = __float2bfloat16_rn(v);
-      float r1 = v - __bfloat162float(hi);
-      __nv_bfloat16 mid = __float2bfloat16_rn(r1);
-      __nv_bfloat16 lo = __float2bfloat16_rn(r1 - __bfloat162float(mid));
-      long o = (long)ei * K4 + (long)code * c.Sp + s;
+      double lg = log((double)s1_util(c, node, s, code));
+      if (!(lg > -1e30)) lg = -1e30;  // log 0 (and NaN) -> a finite -1e30: 0 * inf would poison the sums
+      if (lg > 1e30) lg = 1e30;
+      const float v = (float)lg;
+      const __nv_bfloat16 hi = __float2bfloat16_rn(v);
+      const float r1 = v - __bfloat162float(hi);
+      const __nv_bfloat16 mid = __float2bfloat16_rn(r1);
+      const __nv_bfloat16 lo = __float2bfloat16_rn(r1 - __bfloat162float(mid));
+      const size_t o = ((size_t)code * c.n_edges + ei) * c.Sp + s;
       B3[o] = hi;
       B3[plane + o] = mid;
       B3[2 * plane + o] = lo;
     }
-    int ex = s < c.S ? c.sexp[(long)node * c.S + s] : 0;
-    int ehi = ex >> 8;          // floor(ex / 256)
-    int elo = ex - (ehi << 8);  // 0..255
-    BX[(long)ei * c.Sp + s] = __float2bfloat16_rn((float)ehi);
-    BX[(long)c.Ep * c.Sp + (long)ei * c.Sp + s] = __float2bfloat16_rn((float)elo);
+    const int d = ex[s] - base;
+    bad |= d >= 32768 || d < -32768;
+    const int dh = d >> 8;          // floor(d / 256)
+    const int dl = d - (dh << 8);   // 0..255
+    digits += 256LL * (dh < 0 ? -dh : dh) + dl;
+    BX[(size_t)ei * c.Sp + s] = __float2bfloat16_rn(256.f * (float)dh);
+    BX[(size_t)c.n_edges * c.Sp + (size_t)ei * c.Sp + s] = __float2bfloat16_rn((float)dl);
   }
-}
-
-// Query side: one-hot rows A[q][c * Sp + s] and the informative mask M[q][s].
-__global__ void k_s1_query(int S, int Sp, int prim, const uint8_t *__restrict__ qcode,
-                           const uint8_t *__restrict__ informative, const int *__restrict__ qstatus,
-                           __nv_bfloat16 *A, __nv_bfloat16 *M) {
-  int q = blockIdx.x;
-  bool ok = qstatus[q] == PGB_Q_OK;
-  const __nv_bfloat16 one = __float2bfloat16_rn(1.f), zero = __float2bfloat16_rn(0.f);
-  long K4 = (long)prim * Sp;
-  for (int s = threadIdx.x; s < Sp; s += blockDim.x) {
-    int code = (ok && s < S) ? qcode[(long)q * S + s] : kBadCode;
-    bool inf = code != kBadCode && informative[code];
-    for (int c = 0; c < prim; c++) A[(long)q * K4 + (long)c * Sp + s] = (inf && code == c) ? one : zero;
-    M[(long)q * Sp + s] = inf ? one : zero;
-  }
-}
-
-// scores = T-sum - n log R + ln2 * exponent sum
-__device__ __forceinline__ double s1_score(const float *__restrict__ C, const float *__restrict__ Xhi,
-                                           const float *__restrict__ Xlo, long tp, int qlen, double log_nrates) {
-  long long ex = 256LL * __float2ll_rn(Xhi[tp]) + __float2ll_rn(Xlo[tp]);
-  return (double)C[tp] - (double)(float)qlen * log_nrates + kLn2 * (double)ex;
-}
-
-// rows: the n_rows queries of qlist, or queries 0 .. n_rows - 1 when qlist is null
-__global__ void k_s1_epilogue(int n_rows, const int *__restrict__ qlist, int E, int Ep, const float *__restrict__ C,
-                              const float *__restrict__ Xhi, const float *__restrict__ Xlo,
-                              const int *__restrict__ qlen, const int *__restrict__ qstatus, double log_nrates,
-                              double *scores) {
-  long n = (long)n_rows * E;
-  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
-    int row = (int)(t / E), ei = (int)(t - (long)row * E);
-    int q = qlist ? qlist[row] : row;
-    if (qstatus[q] != PGB_Q_OK) continue;
-    scores[(long)q * E + ei] = s1_score(C, Xhi, Xlo, (long)q * Ep + ei, qlen[q], log_nrates);
+  digits = s1::block_sum_ll(digits, sh);
+  const long long nbad = s1::block_sum_ll(bad, sh);
+  if (threadIdx.x == 0) {
+    ebase[ei] = base;
+    if (nbad || digits >= s1::kMaxExpDigitSum) atomicExch(err, 1);
   }
 }
 
@@ -468,8 +443,8 @@ __device__ __forceinline__ unsigned long long s1_key(double v) {
 // Each lane keeps a sorted cache of its kRankCache best remaining edges; a
 // lane that wins pops its cache and, when it runs dry, refills it from its
 // edges ranked after the last one it gave out.  With rk well below
-// 32 * kRankCache most lanes scan their edges once, reading the scores (or
-// GEMM products) straight from global memory; ranking many edges per query
+// 32 * kRankCache most lanes scan their edges once, reading the scores
+// straight from global memory; ranking many edges per query
 // (rk = E when every edge is tried) stages the row's keys in shared memory
 // first, as the refills rescan it.
 constexpr int kRankCache = 8;
@@ -478,29 +453,15 @@ __device__ __forceinline__ bool rank_before(unsigned long long ka, int ia, unsig
   return ka > kb || (ka == kb && ia < ib);
 }
 
-// The GEMM products, when the ranking forms the scores itself (queries
-// without ambiguity characters; the others read their FP64 scores row).
-struct S1Products {
-  const float *C, *Xhi, *Xlo;
-  const int *qlen, *qamb;
-  int Ep, on;
-  double log_nrates;
-};
-
-__global__ void __launch_bounds__(128) k_rank_warp(const double *__restrict__ scores, S1Products pr, int E, int rk,
-                                                   int Q, const int *__restrict__ qstatus, int *rank,
-                                                   int keys_in_smem) {
+__global__ void __launch_bounds__(128) k_rank_warp(const double *__restrict__ scores, int E, int rk, int Q,
+                                                   const int *__restrict__ qstatus, int *rank, int keys_in_smem) {
   extern __shared__ unsigned long long rk_smem[];
   const int nw = blockDim.x >> 5, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int q = blockIdx.x * nw + w;
   if (q >= Q || qstatus[q] != PGB_Q_OK) return;
   unsigned long long *keys = rk_smem + (long)w * E;
   const double *sc = scores + (long)q * E;
-  const bool direct = pr.on && pr.qamb[q] == 0;
-  const int ql = pr.on ? pr.qlen[q] : 0;
-  auto key_of = [&](int i) {
-    return s1_key(direct ? s1_score(pr.C, pr.Xhi, pr.Xlo, (long)q * pr.Ep + i, ql, pr.log_nrates) : sc[i]);
-  };
+  auto key_of = [&](int i) { return s1_key(sc[i]); };
   if (keys_in_smem)
     for (int i = lane; i < E; i += 32) keys[i] = key_of(i);
   __syncwarp();
@@ -1110,15 +1071,19 @@ struct pgb_engine {
   bool eig_ready = false;
   int *d_dexp = nullptr, *d_pexp = nullptr, *d_sexp = nullptr;
   bool glvs_ready = false;
-  // stage 1: edge tables (bf16 GEMM operands), query operands, GEMM outputs
-  cublasHandle_t blas = nullptr;
-  int Sp = 0;                       // sites padded to a multiple of 8
+  // stage 1: edge tables (bf16 MMA operands, TMA descriptors), per-site
+  // query classes, ambiguity list
+  int Sp = 0;                       // sites padded to a multiple of 8 (table row pitch)
+  int Sc = 0;                       // sites padded to a multiple of 32 (query class row pitch)
   float *d_qe = nullptr;
-  __nv_bfloat16 *d_B3 = nullptr, *d_BX = nullptr, *d_A = nullptr, *d_M = nullptr;
-  float *d_C = nullptr, *d_Xhi = nullptr, *d_Xlo = nullptr;
-  size_t a_cap = 0, c_cap = 0;
+  __nv_bfloat16 *d_B3 = nullptr, *d_BX = nullptr;
+  int *d_ebase = nullptr, *d_s1_err = nullptr;
+  CUtensorMap tmT, tmX;
+  uint8_t *d_qc = nullptr;
+  size_t qc_cap = 0;
+  bool s1_attr = false;
   int *d_qamb = nullptr, *d_amb_list = nullptr;
-  std::vector<int> h_qamb;
+  std::vector<int> h_qamb, h_amb;
   double lt_pend = -1;
   // queries
   int Q = 0, Qcap = 0;
@@ -1217,9 +1182,52 @@ pgb_status ensure_queries(pgb_engine *e, int Q) {
 S1Ctx stage1_ctx(pgb_engine *e) {
   S1Ctx c{};
   c.S = e->S; c.Sp = e->Sp; c.RP = e->RP; c.K = e->K; c.NM = e->NM; c.gcat = e->gcat; c.ncode = e->ncode;
-  c.prim = e->prim; c.n_edges = e->n_edges; c.Ep = (e->n_edges + 15) & ~15; c.snode = e->d_snode; c.sexp = e->d_sexp;
+  c.prim = e->prim; c.n_edges = e->n_edges; c.snode = e->d_snode; c.sexp = e->d_sexp;
   c.edge_nodes = e->d_edge_nodes; c.qe = e->d_qe; c.site_cat = e->d_site_cat;
   return c;
+}
+
+typedef CUresult (*TensorMapEncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                           const cuuint64_t *, const cuuint32_t *, const cuuint32_t *,
+                                           CUtensorMapInterleave, CUtensorMapSwizzle, CUtensorMapL2promotion,
+                                           CUtensorMapFloatOOBfill);
+
+// TMA descriptors of the stage-1 tables: boxes of 32 sites x 128 edges
+// (x 1 code x 3 planes, or x 2 digits), 64-byte swizzle, zero fill past the
+// last site and edge.
+pgb_status encode_stage1_maps(pgb_engine *e) {
+  static TensorMapEncodeTiledFn enc = nullptr;
+  if (!enc) {
+    void *fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !fn) {
+      set_error("stage 1: cuTensorMapEncodeTiled entry point unavailable");
+      return PGB_ERR_CUDA;
+    }
+    enc = reinterpret_cast<TensorMapEncodeTiledFn>(fn);
+  }
+  const cuuint64_t row = (cuuint64_t)e->Sp * 2;
+  {
+    cuuint64_t dim[4] = {(cuuint64_t)e->S, (cuuint64_t)e->n_edges, (cuuint64_t)e->prim, 3};
+    cuuint64_t stride[3] = {row, row * e->n_edges, row * e->n_edges * e->prim};
+    cuuint32_t box[4] = {s1::kSites, s1::kEdges, 1, 3}, es[4] = {1, 1, 1, 1};
+    CUresult r = enc(&e->tmT, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, e->d_B3, dim, stride, box, es,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) { set_error("stage 1: tensor map of the log tables (%d)", (int)r); return PGB_ERR_CUDA; }
+  }
+  {
+    cuuint64_t dim[3] = {(cuuint64_t)e->S, (cuuint64_t)e->n_edges, 2};
+    cuuint64_t stride[2] = {row, row * e->n_edges};
+    cuuint32_t box[3] = {s1::kSites, s1::kEdges, 2}, es[3] = {1, 1, 1};
+    CUresult r = enc(&e->tmX, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, e->d_BX, dim, stride, box, es,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) { set_error("stage 1: tensor map of the exponent digits (%d)", (int)r); return PGB_ERR_CUDA; }
+  }
+  return PGB_OK;
 }
 
 pgb_status build_stage1_table(pgb_engine *e, double start_pend) {
@@ -1240,81 +1248,75 @@ pgb_status build_stage1_table(pgb_engine *e, double start_pend) {
     }
   pgb_status s;
   if ((s = upload(&e->d_qe, qe.data(), qe.size(), e->st))) return s;
-  size_t K4 = (size_t)e->prim * e->Sp;
-  const size_t Ep = (size_t)((e->n_edges + 15) & ~15);
+  const size_t plane = (size_t)e->prim * e->n_edges * e->Sp;
   if (!e->d_B3) {
-    if ((s = dalloc(&e->d_B3, 3 * Ep * K4)) || (s = dalloc(&e->d_BX, 2 * Ep * e->Sp))) return s;
-    PGB_CUDA(cudaMemsetAsync(e->d_B3, 0, 3 * Ep * K4 * sizeof(__nv_bfloat16), e->st));  // zero pad rows
-    PGB_CUDA(cudaMemsetAsync(e->d_BX, 0, 2 * Ep * e->Sp * sizeof(__nv_bfloat16), e->st));
+    if ((s = dalloc(&e->d_B3, 3 * plane)) || (s = dalloc(&e->d_BX, 2 * (size_t)e->n_edges * e->Sp)) ||
+        (s = dalloc(&e->d_ebase, e->n_edges)) || (s = dalloc(&e->d_s1_err, 8)))
+      return s;
+    if ((s = encode_stage1_maps(e))) return s;
   }
-  k_s1_tables<<<grid_for((long)e->n_edges * e->Sp), 256, 0, e->st>>>(stage1_ctx(e), e->d_B3, e->d_BX);
+  PGB_CUDA(cudaMemsetAsync(e->d_s1_err, 0, 8 * sizeof(int), e->st));
+  k_s1_tables<<<e->n_edges, 256, 0, e->st>>>(stage1_ctx(e), e->d_B3, e->d_BX, e->d_ebase, e->d_s1_err);
   PGB_LAUNCH_CHECK();
+  int h = 0;
+  PGB_CUDA(cudaMemcpyAsync(&h, e->d_s1_err, sizeof h, cudaMemcpyDeviceToHost, e->st));
+  PGB_CUDA(cudaStreamSynchronize(e->st));
+  if (h) {
+    set_error("stage 1: supernode exponents vary too much along an edge for exact FP32 sums "
+              "(per-site deviation from the edge mean >= 2^15, or digit sums >= 2^24)");
+    return PGB_ERR_ARG;
+  }
   e->lt_pend = start_pend;
   return PGB_OK;
 }
 
-pgb_status gemm_bf16(pgb_engine *e, const __nv_bfloat16 *B, const __nv_bfloat16 *A, float *C, int m, int n, int k,
-                     int ldc, float beta) {
-  // row-major C[n][ldc] = A[n][k] * B[m][k]^T, i.e. column-major C' = B'^T A'
-  const float alpha = 1.f;
-  cublasStatus_t st = cublasGemmEx(e->blas, CUBLAS_OP_T, CUBLAS_OP_N, m, n, k, &alpha, B, CUDA_R_16BF, k, A,
-                                   CUDA_R_16BF, k, &beta, C, CUDA_R_32F, ldc, CUBLAS_COMPUTE_32F, CUBLAS_GEMM_DEFAULT);
-  if (st != CUBLAS_STATUS_SUCCESS) {
-    set_error("stage 1: cublasGemmEx failed (%d)", (int)st);
-    return PGB_ERR_CUDA;
+// Per-site classes of the loaded queries (the B operands of k_s1_mma) and
+// the list of queries with ambiguity characters; once per query load.
+pgb_status prep_stage1_queries(pgb_engine *e) {
+  pgb_status s;
+  const int rows = (e->Q + s1::kQueries - 1) / s1::kQueries * s1::kQueries;
+  const size_t n = (size_t)rows * e->Sc;
+  if (n > e->qc_cap) {
+    if ((s = dalloc(&e->d_qc, n))) return s;
+    e->qc_cap = n;
   }
+  s1::k_s1_qclass<<<rows, 128, 0, e->st>>>(e->Q, e->S, e->Sc, e->prim, e->d_qcode, e->d_informative, e->d_qstatus,
+                                       e->d_qc);
+  PGB_LAUNCH_CHECK();
+  e->h_amb.clear();
+  for (int q = 0; q < e->Q; q++)
+    if (e->h_qamb[q] > 0) e->h_amb.push_back(q);
+  if (!e->h_amb.empty())
+    PGB_CUDA(cudaMemcpyAsync(e->d_amb_list, e->h_amb.data(), e->h_amb.size() * 4, cudaMemcpyHostToDevice, e->st));
   return PGB_OK;
 }
 
-// all_scores: write every query's FP64 scores; otherwise only the queries
-// with ambiguity characters get them (the ranking forms the others' scores
-// from the GEMM products itself)
-pgb_status run_stage1(pgb_engine *e, bool all_scores = true) {
+// Every query's FP64 scores [Q][n_edges]: the tensor-core contraction, then
+// the ambiguity characters of the queries that have them.
+pgb_status run_stage1(pgb_engine *e) {
   pgb_status s;
-  size_t K4 = (size_t)e->prim * e->Sp;
   size_t qe_n = (size_t)e->Q * e->n_edges;
   if (qe_n > e->scores_cap) {
     if ((s = dalloc(&e->d_scores, qe_n))) return s;
     e->scores_cap = qe_n;
   }
-  if ((size_t)e->Q > e->a_cap) {
-    if ((s = dalloc(&e->d_A, (size_t)e->Q * K4)) || (s = dalloc(&e->d_M, (size_t)e->Q * e->Sp))) return s;
-    e->a_cap = e->Q;
+  if (e->Q < 1) return PGB_OK;
+  s1::MmaCtx c{};
+  c.S = e->S; c.n_chunks = e->Sc / s1::kSites; c.prim = e->prim; c.n_edges = e->n_edges; c.Q = e->Q;
+  c.n_qtiles = (e->Q + s1::kQueries - 1) / s1::kQueries; c.Sc = e->Sc;
+  c.qc = e->d_qc; c.qlen = e->d_qlen; c.qstatus = e->d_qstatus; c.ebase = e->d_ebase;
+  c.log_nrates = e->gcat ? 0.0 : log((double)(float)e->NM);
+  c.scores = e->d_scores;
+  c.err = e->d_s1_err;
+  if (!e->s1_attr) {  // per engine, and so per device
+    PGB_CUDA(cudaFuncSetAttribute(s1::k_s1_mma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s1::kSmemBytes));
+    e->s1_attr = true;
   }
-  // FP32 products in rows of Ep = n_edges rounded up to 16: 64-byte aligned
-  // rows let the GEMM use its widest vector loads and stores
-  const int Ep = (e->n_edges + 15) & ~15;
-  size_t qep_n = (size_t)e->Q * Ep;
-  if (qep_n > e->c_cap) {
-    if ((s = dalloc(&e->d_C, qep_n)) || (s = dalloc(&e->d_Xhi, qep_n)) || (s = dalloc(&e->d_Xlo, qep_n))) return s;
-    e->c_cap = qep_n;
-  }
-  k_s1_query<<<e->Q, 256, 0, e->st>>>(e->S, e->Sp, e->prim, e->d_qcode, e->d_informative, e->d_qstatus, e->d_A,
-                                      e->d_M);
+  const int n_etiles = (e->n_edges + s1::kEdges - 1) / s1::kEdges;
+  s1::k_s1_mma<<<n_etiles * c.n_qtiles, s1::kThreads, s1::kSmemBytes, e->st>>>(e->tmT, e->tmX, c);
   PGB_LAUNCH_CHECK();
-  // m = Ep rows (the pad rows are zero): every extent and leading dimension
-  // a multiple of 16 elements
-  size_t plane = (size_t)Ep * K4;
-  for (int piece = 0; piece < 3; piece++)
-    if ((s = gemm_bf16(e, e->d_B3 + piece * plane, e->d_A, e->d_C, Ep, e->Q, (int)K4, Ep, piece ? 1.f : 0.f)))
-      return s;
-  if ((s = gemm_bf16(e, e->d_BX, e->d_M, e->d_Xhi, Ep, e->Q, e->Sp, Ep, 0.f)) ||
-      (s = gemm_bf16(e, e->d_BX + (size_t)Ep * e->Sp, e->d_M, e->d_Xlo, Ep, e->Q, e->Sp, Ep, 0.f)))
-    return s;
-  double log_nrates = e->gcat ? 0.0 : log((double)(float)e->NM);
-  std::vector<int> amb;
-  for (int q = 0; q < e->Q; q++)
-    if (e->h_qamb[q] > 0) amb.push_back(q);
-  if (!amb.empty()) PGB_CUDA(cudaMemcpyAsync(e->d_amb_list, amb.data(), amb.size() * 4, cudaMemcpyHostToDevice, e->st));
-  if (all_scores || !amb.empty()) {
-    const int rows = all_scores ? e->Q : (int)amb.size();
-    k_s1_epilogue<<<grid_for((long)rows * e->n_edges), 256, 0, e->st>>>(
-        rows, all_scores ? nullptr : e->d_amb_list, e->n_edges, Ep, e->d_C, e->d_Xhi, e->d_Xlo, e->d_qlen,
-        e->d_qstatus, log_nrates, e->d_scores);
-    PGB_LAUNCH_CHECK();
-  }
-  if (!amb.empty()) {
-    dim3 grid((unsigned)amb.size(), (unsigned)((e->n_edges + 127) / 128));
+  if (!e->h_amb.empty()) {
+    dim3 grid((unsigned)e->h_amb.size(), (unsigned)((e->n_edges + 127) / 128));
     k_s1_ambig<<<grid, 128, 0, e->st>>>(stage1_ctx(e), e->d_amb_list, e->d_reind, e->d_mcode, e->d_qlen,
                                         e->d_scores);
     PGB_LAUNCH_CHECK();
@@ -1322,9 +1324,7 @@ pgb_status run_stage1(pgb_engine *e, bool all_scores = true) {
   return PGB_OK;
 }
 
-// fused: the scores of queries without ambiguity characters come from the
-// GEMM products (run_stage1 with all_scores false)
-pgb_status run_rank(pgb_engine *e, int rk, bool fused = false) {
+pgb_status run_rank(pgb_engine *e, int rk) {
   const int E = e->n_edges;
   const size_t keys = (size_t)E * 8;
   // up to 4 warps (queries) per block; keys staged (within 96 KB) only for
@@ -1337,13 +1337,8 @@ pgb_status run_rank(pgb_engine *e, int rk, bool fused = false) {
   size_t smem = in_smem ? nw * keys : 0;
   if (smem > 48 * 1024)
     PGB_CUDA(cudaFuncSetAttribute(k_rank_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  S1Products pr{};
-  pr.on = fused ? 1 : 0;
-  pr.C = e->d_C; pr.Xhi = e->d_Xhi; pr.Xlo = e->d_Xlo; pr.qlen = e->d_qlen; pr.qamb = e->d_qamb;
-  pr.Ep = (E + 15) & ~15;
-  pr.log_nrates = e->gcat ? 0.0 : log((double)(float)e->NM);
-  k_rank_warp<<<(e->Q + nw - 1) / nw, 32 * nw, smem, e->st>>>(e->d_scores, pr, E, rk, e->Q, e->d_qstatus,
-                                                              e->d_rank, in_smem);
+  k_rank_warp<<<(e->Q + nw - 1) / nw, 32 * nw, smem, e->st>>>(e->d_scores, E, rk, e->Q, e->d_qstatus, e->d_rank,
+                                                              in_smem);
   PGB_LAUNCH_CHECK();
   return PGB_OK;
 }
@@ -1470,7 +1465,18 @@ pgb_status launch_trials_tc(pgb_engine *e, cudaStream_t st, TrialCtx c, const in
 }
 
 // the tensor-core kernel's completion-wait flag: an error once set
+// Error records of the tensor-core kernels (bounded waits that timed out).
 pgb_status check_tc_err(pgb_engine *e) {
+  if (e->d_s1_err) {
+    int g[4];
+    PGB_CUDA(cudaMemcpy(g, e->d_s1_err, sizeof g, cudaMemcpyDeviceToHost));
+    if (g[0]) {
+      PGB_CUDA(cudaMemsetAsync(e->d_s1_err, 0, sizeof g, e->st));
+      set_error("stage-1 tensor-core kernel: a pipeline wait timed out (role %d, unit %d, block %d)", g[1], g[2],
+                g[3]);
+      return PGB_ERR_CUDA;
+    }
+  }
   int h[16];
   PGB_CUDA(cudaMemcpy(h, e->d_tc_err, sizeof h, cudaMemcpyDeviceToHost));
   if (h[0]) {
@@ -1833,6 +1839,7 @@ pgb_status pgb_engine_create(const pgb_model_desc *m, const pgb_tree_desc *t, pg
   e->ncode = n_codes(e->K);
   e->prim = e->K;
   e->Sp = (e->S + 7) & ~7;
+  e->Sc = (e->S + s1::kSites - 1) / s1::kSites * s1::kSites;
   int K = e->K;
   e->statd.assign(m->statd, m->statd + K);
   e->X.assign(m->x, m->x + K * K);
@@ -1874,11 +1881,6 @@ pgb_status pgb_engine_create(const pgb_model_desc *m, const pgb_tree_desc *t, pg
   if ((ce = cudaGetDevice(&e->device)) != cudaSuccess || (ce = cudaStreamCreateWithFlags(&e->st, cudaStreamNonBlocking)) != cudaSuccess) {
     set_error("engine_create: %s", cudaGetErrorString(ce));
     delete e;
-    return PGB_ERR_CUDA;
-  }
-  if (cublasCreate(&e->blas) != CUBLAS_STATUS_SUCCESS || cublasSetStream(e->blas, e->st) != CUBLAS_STATUS_SUCCESS) {
-    set_error("engine_create: cuBLAS initialisation failed");
-    pgb_engine_destroy(e);
     return PGB_ERR_CUDA;
   }
   int optin = 0;
@@ -1979,7 +1981,7 @@ pgb_status pgb_engine_destroy(pgb_engine *e) {
   void *ptrs[] = {e->d_bl, e->d_Xd, e->d_Xitd, e->d_lamd, e->d_ratesd, e->d_statdd, e->d_lvd, e->d_pm, e->d_pmh,
                   e->d_mf, e->d_site_cat, e->d_char_code, e->d_informative, e->d_edge_nodes, e->d_parent,
                   e->d_ch_start, e->d_ch_list, e->d_darr, e->d_parr, e->d_snode, e->d_dexp, e->d_pexp, e->d_sexp,
-                  e->d_qe, e->d_B3, e->d_BX, e->d_A, e->d_M, e->d_C, e->d_Xhi, e->d_Xlo, e->d_qamb,
+                  e->d_qe, e->d_B3, e->d_BX, e->d_ebase, e->d_s1_err, e->d_qc, e->d_qamb,
                   e->d_amb_list, e->d_seqs, e->d_qcode, e->d_mcode, e->d_reind, e->d_rcode, e->d_qlen,
                   e->d_qstatus, e->d_scores, e->d_rank, e->d_bb, e->d_res, e->d_tbase, e->d_tcount, e->d_keep_idx, e->d_keep_n,
                   e->d_trials, e->d_tres, e->d_bin_list, e->d_small, e->d_out, e->d_nout, e->d_stats,
@@ -1993,7 +1995,6 @@ pgb_status pgb_engine_destroy(pgb_engine *e) {
     if (e->bin_st[i]) cudaStreamDestroy(e->bin_st[i]);
   for (int i = 0; i < 9; i++)
     if (e->bin_ev[i]) cudaEventDestroy(e->bin_ev[i]);
-  if (e->blas) cublasDestroy(e->blas);
   if (e->st) cudaStreamDestroy(e->st);
   delete e;
   return PGB_OK;
@@ -2181,6 +2182,7 @@ pgb_status pgb_engine_refine_categories(pgb_engine *e, const int *leaf_row, cons
   PGB_CUDA(cudaMemcpyAsync(e->d_site_cat, sc.data(), S, cudaMemcpyHostToDevice, e->st));
   pgb_status us = upload_col_order(e);  // the site lists follow the new categories
   if (!us) us = prep_queries(e);
+  if (!us && e->Q > 0) us = prep_stage1_queries(e);
   if (us) return us;
   PGB_CUDA(cudaStreamSynchronize(e->st));
   e->glvs_ready = false;  // the placement GLVs follow the categories: precompute again
@@ -2284,6 +2286,7 @@ pgb_status pgb_queries_load(pgb_engine *e, int n_queries, const char *seqs) {
   for (int i = 0; i < n_queries; i++) ord[i] = i;
   std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return e->h_qlen[a] > e->h_qlen[b]; });
   PGB_CUDA(cudaMemcpyAsync(e->d_qorder, ord.data(), ord.size() * sizeof(int), cudaMemcpyHostToDevice, e->st));
+  if ((s = prep_stage1_queries(e))) return s;
   PGB_CUDA(cudaStreamSynchronize(e->st));
   return PGB_OK;
 }
@@ -2306,7 +2309,7 @@ pgb_status pgb_queries_stage1(pgb_engine *e, const pgb_prefs *p, double *scores)
   if ((s = check_prefs(p)) || (s = build_stage1_table(e, p->start_pend)) || (s = run_stage1(e))) return s;
   PGB_CUDA(cudaMemcpyAsync(scores, e->d_scores, (size_t)e->Q * e->n_edges * 8, cudaMemcpyDeviceToHost, e->st));
   PGB_CUDA(cudaStreamSynchronize(e->st));
-  return PGB_OK;
+  return check_tc_err(e);
 }
 
 pgb_status pgb_queries_rank(pgb_engine *e, const pgb_prefs *p, int rk, int *rank) {
@@ -2317,11 +2320,11 @@ pgb_status pgb_queries_rank(pgb_engine *e, const pgb_prefs *p, int rk, int *rank
   size_t rn = (size_t)e->Q * rk;
   if (rn > e->rank_cap) { if ((s = dalloc(&e->d_rank, rn))) return s; e->rank_cap = rn; }
   PGB_CUDA(cudaMemsetAsync(e->d_rank, 0xff, rn * sizeof(int), e->st));
-  if ((s = build_stage1_table(e, p->start_pend)) || (s = run_stage1(e, false)) || (s = run_rank(e, rk, true)))
+  if ((s = build_stage1_table(e, p->start_pend)) || (s = run_stage1(e)) || (s = run_rank(e, rk)))
     return s;
   PGB_CUDA(cudaMemcpyAsync(rank, e->d_rank, rn * sizeof(int), cudaMemcpyDeviceToHost, e->st));
   PGB_CUDA(cudaStreamSynchronize(e->st));
-  return PGB_OK;
+  return check_tc_err(e);
 }
 
 pgb_status pgb_queries_run(pgb_engine *e, const pgb_prefs *p) {
@@ -2343,8 +2346,8 @@ pgb_status pgb_queries_run(pgb_engine *e, const pgb_prefs *p) {
   PGB_CUDA(cudaEventRecord(e->ev[0], e->st));
   if ((s = build_stage1_table(e, p->start_pend))) return s;
   PGB_CUDA(cudaEventRecord(e->ev[1], e->st));
-  if ((s = run_stage1(e, false))) return s;
-  if ((s = run_rank(e, rk, true))) return s;
+  if ((s = run_stage1(e))) return s;
+  if ((s = run_rank(e, rk))) return s;
   PGB_CUDA(cudaEventRecord(e->ev[2], e->st));
   e->counts[0] = (double)e->Q * e->n_edges;
   // baseball rounds
