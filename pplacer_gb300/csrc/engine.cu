@@ -335,7 +335,8 @@ __global__ void k_query_prep(const char *__restrict__ seqs, int S, int prim, con
 // ---------------------------------------------------------------------------
 // Stage 1 (core.ml:187-197, Glv.masked_logdot against every supernode): the
 // edge-side tables here, the contraction on the tensor cores in
-// stage1_tc.cuh (k_s1_mma), ambiguity characters in k_s1_ambig.
+// stage1_tc.cuh (k_s1_mma), FP64 scores and ambiguity characters in
+// k_s1_scores.
 // ---------------------------------------------------------------------------
 struct S1Ctx {
   int S, Sp, RP, K, NM, gcat, ncode, prim, n_edges;
@@ -407,23 +408,31 @@ __global__ void __launch_bounds__(256) k_s1_tables(S1Ctx c, __nv_bfloat16 *B3, _
   const long long nbad = s1::block_sum_ll(bad, sh);
   if (threadIdx.x == 0) {
     ebase[ei] = base;
-    if (nbad || digits >= s1::kMaxExpDigitSum) atomicExch(err, 1);
+    // the epilogue's int32 total, base * n_q + digit sum, stays exact
+    if (nbad || digits >= s1::kMaxExpDigitSum || (b < 0 ? -b : b) * c.S >= (1LL << 30)) atomicExch(err, 1);
   }
 }
 
-// Ambiguity characters of the listed queries, every edge.
-__global__ void k_s1_ambig(S1Ctx c, const int *__restrict__ qlist, const uint16_t *__restrict__ reind,
-                           const uint8_t *__restrict__ mcode, const int *__restrict__ qlen, double *scores) {
-  int q = qlist[blockIdx.x];
-  int ei = blockIdx.y * blockDim.x + threadIdx.x;
-  if (ei >= c.n_edges) return;
-  int node = c.edge_nodes[ei];
+// FP64 scores of the n_rows listed queries: the tensor-core pair plus, when
+// `ambig`, the logs of the site likelihoods of their ambiguity characters.
+__global__ void k_s1_scores(S1Ctx c, int n_rows, const int *__restrict__ qlist, int ambig,
+                            const uint16_t *__restrict__ reind, const uint8_t *__restrict__ mcode,
+                            const int *__restrict__ qlen, const int *__restrict__ qstatus,
+                            const int2 *__restrict__ pairs, double log_nrates, double *scores) {
+  const int row = blockIdx.x;
+  if (row >= n_rows) return;
+  const int q = qlist[row];
+  const int ei = blockIdx.y * blockDim.x + threadIdx.x;
+  if (ei >= c.n_edges || qstatus[q] != PGB_Q_OK) return;
+  const int node = c.edge_nodes[ei];
   double acc = 0;
-  for (int i = 0; i < qlen[q]; i++) {
-    int code = mcode[(long)q * c.S + i];
-    if (code >= c.prim) acc += log((double)s1_util(c, node, reind[(long)q * c.S + i], code));
-  }
-  scores[(long)q * c.n_edges + ei] += acc;
+  if (ambig)
+    for (int i = 0; i < qlen[q]; i++) {
+      const int code = mcode[(long)q * c.S + i];
+      if (code >= c.prim) acc += log((double)s1_util(c, node, reind[(long)q * c.S + i], code));
+    }
+  const long o = (long)q * c.n_edges + ei;
+  scores[o] = s1::s1_pair_score(pairs[o], qlen[q], log_nrates) + acc;
 }
 
 // Per-query ranking: edges by score, descending, ties to the lower edge index
@@ -453,15 +462,27 @@ __device__ __forceinline__ bool rank_before(unsigned long long ka, int ia, unsig
   return ka > kb || (ka == kb && ia < ib);
 }
 
-__global__ void __launch_bounds__(128) k_rank_warp(const double *__restrict__ scores, int E, int rk, int Q,
+// The FP64 score of (q, i): formed from the tensor-core pair, or read from
+// the FP64 row of a query with ambiguity characters.
+struct S1Scores {
+  const int2 *pairs;
+  const double *scores;
+  const int *qlen, *qamb;
+  double log_nrates;
+};
+
+__global__ void __launch_bounds__(128) k_rank_warp(S1Scores sv, int E, int rk, int Q,
                                                    const int *__restrict__ qstatus, int *rank, int keys_in_smem) {
   extern __shared__ unsigned long long rk_smem[];
   const int nw = blockDim.x >> 5, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int q = blockIdx.x * nw + w;
   if (q >= Q || qstatus[q] != PGB_Q_OK) return;
   unsigned long long *keys = rk_smem + (long)w * E;
-  const double *sc = scores + (long)q * E;
-  auto key_of = [&](int i) { return s1_key(sc[i]); };
+  const bool amb = sv.qamb[q] > 0;
+  const double *sc = sv.scores + (long)q * E;
+  const int2 *pr = sv.pairs + (long)q * E;
+  const int ql = sv.qlen[q];
+  auto key_of = [&](int i) { return s1_key(amb ? sc[i] : s1::s1_pair_score(pr[i], ql, sv.log_nrates)); };
   if (keys_in_smem)
     for (int i = lane; i < E; i += 32) keys[i] = key_of(i);
   __syncwarp();
@@ -1094,8 +1115,13 @@ struct pgb_engine {
   int *d_qlen = nullptr, *d_qstatus = nullptr;
   std::vector<int> h_qlen;
   // run buffers
-  double *d_scores = nullptr;
+  double *d_scores = nullptr;  // FP64 stage-1 rows of queries with ambiguity characters (or all, on request)
   size_t scores_cap = 0;
+  int2 *d_pairs = nullptr;     // tensor-core stage-1 pairs (C, exponent sum) [Q][n_edges]
+  size_t pairs_cap = 0;
+  int *d_plain_list = nullptr;
+  size_t plain_cap = 0;
+  int s1_nq = 0;               // the last stage-1 launch's query tile width
   int *d_rank = nullptr;
   size_t rank_cap = 0;
   BBState *d_bb = nullptr;
@@ -1262,8 +1288,8 @@ pgb_status build_stage1_table(pgb_engine *e, double start_pend) {
   PGB_CUDA(cudaMemcpyAsync(&h, e->d_s1_err, sizeof h, cudaMemcpyDeviceToHost, e->st));
   PGB_CUDA(cudaStreamSynchronize(e->st));
   if (h) {
-    set_error("stage 1: supernode exponents vary too much along an edge for exact FP32 sums "
-              "(per-site deviation from the edge mean >= 2^15, or digit sums >= 2^24)");
+    set_error("stage 1: supernode exponents out of the exact range of the tensor-core sums "
+              "(per-site deviation from the edge mean >= 2^15, digit sums >= 2^24, or mean x sites >= 2^30)");
     return PGB_ERR_ARG;
   }
   e->lt_pend = start_pend;
@@ -1274,7 +1300,8 @@ pgb_status build_stage1_table(pgb_engine *e, double start_pend) {
 // the list of queries with ambiguity characters; once per query load.
 pgb_status prep_stage1_queries(pgb_engine *e) {
   pgb_status s;
-  const int rows = (e->Q + s1::kQueries - 1) / s1::kQueries * s1::kQueries;
+  // rows for any query tile width up to 256 (n_qtiles * nq < Q + 256)
+  const int rows = (e->Q + s1::kQueries - 1) / s1::kQueries * s1::kQueries + s1::kQueries;
   const size_t n = (size_t)rows * e->Sc;
   if (n > e->qc_cap) {
     if ((s = dalloc(&e->d_qc, n))) return s;
@@ -1291,23 +1318,57 @@ pgb_status prep_stage1_queries(pgb_engine *e) {
   return PGB_OK;
 }
 
-// Every query's FP64 scores [Q][n_edges]: the tensor-core contraction, then
-// the ambiguity characters of the queries that have them.
-pgb_status run_stage1(pgb_engine *e) {
+// Query tile width of k_s1_mma: the multiple of 16 in [128, 256] whose
+// waves over the SMs cost least.  A tile's table stream (TMA of the edge
+// rows from L2) does not shrink with its width; measured on dna_1k shapes it
+// weighs as ~450 query columns, so narrower tiles pay only when they save a
+// wave on small launches.
+int s1_tile_queries(const pgb_engine *e) {
+  const long n_etiles = (e->n_edges + s1::kEdges - 1) / s1::kEdges;
+  int best = s1::kQueries;
+  double best_cost = 1e300;
+  for (int nq = s1::kQueries; nq >= 128; nq -= 16) {
+    const long tiles = n_etiles * ((e->Q + nq - 1) / nq);
+    const long waves = (tiles + e->n_sm - 1) / e->n_sm;
+    const double cost = (double)waves * (nq + 448);
+    if (cost < best_cost - 1e-9) { best_cost = cost; best = nq; }
+  }
+  return best;
+}
+
+pgb_status launch_s1_scores(pgb_engine *e, int rows, const int *d_list, int ambig) {
+  if (rows < 1) return PGB_OK;
+  dim3 grid((unsigned)rows, (unsigned)((e->n_edges + 127) / 128));
+  k_s1_scores<<<grid, 128, 0, e->st>>>(stage1_ctx(e), rows, d_list, ambig, e->d_reind, e->d_mcode, e->d_qlen,
+                                       e->d_qstatus, e->d_pairs, e->gcat ? 0.0 : log((double)(float)e->NM),
+                                       e->d_scores);
+  PGB_LAUNCH_CHECK();
+  return PGB_OK;
+}
+
+// Stage 1 on the loaded queries: the tensor-core pairs [Q][n_edges], and the
+// FP64 score rows of the queries with ambiguity characters (all_scores:
+// every query's FP64 row, for pgb_queries_stage1).
+pgb_status run_stage1(pgb_engine *e, bool all_scores = false) {
   pgb_status s;
-  size_t qe_n = (size_t)e->Q * e->n_edges;
-  if (qe_n > e->scores_cap) {
+  const size_t qe_n = (size_t)e->Q * e->n_edges;
+  if (qe_n > e->pairs_cap) {
+    if ((s = dalloc(&e->d_pairs, qe_n))) return s;
+    e->pairs_cap = qe_n;
+  }
+  if ((all_scores || !e->h_amb.empty()) && qe_n > e->scores_cap) {
     if ((s = dalloc(&e->d_scores, qe_n))) return s;
     e->scores_cap = qe_n;
   }
   if (e->Q < 1) return PGB_OK;
   s1::MmaCtx c{};
   c.S = e->S; c.n_chunks = e->Sc / s1::kSites; c.prim = e->prim; c.n_edges = e->n_edges; c.Q = e->Q;
-  c.n_qtiles = (e->Q + s1::kQueries - 1) / s1::kQueries; c.Sc = e->Sc;
+  c.nq = s1_tile_queries(e);
+  c.n_qtiles = (e->Q + c.nq - 1) / c.nq; c.Sc = e->Sc;
   c.qc = e->d_qc; c.qlen = e->d_qlen; c.qstatus = e->d_qstatus; c.ebase = e->d_ebase;
-  c.log_nrates = e->gcat ? 0.0 : log((double)(float)e->NM);
-  c.scores = e->d_scores;
+  c.pairs = e->d_pairs;
   c.err = e->d_s1_err;
+  e->s1_nq = c.nq;
   if (!e->s1_attr) {  // per engine, and so per device
     PGB_CUDA(cudaFuncSetAttribute(s1::k_s1_mma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s1::kSmemBytes));
     e->s1_attr = true;
@@ -1315,11 +1376,20 @@ pgb_status run_stage1(pgb_engine *e) {
   const int n_etiles = (e->n_edges + s1::kEdges - 1) / s1::kEdges;
   s1::k_s1_mma<<<n_etiles * c.n_qtiles, s1::kThreads, s1::kSmemBytes, e->st>>>(e->tmT, e->tmX, c);
   PGB_LAUNCH_CHECK();
-  if (!e->h_amb.empty()) {
-    dim3 grid((unsigned)e->h_amb.size(), (unsigned)((e->n_edges + 127) / 128));
-    k_s1_ambig<<<grid, 128, 0, e->st>>>(stage1_ctx(e), e->d_amb_list, e->d_reind, e->d_mcode, e->d_qlen,
-                                        e->d_scores);
-    PGB_LAUNCH_CHECK();
+  if ((s = launch_s1_scores(e, (int)e->h_amb.size(), e->d_amb_list, 1))) return s;
+  if (all_scores) {
+    if ((size_t)e->Q > e->plain_cap) {
+      if ((s = dalloc(&e->d_plain_list, e->Q))) return s;
+      e->plain_cap = e->Q;
+    }
+    std::vector<int> plain;
+    for (int q = 0; q < e->Q; q++)
+      if (e->h_qamb[q] == 0) plain.push_back(q);
+    if (!plain.empty()) {
+      PGB_CUDA(cudaMemcpyAsync(e->d_plain_list, plain.data(), plain.size() * 4, cudaMemcpyHostToDevice, e->st));
+      if ((s = launch_s1_scores(e, (int)plain.size(), e->d_plain_list, 0))) return s;
+      PGB_CUDA(cudaStreamSynchronize(e->st));  // plain is a pageable host buffer
+    }
   }
   return PGB_OK;
 }
@@ -1337,7 +1407,8 @@ pgb_status run_rank(pgb_engine *e, int rk) {
   size_t smem = in_smem ? nw * keys : 0;
   if (smem > 48 * 1024)
     PGB_CUDA(cudaFuncSetAttribute(k_rank_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  k_rank_warp<<<(e->Q + nw - 1) / nw, 32 * nw, smem, e->st>>>(e->d_scores, E, rk, e->Q, e->d_qstatus, e->d_rank,
+  S1Scores sv{e->d_pairs, e->d_scores, e->d_qlen, e->d_qamb, e->gcat ? 0.0 : log((double)(float)e->NM)};
+  k_rank_warp<<<(e->Q + nw - 1) / nw, 32 * nw, smem, e->st>>>(sv, E, rk, e->Q, e->d_qstatus, e->d_rank,
                                                               in_smem);
   PGB_LAUNCH_CHECK();
   return PGB_OK;
@@ -1983,7 +2054,7 @@ pgb_status pgb_engine_destroy(pgb_engine *e) {
                   e->d_ch_start, e->d_ch_list, e->d_darr, e->d_parr, e->d_snode, e->d_dexp, e->d_pexp, e->d_sexp,
                   e->d_qe, e->d_B3, e->d_BX, e->d_ebase, e->d_s1_err, e->d_qc, e->d_qamb,
                   e->d_amb_list, e->d_seqs, e->d_qcode, e->d_mcode, e->d_reind, e->d_rcode, e->d_qlen,
-                  e->d_qstatus, e->d_scores, e->d_rank, e->d_bb, e->d_res, e->d_tbase, e->d_tcount, e->d_keep_idx, e->d_keep_n,
+                  e->d_qstatus, e->d_scores, e->d_pairs, e->d_plain_list, e->d_rank, e->d_bb, e->d_res, e->d_tbase, e->d_tcount, e->d_keep_idx, e->d_keep_n,
                   e->d_trials, e->d_tres, e->d_bin_list, e->d_small, e->d_out, e->d_nout, e->d_stats,
                   e->d_qorder, e->d_gl, e->d_prior_mu, e->d_darr_e, e->d_parr_e, e->d_tc_err,
                   e->d_col_order};
@@ -2306,7 +2377,7 @@ static pgb_status check_prefs(const pgb_prefs *p) {
 pgb_status pgb_queries_stage1(pgb_engine *e, const pgb_prefs *p, double *scores) {
   if (!e || !e->glvs_ready || e->Q < 1) { set_error("stage1: no GLVs or no queries"); return PGB_ERR_STATE; }
   pgb_status s;
-  if ((s = check_prefs(p)) || (s = build_stage1_table(e, p->start_pend)) || (s = run_stage1(e))) return s;
+  if ((s = check_prefs(p)) || (s = build_stage1_table(e, p->start_pend)) || (s = run_stage1(e, true))) return s;
   PGB_CUDA(cudaMemcpyAsync(scores, e->d_scores, (size_t)e->Q * e->n_edges * 8, cudaMemcpyDeviceToHost, e->st));
   PGB_CUDA(cudaStreamSynchronize(e->st));
   return check_tc_err(e);

@@ -8,8 +8,8 @@
 // and the supernode exponents ex[e][s], the score of (q, e) is
 //   sum_{s in q, code c primary} T[e][c][s]  - n_q log R
 //   + ln 2 (sum_{s informative in q} ex[e][s]),
-// ambiguity characters added afterwards by k_s1_ambig.  Per tile of 128
-// edges (MMA M, operand A) x 256 queries (MMA N, operand B):
+// ambiguity characters added afterwards by k_s1_scores.  Per tile of 128
+// edges (MMA M, operand A) x N <= 256 queries (MMA N, operand B):
 //   * A: T split into three bf16 terms (hi + mid + lo keep 24 mantissa
 //     bits), layout [plane][code][edge][site], and the exponents rebased per
 //     edge (ex - base_e) as two exact bf16 digits (256 hi, lo), layout
@@ -24,7 +24,11 @@
 //     kernel checks per edge), 256 columns each.
 // Warp roles: warp 0 issues the TMA loads, warp 1 the MMAs (one thread),
 // warps 2-5 build the B tiles and then read TMEM for the epilogue, which
-// writes the FP64 scores.  Stages are handed over through mbarriers; every
+// writes per (query, edge) the pair (C as FP32, the exact total exponent sum
+// as int32); the ranking forms the FP64 score from it (s1_pair_score), so
+// no FP64 arithmetic -- slow on this part -- sits in the tile loop.  The
+// query tile width N (a multiple of 16, up to 256) is chosen per launch to
+// fill the SMs' last wave.  Stages are handed over through mbarriers; every
 // wait is bounded and a timeout records where it happened and returns.
 #pragma once
 #include <cuda.h>
@@ -36,7 +40,7 @@ namespace s1 {
 
 constexpr int kSites = 32;                         // sites per K chunk: 64 B of bf16, one swizzle row
 constexpr int kEdges = 128;                        // MMA M
-constexpr int kQueries = 256;                      // MMA N
+constexpr int kQueries = 256;                      // MMA N at most (the launch's N: MmaCtx::nq)
 constexpr int kStages = 5;
 constexpr int kATile = kEdges * kSites * 2;        // one plane: 8 KB
 constexpr int kABytes = 3 * kATile;                // hi / mid / lo planes (the exponent unit uses two)
@@ -45,14 +49,15 @@ constexpr int kStageBytes = kABytes + kBBytes;     // 40 KB
 constexpr int kThreads = 192;
 constexpr int kGen = 128;                          // B-tile / epilogue threads (warps 2-5)
 constexpr uint32_t kTmemCols = 512;                // C: [0, 256), X: [256, 512)
-constexpr size_t kSmemBytes = (size_t)kStages * kStageBytes + 1024 + 256;
+constexpr size_t kSmemBytes = (size_t)kStages * kStageBytes + 1024 + 256 + kQueries * sizeof(int);
 constexpr int kMaxExpDigitSum = 1 << 24;           // exact FP32 integer range of the X accumulator
 constexpr double kLn2d = 0.69314718055994530942;
 
 // kind::f16 instruction descriptor: D F32, A and B BF16, both K-major,
-// N = 256, M = 128.
-constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kQueries >> 3) << 17) |
-                            ((uint32_t)(kEdges >> 4) << 24);
+// M = 128, N = nq.
+__host__ __device__ constexpr uint32_t idesc_bf16(int nq) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(nq >> 3) << 17) | ((uint32_t)(kEdges >> 4) << 24);
+}
 
 // Shared-memory descriptor of a K-major operand tile in the 64-byte swizzle
 // layout: rows of 64 B, 8-row groups 512 B apart (stride byte offset), the
@@ -64,13 +69,13 @@ __device__ __forceinline__ uint64_t sdesc_sw64(uint32_t saddr) {
          (4ull << 61);
 }
 
-__device__ __forceinline__ void mma_bf16(uint32_t dtmem, uint64_t a, uint64_t b, uint32_t accum) {
+__device__ __forceinline__ void mma_bf16(uint32_t dtmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accum) {
   asm volatile(
       "{\n\t.reg .pred p;\n\t"
       "setp.ne.b32 p, %4, 0;\n\t"
       "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t"
       "}" ::"r"(dtmem),
-      "l"(a), "l"(b), "r"(kIdesc), "r"(accum)
+      "l"(a), "l"(b), "r"(idesc), "r"(accum)
       : "memory");
 }
 
@@ -101,14 +106,20 @@ __device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap *map
 
 struct MmaCtx {
   int S, n_chunks, prim, n_edges, Q, n_qtiles, Sc;
-  const uint8_t *qc;     // [n_qtiles * 256][Sc] site classes: 0 not informative, c + 1 primary code c, 255 other
+  int nq;                // queries per tile (MMA N): a multiple of 16, 16..256
+  const uint8_t *qc;     // [>= n_qtiles * nq][Sc] site classes: 0 not informative, c + 1 primary code c, 255 other
   const int *qlen;       // informative sites per query
   const int *qstatus;
   const int *ebase;      // per-edge exponent base
-  double log_nrates;
-  double *scores;        // [Q][n_edges]
+  int2 *pairs;           // [Q][n_edges]: (C as float bits, total exponent sum)
   int *err;              // [0] flag, [1] role, [2] unit, [3] block
 };
+
+// FP64 stage-1 score of a (C, exponent sum) pair: C - n log R + ln 2 x
+// (masked_logdot's float part and the exponent term of Glv.masked_logdot).
+__device__ __forceinline__ double s1_pair_score(int2 p, int qlen, double log_nrates) {
+  return (double)__int_as_float(p.x) - (double)(float)qlen * log_nrates + kLn2d * (double)p.y;
+}
 
 // Bounded wait; gives up when another role aborted or after the poll limit
 // (then it aborts the block).
@@ -156,6 +167,9 @@ __global__ void __launch_bounds__(kThreads, 1)
   uint64_t *done = empty + kStages;
   uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(done + 1);
   volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
+  // per query column: n_q, or -1 when no score is written
+  int *q_n = reinterpret_cast<int *>(base + (size_t)kStages * kStageBytes + 256);
+  const uint32_t idesc = idesc_bf16(c.nq);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int etile = blockIdx.x / c.n_qtiles, qtile = blockIdx.x - etile * c.n_qtiles;
   const int per_chunk = c.prim + 1;  // prim code units, then the exponent unit
@@ -219,7 +233,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           for (int p = 0; p < 3; p++)
 #pragma unroll
             for (int k = 0; k < 2; k++) {
-              mma_bf16(tmem, sdesc_sw64(a + p * kATile + k * 32), sdesc_sw64(b + k * 32), acc_c);
+              mma_bf16(tmem, sdesc_sw64(a + p * kATile + k * 32), sdesc_sw64(b + k * 32), idesc, acc_c);
               acc_c = 1;
             }
         } else {
@@ -227,7 +241,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           for (int p = 0; p < 2; p++)
 #pragma unroll
             for (int k = 0; k < 2; k++) {
-              mma_bf16(tmem + 256, sdesc_sw64(a + p * kATile + k * 32), sdesc_sw64(b + k * 32), acc_x);
+              mma_bf16(tmem + 256, sdesc_sw64(a + p * kATile + k * 32), sdesc_sw64(b + k * 32), idesc, acc_x);
               acc_x = 1;
             }
         }
@@ -239,18 +253,30 @@ __global__ void __launch_bounds__(kThreads, 1)
     // ---- B tiles: two query rows per thread ----
     const int g = threadIdx.x - 64;
     const int r0 = g, r1 = g + kGen;
-    const uint8_t *row0 = c.qc + (size_t)(qtile * kQueries + r0) * c.Sc;
-    const uint8_t *row1 = c.qc + (size_t)(qtile * kQueries + r1) * c.Sc;
+    const bool has_r1 = r1 < c.nq;
+#pragma unroll
+    for (int i = 0; i < 2; i++) {  // the epilogue's per-query terms
+      const int r = i ? r1 : r0, q = qtile * c.nq + r;
+      if (r < c.nq) q_n[r] = (q < c.Q && c.qstatus[q] == PGB_Q_OK) ? c.qlen[q] : -1;
+    }
+    const uint8_t *row0 = c.qc + (size_t)(qtile * c.nq + r0) * c.Sc;
+    const uint8_t *row1 = c.qc + (size_t)(qtile * c.nq + (has_r1 ? r1 : r0)) * c.Sc;
     bool ok = true;
+    // the next chunk's site classes are loaded while this chunk's tiles are built
+    uint4 nx[4];
+    auto load_chunk = [&](int chunk) {
+      const uint4 *p0 = reinterpret_cast<const uint4 *>(row0 + chunk * kSites);
+      const uint4 *p1 = reinterpret_cast<const uint4 *>(row1 + chunk * kSites);
+      nx[0] = __ldg(p0); nx[1] = __ldg(p0 + 1); nx[2] = __ldg(p1); nx[3] = __ldg(p1 + 1);
+    };
+    load_chunk(0);
     for (int chunk = 0; chunk < c.n_chunks && ok; chunk++) {
       uint32_t w0[8], w1[8];
-      {
-        const uint4 *p0 = reinterpret_cast<const uint4 *>(row0 + chunk * kSites);
-        const uint4 *p1 = reinterpret_cast<const uint4 *>(row1 + chunk * kSites);
-        uint4 a = __ldg(p0), b = __ldg(p0 + 1), d = __ldg(p1), e = __ldg(p1 + 1);
-        w0[0] = a.x; w0[1] = a.y; w0[2] = a.z; w0[3] = a.w; w0[4] = b.x; w0[5] = b.y; w0[6] = b.z; w0[7] = b.w;
-        w1[0] = d.x; w1[1] = d.y; w1[2] = d.z; w1[3] = d.w; w1[4] = e.x; w1[5] = e.y; w1[6] = e.z; w1[7] = e.w;
-      }
+      w0[0] = nx[0].x; w0[1] = nx[0].y; w0[2] = nx[0].z; w0[3] = nx[0].w;
+      w0[4] = nx[1].x; w0[5] = nx[1].y; w0[6] = nx[1].z; w0[7] = nx[1].w;
+      w1[0] = nx[2].x; w1[1] = nx[2].y; w1[2] = nx[2].z; w1[3] = nx[2].w;
+      w1[4] = nx[3].x; w1[5] = nx[3].y; w1[6] = nx[3].z; w1[7] = nx[3].w;
+      if (chunk + 1 < c.n_chunks) load_chunk(chunk + 1);
       for (int j = 0; j < per_chunk; j++) {
         const int u = chunk * per_chunk + j, s = u % kStages;
         if (!wait_bar(&empty[s], ((u / kStages) & 1) ^ 1, abort_flag)) {
@@ -261,20 +287,22 @@ __global__ void __launch_bounds__(kThreads, 1)
         uint8_t *tile = base + (size_t)s * kStageBytes + kABytes;
         const uint32_t cls = j < c.prim ? (uint32_t)(j + 1) : 0u;
         write_b_row(tile, r0, w0, cls);
-        write_b_row(tile, r1, w1, cls);
+        if (has_r1) write_b_row(tile, r1, w1, cls);
         tc::fence_async_smem();
         arrive(&full[s]);
       }
     }
     // ---- epilogue: TMEM lane = edge, column = query ----
+    asm volatile("bar.sync 1, %0;" ::"n"(kGen) : "memory");  // the per-query terms are in place
     if (wait_bar(done, 0, abort_flag) && !*abort_flag) {
       tc::fence_after();
       const int quarter = warp & 3;  // the TMEM lanes this warp may read
       const int e = etile * kEdges + quarter * 32 + lane;
       const bool e_ok = e < c.n_edges;
-      const double eb = e_ok ? (double)c.ebase[e] : 0.0;
+      const int eb = e_ok ? c.ebase[e] : 0;
       const uint32_t lane_addr = tmem + ((uint32_t)(quarter * 32) << 16);
-      for (int c0 = 0; c0 < kQueries; c0 += 16) {
+      int2 *out = c.pairs + (size_t)qtile * c.nq * c.n_edges + e;
+      for (int c0 = 0; c0 < c.nq; c0 += 16) {
         float vc[16], vx[16];
         tc::ld16(lane_addr + c0, vc);
         tc::ld16(lane_addr + 256 + c0, vx);
@@ -283,12 +311,9 @@ __global__ void __launch_bounds__(kThreads, 1)
         tc::pin(vx);
 #pragma unroll
         for (int i = 0; i < 16; i++) {
-          const int q = qtile * kQueries + c0 + i;
-          if (q >= c.Q) break;
-          if (!e_ok || c.qstatus[q] != PGB_Q_OK) continue;
-          const double ql = (double)c.qlen[q];
-          c.scores[(size_t)q * c.n_edges + e] =
-              (double)vc[i] - (double)(float)ql * c.log_nrates + kLn2d * ((double)vx[i] + eb * ql);
+          const int n = q_n[c0 + i];
+          if (e_ok && n >= 0)  // vx holds an exact integer; add back n_q times the edge's base
+            __stcs(out + (size_t)(c0 + i) * c.n_edges, make_int2(__float_as_int(vc[i]), __float2int_rn(vx[i]) + eb * n));
         }
       }
     } else {
@@ -305,7 +330,7 @@ __global__ void __launch_bounds__(kThreads, 1)
 
 // Per-site classes of the loaded queries for the B tiles: 0 not informative
 // (gaps, padding, rows of failed queries), c + 1 for primary code c, 255 for
-// an informative ambiguity character.  [rows][Sc], rows = query tiles x 256.
+// an informative ambiguity character.  [rows][Sc], rows >= Q + 256.
 __global__ void k_s1_qclass(int Q, int S, int Sc, int prim, const uint8_t *__restrict__ qcode,
                             const uint8_t *__restrict__ informative, const int *__restrict__ qstatus, uint8_t *qc) {
   const int q = blockIdx.x;
