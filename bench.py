@@ -364,12 +364,12 @@ def run_ours(args):
     # ---- roofline of the dominant kernel ----
     # Stage 2 + refinement run as one launch of the whole-query warp kernel
     # (k_place_warp) per step; its duration is the engine's stage-2 event
-    # interval.  Algorithmic bytes per site evaluation: the distal and
-    # proximal FP32 window entries of every rate (2 * 4 * R * K) and the
-    # packed (column, code) word of the site (4); the exponent sums are read
-    # once per trial, not per evaluation, and are left out.
+    # interval.  Algorithmic bytes per site evaluation of a fused forward +
+    # adjoint evaluation: the distal and proximal GLV windows, FP32 entries
+    # of every rate plus the int32 exponent, 2 * (4 * R * K + 4), and the
+    # query's character code, 1 -- 137 B for DNA G4.
     R, K = len(w.rates) if w.site_cats is None else 1, w.K
-    bytes_per_site_eval = 2 * 4 * R * K + 4
+    bytes_per_site_eval = 2 * (4 * R * K + 4) + 1
     site_evals = counts[3]
     t_trials = phase[3] / 1e3 / args.steps
     peak, peak_kind = load_peaks()
@@ -383,15 +383,16 @@ def run_ours(args):
     # evaluation (148 per rate with derivatives), against 128 lanes per SM
     fp32_ops = FMA_OPS_PER_SITE_RATE * R * site_evals / args.steps / t_trials if t_trials > 0 else 0.0
     fp32_peak = 128 * N_SM * SM_MAX_HZ
-    # Stage 1 (the masked_logdot score of every (query, edge) pair): five bf16
-    # GEMMs on the tensor cores, [Ep x Q] by K = 3 x (prim x Sp) for the three
-    # bf16 terms of the log-likelihood tables and 2 x Sp for the exponent
-    # digits (Ep, Sp: edges and sites padded to 16 and 8), then the ranking
+    # Stage 1 (the masked_logdot score of every (query, edge) pair): the
+    # tcgen05 kernel k_s1_mma contracts [edges x queries] over K = 3 x prim x
+    # Sc (the bf16 hi / mid / lo terms of the log-likelihood tables, one-hot
+    # in the query's code) + 2 x Sc (the exponent digits), Sc = sites padded
+    # to 32; counted on the unpadded edges and queries, timed alone
     prim = 4 if K == 4 else 20
     n_edges = int(np.sum(np.asarray(w.parent) >= 0))
-    Sp, Ep = (S + 7) // 8 * 8, (n_edges + 15) // 16 * 16
-    s1_flops = 2.0 * Ep * Q * (3 * prim * Sp + 2 * Sp)
-    t_s1 = phase[2] / 1e3 / args.steps
+    Sc = (S + 31) // 32 * 32
+    s1_flops = 2.0 * n_edges * Q * (3 * prim * Sc + 2 * Sc)
+    t_s1 = phase[0] / 1e3 / args.steps
     bf16_peak, bf16_kind = load_bf16_peak()
     s1_tflops = s1_flops / t_s1 / 1e12 if t_s1 > 0 else 0.0
     cpu_v, cpu_threads, cpu_n, cpu_dt = cpu_baseline(w, args.cpu_sample, dict(w.prefs))
@@ -414,18 +415,24 @@ def run_ours(args):
                        "stage2_trials_launched": counts[4] / args.steps,
                        "stage2_trials_consumed": counts[5] / args.steps,
                        "refine_trials": counts[6] / args.steps, "rounds": counts[7] / args.steps,
-                       "phase_ms": {"stage1_table": phase[1] / args.steps, "stage1_rank": phase[2] / args.steps,
+                       "phase_ms": {"stage1_table": phase[1] / args.steps, "stage1_rank": phase[2] / args.steps, "stage1_contraction": phase[0] / args.steps,
                                     "stage2": phase[3] / args.steps, "refine_out": phase[4] / args.steps}},
         "roofline": {"kernel": stage2_kernel(w, tune), "bound": "hbm", "achieved": achieved,
                      "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
-                     "traffic_unit": "bytes per launch", "algorithmic_bytes_per_site_eval": bytes_per_site_eval,
+                     "traffic_unit": "bytes per launch",
+                     "traffic_source": ("ncu capture of the full-size dna_1k launch (dram__bytes_read.sum + "
+                                        "dram__bytes_write.sum), per site evaluation, scaled to this launch"
+                                        if traffic is not None else None),
+                     "algorithmic_bytes_per_site_eval": bytes_per_site_eval,
                      "peak_source": peak_kind,
                      "fp32_pipe": {"achieved": fp32_ops, "peak": fp32_peak, "unit": "FMA-pipe lane ops/s",
                                    "frac": fp32_ops / fp32_peak, "peak_source": "nominal: 128 lanes x 152 SMs x 2070 MHz"},
-                     "stage1": {"kernels": "5 bf16 GEMMs (cuBLAS tcgen05) + k_rank_warp", "bound": "tensor",
+                     "stage1": {"kernel": "k_s1_mma (hand-written tcgen05: TMA bf16 tables, one-hot query tiles "
+                                          "built in shared memory, TMEM accumulators)", "bound": "tensor",
                                 "achieved": s1_tflops, "peak": bf16_peak, "unit": "TFLOP/s",
                                 "frac": s1_tflops / bf16_peak, "peak_source": bf16_kind,
-                                "gemm_flops_per_step": s1_flops, "note": "time includes the ranking"}},
+                                "flops_per_step": s1_flops, "ms_per_step": 1e3 * t_s1,
+                                "note": "the contraction alone; the ranking (k_rank_warp) is in phase_ms.stage1_rank"}},
         "cpu_baseline": {"value": cpu_v, "unit": "placements/s", "cores": cpu_threads, "kind": "port",
                          "sample": "%d queries of %s (%.1f s)" % (cpu_n, args.workload, cpu_dt)},
         "e2e": {"value": e2e, "unit": "placements/s", "h2d_bytes_per_step": Q * S,

@@ -332,8 +332,9 @@ pgb_status pgb_engine_get_tuning(pgb_engine *e, int *threads, int *smem_windows)
 pgb_status pgb_engine_set_tuning(pgb_engine *e, const int *threads, const int *smem_windows);
 
 /* Device time of the last pgb_queries_run by phase, from CUDA events on the
- * engine's stream: [0] query prep, [1] stage-1 tables, [2] stage-1 scores and
- * ranking, [3] stage-2 trials, [4] refinement and output; [5] total.
+ * engine's stream: [0] the stage-1 tensor-core contraction alone (part of
+ * [2]), [1] stage-1 tables, [2] stage-1 scores and ranking, [3] stage-2
+ * trials, [4] refinement and output; [5] total.
  * counts[0..7]: stage-1 (query, edge) pairs, stage-2 + refinement trials,
  * objective evaluations, site evaluations (both trial passes), stage-2 trials
  * launched, stage-2 trials consumed by the baseball stop rule, refinement

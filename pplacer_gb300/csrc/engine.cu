@@ -15,6 +15,8 @@
 //   launches) -> output.
 #include <math.h>
 
+#include <cmath>
+
 #include <algorithm>
 #include <cstring>
 #include <vector>
@@ -972,8 +974,9 @@ __device__ __forceinline__ void place_queries(Team &tm, const TrialCtx &c, const
 }
 
 // A warp as a team (nucleotide Gamma mixtures, CAT): lane 0 leads.
-template <int RP, bool CAT>
+template <int RP, bool CAT, bool EIG = false>
 struct WarpTeam {
+  static constexpr bool kEig = EIG;
   const TrialCtx &c;
   const TrialSmem &sm;
   float4 *ring;
@@ -981,17 +984,19 @@ struct WarpTeam {
   __device__ bool leader() const { return lane == 0; }
   __device__ void sync() const { __syncwarp(); }
   __device__ int bcast(int v) const { return __shfl_sync(0xffffffffu, v, 0); }
-  __device__ TrialRes trial(const TrialIn &t) { return trial_warp<RP, CAT>(c, sm, ring, lane, t); }
+  __device__ TrialRes trial(const TrialIn &t) { return trial_warp<RP, CAT, EIG>(c, sm, ring, lane, t); }
   __device__ bool aborted() const { return false; }
 };
 
-template <int RP, bool CAT = false>
-__global__ void __launch_bounds__(32, kWarpTrialMinCtas) k_place_warp(TrialCtx c, PlaceCtx p) {
+// MINB: resident one-warp CTAs per SM the register allocation aims for
+// (8: 255 registers per thread; 12: 168).
+template <int RP, bool CAT = false, bool EIG = false, int MINB = kWarpTrialMinCtas>
+__global__ void __launch_bounds__(32, MINB) k_place_warp(TrialCtx c, PlaceCtx p) {
   extern __shared__ __align__(16) char t_smem[];
   TrialSmem sm;
   float4 *ring;
   warp_trial_setup(c, t_smem, sm, ring);
-  WarpTeam<RP, CAT> tm{c, sm, ring, (int)(threadIdx.x & 31)};
+  WarpTeam<RP, CAT, EIG> tm{c, sm, ring, (int)(threadIdx.x & 31)};
   place_queries(tm, c, p);
 }
 
@@ -1090,6 +1095,13 @@ struct pgb_engine {
   // tensor-core trial kernel; built on first use after the GLVs change
   float *d_darr_e = nullptr, *d_parr_e = nullptr;
   bool eig_ready = false;
+  // nucleotide eigenbasis warp form: the rate matrix has one zero eigenvalue
+  // whose eigenvector (a column of X) is constant; eig_ord packs its index
+  // (byte 0) and the other three (bytes 1..3), eig_c0 that column's value
+  bool eig_ok = false;
+  int eig_ord = 0;
+  double eig_c0 = 0.0;
+  int warp_variant = 0;  // the nucleotide Gamma warp form (launch_place_warp_gmix)
   int *d_dexp = nullptr, *d_pexp = nullptr, *d_sexp = nullptr;
   bool glvs_ready = false;
   // stage 1: edge tables (bf16 MMA operands, TMA descriptors), per-site
@@ -1434,6 +1446,7 @@ TrialCtx trial_ctx(pgb_engine *e, const pgb_prefs *p, int optimizer, int mode) {
   c.Xit = e->d_mf + e->off_Xit;
   c.tc_err = e->d_tc_err;
   c.darr_e = e->d_darr_e; c.parr_e = e->d_parr_e;
+  c.eig_ord = e->eig_ord;
   c.zcodes = tc_zcodes(e);
   c.log_nrates = e->gcat ? 0.0 : log((double)(float)e->NM);
   c.start_pend = p->start_pend;
@@ -1510,13 +1523,25 @@ pgb_status launch_trials_warp(pgb_engine *e, cudaStream_t st, TrialCtx c, const 
 // the tensor-core trial kernel covers 20-state Gamma mixtures of up to 4 rates
 bool tc_trials_ok(const pgb_engine *e) { return e->K == kTcK && !e->gcat && e->NM == e->RP && e->RP <= kTcMaxRates; }
 
+// the eigenbasis warp form applies (and is the one selected when `selected`)
+bool warp_eig_ok(const pgb_engine *e) { return warp_trials_ok(e) && e->eig_ok; }
+
+// darr / parr in eigen-coordinates, for the kernels that read them: the
+// tensor-core kernel (20 states) and the eigenbasis warp form (nucleotides,
+// the permuted and premultiplied layout of k_eigen_glvs_dna).
 pgb_status ensure_eigen_glvs(pgb_engine *e) {
-  if (e->eig_ready || !tc_trials_ok(e)) return PGB_OK;
+  const bool tc = tc_trials_ok(e), dna = warp_eig_ok(e) && e->warp_variant != 0;
+  if (e->eig_ready || (!tc && !dna)) return PGB_OK;
   const long rows = (long)e->n_nodes * e->S * e->RP;
   pgb_status s;
   if (!e->d_darr_e && ((s = dalloc(&e->d_darr_e, (size_t)rows * e->K)) || (s = dalloc(&e->d_parr_e, (size_t)rows * e->K))))
     return s;
-  k_eigen_glvs<<<grid_for(2 * rows), 256, 0, e->st>>>(e->d_darr, e->d_parr, e->d_Xitd, rows, e->d_darr_e, e->d_parr_e);
+  if (tc)
+    k_eigen_glvs<<<grid_for(2 * rows), 256, 0, e->st>>>(e->d_darr, e->d_parr, e->d_Xitd, rows, e->d_darr_e,
+                                                        e->d_parr_e);
+  else
+    k_eigen_glvs_dna<<<grid_for(2 * rows), 256, 0, e->st>>>(e->d_darr, e->d_parr, e->d_Xitd, rows, e->eig_ord,
+                                                            e->eig_c0, e->d_darr_e, e->d_parr_e);
   PGB_LAUNCH_CHECK();
   e->eig_ready = true;
   return PGB_OK;
@@ -1711,16 +1736,27 @@ pgb_status ensure_prior_means(pgb_engine *e, int prior, double prior_lower) {
   return PGB_OK;
 }
 
-template <int RP, bool CAT = false>
+template <int RP, bool CAT = false, bool EIG = false, int MINB = kWarpTrialMinCtas>
 pgb_status launch_place_warp_rp(pgb_engine *e, TrialCtx c, const PlaceCtx &pc) {
   size_t smem = warp_trial_smem_bytes(e->NM, e->ncode, c.zcodes);
-  PGB_CUDA(cudaFuncSetAttribute(k_place_warp<RP, CAT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  auto kern = k_place_warp<RP, CAT, EIG, MINB>;
+  PGB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int per_sm = 0;
-  PGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_place_warp<RP, CAT>, 32, smem));
+  PGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32, smem));
   int grid = std::max(1, std::min(e->Q, e->n_sm * std::max(1, per_sm)));
-  k_place_warp<RP, CAT><<<grid, 32, smem, e->st>>>(c, pc);
+  kern<<<grid, 32, smem, e->st>>>(c, pc);
   PGB_LAUNCH_CHECK();
   return PGB_OK;
+}
+
+// The nucleotide Gamma warp forms (the autotuner's choice, warp_variant):
+// 0 matrices in registers, 8 warps per SM; 1 eigenbasis, 8 warps per SM;
+// 2 eigenbasis, 12 warps per SM.
+template <int RP>
+pgb_status launch_place_warp_gmix(pgb_engine *e, TrialCtx c, const PlaceCtx &pc) {
+  if (e->warp_variant == 1) return launch_place_warp_rp<RP, false, true, 8>(e, c, pc);
+  if (e->warp_variant == 2) return launch_place_warp_rp<RP, false, true, 12>(e, c, pc);
+  return launch_place_warp_rp<RP>(e, c, pc);
 }
 
 pgb_status launch_place_tc(pgb_engine *e, TrialCtx c, const PlaceCtx &pc, int max_sq) {
@@ -1822,16 +1858,17 @@ pgb_status run_whole_queries(pgb_engine *e, const pgb_prefs *p, const BBCtx &c, 
   else if (e->gcat) s = launch_place_warp_rp<1, true>(e, tc, pc);
   else
     switch (e->RP) {
-      case 1: s = launch_place_warp_rp<1>(e, tc, pc); break;
-      case 2: s = launch_place_warp_rp<2>(e, tc, pc); break;
-      case 4: s = launch_place_warp_rp<4>(e, tc, pc); break;
-      default: s = launch_place_warp_rp<8>(e, tc, pc); break;
+      case 1: s = launch_place_warp_gmix<1>(e, tc, pc); break;
+      case 2: s = launch_place_warp_gmix<2>(e, tc, pc); break;
+      case 4: s = launch_place_warp_gmix<4>(e, tc, pc); break;
+      default: s = launch_place_warp_gmix<8>(e, tc, pc); break;
     }
   if (s) return s;
   PGB_CUDA(cudaEventRecord(e->ev[3], e->st));
   PGB_CUDA(cudaEventRecord(e->ev[4], e->st));
   PGB_CUDA(cudaEventSynchronize(e->ev[4]));
   float ms;
+  cudaEventElapsedTime(&ms, e->ev[1], e->ev[5]); e->t_ms[0] = ms;
   cudaEventElapsedTime(&ms, e->ev[0], e->ev[1]); e->t_ms[1] = ms;
   cudaEventElapsedTime(&ms, e->ev[1], e->ev[2]); e->t_ms[2] = ms;
   cudaEventElapsedTime(&ms, e->ev[2], e->ev[3]); e->t_ms[3] = ms;
@@ -1917,6 +1954,30 @@ pgb_status pgb_engine_create(const pgb_model_desc *m, const pgb_tree_desc *t, pg
   e->lam.assign(m->lambda, m->lambda + K);
   e->Xit.assign(m->xit, m->xit + K * K);
   e->rates.assign(m->rates, m->rates + e->NM);
+  if (K == 4) {  // the eigenbasis warp form needs one zero eigenvalue with a constant eigenvector
+    int kz = 0;
+    double lmax = 0;
+    for (int k = 0; k < K; k++) {
+      lmax = std::max(lmax, std::fabs(e->lam[k]));
+      if (e->lam[k] > e->lam[kz]) kz = k;
+    }
+    bool ok = lmax > 0 && std::fabs(e->lam[kz]) <= 1e-9 * lmax;
+    for (int k = 0; k < K && ok; k++)
+      if (k != kz && std::fabs(e->lam[k]) <= 1e-6 * lmax) ok = false;
+    const double c0 = e->X[kz];
+    for (int i = 0; i < K && ok; i++)
+      if (!(std::fabs(e->X[i * K + kz] - c0) <= 1e-9 * std::fabs(c0))) ok = false;
+    if (ok) {
+      int ord = kz, s = 1;
+      for (int k = 0; k < K; k++)
+        if (k != kz) ord |= k << (8 * s++);
+      e->eig_ok = true;
+      e->eig_ord = ord;
+      double mean = 0;
+      for (int i = 0; i < K; i++) mean += e->X[i * K + kz];
+      e->eig_c0 = mean / K;
+    }
+  }
   if (e->gcat) {
     e->site_cats.assign(m->site_categories, m->site_categories + e->S);
     for (int v : e->site_cats)
@@ -2418,6 +2479,7 @@ pgb_status pgb_queries_run(pgb_engine *e, const pgb_prefs *p) {
   if ((s = build_stage1_table(e, p->start_pend))) return s;
   PGB_CUDA(cudaEventRecord(e->ev[1], e->st));
   if ((s = run_stage1(e))) return s;
+  PGB_CUDA(cudaEventRecord(e->ev[5], e->st));
   if ((s = run_rank(e, rk))) return s;
   PGB_CUDA(cudaEventRecord(e->ev[2], e->st));
   e->counts[0] = (double)e->Q * e->n_edges;
@@ -2513,6 +2575,7 @@ pgb_status pgb_queries_run(pgb_engine *e, const pgb_prefs *p) {
   PGB_CUDA(cudaEventRecord(e->ev[4], e->st));
   PGB_CUDA(cudaEventSynchronize(e->ev[4]));
   float ms;
+  cudaEventElapsedTime(&ms, e->ev[1], e->ev[5]); e->t_ms[0] = ms;
   cudaEventElapsedTime(&ms, e->ev[0], e->ev[1]); e->t_ms[1] = ms;
   cudaEventElapsedTime(&ms, e->ev[1], e->ev[2]); e->t_ms[2] = ms;
   cudaEventElapsedTime(&ms, e->ev[2], e->ev[3]); e->t_ms[3] = ms;
@@ -2533,8 +2596,24 @@ pgb_status pgb_engine_autotune(pgb_engine *e, const pgb_prefs *p) {
   if (!e || !e->glvs_ready || e->Q < 1) { set_error("autotune: no GLVs or no queries"); return PGB_ERR_STATE; }
   pgb_status s;
   if ((s = check_prefs(p))) return s;
-  if (warp_trials_ok(e)) {  // the whole-query warp kernel: nothing to tune
+  if (warp_trials_ok(e)) {
+    // the whole-query warp kernel: time its forms (matrices in registers;
+    // eigenbasis at 8 or 12 warps per SM) on whole runs of the loaded
+    // queries, keep the fastest
     for (int b = 0; b < kBins; b++) { e->tune_threads[b] = 32; e->tune_win[b] = 0; }
+    if (!warp_eig_ok(e)) { e->warp_variant = 0; return PGB_OK; }
+    float best = 1e30f;
+    int bv = 0;
+    for (int v = 0; v < 3; v++) {
+      if (v != e->warp_variant) { e->warp_variant = v; e->eig_ready = false; }
+      float ms_best = 1e30f;
+      for (int rep = 0; rep < 2; rep++) {
+        if ((s = pgb_queries_run(e, p))) return s;
+        ms_best = std::min(ms_best, (float)e->t_ms[3]);
+      }
+      if (ms_best < best) { best = ms_best; bv = v; }
+    }
+    if (bv != e->warp_variant) { e->warp_variant = bv; e->eig_ready = false; }
     return PGB_OK;
   }
   bool all_edges = p->max_strikes == 0;
@@ -2649,19 +2728,34 @@ pgb_status pgb_engine_autotune(pgb_engine *e, const pgb_prefs *p) {
 
 pgb_status pgb_engine_get_tuning(pgb_engine *e, int *threads, int *smem_windows) {
   if (!e) return PGB_ERR_ARG;
-  for (int b = 0; b < kBins; b++) { threads[b] = e->tune_threads[b]; smem_windows[b] = e->tune_win[b]; }
+  for (int b = 0; b < kBins; b++) {
+    threads[b] = e->tune_threads[b];
+    smem_windows[b] = e->tune_threads[b] == 32 && warp_trials_ok(e) ? e->warp_variant : e->tune_win[b];
+  }
   return PGB_OK;
 }
 
 pgb_status pgb_engine_set_tuning(pgb_engine *e, const int *threads, const int *smem_windows) {
   if (!e || !threads || !smem_windows) { set_error("set_tuning: null argument"); return PGB_ERR_ARG; }
-  for (int b = 0; b < kBins; b++)
+  const bool warp_forms = warp_trials_ok(e);
+  for (int b = 0; b < kBins; b++) {
+    const bool wf = threads[b] == 32 && warp_forms;  // smem_windows selects the warp form
     if ((threads[b] != 32 && threads[b] != kTuneTc && threads[b] != 128 && threads[b] != 256) ||
-        (smem_windows[b] & ~1)) {
-      set_error("set_tuning: bin %d: threads must be 1, 32, 128 or 256 and smem_windows 0 or 1", b);
+        (!wf && (smem_windows[b] & ~1)) || (wf && (smem_windows[b] < 0 || smem_windows[b] > 2)) ||
+        (wf && smem_windows[b] > 0 && !warp_eig_ok(e))) {
+      set_error("set_tuning: bin %d: threads must be 1, 32, 128 or 256 and smem_windows 0 or 1 (for the "
+                "nucleotide Gamma warp form 0, 1 or 2 where the eigenbasis forms apply)", b);
       return PGB_ERR_ARG;
     }
-  for (int b = 0; b < kBins; b++) { e->tune_threads[b] = threads[b]; e->tune_win[b] = smem_windows[b]; }
+  }
+  for (int b = 0; b < kBins; b++) {
+    e->tune_threads[b] = threads[b];
+    e->tune_win[b] = threads[b] == 32 && warp_forms ? 0 : smem_windows[b];
+  }
+  if (threads[0] == 32 && warp_forms && smem_windows[0] != e->warp_variant) {
+    e->warp_variant = smem_windows[0];
+    e->eig_ready = false;  // the eigen-coordinate layout follows the form
+  }
   return PGB_OK;
 }
 

@@ -57,7 +57,8 @@ struct TrialCtx {
   const float *X, *W, *Lt, *lvf, *statd, *lam, *rates;
   const float *Xit;           // X^-T (K x K): the tensor-core kernel's P(t) = I + X diag(.) Xit^T
   int *tc_err;                // [16]: [0] set when a tensor-core completion wait timed out, then where
-  const float *darr_e, *parr_e;  // darr / parr rows times X^-1 (the tensor-core kernel's operands)
+  const float *darr_e, *parr_e;  // darr / parr rows times X^-1 (the tensor-core and eigen warp kernels' operands)
+  int eig_ord;                // nucleotide eigen warp form: byte 0 the zero eigenvalue, bytes 1..3 the others
   int zcodes;                 // character codes of the tensor-core kernel's query tables
   double log_nrates;
   double start_pend, max_pend;
@@ -623,9 +624,9 @@ __device__ __forceinline__ void trial_exps(const TrialSmem &sm, int NM, int K, c
 // lengths, its first and second derivatives, and the statd-weighted evolved
 // query vectors Z (and d/dpend, d2/dpend2) of every character code.
 __device__ __forceinline__ void trial_tables(const TrialSmem &sm, const float *W, int NM, int nc, int ncz, int K,
-                                             bool derivs, int i0, int stride) {
+                                             bool derivs, int i0, int stride, bool mats = true) {
   const int nmat = NM * K * K;
-  for (int i = i0; i < 2 * nmat; i += stride) {
+  for (int i = i0; i < (mats ? 2 * nmat : 0); i += stride) {
     int wh = i / nmat, r = i - wh * nmat;
     int m = r / (K * K), ij = r - m * K * K;
     int ii = ij / K, jj = ij - ii * K;

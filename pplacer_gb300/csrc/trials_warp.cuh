@@ -226,6 +226,188 @@ __device__ __forceinline__ void sites_warp(const TrialCtx &c, const TrialSmem &s
   cp_async_wait<0>();  // drain the copies issued past the end
 }
 
+// Eigen-coordinates of the nucleotide windows for sites_warp_eig: rows
+// (node, site, rate) of darr and parr times X^-1 (FP64 accumulation), slot 0
+// the zero eigenvalue's coordinate times its constant eigenvector entry c0,
+// slots 1..3 the other coordinates in eig_ord order.
+__global__ void k_eigen_glvs_dna(const float *__restrict__ darr, const float *__restrict__ parr,
+                                 const double *__restrict__ Xit, long rows, int eig_ord, double c0, float *darr_e,
+                                 float *parr_e) {
+  constexpr int K = 4;
+  int ord[4];
+#pragma unroll
+  for (int k = 0; k < 4; k++) ord[k] = (eig_ord >> (8 * k)) & 255;
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < 2 * rows; t += (long)gridDim.x * blockDim.x) {
+    const bool prox = t >= rows;
+    const long row = prox ? t - rows : t;
+    const float *v = (prox ? parr : darr) + row * K;
+    float *o = (prox ? parr_e : darr_e) + row * K;
+    float x[K];
+#pragma unroll
+    for (int j = 0; j < K; j++) x[j] = v[j];
+#pragma unroll
+    for (int s = 0; s < K; s++) {
+      const int k = ord[s];
+      double a = 0.0;
+#pragma unroll
+      for (int j = 0; j < K; j++) a += Xit[j * K + k] * (double)x[j];  // (X^-1)[k][j] = Xit[j][k]
+      o[s] = (float)(s == 0 ? c0 * a : a);
+    }
+  }
+}
+
+// The same sites in the eigenbasis of the rate matrix (the autotuner's
+// second warp form for nucleotide Gamma mixtures).  With P(t) = X diag(e^{r
+// lambda t}) X^-1 and the windows stored as eigen-coordinates v~ = X^-1 v
+// (k_eigen_glvs_dna), x = P(t) d is X (e o d~), and its first and second
+// length derivatives are X (r lambda e o d~) and X ((r lambda)^2 e o d~).
+// The zero eigenvalue's eigenvector is constant, so its term is the same for
+// every state: the arrays store it premultiplied in slot 0 and the other
+// three eigen-coordinates in slots 1..3 (the order c.eig_ord).  A lane then
+// holds X's three other columns and nine exp factors per window instead of
+// six 4x4 matrices (30 registers instead of 96), and a new branch length
+// only changes the factors; the arithmetic per site and rate is the same
+// (3 scalings and 12 FMA per evolved vector).
+template <int RP, bool DER>
+__device__ __forceinline__ void sites_warp_eig(const TrialCtx &c, const TrialSmem &sm, float4 *ring, int q, int node,
+                                               int Sq, int lane, SiteAcc &acc) {
+  constexpr int K = 4, SPW = 32 / RP;
+  const int r = lane & (RP - 1), slot = lane / RP, zc = c.zcodes, NM = c.NM;
+  int ord[3];
+  ord[0] = (c.eig_ord >> 8) & 255; ord[1] = (c.eig_ord >> 16) & 255; ord[2] = (c.eig_ord >> 24) & 255;
+  float xr[4][3], ed[3], ed1[3], ed2[3], ep[3], ep1[3], ep2[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+#pragma unroll
+    for (int i = 0; i < 4; i++) xr[i][k] = sm.X[i * K + ord[k]];
+    const float lr = sm.Lr[r * K + ord[k]];
+    ed[k] = sm.E[(0 * NM + r) * K + ord[k]];
+    ep[k] = sm.E[(1 * NM + r) * K + ord[k]];
+    ed1[k] = lr * ed[k]; ed2[k] = lr * ed1[k];
+    ep1[k] = lr * ep[k]; ep2[k] = lr * ep1[k];
+  }
+  const float *gd = c.darr_e + (long)node * c.S * RP * K + r * K;
+  const float *gp = c.parr_e + (long)node * c.S * RP * K + r * K;
+  const uint32_t *rc = c.rcode + (long)q * c.S;
+  const float *Zr = sm.Z + r * zc * K, *Z1r = sm.Z1 + r * zc * K, *Z2r = sm.Z2 + r * zc * K;
+  const int last = Sq - 1;
+  constexpr int G = (RP == 2 || RP == 4) ? RP : 1;
+  int off[G];
+#pragma unroll
+  for (int k = 0; k < G; k++) off[k] = (G > 1 ? (k ^ r) : 0) * SPW + slot;
+  // the ring, the code queue and the iteration order are those of sites_warp
+  unsigned long long cq = 0ull;
+  auto issue = [&](int stage, uint32_t pk) {
+    const long col = (long)(pk >> 8);
+    cp_async16(ring + (stage * 32 + lane), gd + col * RP * K);
+    cp_async16(ring + ((kWarpRing + stage) * 32 + lane), gp + col * RP * K);
+    cp_async_commit();
+  };
+#pragma unroll
+  for (int j = 0; j < kWarpRing - 1; j++) {
+    const uint32_t pk = rc[min((j / G) * G * SPW + off[j % G], last)];
+    issue(j, pk);
+    cq |= (unsigned long long)(pk & 255u) << (8 * j);
+  }
+  uint32_t pk_next = rc[min(((kWarpRing - 1) / G) * G * SPW + off[(kWarpRing - 1) % G], last)];
+  uint32_t pk_next2 = rc[min(off[0] + kWarpRing * SPW, last)];
+  int st = 0;
+  auto iteration = [&](int i, int inext, float (&v)[6]) {
+    issue((st + kWarpRing - 1) & (kWarpRing - 1), pk_next);
+    cq |= (unsigned long long)(pk_next & 255u) << (8 * (kWarpRing - 1));
+    const int code = (int)(cq & 255ull);
+    cq >>= 8;
+    pk_next = pk_next2;
+    pk_next2 = rc[min(inext + kWarpRing * SPW, last)];
+    cp_async_wait<kWarpRing - 1>();  // this iteration's copies have landed
+    const float4 dcur = ring[st * 32 + lane];
+    const float4 pcur = ring[(kWarpRing + st) * 32 + lane];
+    st = (st + 1) & (kWarpRing - 1);
+    const float dv[3] = {dcur.y, dcur.z, dcur.w}, pv[3] = {pcur.y, pcur.z, pcur.w};
+    const float4 Z4 = *reinterpret_cast<const float4 *>(Zr + code * K);
+    const float z[4] = {Z4.x, Z4.y, Z4.z, Z4.w};
+    float z1[4], z2[4];
+    if (DER) {
+      float4 a = *reinterpret_cast<const float4 *>(Z1r + code * K);
+      float4 b = *reinterpret_cast<const float4 *>(Z2r + code * K);
+      z1[0] = a.x; z1[1] = a.y; z1[2] = a.z; z1[3] = a.w;
+      z2[0] = b.x; z2[1] = b.y; z2[2] = b.z; z2[3] = b.w;
+    }
+    float ud[3], wp[3], ud1[3], ud2[3], wp1[3], wp2[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      ud[k] = ed[k] * dv[k];
+      wp[k] = ep[k] * pv[k];
+      if (DER) {
+        ud1[k] = ed1[k] * dv[k]; ud2[k] = ed2[k] * dv[k];
+        wp1[k] = ep1[k] * pv[k]; wp2[k] = ep2[k] * pv[k];
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 6; k++) v[k] = 0.f;
+#pragma unroll
+    for (int ii = 0; ii < 4; ii++) {
+      float x = dcur.x, y = pcur.x;
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        x = fmaf(xr[ii][k], ud[k], x);
+        y = fmaf(xr[ii][k], wp[k], y);
+      }
+      float xy = x * y;
+      v[0] = fmaf(z[ii], xy, v[0]);
+      if (DER) {
+        float x1 = xr[ii][0] * ud1[0], x2 = xr[ii][0] * ud2[0], y1 = xr[ii][0] * wp1[0], y2 = xr[ii][0] * wp2[0];
+#pragma unroll
+        for (int k = 1; k < 3; k++) {
+          x1 = fmaf(xr[ii][k], ud1[k], x1);
+          x2 = fmaf(xr[ii][k], ud2[k], x2);
+          y1 = fmaf(xr[ii][k], wp1[k], y1);
+          y2 = fmaf(xr[ii][k], wp2[k], y2);
+        }
+        float aa = x1 * y - x * y1;
+        float bb = x2 * y - 2.f * x1 * y1 + x * y2;
+        v[1] = fmaf(z[ii], aa, v[1]);
+        v[2] = fmaf(z[ii], bb, v[2]);
+        v[3] = fmaf(z1[ii], xy, v[3]);
+        v[4] = fmaf(z2[ii], xy, v[4]);
+        v[5] = fmaf(z1[ii], aa, v[5]);
+      }
+    }
+  };
+  constexpr int NV = DER ? 6 : 1;
+  for (int gbase = 0; gbase < Sq; gbase += G * SPW) {
+    float f[6];
+    if (G == 4) {
+      float v0[6], v1[6], h0[6], h1[6];
+      iteration(gbase + off[0], gbase + off[1], v0);
+      iteration(gbase + off[1], gbase + off[2], v1);
+#pragma unroll
+      for (int k = 0; k < NV; k++) h0[k] = v0[k] + __shfl_xor_sync(0xffffffffu, v1[k], 1);
+      iteration(gbase + off[2], gbase + off[3], v0);
+      iteration(gbase + off[3], gbase + G * SPW + off[0], v1);
+#pragma unroll
+      for (int k = 0; k < NV; k++) h1[k] = v0[k] + __shfl_xor_sync(0xffffffffu, v1[k], 1);
+#pragma unroll
+      for (int k = 0; k < NV; k++) f[k] = h0[k] + __shfl_xor_sync(0xffffffffu, h1[k], 2);
+    } else if (G == 2) {
+      float v0[6], v1[6];
+      iteration(gbase + off[0], gbase + off[1], v0);
+      iteration(gbase + off[1], gbase + G * SPW + off[0], v1);
+#pragma unroll
+      for (int k = 0; k < NV; k++) f[k] = v0[k] + __shfl_xor_sync(0xffffffffu, v1[k], 1);
+    } else {
+      iteration(gbase + off[0], gbase + SPW + off[0], f);
+#pragma unroll
+      for (int o = 1; o < RP; o <<= 1)
+#pragma unroll
+        for (int k = 0; k < NV; k++) f[k] += __shfl_xor_sync(0xffffffffu, f[k], o);
+    }
+    const bool mine = G > 1 ? gbase + r * SPW + slot < Sq : (r == 0 && gbase + slot < Sq);
+    if (mine) acc.add(f[0], f[1], f[2], f[3], f[4], f[5], DER);
+  }
+  cp_async_wait<0>();  // drain the copies issued past the end
+}
+
 // Sites of a per-site CAT model (Gcat_model, one GLV plane): lane = site,
 // 32 sites per iteration, the windows streamed through the same cp.async
 // ring.  A site's matrices are those of its category (the packed word's top
@@ -350,7 +532,7 @@ __device__ __forceinline__ void warp_trial_setup(const TrialCtx &c, char *t_smem
 // One trial (Three_tax.optimize at one location) by the calling warp.  Every
 // lane runs the same optimiser on the same all-reduced values and returns
 // the same result.
-template <int RP, bool CAT = false>
+template <int RP, bool CAT = false, bool EIG = false>
 __device__ TrialRes trial_warp(const TrialCtx &c, const TrialSmem &sm, float4 *ring, int lane, const TrialIn &tr) {
   constexpr int K = 4;
   const int NM = c.NM, nc = c.ncode;
@@ -423,7 +605,7 @@ __device__ TrialRes trial_warp(const TrialCtx &c, const TrialSmem &sm, float4 *r
     __syncwarp();  // the previous evaluation's sites have read the tables
     trial_exps(sm, NM, K, ctl, lane, 32);
     __syncwarp();
-    trial_tables(sm, sm.W, NM, c.zcodes, ncz, K, derivs, lane, 32);  // Z rows of stride zcodes
+    trial_tables(sm, sm.W, NM, c.zcodes, ncz, K, derivs, lane, 32, !EIG);  // Z rows of stride zcodes
     __syncwarp();
     SiteAcc acc;
     acc.init();
@@ -431,6 +613,9 @@ __device__ TrialRes trial_warp(const TrialCtx &c, const TrialSmem &sm, float4 *r
       if (CAT) {
         if (derivs) sites_warp_cat<true>(c, sm, ring, q, node, Sq, lane, acc);
         else sites_warp_cat<false>(c, sm, ring, q, node, Sq, lane, acc);
+      } else if (EIG) {
+        if (derivs) sites_warp_eig<RP, true>(c, sm, ring, q, node, Sq, lane, acc);
+        else sites_warp_eig<RP, false>(c, sm, ring, q, node, Sq, lane, acc);
       } else {
         if (derivs) sites_warp<RP, true>(c, sm, ring, q, node, Sq, lane, acc);
         else sites_warp<RP, false>(c, sm, ring, q, node, Sq, lane, acc);
