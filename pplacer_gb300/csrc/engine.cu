@@ -1750,12 +1750,14 @@ pgb_status launch_place_warp_rp(pgb_engine *e, TrialCtx c, const PlaceCtx &pc) {
 }
 
 // The nucleotide Gamma warp forms (the autotuner's choice, warp_variant):
-// 0 matrices in registers, 8 warps per SM; 1 eigenbasis, 8 warps per SM;
-// 2 eigenbasis, 12 warps per SM.
+// 0 matrices in registers, 8 warps per SM; 1, 2, 3 eigenbasis at 8, 12 and
+// 16 warps per SM (255, 168 and 128 registers).
+constexpr int kWarpForms = 4;
 template <int RP>
 pgb_status launch_place_warp_gmix(pgb_engine *e, TrialCtx c, const PlaceCtx &pc) {
   if (e->warp_variant == 1) return launch_place_warp_rp<RP, false, true, 8>(e, c, pc);
   if (e->warp_variant == 2) return launch_place_warp_rp<RP, false, true, 12>(e, c, pc);
+  if (e->warp_variant == 3) return launch_place_warp_rp<RP, false, true, 16>(e, c, pc);
   return launch_place_warp_rp<RP>(e, c, pc);
 }
 
@@ -2598,13 +2600,13 @@ pgb_status pgb_engine_autotune(pgb_engine *e, const pgb_prefs *p) {
   if ((s = check_prefs(p))) return s;
   if (warp_trials_ok(e)) {
     // the whole-query warp kernel: time its forms (matrices in registers;
-    // eigenbasis at 8 or 12 warps per SM) on whole runs of the loaded
+    // eigenbasis at 8, 12 or 16 warps per SM) on whole runs of the loaded
     // queries, keep the fastest
     for (int b = 0; b < kBins; b++) { e->tune_threads[b] = 32; e->tune_win[b] = 0; }
     if (!warp_eig_ok(e)) { e->warp_variant = 0; return PGB_OK; }
     float best = 1e30f;
     int bv = 0;
-    for (int v = 0; v < 3; v++) {
+    for (int v = 0; v < kWarpForms; v++) {
       if (v != e->warp_variant) { e->warp_variant = v; e->eig_ready = false; }
       float ms_best = 1e30f;
       for (int rep = 0; rep < 2; rep++) {
@@ -2741,10 +2743,10 @@ pgb_status pgb_engine_set_tuning(pgb_engine *e, const int *threads, const int *s
   for (int b = 0; b < kBins; b++) {
     const bool wf = threads[b] == 32 && warp_forms;  // smem_windows selects the warp form
     if ((threads[b] != 32 && threads[b] != kTuneTc && threads[b] != 128 && threads[b] != 256) ||
-        (!wf && (smem_windows[b] & ~1)) || (wf && (smem_windows[b] < 0 || smem_windows[b] > 2)) ||
+        (!wf && (smem_windows[b] & ~1)) || (wf && (smem_windows[b] < 0 || smem_windows[b] >= kWarpForms)) ||
         (wf && smem_windows[b] > 0 && !warp_eig_ok(e))) {
       set_error("set_tuning: bin %d: threads must be 1, 32, 128 or 256 and smem_windows 0 or 1 (for the "
-                "nucleotide Gamma warp form 0, 1 or 2 where the eigenbasis forms apply)", b);
+                "nucleotide Gamma warp form 0 .. 3 where the eigenbasis forms apply)", b);
       return PGB_ERR_ARG;
     }
   }

@@ -264,10 +264,12 @@ __global__ void k_eigen_glvs_dna(const float *__restrict__ darr, const float *__
 // The zero eigenvalue's eigenvector is constant, so its term is the same for
 // every state: the arrays store it premultiplied in slot 0 and the other
 // three eigen-coordinates in slots 1..3 (the order c.eig_ord).  A lane then
-// holds X's three other columns and nine exp factors per window instead of
-// six 4x4 matrices (30 registers instead of 96), and a new branch length
-// only changes the factors; the arithmetic per site and rate is the same
-// (3 scalings and 12 FMA per evolved vector).
+// holds X's three other columns, the same scaled by r lambda and (r
+// lambda)^2, and three exp factors per window instead of six 4x4 matrices
+// (42 registers instead of 96); a new branch length only changes the
+// factors, and the arithmetic per site and rate drops from 96 to 78 FMA-pipe
+// operations for the six evolved vectors (3 scalings of the coordinates per
+// window, then 12 FMA per vector).
 template <int RP, bool DER>
 __device__ __forceinline__ void sites_warp_eig(const TrialCtx &c, const TrialSmem &sm, float4 *ring, int q, int node,
                                                int Sq, int lane, SiteAcc &acc) {
@@ -275,16 +277,20 @@ __device__ __forceinline__ void sites_warp_eig(const TrialCtx &c, const TrialSme
   const int r = lane & (RP - 1), slot = lane / RP, zc = c.zcodes, NM = c.NM;
   int ord[3];
   ord[0] = (c.eig_ord >> 8) & 255; ord[1] = (c.eig_ord >> 16) & 255; ord[2] = (c.eig_ord >> 24) & 255;
-  float xr[4][3], ed[3], ed1[3], ed2[3], ep[3], ep1[3], ep2[3];
+  // xl1, xl2: the columns scaled by r lambda and (r lambda)^2, so the
+  // derivative vectors come from the same scaled coordinates e o d~
+  float xr[4][3], xl1[4][3], xl2[4][3], ed[3], ep[3];
 #pragma unroll
   for (int k = 0; k < 3; k++) {
-#pragma unroll
-    for (int i = 0; i < 4; i++) xr[i][k] = sm.X[i * K + ord[k]];
     const float lr = sm.Lr[r * K + ord[k]];
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+      xr[i][k] = sm.X[i * K + ord[k]];
+      xl1[i][k] = xr[i][k] * lr;
+      xl2[i][k] = xl1[i][k] * lr;
+    }
     ed[k] = sm.E[(0 * NM + r) * K + ord[k]];
     ep[k] = sm.E[(1 * NM + r) * K + ord[k]];
-    ed1[k] = lr * ed[k]; ed2[k] = lr * ed1[k];
-    ep1[k] = lr * ep[k]; ep2[k] = lr * ep1[k];
   }
   const float *gd = c.darr_e + (long)node * c.S * RP * K + r * K;
   const float *gp = c.parr_e + (long)node * c.S * RP * K + r * K;
@@ -333,15 +339,11 @@ __device__ __forceinline__ void sites_warp_eig(const TrialCtx &c, const TrialSme
       z1[0] = a.x; z1[1] = a.y; z1[2] = a.z; z1[3] = a.w;
       z2[0] = b.x; z2[1] = b.y; z2[2] = b.z; z2[3] = b.w;
     }
-    float ud[3], wp[3], ud1[3], ud2[3], wp1[3], wp2[3];
+    float ud[3], wp[3];
 #pragma unroll
     for (int k = 0; k < 3; k++) {
       ud[k] = ed[k] * dv[k];
       wp[k] = ep[k] * pv[k];
-      if (DER) {
-        ud1[k] = ed1[k] * dv[k]; ud2[k] = ed2[k] * dv[k];
-        wp1[k] = ep1[k] * pv[k]; wp2[k] = ep2[k] * pv[k];
-      }
     }
 #pragma unroll
     for (int k = 0; k < 6; k++) v[k] = 0.f;
@@ -356,13 +358,13 @@ __device__ __forceinline__ void sites_warp_eig(const TrialCtx &c, const TrialSme
       float xy = x * y;
       v[0] = fmaf(z[ii], xy, v[0]);
       if (DER) {
-        float x1 = xr[ii][0] * ud1[0], x2 = xr[ii][0] * ud2[0], y1 = xr[ii][0] * wp1[0], y2 = xr[ii][0] * wp2[0];
+        float x1 = xl1[ii][0] * ud[0], x2 = xl2[ii][0] * ud[0], y1 = xl1[ii][0] * wp[0], y2 = xl2[ii][0] * wp[0];
 #pragma unroll
         for (int k = 1; k < 3; k++) {
-          x1 = fmaf(xr[ii][k], ud1[k], x1);
-          x2 = fmaf(xr[ii][k], ud2[k], x2);
-          y1 = fmaf(xr[ii][k], wp1[k], y1);
-          y2 = fmaf(xr[ii][k], wp2[k], y2);
+          x1 = fmaf(xl1[ii][k], ud[k], x1);
+          x2 = fmaf(xl2[ii][k], ud[k], x2);
+          y1 = fmaf(xl1[ii][k], wp[k], y1);
+          y2 = fmaf(xl2[ii][k], wp[k], y2);
         }
         float aa = x1 * y - x * y1;
         float bb = x2 * y - 2.f * x1 * y1 + x * y2;
