@@ -60,6 +60,10 @@ def parse():
     ap.add_argument("--queries", type=int, default=None)
     ap.add_argument("--workload", default="dna_1k")
     ap.add_argument("--cpu-sample", type=int, default=512, help="queries in the CPU-baseline sample")
+    ap.add_argument("--dropin-sample", type=int, default=3,
+                    help="queries placed by pplacer's flow over the plain per-call drop-in (untimed region)")
+    ap.add_argument("--batch", type=int, default=0,
+                    help="device batch of the end-to-end pgb_place_batch calls (0: automatic)")
     return ap.parse_args()
 
 
@@ -221,63 +225,41 @@ def run_reference(args):
     print(json.dumps(line))
 
 
-def plain_dropin_brent(eng, w, evals_per_query, reps=40):
-    """pplacer's own per-query flow over the plain drop-in (linear.ml externals
-    replaced one for one through the pgb_* C ABI), timed call by call: a
-    stage-1 score is one ten_masked_logdot over the full alignment per edge
-    (core.ml:187-197); a Brent evaluation re-evolves the pendant (one
-    evolve) or the distal and proximal edges (two) -- per rate a
-    dediagonalize of the exponentiated eigenvalues and a gemmish
-    (diagd.ml:79-98, gstar_support.ml:70-79) -- then one ten_log_like3
-    (three_tax.ml:30-58).  Placements/s = 1 / (edges x t_score +
-    evals_per_query x t_eval), with evals_per_query measured on the Brent
-    replica (the same algorithm) and t_eval the mean of the pendant and the
-    distal evaluation."""
+def plain_dropin_brent(eng, w, prefs, n_sample, brent_res):
+    """pplacer's own per-query flow over the plain drop-in, measured: the
+    Linear externals (linear.ml:13-89) replaced one for one by the pgb_* C
+    ABI, each call copying its operands in and its result out, the GLVs on
+    the host as the OCaml side keeps them; process_query (core.ml:113-409)
+    with its alternating GSL Brent searches (dropin_flow.place_query).
+    n_sample queries are placed and timed by wall clock; their best edges
+    are compared with the batched Brent replica's."""
     import numpy as np
-    from pplacer_gb300 import linear as Lin
+    from pplacer_gb300 import dropin_flow as DF
     m = eng.model
-    R, K = len(m.rates), m.K
-    S = w.n_sites
-    sq = int(np.mean([sum(ch not in "-?." for ch in q) for q in w.query_seqs[:200]]))
-    rng = np.random.default_rng(7)
-    x = [np.ascontiguousarray(rng.random((sq, K)) + 0.1) for _ in range(R)]
-    xt = np.ascontiguousarray(rng.random((R, sq, K)) + 0.1)
-    util = np.zeros(sq)
-    statd = np.ascontiguousarray(m.statd, dtype=np.float64)
-    u, lam, uit = (np.ascontiguousarray(a, dtype=np.float64) for a in (m.x, m.lam, m.xit))
-    P = np.zeros((K, K))
-    dst = np.zeros((sq, K))
-
-    def evolve(t):
-        for r in range(R):
-            Lin.dediagonalize(P, u, np.exp(m.rates[r] * t * lam), uit)
-            Lin.gemmish(dst, P, x[r])
-
-    def pend_eval():
-        evolve(0.1)
-        Lin.ten_log_like3(statd, xt, xt, xt, util)
-
-    def dist_eval():
-        evolve(0.05)
-        evolve(0.02)
-        Lin.ten_log_like3(statd, xt, xt, xt, util)
-    full = np.ascontiguousarray(rng.random((R, S, K)) + 0.1)
-    mask = np.ascontiguousarray((rng.random(S) < sq / S).astype(np.uint16))
-    futil = np.zeros(S)
-
-    def score():
-        Lin.ten_masked_logdot(full, full, mask, futil)
-    out = {}
-    for name, f in (("pendant_eval", pend_eval), ("distal_eval", dist_eval), ("stage1_score", score)):
-        f()
-        t0 = time.perf_counter()
-        for _ in range(reps):
-            f()
-        out[name] = (time.perf_counter() - t0) / reps
-    t_eval = 0.5 * (out["pendant_eval"] + out["distal_eval"])
-    t_query = (len(w.parent) - 1) * out["stage1_score"] + evals_per_query * t_eval
-    return {"value": 1.0 / t_query, "unit": "placements/s", "method": "per-call timing x measured Brent counts",
-            "seconds": {k: v for k, v in out.items()}, "query_sites": sq}
+    model = DF.Model(m.statd, m.x, m.lam, m.xit, m.rates)
+    nodes = range(len(w.parent))
+    darr, parr, snodes = {}, {}, {}
+    for i in nodes:
+        if w.parent[i] < 0:
+            continue
+        darr[i] = DF.Glv(*eng.get_glv(0, i))
+        parr[i] = DF.Glv(*eng.get_glv(1, i))
+        snodes[i] = DF.Glv(*eng.get_glv(2, i))
+    edges = [i for i in nodes if w.parent[i] >= 0]
+    pf = {k: getattr(prefs, k) for k in ("start_pend", "max_pend", "initial_tolerance", "max_pitches", "max_strikes",
+                                         "strike_box", "keep_at_most", "keep_factor")}
+    t0 = time.perf_counter()
+    calls, agree, placed = 0, 0, []
+    for q in range(n_sample):
+        res, n = DF.place_query(model, w.query_seqs[q], darr, parr, snodes, w.bl, edges, pf)
+        calls += n
+        placed.append(res)
+        agree += int(bool(res) and bool(brent_res[q]) and res[0][0] == brent_res[q][0][0])
+    dt = time.perf_counter() - t0
+    return {"value": n_sample / dt, "unit": "placements/s",
+            "method": "measured: pplacer's per-query flow over the pgb_* drop-in calls, wall clock",
+            "sample_queries": n_sample, "seconds": dt, "brent_evals_per_query": calls / n_sample,
+            "best_edge_agrees_with_batched_brent": "%d/%d" % (agree, n_sample)}
 
 
 def run_ours(args):
@@ -331,7 +313,11 @@ def run_ours(args):
         brent = {"value": Q * args.brent_steps / (bms / 1e3), "unit": "placements/s",
                  "evals_per_trial": bev / btr, "evals_per_query": bev / (args.brent_steps * Q),
                  "steps": args.brent_steps}
-        brent["plain_dropin"] = plain_dropin_brent(eng, w, brent["evals_per_query"])
+        if args.dropin_sample > 0 and w.site_cats is None:
+            bres, _ = eng.fetch()
+            brent["plain_dropin"] = plain_dropin_brent(eng, w, bprefs, min(args.dropin_sample, Q), bres)
+            brent["newton_over_plain_dropin"] = value / brent["plain_dropin"]["value"]
+        brent["newton_over_batched_brent"] = value / brent["value"]
     # ---- posterior probabilities (-p, default exponential prior) on the same path ----
     pp = None
     if args.optimizer == "newton" and args.pp_steps > 0:
@@ -351,12 +337,13 @@ def run_ours(args):
     out = (L.Placement * (Q * kam))()
     n_out = np.zeros(Q, dtype=np.int32)
     qst = np.zeros(Q, dtype=np.int32)
-    lib.pgb_place(eng.h, C.byref(prefs), Q, seqs, C.addressof(out), n_out.ctypes.data, qst.ctypes.data)
+    lib.pgb_place_batch(eng.h, C.byref(prefs), Q, seqs, args.batch, C.addressof(out), n_out.ctypes.data,
+                        qst.ctypes.data)
     barrier(dist)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        L.check(lib.pgb_place(eng.h, C.byref(prefs), Q, seqs, C.addressof(out), n_out.ctypes.data,
-                              qst.ctypes.data), "pgb_place")
+        L.check(lib.pgb_place_batch(eng.h, C.byref(prefs), Q, seqs, args.batch, C.addressof(out), n_out.ctypes.data,
+                                    qst.ctypes.data), "pgb_place_batch")
     t_e2e = max_over_ranks(dist, time.perf_counter() - t0)
     e2e = Q * world * args.steps / t_e2e
     if rank != 0:

@@ -255,10 +255,16 @@ enum {
  * as Pquery.make_ml_sorted (pquery.ml:86-92); n_out[q] placements written;
  * qstatus[q] a PGB_Q_* code.  Host buffers in, host buffers out.  Large
  * query sets run in device batches (1,024 to 65,536 queries, sized so the
- * stage-1 products of a batch stay within 8 GiB; the environment variable
- * PGB_PLACE_BATCH overrides the size). */
+ * stage-1 buffers of a batch stay within 8 GiB; the environment variable
+ * PGB_PLACE_BATCH overrides the size).  Replaces the per-query placement of
+ * Core.pplacer_core (core.ml:113-409) and the forked workers. */
 pgb_status pgb_place(pgb_engine *e, const pgb_prefs *prefs, int n_queries, const char *seqs, pgb_placement *out,
                      int *n_out, int *qstatus);
+
+/* pgb_place with the caller's device batch size: batch queries are loaded,
+ * placed and fetched at a time (0: the automatic size of pgb_place). */
+pgb_status pgb_place_batch(pgb_engine *e, const pgb_prefs *prefs, int n_queries, const char *seqs, int batch,
+                           pgb_placement *out, int *n_out, int *qstatus);
 
 /* The same placement split so the device part can be timed alone: load
  * queries to the device, run the placement on them (no host traffic), fetch

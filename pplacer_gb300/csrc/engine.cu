@@ -1975,6 +1975,7 @@ pgb_status pgb_engine_create(const pgb_model_desc *m, const pgb_tree_desc *t, pg
         if (k != kz) ord |= k << (8 * s++);
       e->eig_ok = true;
       e->eig_ord = ord;
+      e->warp_variant = 3;  // the eigenbasis form at 16 warps per SM until the autotuner says otherwise
       double mean = 0;
       for (int i = 0; i < K; i++) mean += e->X[i * K + kz];
       e->eig_c0 = mean / K;
@@ -2771,19 +2772,23 @@ pgb_status pgb_queries_fetch(pgb_engine *e, pgb_placement *out, int *n_out, int 
   return PGB_OK;
 }
 
-pgb_status pgb_place(pgb_engine *e, const pgb_prefs *p, int n_queries, const char *seqs, pgb_placement *out,
-                     int *n_out, int *qstatus) {
-  if (!e || !p || n_queries < 0 || (n_queries > 0 && (!seqs || !out || !n_out || !qstatus))) {
+pgb_status pgb_place_batch(pgb_engine *e, const pgb_prefs *p, int n_queries, const char *seqs, int batch,
+                           pgb_placement *out, int *n_out, int *qstatus) {
+  if (!e || !p || n_queries < 0 || batch < 0 || (n_queries > 0 && (!seqs || !out || !n_out || !qstatus))) {
     set_error("place: bad argument");
     return PGB_ERR_ARG;
   }
-  // Device batches: the stage-1 products take ~24 bytes per (query, edge),
-  // so a batch holds at most 8 GiB of them (35,791 queries for 10,000 edges),
-  // a small part of the GPU's memory; fewer batches mean fewer stage-1
-  // launches and fewer whole-query tails.
-  const long ep = (e->n_edges + 15) & ~15;
-  int batch = (int)std::max(1024L, std::min(65536L, (8L << 30) / (24 * ep)));
-  if (const char *env = getenv("PGB_PLACE_BATCH")) batch = std::max(1, atoi(env));  // override (tests, tuning)
+  if (batch == 0) {
+    // Automatic device batches: per query the stage-1 pairs (8 bytes per
+    // edge, and 8 more for the FP64 rows of queries with ambiguity
+    // characters) and ~12 bytes per site of query buffers (characters,
+    // codes, the masked-site lists, the stage-1 site classes) stay within
+    // 8 GiB, a small part of the GPU's memory; fewer batches mean fewer
+    // stage-1 launches and fewer whole-query tails.
+    const long per_q = 16L * e->n_edges + 12L * e->S + 256;
+    batch = (int)std::max(1024L, std::min(65536L, (8L << 30) / per_q));
+    if (const char *env = getenv("PGB_PLACE_BATCH")) batch = std::max(1, atoi(env));  // override (tests, tuning)
+  }
   pgb_status s;
   if (n_queries == 0) return pgb_queries_load(e, 0, seqs);
   for (int b0 = 0; b0 < n_queries; b0 += batch) {
@@ -2793,6 +2798,11 @@ pgb_status pgb_place(pgb_engine *e, const pgb_prefs *p, int n_queries, const cha
       return s;
   }
   return PGB_OK;
+}
+
+pgb_status pgb_place(pgb_engine *e, const pgb_prefs *p, int n_queries, const char *seqs, pgb_placement *out,
+                     int *n_out, int *qstatus) {
+  return pgb_place_batch(e, p, n_queries, seqs, 0, out, n_out, qstatus);
 }
 
 pgb_status pgb_queries_trials(pgb_engine *e, const pgb_prefs *p, int optimizer, int mode, int n_trials,

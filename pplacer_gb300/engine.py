@@ -130,16 +130,17 @@ class Engine:
         self.run(prefs)
         return self.fetch()
 
-    def place_host(self, seqs, prefs=None):
-        """Place through the single C-ABI call pgb_place (host buffers in and out, device batches)."""
+    def place_host(self, seqs, prefs=None, batch=0):
+        """Place through the single C-ABI call pgb_place_batch (host buffers in
+        and out, device batches of `batch` queries; 0: automatic)."""
         prefs = prefs or default_prefs()
         Q, kam = len(seqs), prefs.keep_at_most
         out = (_L.Placement * max(1, Q * kam))()
         n_out = np.zeros(max(Q, 1), dtype=np.int32)
         status = np.zeros(max(Q, 1), dtype=np.int32)
         buf = "".join(seqs).encode() if Q else b""
-        _L.check(_L.load().pgb_place(self.h, C.byref(prefs), Q, buf, C.addressof(out), n_out.ctypes.data,
-                                     status.ctypes.data), "pgb_place")
+        _L.check(_L.load().pgb_place_batch(self.h, C.byref(prefs), Q, buf, int(batch), C.addressof(out),
+                                           n_out.ctypes.data, status.ctypes.data), "pgb_place_batch")
         res = [[(out[q * kam + i].edge, out[q * kam + i].like, out[q * kam + i].lwr, out[q * kam + i].dist,
                  out[q * kam + i].pend) for i in range(n_out[q])] for q in range(Q)]
         return res, status[:Q]

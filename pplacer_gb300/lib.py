@@ -97,6 +97,7 @@ def load(build_if_missing=True):
     L.pgb_prefs_default.argtypes = [C.POINTER(Prefs)]
     L.pgb_prefs_default.restype = None
     L.pgb_place.argtypes = [vp, C.POINTER(Prefs), i, C.c_char_p, vp, vp, vp]
+    L.pgb_place_batch.argtypes = [vp, C.POINTER(Prefs), i, C.c_char_p, i, vp, vp, vp]
     L.pgb_queries_load.argtypes = [vp, i, C.c_char_p]
     L.pgb_queries_run.argtypes = [vp, C.POINTER(Prefs)]
     L.pgb_queries_fetch.argtypes = [vp, vp, vp, vp]
@@ -109,7 +110,7 @@ def load(build_if_missing=True):
     L.pgb_engine_set_tuning.argtypes = [vp, vp, vp]
     for name in ["pgb_engine_create", "pgb_engine_destroy", "pgb_engine_precompute", "pgb_engine_refine_categories",
                  "pgb_engine_set_glvs",
-                 "pgb_engine_get_glv", "pgb_place", "pgb_queries_load", "pgb_queries_run", "pgb_queries_fetch",
+                 "pgb_engine_get_glv", "pgb_place", "pgb_place_batch", "pgb_queries_load", "pgb_queries_run", "pgb_queries_fetch",
                  "pgb_queries_stage1", "pgb_queries_rank", "pgb_queries_trials", "pgb_engine_timings", "pgb_engine_autotune",
                  "pgb_engine_get_tuning", "pgb_engine_set_tuning"]:
         getattr(L, name).restype = i

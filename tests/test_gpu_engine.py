@@ -426,11 +426,48 @@ def test_place_host_batches(small, monkeypatch):
     want, wst = eng.place(qs, E.default_prefs())
     monkeypatch.setenv("PGB_PLACE_BATCH", "7")
     got, gst = eng.place_host(qs, E.default_prefs())
-    assert list(gst) == list(wst)
-    for g, r in zip(got, want):
-        assert [p[0] for p in g] == [p[0] for p in r]
-        for a, b in zip(g, r):
-            assert a[1] == b[1] and a[3] == b[3] and a[4] == b[4]
+    got5, gst5 = eng.place_host(qs, E.default_prefs(), batch=5)  # the caller's batch size (pgb_place_batch)
+    for gg, ss in ((got, gst), (got5, gst5)):
+        assert list(ss) == list(wst)
+        for g, r in zip(gg, want):
+            assert [p[0] for p in g] == [p[0] for p in r]
+            for a, b in zip(g, r):
+                assert a[1] == b[1] and a[3] == b[3] and a[4] == b[4]
+
+
+def test_dropin_flow_vs_oracle(oracle_lib):
+    """pplacer's per-query flow over the plain per-call drop-in (the measured
+    Brent arm of the benchmark, dropin_flow.place_query): the same placements
+    as the oracle's FP64 restatement of that flow, up to the FP32 rounding of
+    the GLVs it reads back from the engine."""
+    from pplacer_gb300 import dropin_flow as DF
+    from pplacer_gb300 import engine as E
+    from pplacer_gb300 import synth
+    O = oracle_lib
+    w = synth.make_workload("cpu_small", n_queries=3, taxa=30, sites=240, lo=80, hi=200)
+    eng = E.engine_for_workload(w)
+    m = eng.model
+    model = DF.Model(m.statd, m.x, m.lam, m.xit, m.rates)
+    edges = [i for i in range(len(w.parent)) if w.parent[i] >= 0]
+    darr = {i: DF.Glv(*eng.get_glv(0, i)) for i in edges}
+    parr = {i: DF.Glv(*eng.get_glv(1, i)) for i in edges}
+    snodes = {i: DF.Glv(*eng.get_glv(2, i)) for i in edges}
+    op = O.make_prefs()
+    pf = {k: getattr(op, k) for k in ("start_pend", "max_pend", "initial_tolerance", "max_pitches", "max_strikes",
+                                      "strike_box", "keep_at_most", "keep_factor")}
+    oref = O.Reference(O.Model(w.exch, w.statd, w.rates), w.parent, w.bl, w.leaf_row, w.ref_seqs)
+    ores, _ = oref.place(w.query_seqs, op)
+    for q in range(3):
+        res, calls = DF.place_query(model, w.query_seqs[q], darr, parr, snodes, w.bl, edges, pf)
+        assert calls > 0 and res
+        assert abs(sum(p[2] for p in res) - 1.0) < 1e-9
+        ge, gl = res[0][0], res[0][1]
+        oe, ol = ores[q][0][0], ores[q][0][1]
+        if ge != oe:  # a tie: the same point seen from two edges
+            g_star = O.polish(oref, w.query_seqs[q], ge, res[0][4], res[0][3])[0]
+            o_star = O.polish(oref, w.query_seqs[q], oe, ores[q][0][4], ores[q][0][3])[0]
+            assert abs(g_star - o_star) <= 1e-6 * abs(o_star), (q, ge, oe)
+        assert abs(gl - ol) <= 1e-5 * abs(ol), (q, gl, ol)
 
 
 def test_long_queries_gradients_and_placement(oracle_lib):
