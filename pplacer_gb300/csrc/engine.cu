@@ -434,7 +434,7 @@ __global__ void k_s1_scores(S1Ctx c, int n_rows, const int *__restrict__ qlist, 
       if (code >= c.prim) acc += log((double)s1_util(c, node, reind[(long)q * c.S + i], code));
     }
   const long o = (long)q * c.n_edges + ei;
-  scores[o] = s1::s1_pair_score(pairs[o], qlen[q], log_nrates) + acc;
+  scores[o] = s1::s1_pair_score(pairs[o], s1::s1_qconst(qlen[q], log_nrates)) + acc;
 }
 
 // Per-query ranking: edges by score, descending, ties to the lower edge index
@@ -473,21 +473,14 @@ struct S1Scores {
   double log_nrates;
 };
 
-__global__ void __launch_bounds__(128) k_rank_warp(S1Scores sv, int E, int rk, int Q,
-                                                   const int *__restrict__ qstatus, int *rank, int keys_in_smem) {
-  extern __shared__ unsigned long long rk_smem[];
-  const int nw = blockDim.x >> 5, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int q = blockIdx.x * nw + w;
-  if (q >= Q || qstatus[q] != PGB_Q_OK) return;
-  unsigned long long *keys = rk_smem + (long)w * E;
-  const bool amb = sv.qamb[q] > 0;
-  const double *sc = sv.scores + (long)q * E;
-  const int2 *pr = sv.pairs + (long)q * E;
-  const int ql = sv.qlen[q];
-  auto key_of = [&](int i) { return s1_key(amb ? sc[i] : s1::s1_pair_score(pr[i], ql, sv.log_nrates)); };
-  if (keys_in_smem)
-    for (int i = lane; i < E; i += 32) keys[i] = key_of(i);
-  __syncwarp();
+// Top-rk extraction of one warp over the edges i with use(i): each lane
+// keeps a sorted cache of its kRankCache best remaining edges and refills it
+// from its edges ranked after the last one it gave out; the warp's winner of
+// each round is the arg-max over the lanes' heads (an xor butterfly, the
+// same in every lane).  out(r, i, key) is called in every lane for each
+// round r (i < 0 when fewer than rk edges are used).
+template <typename KeyFn, typename UseFn, typename OutFn>
+__device__ __forceinline__ void warp_topk(int E, int rk, int lane, KeyFn key_of, UseFn use, OutFn out) {
   unsigned long long ck[kRankCache];
   int ci[kRankCache];
   unsigned long long lk = 0ull;  // last edge this lane gave out (li < 0: none yet)
@@ -496,7 +489,8 @@ __global__ void __launch_bounds__(128) k_rank_warp(S1Scores sv, int E, int rk, i
 #pragma unroll
     for (int c = 0; c < kRankCache; c++) { ck[c] = 0ull; ci[c] = -1; }
     for (int i = lane; i < E; i += 32) {
-      unsigned long long k = keys_in_smem ? keys[i] : key_of(i);
+      if (!use(i)) continue;
+      unsigned long long k = key_of(i);
       if (li >= 0 && !rank_before(lk, li, k, i)) continue;
       if (ci[kRankCache - 1] >= 0 && !rank_before(k, i, ck[kRankCache - 1], ci[kRankCache - 1])) continue;
       // insert into the sorted cache
@@ -523,7 +517,7 @@ __global__ void __launch_bounds__(128) k_rank_warp(S1Scores sv, int E, int rk, i
       int oi = __shfl_xor_sync(0xffffffffu, wi, o);
       if (oi >= 0 && (wi < 0 || rank_before(ok, oi, wk, wi))) { wk = ok; wi = oi; }
     }
-    if (lane == 0) rank[(long)q * rk + r] = wi;
+    out(r, wi, wk);
     if (wi >= 0 && wi == ci[0]) {  // this lane's head: pop it
       lk = ck[0];
       li = ci[0];
@@ -534,6 +528,36 @@ __global__ void __launch_bounds__(128) k_rank_warp(S1Scores sv, int E, int rk, i
       if (ci[0] < 0) refill();
     }
   }
+}
+
+// Ranking of one query per warp by the stage-1 score of each edge (a query
+// with ambiguity characters reads its FP64 row; the others form the score
+// from the tensor-core pair as s1::s1_pair_df, in FP32 arithmetic, which
+// FP64's slow rate on this part makes the cheaper key).
+__global__ void __launch_bounds__(128) k_rank_warp(S1Scores sv, int E, int rk, int Q,
+                                                   const int *__restrict__ qstatus, int *rank, int keys_in_smem) {
+  extern __shared__ unsigned long long rk_smem[];
+  const int nw = blockDim.x >> 5, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int q = blockIdx.x * nw + w;
+  if (q >= Q || qstatus[q] != PGB_Q_OK) return;
+  unsigned long long *keys = rk_smem + (long)w * E;
+  const bool amb = sv.qamb[q] > 0;
+  const double *sc = sv.scores + (long)q * E;
+  const int2 *pr = sv.pairs + (long)q * E;
+  const s1::QConst qc = s1::s1_qconst(sv.qlen[q], sv.log_nrates);
+  auto key_of = [&](int i) { return amb ? s1_key(sc[i]) : s1::s1_pair_key(pr[i], qc); };
+  int *out_row = rank + (long)q * rk;
+  auto write = [&](int r, int i, unsigned long long) {
+    if (lane == 0) out_row[r] = i;
+  };
+  auto all = [](int) { return true; };
+  if (keys_in_smem) {
+    for (int i = lane; i < E; i += 32) keys[i] = key_of(i);
+    __syncwarp();
+    warp_topk(E, rk, lane, [&](int i) { return keys[i]; }, all, write);
+    return;
+  }
+  warp_topk(E, rk, lane, key_of, all, write);
 }
 
 #include "trials.cuh"

@@ -115,10 +115,59 @@ struct MmaCtx {
   int *err;              // [0] flag, [1] role, [2] unit, [3] block
 };
 
-// FP64 stage-1 score of a (C, exponent sum) pair: C - n log R + ln 2 x
-// (masked_logdot's float part and the exponent term of Glv.masked_logdot).
-__device__ __forceinline__ double s1_pair_score(int2 p, int qlen, double log_nrates) {
-  return (double)__int_as_float(p.x) - (double)(float)qlen * log_nrates + kLn2d * (double)p.y;
+// The stage-1 score of a (C, exponent sum x) pair, C - n log R + ln 2 x
+// (masked_logdot's float part and the exponent term of Glv.masked_logdot),
+// as an unevaluated sum hi + lo of two floats: exact products and sums
+// (Dekker / Knuth error-free transformations on FMA) keep about 44 bits,
+// and FP32 runs at many times FP64's rate on this part.  hi + lo is exact in
+// FP64, which is the score pgb_queries_stage1 returns; the ranking compares
+// the pairs, normalised so that |lo| <= ulp(hi) / 2, by (hi, lo).
+struct QConst {
+  float hi, lo;  // -n log R as a float pair
+};
+__device__ __forceinline__ QConst s1_qconst(int qlen, double log_nrates) {
+  const double v = -(double)(float)qlen * log_nrates;
+  QConst c;
+  c.hi = (float)v;
+  c.lo = (float)(v - (double)c.hi);
+  return c;
+}
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+__device__ __forceinline__ float2 s1_pair_df(int2 p, QConst qc) {
+  constexpr float kL2H = 0.693147182464599609375f;      // ln 2 rounded to float
+  constexpr float kL2L = -1.904654299957768e-09f;       // ln 2 - kL2H
+  const float c = __int_as_float(p.x);
+  const float xh = (float)p.y;                           // x within 64 of xh
+  const float xl = (float)(p.y - (int)xh);               // exact
+  const float ph = kL2H * xh;
+  float pl = fmaf(kL2H, xh, -ph);                        // exact error of ph
+  pl = fmaf(kL2L, xh, fmaf(kL2H, xl, pl));
+  float s1, e1, s2, e2;
+  two_sum(c, ph, s1, e1);
+  two_sum(s1, qc.hi, s2, e2);
+  const float t = e1 + e2 + pl + qc.lo;
+  float hi, lo;
+  two_sum(s2, t, hi, lo);
+  return make_float2(hi, lo);
+}
+__device__ __forceinline__ double s1_pair_score(int2 p, QConst qc) {
+  const float2 v = s1_pair_df(p, qc);
+  return (double)v.x + (double)v.y;
+}
+// Order-preserving 64-bit key of the pair: hi's order bits, then lo's (NaN
+// lowest).
+__device__ __forceinline__ uint32_t s1_fkey(float v) {
+  const uint32_t b = __float_as_uint(v);
+  return (b >> 31) ? ~b : (b | 0x80000000u);
+}
+__device__ __forceinline__ unsigned long long s1_pair_key(int2 p, QConst qc) {
+  const float2 v = s1_pair_df(p, qc);
+  if (isnan(v.x) || isnan(v.y)) return 0ull;
+  return ((unsigned long long)s1_fkey(v.x) << 32) | s1_fkey(v.y);
 }
 
 // Bounded wait; gives up when another role aborted or after the poll limit
