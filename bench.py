@@ -40,7 +40,7 @@ MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 
 
 # measured constants of the stage-2 roofline (see the roofline block below)
-DRAM_BYTES_PER_SITE_EVAL = 65.9  # k_place_warp on dna_1k: 20.10 GB DRAM read + write / 305.3 M site evaluations
+DRAM_BYTES_PER_SITE_EVAL = 84.75  # k_place_warp (eigenbasis form, 16 warps/SM) on dna_1k: 25.877 GB DRAM read + write / 305.3 M site evaluations
 FMA_OPS_PER_SITE_RATE = 148      # FFMA + FMUL per site and rate with derivatives (the kernel's arithmetic)
 N_SM = 152
 SM_MAX_HZ = 2.07e9
