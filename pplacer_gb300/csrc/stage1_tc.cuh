@@ -25,8 +25,9 @@
 // Warp roles: warp 0 issues the TMA loads, warp 1 the MMAs (one thread),
 // warps 2-5 build the B tiles and then read TMEM for the epilogue, which
 // writes per (query, edge) the pair (C as FP32, the exact total exponent sum
-// as int32); the ranking forms the FP64 score from it (s1_pair_score), so
-// no FP64 arithmetic -- slow on this part -- sits in the tile loop.  The
+// as int32); the ranking forms the score from it as an exact pair of
+// floats (s1_pair_df), so no FP64 arithmetic -- slow on this part -- sits
+// in the tile loop or the ranking.  The
 // query tile width N (a multiple of 16, up to 256) is chosen per launch to
 // fill the SMs' last wave.  Stages are handed over through mbarriers; every
 // wait is bounded and a timeout records where it happened and returns.
