@@ -41,7 +41,10 @@ MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 
 # measured constants of the stage-2 roofline (see the roofline block below)
 DRAM_BYTES_PER_SITE_EVAL = 84.75  # k_place_warp (eigenbasis form, 16 warps/SM) on dna_1k: 25.877 GB DRAM read + write / 305.3 M site evaluations
-FMA_OPS_PER_SITE_RATE = 148      # FFMA + FMUL per site and rate with derivatives (the kernel's arithmetic)
+# FFMA + FMUL per site and rate with derivatives (the kernel's arithmetic):
+# six 4x4 matrix-vector products (96) + the six sums (52) in the matrix form;
+# 2 x 3 coordinate scalings + 6 x 12 column FMAs (78) + 52 in the eigenbasis form
+FMA_OPS_PER_SITE_RATE = {"matrix": 148, "eigenbasis": 130}
 N_SM = 152
 SM_MAX_HZ = 2.07e9
 
@@ -146,12 +149,25 @@ class ClockSampler:
         return {"sm_mhz": med, "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
+# The nucleotide Gamma warp forms by the engine's tuning value (smem_windows
+# of a warp bin): 0 matrices in registers, 1-3 the eigenbasis form
+WARP_FORM_WARPS = {0: 8, 1: 8, 2: 12, 3: 16}
+
+
+def warp_form(w, tune):
+    """'matrix' or 'eigenbasis' for the nucleotide warp kernel; None otherwise."""
+    if w.site_cats is not None or w.K != 4 or set(int(v) for v in tune[0]) != {32}:
+        return None
+    return "eigenbasis" if int(tune[1][0]) >= 1 else "matrix"
+
+
 def stage2_kernel(w, tune):
     """The trial kernel that ran stage 2 + refinement for this workload and tuning."""
     th = set(int(v) for v in tune[0])
     if th == {32}:
         return "k_place_warp (stage 2 + refinement, whole queries, one warp each%s)" % (
-            ", per-site categories" if w.site_cats is not None else "")
+            ", per-site categories" if w.site_cats is not None else
+            ", %s form, %d warps per SM" % (warp_form(w, tune), WARP_FORM_WARPS[int(tune[1][0])]))
     if th == {1}:
         return "k_place_tc (stage 2 + refinement, whole queries, one CTA each, tcgen05 evolves)"
     if len(th) == 1:
@@ -366,9 +382,14 @@ def run_ours(args):
     # launch's site evaluations, full-size dna_1k capture)
     traffic = (DRAM_BYTES_PER_SITE_EVAL * site_evals / args.steps
                if args.workload == "dna_1k" and DRAM_BYTES_PER_SITE_EVAL else None)
-    # the binding unit is the FP32 pipe: FMA-pipe lane operations per site
-    # evaluation (148 per rate with derivatives), against 128 lanes per SM
-    fp32_ops = FMA_OPS_PER_SITE_RATE * R * site_evals / args.steps / t_trials if t_trials > 0 else 0.0
+    # the binding unit is instruction issue on the FP32 pipe: FMA-pipe lane
+    # operations per site evaluation of the form that ran (per rate, with
+    # derivatives), against 128 lanes per SM; CAT runs the matrix arithmetic
+    # on its one plane, the 20-state tensor-core form has no such count
+    form = warp_form(w, tune) or ("matrix" if w.site_cats is not None and set(int(v) for v in tune[0]) == {32}
+                                  else None)
+    fp32_ops = (FMA_OPS_PER_SITE_RATE[form] * R * site_evals / args.steps / t_trials
+                if form and t_trials > 0 else None)
     fp32_peak = 128 * N_SM * SM_MAX_HZ
     # Stage 1 (the masked_logdot score of every (query, edge) pair): the
     # tcgen05 kernel k_s1_mma contracts [edges x queries] over K = 3 x prim x
@@ -412,8 +433,10 @@ def run_ours(args):
                                         if traffic is not None else None),
                      "algorithmic_bytes_per_site_eval": bytes_per_site_eval,
                      "peak_source": peak_kind,
-                     "fp32_pipe": {"achieved": fp32_ops, "peak": fp32_peak, "unit": "FMA-pipe lane ops/s",
-                                   "frac": fp32_ops / fp32_peak, "peak_source": "nominal: 128 lanes x 152 SMs x 2070 MHz"},
+                     "fp32_pipe": ({"achieved": fp32_ops, "peak": fp32_peak, "unit": "FMA-pipe lane ops/s",
+                                    "frac": fp32_ops / fp32_peak, "ops_per_site_rate": FMA_OPS_PER_SITE_RATE[form],
+                                    "form": form, "peak_source": "nominal: 128 lanes x 152 SMs x 2070 MHz"}
+                                   if fp32_ops is not None else None),
                      "stage1": {"kernel": "k_s1_mma (hand-written tcgen05: TMA bf16 tables, one-hot query tiles "
                                           "built in shared memory, TMEM accumulators)", "bound": "tensor",
                                 "achieved": s1_tflops, "peak": bf16_peak, "unit": "TFLOP/s",

@@ -69,6 +69,29 @@ def test_stage1_scores_match_oracle(small, oracle_lib):
         np.testing.assert_allclose(got, ref, rtol=1e-6)
 
 
+def test_stage1_ranking_matches_oracle_order(small, oracle_lib):
+    """The GPU's ranked edge order against the oracle's ranking (core.ml:
+    187-197 scored, fig.ml:143-147 sorted): position by position, the
+    oracle's score of the GPU's edge equals the oracle's score at that
+    position to the stage-1 tolerance (1e-6 relative), so the orders differ
+    at most by swaps of scores that agree to that tolerance."""
+    w, oref, eng = small
+    eng.stage1()
+    edges = [i for i in range(w.n_nodes) if w.parent[i] >= 0]
+    E = len(edges)
+    got = eng.rank(E)
+    for q in range(0, 60, 5):
+        st, ranking, _ = oref.trace(w.query_seqs[q], oracle_lib.make_prefs(max_strikes=1, max_pitches=0))
+        if st != 0 or not ranking:
+            continue
+        want = dict(ranking)
+        ordered = [s for _, s in ranking]
+        assert len(ordered) == E
+        for j in range(E):
+            g = want[edges[got[q][j]]]
+            assert abs(g - ordered[j]) <= 1e-6 * abs(ordered[j]), (q, j, g, ordered[j])
+
+
 @pytest.mark.parametrize("rk", [1, 65, 130, 0])
 def test_stage1_ranking(small, rk):
     """The rk best edges per query (0: every edge): scores descending, equal

@@ -6,7 +6,8 @@ allocate only at start-up): they pass device buffers, and the function's
 scratch is a fixed array inside the library.  This test owns the device
 buffers (through torch), calls the entry point through the C ABI twice in a
 row on different inputs, and checks each result against the host-pointer
-drop-in pgb_ten_log_like3 at the drop-in tolerance.  The file is named so
+drop-in pgb_ten_log_like3 and against the FP64 oracle (oracle.cpp's
+restatement of linear_c.c's ten_log_like3_c) at the drop-in tolerance.  The file is named so
 pytest collects it last.
 """
 import ctypes as C
@@ -27,7 +28,7 @@ def _lib():
     return L, lib, f
 
 
-def test_noalloc_matches_dropin_twice():
+def test_noalloc_matches_dropin_twice(oracle_lib):
     import torch
     from pplacer_gb300 import linear
     L, lib, f = _lib()
@@ -37,6 +38,7 @@ def test_noalloc_matches_dropin_twice():
         statd = rng.dirichlet(np.ones(K))
         x, y, z = (rng.random((R, S, K)) + 0.01 for _ in range(3))
         want = linear.ten_log_like3(statd, x, y, z, np.zeros(S))
+        want_orc = oracle_lib.lib().orc_ten_log_like3(statd, x, y, z, np.zeros(S), R, S, K)
         t = [torch.from_numpy(np.ascontiguousarray(a)).to(dev) for a in (statd, x, y, z)]
         out = torch.full((1,), float("nan"), dtype=torch.float64, device=dev)
         torch.cuda.synchronize()
@@ -45,6 +47,7 @@ def test_noalloc_matches_dropin_twice():
         torch.cuda.synchronize()
         got = float(out.item())
         assert math.isclose(got, want, rel_tol=1e-12), (call, got, want)
+        assert math.isclose(got, want_orc, rel_tol=1e-12), (call, got, want_orc)
 
 
 def test_noalloc_rejects_oversized_input():
