@@ -169,7 +169,8 @@ def stage2_kernel(w, tune):
             ", per-site categories" if w.site_cats is not None else
             ", %s form, %d warps per SM" % (warp_form(w, tune), WARP_FORM_WARPS[int(tune[1][0])]))
     if th == {1}:
-        return "k_place_tc (stage 2 + refinement, whole queries, one CTA each, tcgen05 evolves)"
+        return ("k_place_tc (stage 2 + refinement, whole queries, one 128-thread team each, two teams per CTA, "
+                "tcgen05 evolves)")
     if len(th) == 1:
         return "k_place_cta (stage 2 + refinement, whole queries, one CTA of %d threads each)" % th.pop()
     return "k_trials (stage 2 + refinement in baseball rounds, CTA per trial, %s threads)" % "/".join(

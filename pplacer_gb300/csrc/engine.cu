@@ -1024,8 +1024,9 @@ __global__ void __launch_bounds__(32, MINB) k_place_warp(TrialCtx c, PlaceCtx p)
   place_queries(tm, c, p);
 }
 
-// The tensor-core CTA as a team: thread 0 leads, the CTA's barriers order,
-// a shared int broadcasts.
+// A team of the tensor-core kernel (128 threads, its own named barrier,
+// mbarrier and TMEM columns): thread 0 leads, the team's barrier orders, a
+// shared int broadcasts.
 struct TcTeam {
   const TrialCtx &c;
   const TcSmem &sm;
@@ -1034,11 +1035,11 @@ struct TcTeam {
   bool &failed;
   int tid;
   __device__ bool leader() const { return tid == 0; }
-  __device__ void sync() const { __syncthreads(); }
+  __device__ void sync() const { pgb::tc::team_sync(sm.bar_id); }
   __device__ int bcast(int v) const {
-    __syncthreads();  // earlier readers of the slot are done
+    pgb::tc::team_sync(sm.bar_id);  // earlier readers of the slot are done
     if (tid == 0) *sm.redi = v;
-    __syncthreads();
+    pgb::tc::team_sync(sm.bar_id);
     return *sm.redi;
   }
   __device__ TrialRes trial(const TrialIn &t) { return tc_trial(c, sm, tmem, phase, failed, t, tid); }
@@ -1072,18 +1073,21 @@ __global__ void __launch_bounds__(T, 1) k_place_cta(TrialCtx c, PlaceCtx p) {
   place_queries(tm, c, p);
 }
 
-// Whole queries, one per CTA of the tensor-core trial kernel (20-state
-// Gamma mixtures): the shared search with each trial run by the CTA.
-__global__ void __launch_bounds__(kTcThreads, 1) k_place_tc(TrialCtx c, PlaceCtx p) {
+// Whole queries on the tensor-core trial kernel (20-state Gamma mixtures):
+// blockDim.x / 128 teams per CTA, each running the shared search on its own
+// queries, with each trial run by the team; the teams share the CTA's
+// constant B tiles and split its 512 TMEM columns.
+__global__ void __launch_bounds__(kTcThreads * kTcMaxTeams, 1) k_place_tc(TrialCtx c, PlaceCtx p) {
   extern __shared__ __align__(16) char t_smem[];
-  const int tid = threadIdx.x;
-  const TcSmem sm = tc_carve(t_smem, c.cap, c.NM, c.ncode, c.zcodes);
-  const uint32_t tmem = tc_setup(c, sm, tid);
+  const int teams = blockDim.x / kTcThreads;
+  const int team = threadIdx.x / kTcThreads, tid = threadIdx.x - team * kTcThreads;
+  const TcSmem sm = tc_carve(t_smem, c.cap, c.NM, c.ncode, c.zcodes, team);
+  const uint32_t tmem = tc_setup(c, sm, threadIdx.x, blockDim.x, teams) + kTcTeamCols * (uint32_t)team;
   uint32_t phase = 0;
   bool failed = false;
   TcTeam tm{c, sm, tmem, phase, failed, tid};
   place_queries(tm, c, p);
-  tc_teardown(sm, tmem, phase, failed, tid);
+  tc_teardown(sm, phase, failed, threadIdx.x, teams);
 }
 
 }  // namespace
@@ -1194,7 +1198,6 @@ namespace {
 
 constexpr int kBins = 6;
 constexpr int kTuneTc = 1;  // tuning code of the tensor-core trial kernel
-constexpr int kTcMaxInstances = 4;  // concurrent launches of the whole-query tensor-core kernel
 
 template <class T>
 pgb_status dalloc(T **p, size_t n) {
@@ -1571,13 +1574,24 @@ pgb_status ensure_eigen_glvs(pgb_engine *e) {
   return PGB_OK;
 }
 
+// Dynamic shared memory of a tensor-core trial launch: at least enough that
+// no more CTAs fit on an SM than its 512 TMEM columns serve (2 with one team
+// of 256 columns each, 1 with two teams), so no CTA ever waits for columns.
+size_t tc_launch_smem(pgb_engine *e, size_t smem, int teams) {
+  int sm_smem = 0;
+  cudaDeviceGetAttribute(&sm_smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor, e->device);
+  const size_t per_cta = (size_t)sm_smem / (teams == 1 ? 3 : 2) + 1024;
+  return std::min(std::max(smem, per_cta), e->smem_optin);
+}
+
 pgb_status launch_trials_tc(pgb_engine *e, cudaStream_t st, TrialCtx c, const int *d_order, int n, int cap,
                             TrialRes *out) {
   c.smem_win = 0;
   c.cap = std::max(cap, 1);
   c.zcodes = tc_zcodes(e);
-  size_t smem = tc_trial_smem_bytes(c.cap, e->NM, e->ncode, c.zcodes);
+  size_t smem = tc_trial_smem_bytes(c.cap, e->NM, e->ncode, c.zcodes, 1);
   if (smem > e->smem_optin) { set_error("tensor-core trial shared memory %zu exceeds %zu", smem, e->smem_optin); return PGB_ERR_ARG; }
+  smem = tc_launch_smem(e, smem, 1);
   PGB_CUDA(cudaFuncSetAttribute(k_trials_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   k_trials_tc<<<n, kTcThreads, smem, st>>>(c, e->d_trials, d_order, n, out);
   PGB_LAUNCH_CHECK();
@@ -1788,31 +1802,21 @@ pgb_status launch_place_warp_gmix(pgb_engine *e, TrialCtx c, const PlaceCtx &pc)
 pgb_status launch_place_tc(pgb_engine *e, TrialCtx c, const PlaceCtx &pc, int max_sq) {
   c.cap = std::max(max_sq, 1);
   c.zcodes = tc_zcodes(e);
-  size_t smem = tc_trial_smem_bytes(c.cap, e->NM, e->ncode, c.zcodes);
+  // Two teams per CTA when the shared memory holds them (they share the B
+  // tiles and split the SM's TMEM columns), else one; one persistent CTA per
+  // SM, the teams taking queries from the shared counter.
+  int teams = kTcMaxTeams;
+  size_t smem = tc_trial_smem_bytes(c.cap, e->NM, e->ncode, c.zcodes, teams);
+  if (smem > e->smem_optin) {
+    teams = 1;
+    smem = tc_trial_smem_bytes(c.cap, e->NM, e->ncode, c.zcodes, teams);
+  }
   if (smem > e->smem_optin) { set_error("tensor-core trial shared memory %zu exceeds %zu", smem, e->smem_optin); return PGB_ERR_ARG; }
+  smem = tc_launch_smem(e, smem, teams);
   PGB_CUDA(cudaFuncSetAttribute(k_place_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  int per_sm = 0;
-  PGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_place_tc, kTcThreads, smem));
-  // The runtime places one CTA of a tcgen05 kernel per SM per launch (its
-  // occupancy is 1 whatever the registers and shared memory), but CTAs of
-  // concurrent launches share an SM.  So the persistent grid runs as several
-  // launches on separate streams, sharing the query counter: as many as the
-  // SM's shared memory holds, at most 4 (4 x 128 TMEM columns).
-  int sm_smem = 0, rsv = 0;
-  cudaDeviceGetAttribute(&sm_smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor, e->device);
-  cudaDeviceGetAttribute(&rsv, cudaDevAttrReservedSharedMemoryPerBlock, e->device);
-  const int inst = std::max(1, std::min(kTcMaxInstances, (int)((size_t)sm_smem / (smem + (size_t)rsv))));
-  const int grid = std::max(1, std::min(e->Q, e->n_sm * std::max(1, per_sm)));
-  PGB_CUDA(cudaEventRecord(e->bin_ev[8], e->st));
-  for (int k = 1; k < inst; k++) PGB_CUDA(cudaStreamWaitEvent(e->bin_st[k - 1], e->bin_ev[8], 0));
-  for (int k = 0; k < inst; k++) {
-    k_place_tc<<<grid, kTcThreads, smem, k == 0 ? e->st : e->bin_st[k - 1]>>>(c, pc);
-    PGB_LAUNCH_CHECK();
-  }
-  for (int k = 1; k < inst; k++) {
-    PGB_CUDA(cudaEventRecord(e->bin_ev[k - 1], e->bin_st[k - 1]));
-    PGB_CUDA(cudaStreamWaitEvent(e->st, e->bin_ev[k - 1], 0));
-  }
+  const int grid = std::max(1, std::min((e->Q + teams - 1) / teams, e->n_sm));
+  k_place_tc<<<grid, kTcThreads * teams, smem, e->st>>>(c, pc);
+  PGB_LAUNCH_CHECK();
   return PGB_OK;
 }
 

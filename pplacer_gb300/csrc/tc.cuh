@@ -151,6 +151,80 @@ __device__ __forceinline__ void pin(float (&v)[N]) {
   for (int i = 0; i < N; i++) asm volatile("" : "+f"(v[i]));
 }
 
+// The same MMA with A in tensor memory: row m of the 128-row A tile in TMEM
+// lane m, its K elements (TF32, one per 32-bit column) in consecutive
+// columns from atmem; B from shared memory.
+__device__ __forceinline__ void mma_tf32_ts(uint32_t dtmem, uint32_t atmem, uint64_t b, uint32_t idesc,
+                                            uint32_t accum) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n\t"
+      "}" ::"r"(dtmem),
+      "r"(atmem), "l"(b), "r"(idesc), "r"(accum)
+      : "memory");
+}
+
+// 8 consecutive 32-bit columns of the warp's 32 TMEM lanes from registers
+// (thread i writes lane base + i); complete after st_wait().
+__device__ __forceinline__ void st8(uint32_t taddr, const float (&v)[8]) {
+  asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"r"(taddr),
+               "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])),
+               "r"(__float_as_uint(v[3])), "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])),
+               "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7]))
+               : "memory");
+}
+__device__ __forceinline__ void st_wait() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
+
+// A row of kKPad FP32 values (zero past the states) into TMEM as TF32 hi at
+// columns [col_hi, col_hi + 24) and lo at [col_lo, col_lo + 24) of the
+// thread's lane; taddr_lane = TMEM base with the warp's lane quarter.
+__device__ __forceinline__ void st_split_row(uint32_t taddr_lane, uint32_t col_hi, uint32_t col_lo,
+                                             const float (&v)[kKPad]) {
+#pragma unroll
+  for (int b = 0; b < kKPad / 8; b++) {
+    float h[8], l[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++) split_tf32(v[8 * b + j], h[j], l[j]);
+    st8(taddr_lane + col_hi + 8 * b, h);
+    st8(taddr_lane + col_lo + 8 * b, l);
+  }
+}
+
+// D[0:M, 0:N] (+)= A B^T over the three K steps of the padded states, with
+// the 3xTF32 products: hi*hi, hi*lo, lo*hi, A in TMEM (columns a_hi, a_lo),
+// B in shared memory; issued by one thread.
+__device__ __forceinline__ void mma_3xtf32_ts(uint32_t dtmem, uint32_t a_hi, uint32_t a_lo, uint32_t b_hi,
+                                              uint32_t b_lo, uint32_t idesc) {
+#pragma unroll
+  for (int s = 0; s < kKPad / 8; s++) {
+    const uint32_t o = s * kKStepBytes;
+    mma_tf32_ts(dtmem, a_lo + 8 * s, sdesc(b_hi + o), idesc, s > 0 ? 1u : 0u);
+    mma_tf32_ts(dtmem, a_hi + 8 * s, sdesc(b_lo + o), idesc, 1u);
+    mma_tf32_ts(dtmem, a_hi + 8 * s, sdesc(b_hi + o), idesc, 1u);
+  }
+}
+
+// Barrier of one team of kTeamThreads threads (named barrier id >= 1), and
+// the same barrier as a vote: true when v is true in every thread.
+constexpr int kTeamThreads = 128;
+__device__ __forceinline__ void team_sync(int id) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(kTeamThreads) : "memory");
+}
+__device__ __forceinline__ bool team_and(int id, bool v) {
+  uint32_t out;
+  asm volatile(
+      "{\n\t.reg .pred p, q;\n\t"
+      "setp.ne.u32 p, %1, 0;\n\t"
+      "bar.red.and.pred q, %2, %3, p;\n\t"
+      "selp.u32 %0, 1, 0, q;\n\t"
+      "}"
+      : "=r"(out)
+      : "r"((uint32_t)v), "r"(id), "r"(kTeamThreads)
+      : "memory");
+  return out != 0;
+}
+
 // D[0:M, 0:N] (+)= A B^T over the three K steps of the padded states, with
 // the 3xTF32 products: hi*hi, hi*lo, lo*hi.  a_hi, a_lo, b_hi, b_lo: shared
 // addresses of the operand tiles; issued by one thread.

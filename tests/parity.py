@@ -25,11 +25,15 @@ distal_length, pendant_length).  `compare` checks all of it:
     for Newton; the Brent replica compares FP32 likelihoods whose rounding
     exceeds the differences its 1e-5 length tolerance resolves, and is held
     to 1e-4);
+  * the GPU's reported logL of every placement kept by both against the
+    FP64 logL at its own lengths: within 1e-6 relative (the evaluation's
+    FP32 arithmetic);
   * like_weight_ratio of every placement kept by both, when the kept sets
     agree: against the softmax of the polished optima, `lwr_tol` absolute
-    plus twice the largest FP64 logL gap of the query's GPU placements (a
-    ratio moves by at most about that much), and against the oracle's, that
-    plus the oracle's own distance from the softmax.
+    plus twice the largest distance of the query's reported GPU logLs from
+    those optima (the FP64 gap plus the evaluation error; a ratio moves by
+    at most about that much), and against the oracle's, that plus the
+    oracle's own distance from the softmax.
 
 The measured worst cases are returned so tests can report them.
 """
@@ -67,7 +71,8 @@ def compare(O, oref, seqs, res_gpu, res_orc, keep_at_most=7, keep_factor=0.01, d
             max_mismatch_frac=0.001):
     st = dict(queries=0, non_tied=0, mismatch=0, better=0, logl_ok=0, same_set=0, boundary_swaps=0,
               records=0, bl_within_1e4=0, max_dpend=0.0, max_ddist=0.0, max_gap_rel=0.0, max_gap=0.0,
-              max_lwr_vs_oracle=0.0, max_lwr_vs_optimum=0.0, max_oracle_lwr_vs_optimum=0.0, oracle_only=0, gpu_only=0, gpu_only_boundary=0,
+              max_lwr_vs_oracle=0.0, max_lwr_vs_optimum=0.0, max_oracle_lwr_vs_optimum=0.0, max_eval_err_rel=0.0,
+              oracle_only=0, gpu_only=0, gpu_only_boundary=0,
               gpu_only_oracle_brent_short=0, gpu_only_oracle_not_evaluated=0, gpu_only_unclassified=0,
               max_oracle_stage2_shortfall=0.0)
     bad = []
@@ -170,13 +175,17 @@ def compare(O, oref, seqs, res_gpu, res_orc, keep_at_most=7, keep_factor=0.01, d
             else:
                 bad.append("q%d: edge %d (polished %.4f, oracle stage 2 %.4f) kept by the GPU only" % (q, e, Ls[e], s2[e]))
         # ---- branch lengths of the placements both keep ----
-        q_gap = 0.0
+        q_dev = 0.0
         for e in set(gset) & set(oset):
             L, ps, ds, v = cache[(q, e)]
-            _, gpd, gdd = gset[e][1], gset[e][4], gset[e][3]
+            gll, gpd, gdd = gset[e][1], gset[e][4], gset[e][3]
             st_, vg = oref.loglike_derivs(seqs[q], e, gpd, gdd)
             gap = max(L - vg[0], 0.0)
-            q_gap = max(q_gap, gap)
+            q_dev = max(q_dev, abs(gll - L))
+            err = abs(gll - vg[0])
+            st["max_eval_err_rel"] = max(st["max_eval_err_rel"], err / abs(L))
+            if err > LOGL_RTOL * abs(L):
+                bad.append("q%d e%d: GPU logL %.9g vs FP64 %.9g at its lengths" % (q, e, gll, vg[0]))
             st["records"] += 1
             st["max_gap_rel"] = max(st["max_gap_rel"], gap / abs(L))
             st["max_gap"] = max(st["max_gap"], gap)
@@ -207,8 +216,9 @@ def compare(O, oref, seqs, res_gpu, res_orc, keep_at_most=7, keep_factor=0.01, d
                 st["max_lwr_vs_optimum"] = max(st["max_lwr_vs_optimum"], d2)
                 st["max_oracle_lwr_vs_optimum"] = max(st["max_oracle_lwr_vs_optimum"], d_or)
                 # a ratio moves by at most ~2x the largest logL error among
-                # the query's placements; the GPU's FP64 gaps bound its own
-                tol = lwr_tol + 2.0 * q_gap
+                # the query's placements: the GPU's reported logLs against
+                # the polished optima
+                tol = lwr_tol + 2.0 * q_dev
                 if d2 > tol or d1 > tol + d_or:
                     bad.append("q%d e%d: like_weight_ratio %.8f vs oracle %.8f, vs optimum %.8f" %
                                (q, e, gset[e][2], oset[e][2], ideal))
