@@ -16,8 +16,9 @@ like_weight_ratio), after the reference-tree precompute, as pplacer times it.
 value: placements/s with queries and GLVs already resident in HBM, timed with
        CUDA events on the engine's stream; the GLV arrays (3 x 192 MB) exceed
        the 129 MB L2, so no L2 flush is needed between steps.
-e2e:   placements/s through pgb_place (the C ABI call a caller makes) with the
-       query rows in host memory and the placements copied back every step.
+e2e:   placements/s through pgb_place_batch (the C ABI call a caller makes)
+       with the query rows in page-locked host memory (pgb_host_alloc),
+       uploaded, placed and the placements copied back every step.
 
 --workload aa_500 | cat_5k | dna_2k runs the other configurations through the
 same line (20-state + G4 on the tensor-core kernel, GTR + CAT 20 and the long
@@ -348,20 +349,25 @@ def run_ours(args):
             pev += cnt[2]
         pp = {"value": Q * args.pp_steps / (pms / 1e3), "unit": "placements/s",
               "evals_per_step": pev / args.pp_steps, "steps": args.pp_steps}
-    # ---- end to end through pgb_place, host buffers ----
-    seqs = "".join(w.query_seqs).encode()
+    # ---- end to end through pgb_place_batch: the query rows in, the
+    # placements out, both in page-locked host memory (pgb_host_alloc) ----
     kam = prefs.keep_at_most
-    out = (L.Placement * (Q * kam))()
-    n_out = np.zeros(Q, dtype=np.int32)
-    qst = np.zeros(Q, dtype=np.int32)
-    lib.pgb_place_batch(eng.h, C.byref(prefs), Q, seqs, args.batch, C.addressof(out), n_out.ctypes.data,
-                        qst.ctypes.data)
+    hb_in = L.HostBuffer(Q * S)
+    hb_in.array(np.uint8, Q * S)[:] = np.frombuffer("".join(w.query_seqs).encode(), dtype=np.uint8)
+    hb_out = L.HostBuffer(Q * kam * C.sizeof(L.Placement) + 8 * Q)
+    out_p = hb_out.address
+    n_out_p = out_p + Q * kam * C.sizeof(L.Placement)
+    qst_p = n_out_p + 4 * Q
+    lib.pgb_place_batch(eng.h, C.byref(prefs), Q, hb_in.address, args.batch, out_p, n_out_p, qst_p)
     barrier(dist)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        L.check(lib.pgb_place_batch(eng.h, C.byref(prefs), Q, seqs, args.batch, C.addressof(out), n_out.ctypes.data,
-                                    qst.ctypes.data), "pgb_place_batch")
+        L.check(lib.pgb_place_batch(eng.h, C.byref(prefs), Q, hb_in.address, args.batch, out_p, n_out_p, qst_p),
+                "pgb_place_batch")
     t_e2e = max_over_ranks(dist, time.perf_counter() - t0)
+    assert int(hb_out.array(np.int32, Q * kam * C.sizeof(L.Placement) // 4 + Q)[-Q:].sum()) > 0  # placements came back
+    hb_in.close()
+    hb_out.close()
     e2e = Q * world * args.steps / t_e2e
     if rank != 0:
         return

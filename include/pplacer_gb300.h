@@ -266,6 +266,15 @@ pgb_status pgb_place(pgb_engine *e, const pgb_prefs *prefs, int n_queries, const
 pgb_status pgb_place_batch(pgb_engine *e, const pgb_prefs *prefs, int n_queries, const char *seqs, int batch,
                            pgb_placement *out, int *n_out, int *qstatus);
 
+/* Page-locked host memory for the query and result buffers of pgb_place /
+ * pgb_place_batch: copies from and to it run at the host link's full rate
+ * instead of through the driver's staging buffers.  pgb_host_free releases
+ * a buffer of pgb_host_alloc.  No counterpart in the reference (its buffers
+ * are OCaml bigarrays, gstar_support.ml:100-115); a caller that keeps its
+ * query rows in such a buffer passes it to pgb_place_batch unchanged. */
+pgb_status pgb_host_alloc(size_t bytes, void **ptr);
+pgb_status pgb_host_free(void *ptr);
+
 /* The same placement split so the device part can be timed alone: load
  * queries to the device, run the placement on them (no host traffic), fetch
  * the results. */

@@ -1154,6 +1154,7 @@ struct pgb_engine {
   uint32_t *d_rcode = nullptr;  // (alignment column << 8) | code per informative site
   int *d_qlen = nullptr, *d_qstatus = nullptr;
   std::vector<int> h_qlen;
+  std::vector<int> h_qorder, h_len_at;  // the whole-query order (longest first) and its counting-sort bins
   // run buffers
   double *d_scores = nullptr;  // FP64 stage-1 rows of queries with ambiguity characters (or all, on request)
   size_t scores_cap = 0;
@@ -2445,13 +2446,16 @@ pgb_status pgb_queries_load(pgb_engine *e, int n_queries, const char *seqs) {
     if ((s = dalloc(&e->d_qorder, n_queries))) return s;
     e->qorder_cap = n_queries;
   }
-  std::vector<int> ord(n_queries);
-  for (int i = 0; i < n_queries; i++) ord[i] = i;
-  std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return e->h_qlen[a] > e->h_qlen[b]; });
+  // longest first, equal lengths in query order: a counting sort over the
+  // lengths 0..S (O(Q + S) on the host, between two launches)
+  std::vector<int> &ord = e->h_qorder, &at = e->h_len_at;
+  ord.resize(n_queries);
+  at.assign(e->S + 2, 0);
+  for (int q = 0; q < n_queries; q++) at[e->S - e->h_qlen[q] + 1]++;
+  for (int l = 1; l <= e->S + 1; l++) at[l] += at[l - 1];
+  for (int q = 0; q < n_queries; q++) ord[at[e->S - e->h_qlen[q]]++] = q;
   PGB_CUDA(cudaMemcpyAsync(e->d_qorder, ord.data(), ord.size() * sizeof(int), cudaMemcpyHostToDevice, e->st));
-  if ((s = prep_stage1_queries(e))) return s;
-  PGB_CUDA(cudaStreamSynchronize(e->st));
-  return PGB_OK;
+  return prep_stage1_queries(e);
 }
 
 static pgb_status check_prefs(const pgb_prefs *p) {
@@ -2825,6 +2829,18 @@ pgb_status pgb_place_batch(pgb_engine *e, const pgb_prefs *p, int n_queries, con
         (s = pgb_queries_fetch(e, out + (size_t)b0 * p->keep_at_most, n_out + b0, qstatus + b0)))
       return s;
   }
+  return PGB_OK;
+}
+
+pgb_status pgb_host_alloc(size_t bytes, void **ptr) {
+  if (!ptr) { set_error("host_alloc: null pointer"); return PGB_ERR_ARG; }
+  *ptr = nullptr;
+  PGB_CUDA(cudaHostAlloc(ptr, std::max<size_t>(bytes, 1), cudaHostAllocPortable));
+  return PGB_OK;
+}
+
+pgb_status pgb_host_free(void *ptr) {
+  if (ptr) PGB_CUDA(cudaFreeHost(ptr));
   return PGB_OK;
 }
 

@@ -97,7 +97,9 @@ def load(build_if_missing=True):
     L.pgb_prefs_default.argtypes = [C.POINTER(Prefs)]
     L.pgb_prefs_default.restype = None
     L.pgb_place.argtypes = [vp, C.POINTER(Prefs), i, C.c_char_p, vp, vp, vp]
-    L.pgb_place_batch.argtypes = [vp, C.POINTER(Prefs), i, C.c_char_p, i, vp, vp, vp]
+    L.pgb_place_batch.argtypes = [vp, C.POINTER(Prefs), i, vp, i, vp, vp, vp]
+    L.pgb_host_alloc.argtypes = [C.c_size_t, C.POINTER(C.c_void_p)]
+    L.pgb_host_free.argtypes = [vp]
     L.pgb_queries_load.argtypes = [vp, i, C.c_char_p]
     L.pgb_queries_run.argtypes = [vp, C.POINTER(Prefs)]
     L.pgb_queries_fetch.argtypes = [vp, vp, vp, vp]
@@ -112,7 +114,7 @@ def load(build_if_missing=True):
                  "pgb_engine_set_glvs",
                  "pgb_engine_get_glv", "pgb_place", "pgb_place_batch", "pgb_queries_load", "pgb_queries_run", "pgb_queries_fetch",
                  "pgb_queries_stage1", "pgb_queries_rank", "pgb_queries_trials", "pgb_engine_timings", "pgb_engine_autotune",
-                 "pgb_engine_get_tuning", "pgb_engine_set_tuning"]:
+                 "pgb_engine_get_tuning", "pgb_engine_set_tuning", "pgb_host_alloc", "pgb_host_free"]:
         getattr(L, name).restype = i
     _lib = L
     return L
@@ -134,3 +136,35 @@ def header_symbols():
     hdr = os.path.join(os.path.dirname(HERE), "include", "pplacer_gb300.h")
     text = re.sub(r"/\*.*?\*/", "", open(hdr).read(), flags=re.S)
     return sorted(set(re.findall(r"\b(pgb_[a-z0-9_]+)\s*\(", text)))
+
+
+class HostBuffer:
+    """Page-locked host memory from pgb_host_alloc, freed on close / deletion."""
+
+    def __init__(self, nbytes):
+        self.ptr = C.c_void_p()
+        self.nbytes = int(nbytes)
+        check(load().pgb_host_alloc(self.nbytes, C.byref(self.ptr)), "pgb_host_alloc")
+
+    @property
+    def address(self):
+        return self.ptr.value
+
+    def array(self, dtype, count):
+        """A numpy view of the first count elements of dtype."""
+        import numpy as np
+        dt = np.dtype(dtype)
+        assert count * dt.itemsize <= self.nbytes
+        buf = (C.c_char * (count * dt.itemsize)).from_address(self.ptr.value)
+        return np.frombuffer(buf, dtype=dt, count=count)
+
+    def close(self):
+        if self.ptr and self.ptr.value:
+            load().pgb_host_free(self.ptr)
+            self.ptr = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -458,6 +458,36 @@ def test_place_host_batches(small, monkeypatch):
                 assert a[1] == b[1] and a[3] == b[3] and a[4] == b[4]
 
 
+def test_place_batch_from_page_locked_buffers(small):
+    """pgb_place_batch with the query rows and the results in page-locked
+    host memory from pgb_host_alloc: the same placements as load/run/fetch."""
+    import ctypes as C
+    from pplacer_gb300 import engine as E
+    from pplacer_gb300 import lib as L
+    w, oref, eng = small
+    qs = w.query_seqs[:20]
+    prefs = E.default_prefs()
+    want, wst = eng.place(qs, prefs)
+    Q, S, kam = len(qs), len(qs[0]), prefs.keep_at_most
+    hin = L.HostBuffer(Q * S)
+    hin.array(np.uint8, Q * S)[:] = np.frombuffer("".join(qs).encode(), dtype=np.uint8)
+    psz = C.sizeof(L.Placement)
+    hout = L.HostBuffer(Q * kam * psz + 8 * Q)
+    L.check(L.load().pgb_place_batch(eng.h, C.byref(prefs), Q, hin.address, 6, hout.address,
+                                     hout.address + Q * kam * psz, hout.address + Q * kam * psz + 4 * Q),
+            "pgb_place_batch")
+    out = (L.Placement * (Q * kam)).from_address(hout.address)
+    tail = hout.array(np.int32, (Q * kam * psz) // 4 + 2 * Q)
+    n_out, qst = tail[-2 * Q:-Q], tail[-Q:]
+    assert list(qst) == list(wst)
+    for q in range(Q):
+        got = [(out[q * kam + i].edge, out[q * kam + i].like, out[q * kam + i].dist, out[q * kam + i].pend)
+               for i in range(n_out[q])]
+        assert got == [(r[0], r[1], r[3], r[4]) for r in want[q]]
+    hin.close()
+    hout.close()
+
+
 def test_dropin_flow_vs_oracle(oracle_lib):
     """pplacer's per-query flow over the plain per-call drop-in (the measured
     Brent arm of the benchmark, dropin_flow.place_query): the same placements
