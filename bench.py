@@ -348,7 +348,17 @@ def run_ours(args):
             pms += ms[5]
             pev += cnt[2]
         pp = {"value": Q * args.pp_steps / (pms / 1e3), "unit": "placements/s",
-              "evals_per_step": pev / args.pp_steps, "steps": args.pp_steps}
+              "evals_per_step": pev / args.pp_steps, "steps": args.pp_steps,
+              "quadrature": "Gauss-Legendre panels around the optimum (pp_rule 0)"}
+        # the reference's own computation of the marginal likelihood (pp_rule
+        # 1: find_upper_limit's Brent search, nested QNG to pp_rel_err, ETOL
+        # retries), on the CTA kernels that carry it
+        qprefs = E.default_prefs(optimizer=1, calc_pp=1, pp_rule=1, **w.prefs)
+        eng.run(qprefs)
+        eng.run(qprefs)
+        ms, cnt = eng.timings()
+        pp["reference_qng"] = {"value": Q / (ms[5] / 1e3), "unit": "placements/s", "evals_per_step": cnt[2],
+                               "steps": 1}
     # ---- end to end through pgb_place_batch: the query rows in, the
     # placements out, both in page-locked host memory (pgb_host_alloc) ----
     kam = prefs.keep_at_most

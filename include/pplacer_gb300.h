@@ -223,8 +223,15 @@ typedef struct {
   int prior;                 /* [0] pendant prior: 0 exponential with mean = tree length / edges,
                                 1 uniform (--unif-prior), 2 informative exponential
                                 (--inform-prior, core.ml:34-51) */
-  double pp_rel_err;         /* [0.01] accepted; the quadrature is fixed (see marginal_like) */
+  double pp_rel_err;         /* [0.01] relative error of the QNG integrals (pp_rule 1) */
   double prior_lower;        /* [0.0] added to the informative prior's means (--prior-lower) */
+  int pp_rule;               /* [0] the marginal likelihood's quadrature: 0 Gauss-Legendre
+                                panels around the optimum (accurate to ~1e-3 in log units);
+                                1 the reference's own computation, Three_tax.calc_marg_prob
+                                (three_tax.ml:124-215): find_upper_limit's Brent search,
+                                nested QNG (Gsl.Integration.qng) to pp_rel_err, and on
+                                ETOL the upper limit halved and the integral retried, at
+                                most 10 times */
 } pgb_prefs;
 
 void pgb_prefs_default(pgb_prefs *p);

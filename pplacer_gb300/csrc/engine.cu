@@ -24,6 +24,7 @@
 #include <cuda_bf16.h>
 
 #include "pgb_common.cuh"
+#include "qng_rules.h"
 #include "stage1_tc.cuh"
 #include "tc.cuh"
 
@@ -1048,7 +1049,7 @@ struct TcTeam {
 
 // The CTA of the CUDA-core trial kernel as a team (CAT models and the
 // other CTA-tuned cases).
-template <int K, int T>
+template <int K, int T, bool QNG = false>
 struct CtaTeam {
   const TrialCtx &c;
   const TrialSmem &sm;
@@ -1060,16 +1061,16 @@ struct CtaTeam {
     __syncthreads();
     return *sm.redi;
   }
-  __device__ TrialRes trial(const TrialIn &t) { return trial_cta<K, T>(c, sm, t); }
+  __device__ TrialRes trial(const TrialIn &t) { return trial_cta<K, T, QNG>(c, sm, t); }
   __device__ bool aborted() const { return false; }
 };
 
-template <int K, int T>
+template <int K, int T, bool QNG = false>
 __global__ void __launch_bounds__(T, 1) k_place_cta(TrialCtx c, PlaceCtx p) {
   extern __shared__ __align__(16) char t_smem[];
   const TrialSmem sm = carve(t_smem, c.cap, c.smem_win, c.RP, K, c.NM, c.ncode);
   trial_cta_setup<K, T>(c, sm);
-  CtaTeam<K, T> tm{c, sm};
+  CtaTeam<K, T, QNG> tm{c, sm};
   place_queries(tm, c, p);
 }
 
@@ -1483,6 +1484,8 @@ TrialCtx trial_ctx(pgb_engine *e, const pgb_prefs *p, int optimizer, int mode) {
   c.mode = mode;
   c.stats = e->d_stats;
   c.gl = e->d_gl;
+  c.pp_rule = (p->calc_pp || mode == 2) ? p->pp_rule : 0;  // only marginal likelihoods use it
+  c.pp_rel_err = p->pp_rel_err;
   return c;
 }
 
@@ -1496,15 +1499,15 @@ void bin_limits(const pgb_engine *e, int *lim) {
   }
 }
 
-template <int K, int T>
+template <int K, int T, bool QNG = false>
 pgb_status launch_trials_kt(pgb_engine *e, cudaStream_t st, TrialCtx c, const int *d_order, int n, int cap, bool win,
                             TrialRes *out) {
   c.smem_win = win ? 1 : 0;
   c.cap = cap;
   size_t smem = trial_smem_bytes(cap, c.smem_win, e->RP, K, e->NM, e->ncode);
   if (smem > e->smem_optin) { set_error("trial shared memory %zu exceeds %zu", smem, e->smem_optin); return PGB_ERR_ARG; }
-  PGB_CUDA(cudaFuncSetAttribute(k_trials<K, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  k_trials<K, T><<<n, T, smem, st>>>(c, e->d_trials, d_order, n, out);
+  PGB_CUDA(cudaFuncSetAttribute(k_trials<K, T, QNG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  k_trials<K, T, QNG><<<n, T, smem, st>>>(c, e->d_trials, d_order, n, out);
   PGB_LAUNCH_CHECK();
   return PGB_OK;
 }
@@ -1630,6 +1633,15 @@ pgb_status check_tc_err(pgb_engine *e) {
 pgb_status launch_trials(pgb_engine *e, cudaStream_t st, TrialCtx c, const int *d_order, int n, int cap, bool win,
                          TrialRes *out, int threads) {
   if (n <= 0) return PGB_OK;
+  if (c.pp_rule == 1) {  // the reference's marginal likelihood: only the CTA kernels built with it carry it
+    if (threads != 128) threads = 256;
+    if (threads == 256 && trial_smem_bytes(cap, win, e->RP, e->K, e->NM, e->ncode) > e->smem_optin) win = false;
+    if (e->K == 4)
+      return threads == 128 ? launch_trials_kt<4, 128, true>(e, st, c, d_order, n, cap, win, out)
+                            : launch_trials_kt<4, 256, true>(e, st, c, d_order, n, cap, win, out);
+    return threads == 128 ? launch_trials_kt<20, 128, true>(e, st, c, d_order, n, cap, win, out)
+                          : launch_trials_kt<20, 256, true>(e, st, c, d_order, n, cap, win, out);
+  }
   if (threads == kTuneTc) {
     if (tc_trials_ok(e)) return launch_trials_tc(e, st, c, d_order, n, cap, out);
     threads = 256;
@@ -1666,7 +1678,7 @@ void bin_shape(const pgb_engine *e, int b, int max_sq, int allow_win, int *cap, 
 // Launch every non-empty bin of the trial lists, concurrently (one stream
 // each, longest windows first), and join them on the engine stream.
 pgb_status run_bins(pgb_engine *e, TrialCtx c, const int *h_bin_count, int max_sq) {
-  bool all_warp = warp_form_ok(e);
+  bool all_warp = warp_form_ok(e) && c.pp_rule != 1;  // the QNG replica runs on the CTA kernels
   for (int b = 0; b < kBins; b++)
     if (h_bin_count[b] > 0 && e->tune_threads[b] != 32) all_warp = false;
   if (all_warp) {  // one launch over every bin, longest bin first
@@ -1821,7 +1833,7 @@ pgb_status launch_place_tc(pgb_engine *e, TrialCtx c, const PlaceCtx &pc, int ma
   return PGB_OK;
 }
 
-template <int K, int T>
+template <int K, int T, bool QNG = false>
 pgb_status launch_place_cta_kt(pgb_engine *e, TrialCtx c, const PlaceCtx &pc, int max_sq, int win) {
   int cap = std::max(max_sq, 1);
   size_t smem = trial_smem_bytes(cap, win, e->RP, K, e->NM, e->ncode);
@@ -1832,11 +1844,11 @@ pgb_status launch_place_cta_kt(pgb_engine *e, TrialCtx c, const PlaceCtx &pc, in
   if (smem > e->smem_optin) { set_error("trial shared memory %zu exceeds %zu", smem, e->smem_optin); return PGB_ERR_ARG; }
   c.cap = cap;
   c.smem_win = win;
-  PGB_CUDA(cudaFuncSetAttribute(k_place_cta<K, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  PGB_CUDA(cudaFuncSetAttribute(k_place_cta<K, T, QNG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int per_sm = 0;
-  PGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_place_cta<K, T>, T, smem));
+  PGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_place_cta<K, T, QNG>, T, smem));
   int grid = std::max(1, std::min(e->Q, e->n_sm * std::max(1, per_sm)));
-  k_place_cta<K, T><<<grid, T, smem, e->st>>>(c, pc);
+  k_place_cta<K, T, QNG><<<grid, T, smem, e->st>>>(c, pc);
   PGB_LAUNCH_CHECK();
   return PGB_OK;
 }
@@ -1844,6 +1856,13 @@ pgb_status launch_place_cta_kt(pgb_engine *e, TrialCtx c, const PlaceCtx &pc, in
 // the CTA form of whole queries, with the bins' common tuning
 pgb_status launch_place_cta(pgb_engine *e, TrialCtx c, const PlaceCtx &pc, int max_sq) {
   const int T = e->tune_threads[0], win = e->tune_win[0];
+  if (c.pp_rule == 1) {  // the reference's marginal likelihood: the CTA kernels built with it
+    if (e->K == 4)
+      return T == 128 ? launch_place_cta_kt<4, 128, true>(e, c, pc, max_sq, win)
+                      : launch_place_cta_kt<4, 256, true>(e, c, pc, max_sq, T == 256 ? win : 0);
+    return T == 128 ? launch_place_cta_kt<20, 128, true>(e, c, pc, max_sq, win)
+                    : launch_place_cta_kt<20, 256, true>(e, c, pc, max_sq, T == 256 ? win : 0);
+  }
   if (e->K == 4)
     return T == 128 ? launch_place_cta_kt<4, 128>(e, c, pc, max_sq, win)
                     : launch_place_cta_kt<4, 256>(e, c, pc, max_sq, win);
@@ -1884,7 +1903,8 @@ pgb_status run_whole_queries(pgb_engine *e, const pgb_prefs *p, const BBCtx &c, 
   pc.prior_kind = p->prior == 1 ? 0 : 1;
   if ((s = ensure_prior_means(e, p->prior, p->prior_lower))) return s;
   pc.prior_mu = e->d_prior_mu;
-  if (e->tune_threads[0] == kTuneTc && tc_trials_ok(e)) s = launch_place_tc(e, tc, pc, max_sq);
+  if (tc.pp_rule == 1) s = launch_place_cta(e, tc, pc, max_sq);  // the CTA kernels carry the QNG replica
+  else if (e->tune_threads[0] == kTuneTc && tc_trials_ok(e)) s = launch_place_tc(e, tc, pc, max_sq);
   else if (e->tune_threads[0] != 32 || !warp_form_ok(e)) s = launch_place_cta(e, tc, pc, max_sq);
   else if (e->gcat) s = launch_place_warp_rp<1, true>(e, tc, pc);
   else
@@ -1935,6 +1955,7 @@ void pgb_prefs_default(pgb_prefs *p) {
   p->prior = 0;
   p->pp_rel_err = 0.01;
   p->prior_lower = 0.0;
+  p->pp_rule = 0;
 }
 
 static pgb_status prep_queries(pgb_engine *e);
@@ -2462,9 +2483,11 @@ static pgb_status check_prefs(const pgb_prefs *p) {
   if (!p || p->keep_at_most < 1 || p->keep_at_most > 64 || p->max_pitches < 0 || p->max_strikes < 0 ||
       !(p->max_pend > 1e-8) || !(p->start_pend > 0) || !(p->initial_tolerance > 0) || p->optimizer < 0 ||
       p->optimizer > 1 || p->calc_pp < 0 || p->calc_pp > 1 || p->prior < 0 || p->prior > 2 ||
-      !(p->pp_rel_err > 0) || !(p->prior_lower >= 0)) {
+      !(p->pp_rel_err > 0) || !(p->prior_lower >= 0) || p->pp_rule < 0 || p->pp_rule > 1 ||
+      (p->pp_rule == 1 && !(p->pp_rel_err >= 50 * 2.220446049250313e-16))) {
     set_error("invalid prefs (keep_at_most 1..64, max_pend > 1e-8, tolerances > 0, optimizer 0|1, calc_pp 0|1, "
-              "prior 0|1|2, pp_rel_err > 0, prior_lower >= 0)");
+              "prior 0|1|2, pp_rel_err > 0 and with pp_rule 1 at least 50 DBL_EPSILON (GSL_EBADTOL), "
+              "prior_lower >= 0, pp_rule 0|1)");
     return PGB_ERR_ARG;
   }
   return PGB_OK;

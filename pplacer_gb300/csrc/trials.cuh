@@ -66,6 +66,8 @@ struct TrialCtx {
   int smem_win, cap;
   unsigned long long *stats;  // [0] objective evaluations, [1] site evaluations
   const double *gl;           // Gauss-Legendre rule on [-1, 1]: kGlPoints nodes, then weights
+  int pp_rule;                // marginal likelihood: 0 Gauss-Legendre panels, 1 the reference's nested QNG
+  double pp_rel_err;          // the QNG's relative error (pp_rel_err, prefs.ml)
 };
 
 constexpr int kGlPoints = 12;  // nodes per panel of the marginal-likelihood quadrature
@@ -152,6 +154,99 @@ __device__ inline TrialSmem carve(char *base, int cap, int win, int RP, int K, i
     case label:;         \
   } while (0)
 
+// One QNG integral of the reference's posterior-probability integral
+// (Gsl.Integration.qng, pplacer_src/integration.ml:27-31; QUADPACK's
+// non-adaptive 21/43/87-point Gauss-Kronrod-Patterson scheme) fed one
+// function value at a time, in the order QNG evaluates them: point j of
+// [a, b] is node(j, a, b); accept(j, f) returns 0 for the next point, 1 when
+// a stage met the tolerance (result), 2 when the 87-point stage failed
+// (GSL_ETOL).  buf holds the 20 values of the 21-point stage, then the pair
+// sums f(c + h x) + f(c - h x) the later stages reuse.
+struct QngAcc {
+  double fc, res10, res21, res43, res87, resabs, resasc, first, result;
+  float buf[21];
+
+  __device__ static double node(int j, double a, double b) {
+    const double c = 0.5 * (a + b), h = 0.5 * (b - a);
+    if (j == 0) return c;
+    double x;
+    int i;
+    if (j <= 10) { i = j - 1; x = pgb::qng::x1[i >> 1]; }
+    else if (j <= 20) { i = j - 11; x = pgb::qng::x2[i >> 1]; }
+    else if (j <= 42) { i = j - 21; x = pgb::qng::x3[i >> 1]; }
+    else { i = j - 43; x = pgb::qng::x4[i >> 1]; }
+    return (i & 1) ? c - h * x : c + h * x;
+  }
+  // rescale_error of QUADPACK: the stage difference scaled by the
+  // integrand's variation, at least 50 eps |integral|
+  __device__ static double rescale(double err, double rabs, double rasc) {
+    err = fabs(err);
+    if (rasc != 0.0 && err != 0.0) {
+      const double scale = pow(200.0 * err / rasc, 1.5);
+      err = scale < 1.0 ? rasc * scale : rasc;
+    }
+    if (rabs > 2.2250738585072014e-308 / (50.0 * 2.220446049250313e-16)) {
+      const double min_err = 50.0 * 2.220446049250313e-16 * rabs;
+      if (min_err > err) err = min_err;
+    }
+    return err;
+  }
+  __device__ int accept(int j, double f, double half, double epsrel) {
+    namespace Q = pgb::qng;
+    if (j == 0) { fc = f; return 0; }
+    if (j <= 20) {
+      buf[j - 1] = (float)f;
+      if (j < 20) return 0;
+      res10 = 0.0;
+      res21 = Q::w21b[5] * fc;
+      resabs = Q::w21b[5] * fabs(fc);
+      for (int k = 0; k < 5; k++) {
+        const double a1 = buf[2 * k], a2 = buf[2 * k + 1], s = a1 + a2;
+        res10 += Q::w10[k] * s;
+        res21 += Q::w21a[k] * s;
+        resabs += Q::w21a[k] * (fabs(a1) + fabs(a2));
+      }
+      for (int k = 0; k < 5; k++) {
+        const double a1 = buf[10 + 2 * k], a2 = buf[11 + 2 * k];
+        res21 += Q::w21b[k] * (a1 + a2);
+        resabs += Q::w21b[k] * (fabs(a1) + fabs(a2));
+      }
+      resabs *= fabs(half);
+      const double mean = 0.5 * res21;
+      resasc = Q::w21b[5] * fabs(fc - mean);
+      for (int k = 0; k < 5; k++)
+        resasc += Q::w21a[k] * (fabs(buf[2 * k] - mean) + fabs(buf[2 * k + 1] - mean)) +
+                  Q::w21b[k] * (fabs(buf[10 + 2 * k] - mean) + fabs(buf[11 + 2 * k] - mean));
+      resasc *= fabs(half);
+      for (int k = 0; k < 10; k++) buf[k] = buf[2 * k] + buf[2 * k + 1];  // pair sums, in place
+      result = res21 * half;
+      if (rescale((res21 - res10) * half, resabs, resasc) < epsrel * fabs(result)) return 1;
+      res43 = Q::w43b[11] * fc;
+      for (int k = 0; k < 10; k++) res43 += buf[k] * Q::w43a[k];
+      return 0;
+    }
+    if (j <= 42) {
+      const int i = j - 21;
+      if (!(i & 1)) { first = f; return 0; }
+      const double s = first + f;
+      res43 += s * Q::w43b[i >> 1];
+      buf[10 + (i >> 1)] = (float)s;
+      if (j < 42) return 0;
+      result = res43 * half;
+      if (rescale((res43 - res21) * half, resabs, resasc) < epsrel * fabs(result)) return 1;
+      res87 = Q::w87b[22] * fc;
+      for (int k = 0; k < 21; k++) res87 += buf[k] * Q::w87a[k];
+      return 0;
+    }
+    const int i = j - 43;
+    if (!(i & 1)) { first = f; return 0; }
+    res87 += Q::w87b[i >> 1] * (first + f);
+    if (j < 86) return 0;
+    result = res87 * half;
+    return rescale((res87 - res43) * half, resabs, resasc) < epsrel * fabs(result) ? 1 : 2;
+  }
+};
+
 struct Optimiser {
   // inputs
   int optimizer, mode;
@@ -165,7 +260,7 @@ struct Optimiser {
   float req_p, req_d, req_x;
   bool req_derivs;
   // coroutine
-  int pc;
+  int pc, qpc;  // next()'s and marg_qng()'s resume points
   int attempt;
   // Brent replica state
   int outer, which, iter, bstep, err;
@@ -177,9 +272,22 @@ struct Optimiser {
   int prior_kind;
   double prior_mu;
   const double *gl;
-  double base, tgt, lo_b, hi_b, stp, sig_p, sig_d, acc_in, acc_out, qp, qd, wd;
-  double ppan[3], dpan[3];
-  int k_srch, n_ppan, n_dpan, ipan, jpan, ip, jd;
+  int pp_rule;    // 0: Gauss-Legendre panels; 1: the reference's nested QNG (to pp_rel)
+  double pp_rel;
+  double base, tgt, lo_b, hi_b, stp, sig_p, sig_d, qp, qd;
+  int k_srch;
+  union {
+    struct {  // Gauss-Legendre panels
+      double acc_in, acc_out, wd;
+      double ppan[3], dpan[3];
+      int n_ppan, n_dpan, ipan, jpan, ip, jd;
+    };
+    struct {  // nested QNG: inner (pendant) and outer (distal) integrals
+      QngAcc qi, qo;
+      double qU;
+      int ij, oj, n_exc, qerr;
+    };
+  };
   // Newton state
   bool seeded;
   EvalOut seed;
@@ -202,6 +310,59 @@ struct Optimiser {
   // Gsl.Randist.exponential_pdf with mean mu
   __device__ double log_prior(double pnd) const { return prior_kind == 0 ? 0.0 : -log(prior_mu) - pnd / prior_mu; }
   __device__ double value_of(const EvalOut &o, double pnd) const { return full(o) + log_prior(pnd); }
+
+  // find_upper_limit's objective at pendant x from the last evaluation:
+  // |target - (L + log prior)|, an infinite value as 1e5 (three_tax.ml:142-148)
+  __device__ double qng_objective(double x) const {
+    const double y = fabs(tgt - value_of(last, x));
+    return isinf(y) ? 100000.0 : y;
+  }
+  // One iteration of GSL's Brent minimiser on the state (xl, xu, xm, fm, v,
+  // fv, w, fw, bd, be): the next probe u (a parabolic step, else golden
+  // section).
+  __device__ void gsl_brent_step() {
+    z = xm;
+    fz = fm;
+    double dd = be, ee = bd;
+    const double wl = z - xl, wu = xu - z;
+    const double tolerance = 1.4901161193847656e-08 * fabs(z);
+    double pp = 0, qq = 0, r = 0;
+    const double mid = 0.5 * (xl + xu);
+    if (fabs(ee) > tolerance) {
+      r = (z - w) * (fz - fv);
+      qq = (z - v) * (fz - fw);
+      pp = (z - v) * qq - (z - w) * r;
+      qq = 2 * (qq - r);
+      if (qq > 0) pp = -pp; else qq = -qq;
+      r = ee;
+      ee = dd;
+    }
+    if (fabs(pp) < fabs(0.5 * qq * r) && pp < qq * wl && pp < qq * wu) {
+      const double t2 = 2 * tolerance;
+      dd = pp / qq;
+      u = z + dd;
+      if ((u - xl) < t2 || (xu - u) < t2) dd = (z < mid) ? tolerance : -tolerance;
+    } else {
+      ee = (z < mid) ? xu - z : -(z - xl);
+      dd = 0.3819660 * ee;
+    }
+    if (fabs(dd) >= tolerance) u = z + dd;
+    else u = z + ((dd > 0) ? tolerance : -tolerance);
+    be = ee;
+    bd = dd;
+  }
+  // The bracket and the (v, w, x) points after the value fval at u.
+  __device__ void gsl_brent_update() {
+    if (fval <= fz) {
+      if (u < z) { xu = z; fu = fz; } else { xl = z; fl = fz; }
+      v = w; fv = fw; w = z; fw = fz;
+      xm = u; fm = fval;
+    } else {
+      if (u < z) { xl = u; fl = fval; } else { xu = u; fu = fval; }
+      if (fval <= fw || w == z) { v = w; fv = fw; w = u; fw = fval; }
+      else if (fval <= fv || v == z || v == w) { v = u; fv = fval; }
+    }
+  }
 
   __device__ void request(double pp, double dd, double xx, bool derivs) {
     req_p = (float)pp;
@@ -229,6 +390,124 @@ struct Optimiser {
     n_evals++;
   }
 
+  // The marginal likelihood as the reference computes it (pp_rule 1),
+  // resumed after each evaluation like next(); only the kernels
+  // instantiated with next<true>() contain it, so it adds nothing to the
+  // trial kernels' site loops:
+  // Three_tax.calc_marg_prob (three_tax.ml:169-215): the upper pendant
+  // limit of find_upper_limit (three_tax.ml:124-159: Minimization.brent
+  // with 10 iterations at tolerance 0.02 on |target - L - log prior|,
+  // minimization.ml:24-41,83-101), then nested QNG to pp_rel -- the
+  // distal integral over [0, cut] of the pendant integral over
+  // [0, U] -- and on GSL_ETOL from either, U halved and the whole
+  // integral retried, at most 10 times, after which the base
+  // likelihood is the result.  A start-finder or iteration-limit
+  // exception of the upper-limit search, or a non-finite objective (GSL's
+  // EBADFUNC) -- which the reference does not catch there -- integrates to
+  // max_pend, as its EINVAL does.
+#define QNG_YIELD(label) \
+  do {                   \
+    qpc = label;         \
+    return true;         \
+    case label:;         \
+  } while (0)
+  __device__ __forceinline__ bool marg_qng() {
+    switch (qpc) {
+      case 0:
+        qerr = 0;
+        if (prior_kind == 1 && exp(log_prior(p)) == 0.0) {  // a zero prior: rewind (three_tax.ml:127-133)
+          qU = p;
+          for (k_srch = 0; k_srch < 1100 && !(exp(log_prior(qU * 0.5)) > exp(-10.0)); k_srch++) qU *= 0.5;
+          goto QNG_RUN;
+        }
+        tgt = value_of(cur, p) - 10.0;
+        left = p;
+        right = max_pend;
+        raw = p + (max_pend - p) / 2.0;
+        if (left >= raw || raw >= right) { qerr = 1; qU = max_pend; goto QNG_RUN; }
+        request(right, d, (float)cut - d, false);
+        QNG_YIELD(40);
+        righty = qng_objective(right);
+        request(left, d, (float)cut - d, false);
+        QNG_YIELD(41);
+        lefty = qng_objective(left);
+        smaller = lefty < righty ? left : right;
+        miny = lefty <= righty ? lefty : righty;
+        prevx = raw;
+        for (iter = 1;; iter++) {
+          request(prevx, d, (float)cut - d, false);
+          QNG_YIELD(42);
+          pv = qng_objective(prevx);
+          if (pv < miny) break;
+          if (fabs(prevx - smaller) < 0.02) { qU = smaller; goto QNG_RUN; }  // FoundMin
+          if (iter > 10) { qerr = 2; qU = max_pend; goto QNG_RUN; }          // FindStartFailure
+          prevx = 0.5 * (prevx + smaller);
+        }
+        xl = left; xu = right; xm = prevx;
+        fl = lefty; fu = righty; fm = pv;
+        if (!isfinite(fl) || !isfinite(fu) || !isfinite(fm)) { qerr = 5; qU = max_pend; goto QNG_RUN; }  // EBADFUNC
+        if (!(fm < fl && fm < fu)) { qerr = 3; qU = max_pend; goto QNG_RUN; }  // GSL_EINVAL
+        v = xl + 0.3819660 * (xu - xl);
+        w = v;
+        request(v, d, (float)cut - d, false);
+        QNG_YIELD(43);
+        fv = qng_objective(v);
+        if (!isfinite(fv)) { qerr = 5; qU = max_pend; goto QNG_RUN; }
+        fw = fv;
+        bd = 0;
+        be = 0;
+        for (bstep = 1;; bstep++) {
+          if (bstep > 10) { qerr = 4; qU = max_pend; goto QNG_RUN; }  // ExceededMaxIter
+          gsl_brent_step();
+          request(u, d, (float)cut - d, false);
+          QNG_YIELD(44);
+          fval = qng_objective(u);
+          if (!isfinite(fval)) { qerr = 5; qU = max_pend; goto QNG_RUN; }
+          gsl_brent_update();
+          if (xu - xl < 0.02) { qU = xm; break; }
+        }
+      QNG_RUN:
+        n_exc = 0;
+      QNG_PERFORM:
+        if (n_exc >= 10) {  // "integration did not converge after changing bounds 10 times"
+          L_last = base;
+          goto QNG_END;
+        }
+        oj = 0;
+      QNG_OUTER:
+        qd = fabs(cut) < 1e-5 ? 0.5 * cut : QngAcc::node(oj, 0.0, cut);
+        ij = 0;
+      QNG_INNER:
+        qp = QngAcc::node(ij, 0.0, qU);
+        request(qp, qd, cut - qd, false);
+        QNG_YIELD(45);
+        k_srch = qi.accept(ij, exp(full(last) - base + log_prior(qp)), 0.5 * qU, pp_rel);
+        ij++;
+        if (k_srch == 0) goto QNG_INNER;
+        if (k_srch == 2) { n_exc++; qU *= 0.5; goto QNG_PERFORM; }
+        if (fabs(cut) < 1e-5) {  // cut_bl =~ 0 (ppatteries.ml:96-97): the pendant integral alone
+          L_last = base + log(qi.result);
+          goto QNG_END;
+        }
+        k_srch = qo.accept(oj, qi.result, 0.5 * cut, pp_rel);
+        oj++;
+        if (k_srch == 0) goto QNG_OUTER;
+        if (k_srch == 2) { n_exc++; qU *= 0.5; goto QNG_PERFORM; }
+        L_last = base + log(qo.result / cut);
+      QNG_END:
+        status = isfinite(L_last) ? ST_OK : ST_FAILED;
+        pend = p;
+        dist = d;
+        prox = (double)((float)cut - d);
+        last = cur;
+        return false;
+    }
+    return false;
+  }
+#undef QNG_YIELD
+
+
+  template <bool QNG = false>
   __device__ __forceinline__ bool next(const EvalOut *res) {
     if (res) record(res);
     switch (pc) {
@@ -501,6 +780,11 @@ struct Optimiser {
         dist = d;
         prox = (double)((float)cut - d);
         if (!isfinite(base)) { status = ST_FAILED; L_last = base; return false; }
+        if (pp_rule == 1) {  // only kernels built with QNG carry that computation
+          if (!QNG) { status = ST_FAILED; L_last = NAN; return false; }
+          qpc = 0;
+          goto QNG_STEP;
+        }
         tgt = value_of(cur, p) - 10.0;
         {
           const double hpp = cur.h[0], hdd = cur.h[1], hpd = cur.h[2];
@@ -595,6 +879,13 @@ struct Optimiser {
         L_last = base + log(n_dpan ? acc_out / cut : acc_out);
         status = isfinite(L_last) ? ST_OK : ST_FAILED;
         last = cur;
+        return false;
+      case 46:  // the reference's computation (marg_qng), resumed after each evaluation
+      QNG_STEP:
+        if (QNG && marg_qng()) {
+          pc = 46;
+          return true;
+        }
         return false;
       default:
         return false;
@@ -895,7 +1186,7 @@ __device__ __forceinline__ void trial_cta_setup(const TrialCtx &c, const TrialSm
 
 // One trial by the CTA (after trial_cta_setup); every thread returns the
 // same result.
-template <int K, int T>
+template <int K, int T, bool QNG = false>
 __device__ TrialRes trial_cta(const TrialCtx &c, const TrialSmem &sm, const TrialIn &tr) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int q = tr.q, node = tr.node;
@@ -948,6 +1239,8 @@ __device__ TrialRes trial_cta(const TrialCtx &c, const TrialSmem &sm, const Tria
     opt.seed = tr.seed;
     if (tr.marginal) opt.mode = 2;
     opt.prior_kind = tr.prior_kind;
+    opt.pp_rule = c.pp_rule;
+    opt.pp_rel = c.pp_rel_err;
     opt.prior_mu = tr.prior_mu;
     opt.gl = c.gl;
     opt.pc = 0;
@@ -959,7 +1252,7 @@ __device__ TrialRes trial_cta(const TrialCtx &c, const TrialSmem &sm, const Tria
   for (int ev = 0; ev < kMaxTrialEvals; ev++) {
     // ---- warp 0: next point, exp factors ----
     if (warp == 0) {
-      bool more = opt.next(ev == 0 ? nullptr : &res);
+      bool more = opt.template next<QNG>(ev == 0 ? nullptr : &res);
       if (lane == 0) {
         sm.ctrl->cmd = more ? (opt.req_derivs ? 2 : 1) : 0;
         sm.ctrl->pend = opt.req_p;
@@ -1056,7 +1349,7 @@ __device__ TrialRes trial_cta(const TrialCtx &c, const TrialSmem &sm, const Tria
   return *sm.res;
 }
 
-template <int K, int T>
+template <int K, int T, bool QNG = false>
 __global__ void __launch_bounds__(T, 1) k_trials(TrialCtx c, const TrialIn *__restrict__ trials,
                                                  const int *__restrict__ order, int n, TrialRes *out) {
   extern __shared__ __align__(16) char t_smem[];
@@ -1064,6 +1357,6 @@ __global__ void __launch_bounds__(T, 1) k_trials(TrialCtx c, const TrialIn *__re
   const int ti = order ? order[blockIdx.x] : blockIdx.x;
   const TrialSmem sm = carve(t_smem, c.cap, c.smem_win, c.RP, K, c.NM, c.ncode);
   trial_cta_setup<K, T>(c, sm);
-  const TrialRes r = trial_cta<K, T>(c, sm, trials[ti]);
+  const TrialRes r = trial_cta<K, T, QNG>(c, sm, trials[ti]);
   if (threadIdx.x == 0) out[ti] = r;
 }

@@ -498,6 +498,8 @@ __device__ TrialRes tc_trial(const TrialCtx &c, const TcSmem &sm, uint32_t tmem,
     opt.seed = tr.seed;
     if (tr.marginal) opt.mode = 2;
     opt.prior_kind = tr.prior_kind;
+    opt.pp_rule = c.pp_rule;
+    opt.pp_rel = c.pp_rel_err;
     opt.prior_mu = tr.prior_mu;
     opt.gl = c.gl;
     opt.pc = 0;

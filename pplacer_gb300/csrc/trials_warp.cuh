@@ -581,6 +581,8 @@ __device__ TrialRes trial_warp(const TrialCtx &c, const TrialSmem &sm, float4 *r
     opt.seed = tr.seed;
     if (tr.marginal) opt.mode = 2;
     opt.prior_kind = tr.prior_kind;
+    opt.pp_rule = c.pp_rule;
+    opt.pp_rel = c.pp_rel_err;
     opt.prior_mu = tr.prior_mu;
     opt.gl = c.gl;
     opt.pc = 0;

@@ -106,10 +106,12 @@ def _gsl_brent(f, x_min, lower, upper, tol, max_iters):
     fv = fw = f(v)
     z, fz = x_min, f_min
     for _ in range(max_iters):
+        dd, ee = e, d  # GSL's iteration takes d and e with their roles swapped
         wl, wu = z - lower, upper - z
         tolerance = SQRT_DBL_EPS * abs(z)
         mid = 0.5 * (lower + upper)
-        if abs(e) > tolerance:
+        p = q = r = 0.0
+        if abs(ee) > tolerance:
             r = (z - w) * (fz - fv)
             q = (z - v) * (fz - fw)
             p = (z - v) * q - (z - w) * r
@@ -118,20 +120,18 @@ def _gsl_brent(f, x_min, lower, upper, tol, max_iters):
                 p = -p
             else:
                 q = -q
-            r, e = e, d
-            if abs(p) < abs(0.5 * q * r) and p < q * wl and p < q * wu:
-                t2 = 2.0 * tolerance
-                d = p / q
-                u = z + d
-                if (u - lower) < t2 or (upper - u) < t2:
-                    d = tolerance if z < mid else -tolerance
-            else:
-                e = (upper - z) if z < mid else -(z - lower)
-                d = GOLDEN * e
+            r, ee = ee, dd
+        if abs(p) < abs(0.5 * q * r) and p < q * wl and p < q * wu:
+            t2 = 2.0 * tolerance
+            dd = p / q
+            u = z + dd
+            if (u - lower) < t2 or (upper - u) < t2:
+                dd = tolerance if z < mid else -tolerance
         else:
-            e = (upper - z) if z < mid else -(z - lower)
-            d = GOLDEN * e
-        u = z + d if abs(d) >= tolerance else z + (tolerance if d > 0 else -tolerance)
+            ee = (upper - z) if z < mid else -(z - lower)
+            dd = GOLDEN * ee
+        u = z + dd if abs(dd) >= tolerance else z + (tolerance if dd > 0 else -tolerance)
+        e, d = ee, dd
         fu = f(u)
         if fu <= fz:
             if u < z:

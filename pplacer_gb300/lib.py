@@ -33,7 +33,8 @@ class Prefs(C.Structure):
     _fields_ = [("start_pend", C.c_double), ("max_pend", C.c_double), ("initial_tolerance", C.c_double),
                 ("max_strikes", C.c_int), ("strike_box", C.c_double), ("max_pitches", C.c_int),
                 ("keep_at_most", C.c_int), ("keep_factor", C.c_double), ("optimizer", C.c_int),
-                ("calc_pp", C.c_int), ("prior", C.c_int), ("pp_rel_err", C.c_double), ("prior_lower", C.c_double)]
+                ("calc_pp", C.c_int), ("prior", C.c_int), ("pp_rel_err", C.c_double), ("prior_lower", C.c_double),
+                ("pp_rule", C.c_int)]
 
 
 class Placement(C.Structure):

@@ -414,6 +414,120 @@ def test_marginal_trials_mode(oracle_lib):
         assert g["status"] == 0 and abs(g["like"] - ref_m) <= 2e-3, (q, e, g["like"], ref_m)
 
 
+def _qng_oracle_marginal(oref, seq, e, p, d, prior_kind, mu, rel, max_pend=2.0):
+    """The reference's calc_marg_prob (oracle/qng.py) on the oracle's FP64
+    likelihood; prior_kind as the engine's prefs.prior: 0 exponential
+    (mean mu), 1 uniform."""
+    import math
+    from oracle import qng as Q
+    cut = float(oref.bl[e])
+    L = lambda pp, dd: oref.loglike_derivs(seq, e, max(pp, 1e-12), min(max(dd, 0.0), cut))[1][0]
+    prior = (lambda x: 1.0) if prior_kind == 1 else (lambda x: math.exp(-x / mu) / mu)
+    return Q.calc_marg_prob(L, p, d, cut, prior, max_pend, rel)
+
+
+@pytest.mark.parametrize("prior", [0, 1])
+def test_marginal_qng_replica(oracle_lib, prior):
+    """pp_rule 1: the reference's own marginal likelihood (find_upper_limit's
+    Brent search, nested QNG to pp_rel_err, ETOL retries) in the trial
+    kernel, against the same computation in the oracle on the FP64
+    likelihood: within pp_rel_err in log units (the two may stop at
+    different QNG stages where the FP32 and FP64 integrands straddle a
+    stage's tolerance), and most within 1e-3."""
+    from pplacer_gb300 import engine as E
+    from pplacer_gb300 import synth
+    O = oracle_lib
+    w = synth.make_workload("cpu_small", n_queries=6, taxa=60, sites=400, lo=100, hi=300)
+    oref = O.Reference(O.Model(w.exch, w.statd, w.rates), w.parent, w.bl, w.leaf_row, w.ref_seqs)
+    eng = E.engine_for_workload(w)
+    eng.load_queries(w.query_seqs)
+    mu = O.prior_means(w.parent, w.bl, 0)
+    edges = np.where(w.parent >= 0)[0]
+    trials = []
+    for q, e in ((0, edges[5]), (1, edges[17]), (2, edges[29]), (3, edges[41]), (4, edges[53])):
+        like, p, d = O.polish(oref, w.query_seqs[q], int(e), 0.1, float(w.bl[e]) / 2)
+        trials.append((q, int(e), p, d, 0.01))
+    got = eng.trials(trials, optimizer=E.NEWTON, mode=2, prefs=E.default_prefs(prior=prior, pp_rule=1))
+    close = 0
+    for (q, e, p, d, _), g in zip(trials, got):
+        ref_m, info = _qng_oracle_marginal(oref, w.query_seqs[q], e, p, d, prior, mu[e], 0.01)
+        assert g["status"] == 0 and abs(g["like"] - ref_m) <= 0.0101, (q, e, g["like"], ref_m, info)
+        close += abs(g["like"] - ref_m) <= 1e-3
+    assert close >= len(trials) - 1
+
+
+def test_marginal_qng_retries_exhausted(oracle_lib):
+    """pp_rule 1 at the smallest relative error QNG accepts (just above 50
+    DBL_EPSILON): no stage meets it on the FP32-evaluated integrand, so every
+    attempt ends in ETOL, the upper limit halves ten times, and the result is
+    the base likelihood, the trial's own evaluation at the optimum
+    (three_tax.ml:177-183).  A converged integral (the oracle's, at 0.01)
+    lies well below it, so the two outcomes are told apart."""
+    from pplacer_gb300 import engine as E
+    from pplacer_gb300 import synth
+    O = oracle_lib
+    w = synth.make_workload("cpu_small", n_queries=3, taxa=60, sites=400, lo=100, hi=300)
+    oref = O.Reference(O.Model(w.exch, w.statd, w.rates), w.parent, w.bl, w.leaf_row, w.ref_seqs)
+    eng = E.engine_for_workload(w)
+    eng.load_queries(w.query_seqs)
+    edges = np.where(w.parent >= 0)[0]
+    trials = []
+    for q, e in ((0, edges[7]), (1, edges[19])):
+        like, p, d = O.polish(oref, w.query_seqs[q], int(e), 0.1, float(w.bl[e]) / 2)
+        trials.append((q, int(e), p, d, 0.01))
+    prefs = E.default_prefs(prior=1, pp_rule=1, pp_rel_err=1.2e-14)
+    got = eng.trials(trials, optimizer=E.NEWTON, mode=2, prefs=prefs)
+    at = eng.trials(trials, optimizer=E.NEWTON, mode=1, prefs=prefs)
+    for (q, e, p, d, _), g, a in zip(trials, got, at):
+        ref_m, info = _qng_oracle_marginal(oref, w.query_seqs[q], e, p, d, 1, None, 0.01)
+        assert g["status"] == 0 and abs(g["like"] - a["like"]) <= 1e-7 * abs(a["like"]), (g, a)
+        assert ref_m < a["like"] - 0.05, (ref_m, a["like"])
+
+
+def test_qng_tolerance_below_gsl_minimum_is_rejected():
+    """pp_rule 1 refuses a pp_rel_err below 50 DBL_EPSILON, where GSL's qng
+    returns GSL_EBADTOL."""
+    import ctypes as C
+    from pplacer_gb300 import engine as E
+    from pplacer_gb300 import lib as L
+    from pplacer_gb300 import synth
+    w = synth.make_workload("cpu_small", n_queries=2)
+    eng = E.engine_for_workload(w)
+    eng.load_queries(w.query_seqs)
+    prefs = E.default_prefs(pp_rule=1, pp_rel_err=1e-15, calc_pp=1)
+    assert L.load().pgb_queries_run(eng.h, C.byref(prefs)) == 1
+    assert b"pp_rel_err" in L.load().pgb_last_error()
+
+
+def test_place_pp_qng_replica(oracle_lib):
+    """Whole queries with calc_pp and pp_rule 1: each kept placement's
+    marginal likelihood against the oracle's calc_marg_prob at the GPU's
+    refined lengths, and post_prob their normalised ratios."""
+    import math
+    from pplacer_gb300 import engine as E
+    from pplacer_gb300 import synth
+    O = oracle_lib
+    w = synth.make_workload("cpu_small", n_queries=5, taxa=60, sites=400, lo=100, hi=300)
+    oref = O.Reference(O.Model(w.exch, w.statd, w.rates), w.parent, w.bl, w.leaf_row, w.ref_seqs)
+    eng = E.engine_for_workload(w)
+    mu = O.prior_means(w.parent, w.bl, 0)
+    res, st = eng.place(w.query_seqs, E.default_prefs(optimizer=1, calc_pp=1, prior=0, pp_rule=1))
+    n = 0
+    for q, rows in enumerate(res):
+        if not rows:
+            continue
+        for (e, like, lwr, dist, pend, pp, ml) in rows[:2]:
+            ref_m, info = _qng_oracle_marginal(oref, w.query_seqs[q], e, pend, dist, 0, mu[e], 0.01)
+            assert abs(ml - ref_m) <= 0.0101, (q, e, ml, ref_m, info)
+            n += 1
+        mls = [r[6] for r in rows]
+        top = max(mls)
+        tot = sum(math.exp(m - top) for m in mls)
+        for r in rows:
+            assert abs(r[5] - math.exp(r[6] - top) / tot) <= 1e-9
+    assert n >= 5
+
+
 def test_refine_categories(oracle_lib):
     """Gcat site-category refinement (gcat_model.ml:387-419) against the
     oracle, then placement with the refined categories."""
