@@ -1144,6 +1144,16 @@ struct pgb_engine {
   uint8_t *d_qc = nullptr;
   size_t qc_cap = 0;
   bool s1_attr = false;
+  // kernel launch shapes, set and queried once: the largest dynamic shared
+  // memory set per kernel, and resident CTAs per SM per (kernel, threads, bytes)
+  struct KernelSmem { const void *kern; size_t smem; };
+  struct KernelFit { const void *kern; int threads; size_t smem; int per_sm; };
+  std::vector<KernelSmem> k_smem;
+  std::vector<KernelFit> k_fit;
+  // page-locked status block a run copies back once: the trial counters and
+  // the tensor-core kernels' error records
+  struct RunStatus { unsigned long long stats[4]; int s1_err[4]; int tc_err[16]; };
+  RunStatus *h_run = nullptr;
   int *d_qamb = nullptr, *d_amb_list = nullptr;
   std::vector<int> h_qamb, h_amb;
   double lt_pend = -1;
@@ -1155,7 +1165,9 @@ struct pgb_engine {
   uint32_t *d_rcode = nullptr;  // (alignment column << 8) | code per informative site
   int *d_qlen = nullptr, *d_qstatus = nullptr;
   std::vector<int> h_qlen;
-  std::vector<int> h_qorder, h_len_at;  // the whole-query order (longest first) and its counting-sort bins
+  std::vector<int> h_len_at;  // counting-sort bins of the whole-query order (longest first)
+  int *h_qinfo = nullptr;       // page-locked [3][Q]: lengths, ambiguity counts, the query order
+  size_t h_qinfo_cap = 0;
   // run buffers
   double *d_scores = nullptr;  // FP64 stage-1 rows of queries with ambiguity characters (or all, on request)
   size_t scores_cap = 0;
@@ -1169,6 +1181,7 @@ struct pgb_engine {
   BBState *d_bb = nullptr;
   ResEntry *d_res = nullptr;
   size_t res_cap = 0;
+  size_t run_qcap = 0, run_kcap = 0;  // per-query run buffers (d_bb .. d_out) and the kept-placement slots
   int *d_tbase = nullptr, *d_tcount = nullptr, *d_keep_idx = nullptr, *d_keep_n = nullptr;
   TrialIn *d_trials = nullptr;
   TrialRes *d_tres = nullptr;
@@ -1195,6 +1208,39 @@ struct pgb_engine {
   double t_ms[6] = {0, 0, 0, 0, 0, 0};
   double counts[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 };
+
+namespace pgb {
+namespace {
+// A kernel's dynamic shared-memory limit, raised (never lowered) to smem
+// once per engine, so a placement run's launches make no attribute calls.
+pgb_status kernel_smem(pgb_engine *e, const void *kern, size_t smem) {
+  for (auto &k : e->k_smem)
+    if (k.kern == kern) {
+      if (k.smem >= smem) return PGB_OK;
+      PGB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      k.smem = smem;
+      return PGB_OK;
+    }
+  PGB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  e->k_smem.push_back({kern, smem});
+  return PGB_OK;
+}
+
+// kernel_smem plus the resident CTAs per SM at that launch shape (cached).
+pgb_status kernel_fit(pgb_engine *e, const void *kern, int threads, size_t smem, int *per_sm) {
+  pgb_status s;
+  if ((s = kernel_smem(e, kern, smem))) return s;
+  for (const auto &f : e->k_fit)
+    if (f.kern == kern && f.threads == threads && f.smem == smem) { *per_sm = f.per_sm; return PGB_OK; }
+  int n = 0;
+  PGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, threads, smem));
+  e->k_fit.push_back({kern, threads, smem, n});
+  *per_sm = n;
+  return PGB_OK;
+}
+
+}  // namespace
+}  // namespace pgb
 
 namespace {
 
@@ -1446,8 +1492,10 @@ pgb_status run_rank(pgb_engine *e, int rk) {
     if (nw * keys > e->smem_optin) in_smem = 0;
   }
   size_t smem = in_smem ? nw * keys : 0;
-  if (smem > 48 * 1024)
-    PGB_CUDA(cudaFuncSetAttribute(k_rank_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  if (smem > 48 * 1024) {
+    pgb_status s = kernel_smem(e, (const void *)k_rank_warp, smem);
+    if (s) return s;
+  }
   S1Scores sv{e->d_pairs, e->d_scores, e->d_qlen, e->d_qamb, e->gcat ? 0.0 : log((double)(float)e->NM)};
   k_rank_warp<<<(e->Q + nw - 1) / nw, 32 * nw, smem, e->st>>>(sv, E, rk, e->Q, e->d_qstatus, e->d_rank,
                                                               in_smem);
@@ -1506,7 +1554,8 @@ pgb_status launch_trials_kt(pgb_engine *e, cudaStream_t st, TrialCtx c, const in
   c.cap = cap;
   size_t smem = trial_smem_bytes(cap, c.smem_win, e->RP, K, e->NM, e->ncode);
   if (smem > e->smem_optin) { set_error("trial shared memory %zu exceeds %zu", smem, e->smem_optin); return PGB_ERR_ARG; }
-  PGB_CUDA(cudaFuncSetAttribute(k_trials<K, T, QNG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  pgb_status s = kernel_smem(e, (const void *)k_trials<K, T, QNG>, smem);
+  if (s) return s;
   k_trials<K, T, QNG><<<n, T, smem, st>>>(c, e->d_trials, d_order, n, out);
   PGB_LAUNCH_CHECK();
   return PGB_OK;
@@ -1531,7 +1580,8 @@ template <int RP, bool CAT = false>
 pgb_status launch_trials_warp_rp(pgb_engine *e, cudaStream_t st, TrialCtx c, const WarpSegs &segs, TrialRes *out) {
   size_t smem = warp_trial_smem_bytes(e->NM, e->ncode, c.zcodes);
   if (smem > e->smem_optin) { set_error("warp trial shared memory %zu exceeds %zu", smem, e->smem_optin); return PGB_ERR_ARG; }
-  PGB_CUDA(cudaFuncSetAttribute(k_trials_warp<RP, CAT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  pgb_status s = kernel_smem(e, (const void *)k_trials_warp<RP, CAT>, smem);
+  if (s) return s;
   int grid = (segs.n + kWarpTrialWarps - 1) / kWarpTrialWarps;
   k_trials_warp<RP, CAT><<<grid, 32 * kWarpTrialWarps, smem, st>>>(c, e->d_trials, segs, out);
   PGB_LAUNCH_CHECK();
@@ -1596,14 +1646,33 @@ pgb_status launch_trials_tc(pgb_engine *e, cudaStream_t st, TrialCtx c, const in
   size_t smem = tc_trial_smem_bytes(c.cap, e->NM, e->ncode, c.zcodes, 1);
   if (smem > e->smem_optin) { set_error("tensor-core trial shared memory %zu exceeds %zu", smem, e->smem_optin); return PGB_ERR_ARG; }
   smem = tc_launch_smem(e, smem, 1);
-  PGB_CUDA(cudaFuncSetAttribute(k_trials_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  pgb_status s = kernel_smem(e, (const void *)k_trials_tc, smem);
+  if (s) return s;
   k_trials_tc<<<n, kTcThreads, smem, st>>>(c, e->d_trials, d_order, n, out);
   PGB_LAUNCH_CHECK();
   return PGB_OK;
 }
 
-// the tensor-core kernel's completion-wait flag: an error once set
-// Error records of the tensor-core kernels (bounded waits that timed out).
+// Error records of the tensor-core kernels (bounded waits that timed out),
+// g: the stage-1 record, h: the trial kernels' record, both already on the
+// host; a set record is cleared on the device and reported.
+pgb_status report_tc_err(pgb_engine *e, const int *g, const int *h) {
+  if (e->d_s1_err && g[0]) {
+    PGB_CUDA(cudaMemsetAsync(e->d_s1_err, 0, 4 * sizeof(int), e->st));
+    set_error("stage-1 tensor-core kernel: a pipeline wait timed out (role %d, unit %d, block %d)", g[1], g[2], g[3]);
+    return PGB_ERR_CUDA;
+  }
+  if (h[0]) {
+    PGB_CUDA(cudaMemsetAsync(e->d_tc_err, 0, 16 * sizeof(int), e->st));
+    set_error("tensor-core trial kernel: an MMA completion wait timed out (cta %d rate %d chunk %d phase %d: "
+              "wait %d test %d/%d; tmem 0x%x, tiles 0x%x, barrier 0x%x; sites %d chunks %d)",
+              h[1], h[2], h[3], h[4], h[5], h[6], h[7], h[8], h[9], h[10], h[11], h[12]);
+    return PGB_ERR_CUDA;
+  }
+  return PGB_OK;
+}
+
+// the same, reading the records from the device
 pgb_status check_tc_err(pgb_engine *e) {
   if (e->d_s1_err) {
     int g[4];
@@ -1721,10 +1790,19 @@ pgb_status ensure_run_buffers(pgb_engine *e, const pgb_prefs *p, int rk, int max
   if (rn > e->rank_cap) { if ((s = dalloc(&e->d_rank, rn))) return s; e->rank_cap = rn; }
   size_t resn = (size_t)e->Q * maxr;
   if (resn > e->res_cap) { if ((s = dalloc(&e->d_res, resn))) return s; e->res_cap = resn; }
-  if ((s = dalloc(&e->d_bb, e->Q)) || (s = dalloc(&e->d_tbase, e->Q)) || (s = dalloc(&e->d_tcount, e->Q)) ||
-      (s = dalloc(&e->d_keep_n, e->Q)) || (s = dalloc(&e->d_keep_idx, (size_t)e->Q * p->keep_at_most)) ||
-      (s = dalloc(&e->d_nout, e->Q)) || (s = dalloc(&e->d_out, (size_t)e->Q * p->keep_at_most)))
-    return s;
+  // per-query run buffers: reallocated only when the query count or
+  // keep_at_most outgrows them (a reallocation synchronises the device)
+  if ((size_t)e->Q > e->run_qcap || (size_t)e->Q * p->keep_at_most > e->run_kcap) {
+    const size_t nq = std::max((size_t)e->Q, e->run_qcap), nk = std::max((size_t)e->Q * p->keep_at_most, e->run_kcap);
+    if ((s = dalloc(&e->d_bb, nq)) || (s = dalloc(&e->d_tbase, nq)) || (s = dalloc(&e->d_tcount, nq)) ||
+        (s = dalloc(&e->d_keep_n, nq)) || (s = dalloc(&e->d_keep_idx, nk)) || (s = dalloc(&e->d_nout, nq)) ||
+        (s = dalloc(&e->d_out, nk))) {
+      e->run_qcap = e->run_kcap = 0;
+      return s;
+    }
+    e->run_qcap = nq;
+    e->run_kcap = nk;
+  }
   if (tcap > e->trials_cap) {
     if ((s = dalloc(&e->d_trials, tcap)) || (s = dalloc(&e->d_tres, tcap)) ||
         (s = dalloc(&e->d_bin_list, tcap * kBins)))
@@ -1791,9 +1869,9 @@ template <int RP, bool CAT = false, bool EIG = false, int MINB = kWarpTrialMinCt
 pgb_status launch_place_warp_rp(pgb_engine *e, TrialCtx c, const PlaceCtx &pc) {
   size_t smem = warp_trial_smem_bytes(e->NM, e->ncode, c.zcodes);
   auto kern = k_place_warp<RP, CAT, EIG, MINB>;
-  PGB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int per_sm = 0;
-  PGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32, smem));
+  pgb_status s = kernel_fit(e, (const void *)kern, 32, smem, &per_sm);
+  if (s) return s;
   int grid = std::max(1, std::min(e->Q, e->n_sm * std::max(1, per_sm)));
   kern<<<grid, 32, smem, e->st>>>(c, pc);
   PGB_LAUNCH_CHECK();
@@ -1826,7 +1904,8 @@ pgb_status launch_place_tc(pgb_engine *e, TrialCtx c, const PlaceCtx &pc, int ma
   }
   if (smem > e->smem_optin) { set_error("tensor-core trial shared memory %zu exceeds %zu", smem, e->smem_optin); return PGB_ERR_ARG; }
   smem = tc_launch_smem(e, smem, teams);
-  PGB_CUDA(cudaFuncSetAttribute(k_place_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  pgb_status s = kernel_smem(e, (const void *)k_place_tc, smem);
+  if (s) return s;
   const int grid = std::max(1, std::min((e->Q + teams - 1) / teams, e->n_sm));
   k_place_tc<<<grid, kTcThreads * teams, smem, e->st>>>(c, pc);
   PGB_LAUNCH_CHECK();
@@ -1844,9 +1923,9 @@ pgb_status launch_place_cta_kt(pgb_engine *e, TrialCtx c, const PlaceCtx &pc, in
   if (smem > e->smem_optin) { set_error("trial shared memory %zu exceeds %zu", smem, e->smem_optin); return PGB_ERR_ARG; }
   c.cap = cap;
   c.smem_win = win;
-  PGB_CUDA(cudaFuncSetAttribute(k_place_cta<K, T, QNG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int per_sm = 0;
-  PGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_place_cta<K, T, QNG>, T, smem));
+  pgb_status s = kernel_fit(e, (const void *)k_place_cta<K, T, QNG>, T, smem, &per_sm);
+  if (s) return s;
   int grid = std::max(1, std::min(e->Q, e->n_sm * std::max(1, per_sm)));
   k_place_cta<K, T, QNG><<<grid, T, smem, e->st>>>(c, pc);
   PGB_LAUNCH_CHECK();
@@ -1917,7 +1996,12 @@ pgb_status run_whole_queries(pgb_engine *e, const pgb_prefs *p, const BBCtx &c, 
   if (s) return s;
   PGB_CUDA(cudaEventRecord(e->ev[3], e->st));
   PGB_CUDA(cudaEventRecord(e->ev[4], e->st));
-  PGB_CUDA(cudaEventSynchronize(e->ev[4]));
+  // the counters and error records in one page-locked block, one wait
+  pgb_engine::RunStatus *hr = e->h_run;
+  PGB_CUDA(cudaMemcpyAsync(hr->stats, e->d_stats, sizeof hr->stats, cudaMemcpyDeviceToHost, e->st));
+  if (e->d_s1_err) PGB_CUDA(cudaMemcpyAsync(hr->s1_err, e->d_s1_err, sizeof hr->s1_err, cudaMemcpyDeviceToHost, e->st));
+  PGB_CUDA(cudaMemcpyAsync(hr->tc_err, e->d_tc_err, sizeof hr->tc_err, cudaMemcpyDeviceToHost, e->st));
+  PGB_CUDA(cudaStreamSynchronize(e->st));
   float ms;
   cudaEventElapsedTime(&ms, e->ev[1], e->ev[5]); e->t_ms[0] = ms;
   cudaEventElapsedTime(&ms, e->ev[0], e->ev[1]); e->t_ms[1] = ms;
@@ -1925,9 +2009,8 @@ pgb_status run_whole_queries(pgb_engine *e, const pgb_prefs *p, const BBCtx &c, 
   cudaEventElapsedTime(&ms, e->ev[2], e->ev[3]); e->t_ms[3] = ms;
   e->t_ms[4] = 0;
   cudaEventElapsedTime(&ms, e->ev[0], e->ev[4]); e->t_ms[5] = ms;
-  unsigned long long st_h[4] = {0, 0, 0, 0};
-  PGB_CUDA(cudaMemcpy(st_h, e->d_stats, sizeof st_h, cudaMemcpyDeviceToHost));
-  if ((s = check_tc_err(e))) return s;
+  const unsigned long long *st_h = hr->stats;
+  if ((s = report_tc_err(e, hr->s1_err, hr->tc_err))) return s;
   e->counts[1] = (double)(st_h[2] + st_h[3]);
   e->counts[2] = (double)st_h[0];
   e->counts[3] = (double)st_h[1];
@@ -2077,6 +2160,12 @@ pgb_status pgb_engine_create(const pgb_model_desc *m, const pgb_tree_desc *t, pg
   if (tc_trials_ok(e))  // tensor-core CTAs unless the autotuner finds better
     for (int b = 0; b < kBins; b++) { e->tune_threads[b] = kTuneTc; e->tune_win[b] = 0; }
   for (int i = 0; i < 8; i++) cudaEventCreate(&e->ev[i]);
+  if ((ce = cudaHostAlloc((void **)&e->h_run, sizeof(pgb_engine::RunStatus), cudaHostAllocDefault)) != cudaSuccess) {
+    set_error("engine_create: %s", cudaGetErrorString(ce));
+    delete e;
+    return PGB_ERR_CUDA;
+  }
+  memset(e->h_run, 0, sizeof(pgb_engine::RunStatus));
   for (int i = 0; i < 8; i++) cudaStreamCreateWithFlags(&e->bin_st[i], cudaStreamNonBlocking);
   for (int i = 0; i < 9; i++) cudaEventCreateWithFlags(&e->bin_ev[i], cudaEventDisableTiming);
 
@@ -2163,6 +2252,8 @@ pgb_status pgb_engine_create(const pgb_model_desc *m, const pgb_tree_desc *t, pg
 pgb_status pgb_engine_destroy(pgb_engine *e) {
   if (!e) return PGB_OK;
   if (e->st) cudaStreamSynchronize(e->st);
+  if (e->h_run) cudaFreeHost(e->h_run);
+  if (e->h_qinfo) cudaFreeHost(e->h_qinfo);
   void *ptrs[] = {e->d_bl, e->d_Xd, e->d_Xitd, e->d_lamd, e->d_ratesd, e->d_statdd, e->d_lvd, e->d_pm, e->d_pmh,
                   e->d_mf, e->d_site_cat, e->d_char_code, e->d_informative, e->d_edge_nodes, e->d_parent,
                   e->d_ch_start, e->d_ch_list, e->d_darr, e->d_parr, e->d_snode, e->d_dexp, e->d_pexp, e->d_sexp,
@@ -2457,11 +2548,21 @@ pgb_status pgb_queries_load(pgb_engine *e, int n_queries, const char *seqs) {
   if (!n_queries) return PGB_OK;
   PGB_CUDA(cudaMemcpyAsync(e->d_seqs, seqs, (size_t)n_queries * e->S, cudaMemcpyHostToDevice, e->st));
   if ((s = prep_queries(e))) return s;
-  e->h_qlen.resize(n_queries);
-  PGB_CUDA(cudaMemcpyAsync(e->h_qlen.data(), e->d_qlen, (size_t)n_queries * 4, cudaMemcpyDeviceToHost, e->st));
-  e->h_qamb.resize(n_queries);
-  PGB_CUDA(cudaMemcpyAsync(e->h_qamb.data(), e->d_qamb, (size_t)n_queries * 4, cudaMemcpyDeviceToHost, e->st));
+  // lengths and ambiguity counts back through a page-locked staging block
+  if ((size_t)n_queries > e->h_qinfo_cap) {
+    PGB_CUDA(cudaStreamSynchronize(e->st));  // the previous load's order upload reads the old block
+    if (e->h_qinfo) cudaFreeHost(e->h_qinfo);
+    e->h_qinfo = nullptr;
+    e->h_qinfo_cap = 0;
+    PGB_CUDA(cudaHostAlloc((void **)&e->h_qinfo, (size_t)n_queries * 3 * sizeof(int), cudaHostAllocDefault));
+    e->h_qinfo_cap = n_queries;
+  }
+  int *hq = e->h_qinfo;
+  PGB_CUDA(cudaMemcpyAsync(hq, e->d_qlen, (size_t)n_queries * 4, cudaMemcpyDeviceToHost, e->st));
+  PGB_CUDA(cudaMemcpyAsync(hq + n_queries, e->d_qamb, (size_t)n_queries * 4, cudaMemcpyDeviceToHost, e->st));
   PGB_CUDA(cudaStreamSynchronize(e->st));
+  e->h_qlen.assign(hq, hq + n_queries);
+  e->h_qamb.assign(hq + n_queries, hq + 2 * n_queries);
   // the whole-query kernels take queries longest first from this order
   if ((size_t)n_queries > e->qorder_cap) {
     if ((s = dalloc(&e->d_qorder, n_queries))) return s;
@@ -2469,13 +2570,13 @@ pgb_status pgb_queries_load(pgb_engine *e, int n_queries, const char *seqs) {
   }
   // longest first, equal lengths in query order: a counting sort over the
   // lengths 0..S (O(Q + S) on the host, between two launches)
-  std::vector<int> &ord = e->h_qorder, &at = e->h_len_at;
-  ord.resize(n_queries);
+  std::vector<int> &at = e->h_len_at;
+  int *ord = hq + 2 * n_queries;  // page-locked: the copy below runs asynchronously
   at.assign(e->S + 2, 0);
   for (int q = 0; q < n_queries; q++) at[e->S - e->h_qlen[q] + 1]++;
   for (int l = 1; l <= e->S + 1; l++) at[l] += at[l - 1];
   for (int q = 0; q < n_queries; q++) ord[at[e->S - e->h_qlen[q]]++] = q;
-  PGB_CUDA(cudaMemcpyAsync(e->d_qorder, ord.data(), ord.size() * sizeof(int), cudaMemcpyHostToDevice, e->st));
+  PGB_CUDA(cudaMemcpyAsync(e->d_qorder, ord, (size_t)n_queries * sizeof(int), cudaMemcpyHostToDevice, e->st));
   return prep_stage1_queries(e);
 }
 
