@@ -165,6 +165,9 @@ def warp_form(w, tune):
 def stage2_kernel(w, tune):
     """The trial kernel that ran stage 2 + refinement for this workload and tuning."""
     th = set(int(v) for v in tune[0])
+    if w.prefs.get("max_strikes") == 0 and len(w.query_seqs) < 2 * 8 * N_SM and th == {32}:
+        return ("k_trials_warp (every edge of every query: all stage-2 trials in one launch, one warp each; "
+                "then the refinement trials)")
     if th == {32}:
         return "k_place_warp (stage 2 + refinement, whole queries, one warp each%s)" % (
             ", per-site categories" if w.site_cats is not None else

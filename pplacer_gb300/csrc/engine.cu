@@ -2659,7 +2659,11 @@ pgb_status pgb_queries_run(pgb_engine *e, const pgb_prefs *p) {
   if ((s = ensure_eigen_glvs(e))) return s;
   TrialCtx tc = trial_ctx(e, p, p->optimizer, 0);
   int n = e->Q;
-  if (whole_query_form(e)) return run_whole_queries(e, p, c, tc, max_sq);
+  // Every edge of every query (max_strikes 0): the trials are independent,
+  // so with fewer queries than the GPU has trial warps they run as one
+  // batch of all trials rather than one query per warp
+  const bool few_queries = all_edges && e->Q < 2 * kWarpTrialMinCtas * e->n_sm;
+  if (whole_query_form(e) && !few_queries) return run_whole_queries(e, p, c, tc, max_sq);
   if (p->calc_pp && (s = ensure_prior_means(e, p->prior, p->prior_lower))) return s;
   k_bb_init<<<(n + 255) / 256, 256, 0, e->st>>>(c);
   PGB_LAUNCH_CHECK();
