@@ -57,6 +57,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--optimizer", default="newton", choices=["newton", "brent"])
+    ap.add_argument("--qng-sample", type=int, default=1000,
+                    help="queries of the posterior-probability leg computed as the reference does (pp_rule 1)")
     ap.add_argument("--pp-steps", type=int, default=1,
                     help="untimed-region comparison: placement steps with posterior probabilities")
     ap.add_argument("--brent-steps", type=int, default=2,
@@ -355,13 +357,17 @@ def run_ours(args):
               "quadrature": "Gauss-Legendre panels around the optimum (pp_rule 0)"}
         # the reference's own computation of the marginal likelihood (pp_rule
         # 1: find_upper_limit's Brent search, nested QNG to pp_rel_err, ETOL
-        # retries), on the CTA kernels that carry it
+        # retries), on the CTA kernels that carry it; a bounded sample of the
+        # queries (it evaluates ~20x more points per placement)
+        nq = min(Q, args.qng_sample)
+        eng.load_queries(w.query_seqs[:nq])
         qprefs = E.default_prefs(optimizer=1, calc_pp=1, pp_rule=1, **w.prefs)
         eng.run(qprefs)
         eng.run(qprefs)
         ms, cnt = eng.timings()
-        pp["reference_qng"] = {"value": Q / (ms[5] / 1e3), "unit": "placements/s", "evals_per_step": cnt[2],
-                               "steps": 1}
+        pp["reference_qng"] = {"value": nq / (ms[5] / 1e3), "unit": "placements/s", "evals_per_step": cnt[2],
+                               "steps": 1, "queries": nq}
+        eng.load_queries(w.query_seqs)
     # ---- end to end through pgb_place_batch: the query rows in, the
     # placements out, both in page-locked host memory (pgb_host_alloc) ----
     kam = prefs.keep_at_most
