@@ -154,7 +154,7 @@ class ClockSampler:
 
 # The nucleotide Gamma warp forms by the engine's tuning value (smem_windows
 # of a warp bin): 0 matrices in registers, 1-3 the eigenbasis form
-WARP_FORM_WARPS = {0: 8, 1: 8, 2: 12, 3: 16}
+WARP_FORM_WARPS = {0: 8, 1: 8, 2: 12, 3: 16, 4: 12, 5: 16}
 
 
 def warp_form(w, tune):
@@ -173,7 +173,8 @@ def stage2_kernel(w, tune):
     if th == {32}:
         return "k_place_warp (stage 2 + refinement, whole queries, one warp each%s)" % (
             ", per-site categories" if w.site_cats is not None else
-            ", %s form, %d warps per SM" % (warp_form(w, tune), WARP_FORM_WARPS[int(tune[1][0])]))
+            ", %s form%s, %d warps per SM" % (warp_form(w, tune), " on packed FP32 pairs" if int(tune[1][0]) >= 4 else "",
+                                             WARP_FORM_WARPS[int(tune[1][0])]))
     if th == {1}:
         return ("k_place_tc (stage 2 + refinement, whole queries, one 128-thread team each, two teams per CTA, "
                 "tcgen05 evolves)")

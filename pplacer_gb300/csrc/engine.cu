@@ -999,9 +999,9 @@ __device__ __forceinline__ void place_queries(Team &tm, const TrialCtx &c, const
 }
 
 // A warp as a team (nucleotide Gamma mixtures, CAT): lane 0 leads.
-template <int RP, bool CAT, bool EIG = false>
+template <int RP, bool CAT, int EIG = 0>
 struct WarpTeam {
-  static constexpr bool kEig = EIG;
+  static constexpr bool kEig = EIG != 0;
   const TrialCtx &c;
   const TrialSmem &sm;
   float4 *ring;
@@ -1015,7 +1015,7 @@ struct WarpTeam {
 
 // MINB: resident one-warp CTAs per SM the register allocation aims for
 // (8: 255 registers per thread; 12: 168).
-template <int RP, bool CAT = false, bool EIG = false, int MINB = kWarpTrialMinCtas>
+template <int RP, bool CAT = false, int EIG = 0, int MINB = kWarpTrialMinCtas>
 __global__ void __launch_bounds__(32, MINB) k_place_warp(TrialCtx c, PlaceCtx p) {
   extern __shared__ __align__(16) char t_smem[];
   TrialSmem sm;
@@ -1865,7 +1865,7 @@ pgb_status ensure_prior_means(pgb_engine *e, int prior, double prior_lower) {
   return PGB_OK;
 }
 
-template <int RP, bool CAT = false, bool EIG = false, int MINB = kWarpTrialMinCtas>
+template <int RP, bool CAT = false, int EIG = 0, int MINB = kWarpTrialMinCtas>
 pgb_status launch_place_warp_rp(pgb_engine *e, TrialCtx c, const PlaceCtx &pc) {
   size_t smem = warp_trial_smem_bytes(e->NM, e->ncode, c.zcodes);
   auto kern = k_place_warp<RP, CAT, EIG, MINB>;
@@ -1880,13 +1880,16 @@ pgb_status launch_place_warp_rp(pgb_engine *e, TrialCtx c, const PlaceCtx &pc) {
 
 // The nucleotide Gamma warp forms (the autotuner's choice, warp_variant):
 // 0 matrices in registers, 8 warps per SM; 1, 2, 3 eigenbasis at 8, 12 and
-// 16 warps per SM (255, 168 and 128 registers).
-constexpr int kWarpForms = 4;
+// 16 warps per SM (255, 168 and 128 registers); 4, 5 the eigenbasis on
+// packed FP32 pairs at 12 and 16 warps per SM.
+constexpr int kWarpForms = 6;
 template <int RP>
 pgb_status launch_place_warp_gmix(pgb_engine *e, TrialCtx c, const PlaceCtx &pc) {
-  if (e->warp_variant == 1) return launch_place_warp_rp<RP, false, true, 8>(e, c, pc);
-  if (e->warp_variant == 2) return launch_place_warp_rp<RP, false, true, 12>(e, c, pc);
-  if (e->warp_variant == 3) return launch_place_warp_rp<RP, false, true, 16>(e, c, pc);
+  if (e->warp_variant == 1) return launch_place_warp_rp<RP, false, 1, 8>(e, c, pc);
+  if (e->warp_variant == 2) return launch_place_warp_rp<RP, false, 1, 12>(e, c, pc);
+  if (e->warp_variant == 3) return launch_place_warp_rp<RP, false, 1, 16>(e, c, pc);
+  if (e->warp_variant == 4) return launch_place_warp_rp<RP, false, 2, 12>(e, c, pc);
+  if (e->warp_variant == 5) return launch_place_warp_rp<RP, false, 2, 16>(e, c, pc);
   return launch_place_warp_rp<RP>(e, c, pc);
 }
 
@@ -2907,7 +2910,7 @@ pgb_status pgb_engine_set_tuning(pgb_engine *e, const int *threads, const int *s
         (!wf && (smem_windows[b] & ~1)) || (wf && (smem_windows[b] < 0 || smem_windows[b] >= kWarpForms)) ||
         (wf && smem_windows[b] > 0 && !warp_eig_ok(e))) {
       set_error("set_tuning: bin %d: threads must be 1, 32, 128 or 256 and smem_windows 0 or 1 (for the "
-                "nucleotide Gamma warp form 0 .. 3 where the eigenbasis forms apply)", b);
+                "nucleotide Gamma warp form 0 .. 5 where the eigenbasis forms apply)", b);
       return PGB_ERR_ARG;
     }
   }

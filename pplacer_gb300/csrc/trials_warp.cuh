@@ -410,6 +410,165 @@ __device__ __forceinline__ void sites_warp_eig(const TrialCtx &c, const TrialSme
   cp_async_wait<0>();  // drain the copies issued past the end
 }
 
+// The eigenbasis form on packed FP32 pairs (fma.rn.f32x2, two lanes of
+// arithmetic per instruction): the states (0, 1) and (2, 3) of a site share
+// each instruction -- X's columns pair across the two states, the scaled
+// eigen-coordinates are duplicated into both halves -- so the evolves and
+// the six sums take about 74 instructions per site and rate instead of 130.
+// The proximal first derivative is formed negated (-y') with the negated
+// exp factors, as it only enters the sums as -x y' and -2 x' y'.
+template <int RP, bool DER>
+__device__ __forceinline__ void sites_warp_eig2(const TrialCtx &c, const TrialSmem &sm, float4 *ring, int q, int node,
+                                                int Sq, int lane, SiteAcc &acc) {
+  constexpr int K = 4, SPW = 32 / RP;
+  const int r = lane & (RP - 1), slot = lane / RP, zc = c.zcodes, NM = c.NM;
+  int ord[3];
+  ord[0] = (c.eig_ord >> 8) & 255; ord[1] = (c.eig_ord >> 16) & 255; ord[2] = (c.eig_ord >> 24) & 255;
+  // xp[h][k] = (X[2h][k], X[2h+1][k]); xq1, xq2 the same scaled by r lambda, (r lambda)^2
+  float2 xp[2][3], xq1[2][3], xq2[2][3];
+  float ed[3], ep[3], epn[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    const float lr = sm.Lr[r * K + ord[k]];
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      const float a = sm.X[(2 * h) * K + ord[k]], b = sm.X[(2 * h + 1) * K + ord[k]];
+      const float a1 = a * lr, b1 = b * lr;
+      xp[h][k] = make_float2(a, b);
+      xq1[h][k] = make_float2(a1, b1);
+      xq2[h][k] = make_float2(a1 * lr, b1 * lr);
+    }
+    ed[k] = sm.E[(0 * NM + r) * K + ord[k]];
+    ep[k] = sm.E[(1 * NM + r) * K + ord[k]];
+    epn[k] = -ep[k];
+  }
+  const float *gd = c.darr_e + (long)node * c.S * RP * K + r * K;
+  const float *gp = c.parr_e + (long)node * c.S * RP * K + r * K;
+  const uint32_t *rc = c.rcode + (long)q * c.S;
+  const float *Zr = sm.Z + r * zc * K, *Z1r = sm.Z1 + r * zc * K, *Z2r = sm.Z2 + r * zc * K;
+  const int last = Sq - 1;
+  constexpr int G = (RP == 2 || RP == 4) ? RP : 1;
+  int off[G];
+#pragma unroll
+  for (int k = 0; k < G; k++) off[k] = (G > 1 ? (k ^ r) : 0) * SPW + slot;
+  // the ring, the code queue and the iteration order are those of sites_warp
+  unsigned long long cq = 0ull;
+  auto issue = [&](int stage, uint32_t pk) {
+    const long col = (long)(pk >> 8);
+    cp_async16(ring + (stage * 32 + lane), gd + col * RP * K);
+    cp_async16(ring + ((kWarpRing + stage) * 32 + lane), gp + col * RP * K);
+    cp_async_commit();
+  };
+#pragma unroll
+  for (int j = 0; j < kWarpRing - 1; j++) {
+    const uint32_t pk = rc[min((j / G) * G * SPW + off[j % G], last)];
+    issue(j, pk);
+    cq |= (unsigned long long)(pk & 255u) << (8 * j);
+  }
+  uint32_t pk_next = rc[min(((kWarpRing - 1) / G) * G * SPW + off[(kWarpRing - 1) % G], last)];
+  uint32_t pk_next2 = rc[min(off[0] + kWarpRing * SPW, last)];
+  int st = 0;
+  auto iteration = [&](int i, int inext, float (&v)[6]) {
+    issue((st + kWarpRing - 1) & (kWarpRing - 1), pk_next);
+    cq |= (unsigned long long)(pk_next & 255u) << (8 * (kWarpRing - 1));
+    const int code = (int)(cq & 255ull);
+    cq >>= 8;
+    pk_next = pk_next2;
+    pk_next2 = rc[min(inext + kWarpRing * SPW, last)];
+    cp_async_wait<kWarpRing - 1>();  // this iteration's copies have landed
+    const float4 dcur = ring[st * 32 + lane];
+    const float4 pcur = ring[(kWarpRing + st) * 32 + lane];
+    st = (st + 1) & (kWarpRing - 1);
+    const float dv[3] = {dcur.y, dcur.z, dcur.w}, pv[3] = {pcur.y, pcur.z, pcur.w};
+    const float4 Z4 = *reinterpret_cast<const float4 *>(Zr + code * K);
+    const float2 zz[2] = {make_float2(Z4.x, Z4.y), make_float2(Z4.z, Z4.w)};
+    float2 z1p[2], z2p[2];
+    if (DER) {
+      const float4 a = *reinterpret_cast<const float4 *>(Z1r + code * K);
+      const float4 b = *reinterpret_cast<const float4 *>(Z2r + code * K);
+      z1p[0] = make_float2(a.x, a.y); z1p[1] = make_float2(a.z, a.w);
+      z2p[0] = make_float2(b.x, b.y); z2p[1] = make_float2(b.z, b.w);
+    }
+    float2 ud[3], wp[3], wn[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      const float u = ed[k] * dv[k], w = ep[k] * pv[k];
+      ud[k] = make_float2(u, u);
+      wp[k] = make_float2(w, w);
+      if (DER) {
+        const float wq = epn[k] * pv[k];
+        wn[k] = make_float2(wq, wq);
+      }
+    }
+    float2 V[6];
+#pragma unroll
+    for (int k = 0; k < 6; k++) V[k] = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      float2 X = make_float2(dcur.x, dcur.x), Y = make_float2(pcur.x, pcur.x);
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        X = __ffma2_rn(xp[h][k], ud[k], X);
+        Y = __ffma2_rn(xp[h][k], wp[k], Y);
+      }
+      const float2 XY = __fmul2_rn(X, Y);
+      V[0] = __ffma2_rn(zz[h], XY, V[0]);
+      if (DER) {
+        float2 X1 = __fmul2_rn(xq1[h][0], ud[0]), X2 = __fmul2_rn(xq2[h][0], ud[0]);
+        float2 Y1n = __fmul2_rn(xq1[h][0], wn[0]), Y2 = __fmul2_rn(xq2[h][0], wp[0]);
+#pragma unroll
+        for (int k = 1; k < 3; k++) {
+          X1 = __ffma2_rn(xq1[h][k], ud[k], X1);
+          X2 = __ffma2_rn(xq2[h][k], ud[k], X2);
+          Y1n = __ffma2_rn(xq1[h][k], wn[k], Y1n);
+          Y2 = __ffma2_rn(xq2[h][k], wp[k], Y2);
+        }
+        const float2 AA = __ffma2_rn(X, Y1n, __fmul2_rn(X1, Y));                        // x' y - x y'
+        const float2 BB = __ffma2_rn(X, Y2, __ffma2_rn(X1, __fadd2_rn(Y1n, Y1n), __fmul2_rn(X2, Y)));
+        V[1] = __ffma2_rn(zz[h], AA, V[1]);
+        V[2] = __ffma2_rn(zz[h], BB, V[2]);
+        V[3] = __ffma2_rn(z1p[h], XY, V[3]);
+        V[4] = __ffma2_rn(z2p[h], XY, V[4]);
+        V[5] = __ffma2_rn(z1p[h], AA, V[5]);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 6; k++) v[k] = V[k].x + V[k].y;
+  };
+  constexpr int NV = DER ? 6 : 1;
+  for (int gbase = 0; gbase < Sq; gbase += G * SPW) {
+    float f[6];
+    if (G == 4) {
+      float v0[6], v1[6], h0[6], h1[6];
+      iteration(gbase + off[0], gbase + off[1], v0);
+      iteration(gbase + off[1], gbase + off[2], v1);
+#pragma unroll
+      for (int k = 0; k < NV; k++) h0[k] = v0[k] + __shfl_xor_sync(0xffffffffu, v1[k], 1);
+      iteration(gbase + off[2], gbase + off[3], v0);
+      iteration(gbase + off[3], gbase + G * SPW + off[0], v1);
+#pragma unroll
+      for (int k = 0; k < NV; k++) h1[k] = v0[k] + __shfl_xor_sync(0xffffffffu, v1[k], 1);
+#pragma unroll
+      for (int k = 0; k < NV; k++) f[k] = h0[k] + __shfl_xor_sync(0xffffffffu, h1[k], 2);
+    } else if (G == 2) {
+      float v0[6], v1[6];
+      iteration(gbase + off[0], gbase + off[1], v0);
+      iteration(gbase + off[1], gbase + G * SPW + off[0], v1);
+#pragma unroll
+      for (int k = 0; k < NV; k++) f[k] = v0[k] + __shfl_xor_sync(0xffffffffu, v1[k], 1);
+    } else {
+      iteration(gbase + off[0], gbase + SPW + off[0], f);
+#pragma unroll
+      for (int o = 1; o < RP; o <<= 1)
+#pragma unroll
+        for (int k = 0; k < NV; k++) f[k] += __shfl_xor_sync(0xffffffffu, f[k], o);
+    }
+    const bool mine = G > 1 ? gbase + r * SPW + slot < Sq : (r == 0 && gbase + slot < Sq);
+    if (mine) acc.add(f[0], f[1], f[2], f[3], f[4], f[5], DER);
+  }
+  cp_async_wait<0>();  // drain the copies issued past the end
+}
+
 // Sites of a per-site CAT model (Gcat_model, one GLV plane): lane = site,
 // 32 sites per iteration, the windows streamed through the same cp.async
 // ring.  A site's matrices are those of its category (the packed word's top
@@ -534,7 +693,7 @@ __device__ __forceinline__ void warp_trial_setup(const TrialCtx &c, char *t_smem
 // One trial (Three_tax.optimize at one location) by the calling warp.  Every
 // lane runs the same optimiser on the same all-reduced values and returns
 // the same result.
-template <int RP, bool CAT = false, bool EIG = false>
+template <int RP, bool CAT = false, int EIG = 0>
 __device__ TrialRes trial_warp(const TrialCtx &c, const TrialSmem &sm, float4 *ring, int lane, const TrialIn &tr) {
   constexpr int K = 4;
   const int NM = c.NM, nc = c.ncode;
@@ -617,6 +776,9 @@ __device__ TrialRes trial_warp(const TrialCtx &c, const TrialSmem &sm, float4 *r
       if (CAT) {
         if (derivs) sites_warp_cat<true>(c, sm, ring, q, node, Sq, lane, acc);
         else sites_warp_cat<false>(c, sm, ring, q, node, Sq, lane, acc);
+      } else if (EIG == 2) {
+        if (derivs) sites_warp_eig2<RP, true>(c, sm, ring, q, node, Sq, lane, acc);
+        else sites_warp_eig2<RP, false>(c, sm, ring, q, node, Sq, lane, acc);
       } else if (EIG) {
         if (derivs) sites_warp_eig<RP, true>(c, sm, ring, q, node, Sq, lane, acc);
         else sites_warp_eig<RP, false>(c, sm, ring, q, node, Sq, lane, acc);

@@ -22,8 +22,10 @@ LOGL_RTOL = 1e-6
 # trial-kernel forms: one CTA (256 threads, windows in shared memory) or one
 # warp per trial; for the nucleotide Gamma warp kernel the second number picks
 # its form: 0 the transition matrices in registers, 1 the eigenbasis (8 warps
-# per SM), 2 and 3 the eigenbasis at 12 and 16 warps per SM
-FORMS = {"cta": (256, 1), "warp": (32, 0), "eig": (32, 1), "eig12": (32, 2), "eig16": (32, 3)}
+# per SM), 2 and 3 the eigenbasis at 12 and 16 warps per SM, 4 and 5 the
+# eigenbasis on packed FP32 pairs at 12 and 16 warps per SM
+FORMS = {"cta": (256, 1), "warp": (32, 0), "eig": (32, 1), "eig12": (32, 2), "eig16": (32, 3),
+         "eig12x2": (32, 4), "eig16x2": (32, 5)}
 
 
 @pytest.fixture(scope="module", params=sorted(FORMS))
