@@ -41,7 +41,7 @@ MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 
 
 # measured constants of the stage-2 roofline (see the roofline block below)
-DRAM_BYTES_PER_SITE_EVAL = 84.75  # k_place_warp (eigenbasis form, 16 warps/SM) on dna_1k: 25.877 GB DRAM read + write / 305.3 M site evaluations
+DRAM_BYTES_PER_SITE_EVAL = 78.63  # k_place_warp (eigenbasis form on packed FP32 pairs, 12 warps/SM) on dna_1k: 24.004 GB DRAM read + write / 305.3 M site evaluations
 # FFMA + FMUL per site and rate with derivatives (the kernel's arithmetic):
 # six 4x4 matrix-vector products (96) + the six sums (52) in the matrix form;
 # 2 x 3 coordinate scalings + 6 x 12 column FMAs (78) + 52 in the eigenbasis form

@@ -2111,7 +2111,7 @@ pgb_status pgb_engine_create(const pgb_model_desc *m, const pgb_tree_desc *t, pg
         if (k != kz) ord |= k << (8 * s++);
       e->eig_ok = true;
       e->eig_ord = ord;
-      e->warp_variant = 3;  // the eigenbasis form at 16 warps per SM until the autotuner says otherwise
+      e->warp_variant = 4;  // the eigenbasis form on packed FP32 pairs, 12 warps per SM, until the autotuner says otherwise
       double mean = 0;
       for (int i = 0; i < K; i++) mean += e->X[i * K + kz];
       e->eig_c0 = mean / K;
