@@ -45,7 +45,8 @@ DRAM_BYTES_PER_SITE_EVAL = 78.63  # k_place_warp (eigenbasis form on packed FP32
 # FFMA + FMUL per site and rate with derivatives (the kernel's arithmetic):
 # six 4x4 matrix-vector products (96) + the six sums (52) in the matrix form;
 # 2 x 3 coordinate scalings + 6 x 12 column FMAs (78) + 52 in the eigenbasis form
-FMA_OPS_PER_SITE_RATE = {"matrix": 148, "eigenbasis": 130}
+# CAT in the eigenbasis: 6 x 3 scalings + 6 x 12 column FMAs (90) + 52
+FMA_OPS_PER_SITE_RATE = {"matrix": 148, "eigenbasis": 130, "CAT eigenbasis": 142}
 N_SM = 152
 SM_MAX_HZ = 2.07e9
 
@@ -172,7 +173,8 @@ def stage2_kernel(w, tune):
                 "then the refinement trials)")
     if th == {32}:
         return "k_place_warp (stage 2 + refinement, whole queries, one warp each%s)" % (
-            ", per-site categories" if w.site_cats is not None else
+            ", per-site categories, %s form" % ("eigenbasis" if int(tune[1][0]) == 1 else "matrix")
+            if w.site_cats is not None else
             ", %s form%s, %d warps per SM" % (warp_form(w, tune), " on packed FP32 pairs" if int(tune[1][0]) >= 4 else "",
                                              WARP_FORM_WARPS[int(tune[1][0])]))
     if th == {1}:
@@ -413,8 +415,8 @@ def run_ours(args):
     # operations per site evaluation of the form that ran (per rate, with
     # derivatives), against 128 lanes per SM; CAT runs the matrix arithmetic
     # on its one plane, the 20-state tensor-core form has no such count
-    form = warp_form(w, tune) or ("matrix" if w.site_cats is not None and set(int(v) for v in tune[0]) == {32}
-                                  else None)
+    cat_warp = w.site_cats is not None and set(int(v) for v in tune[0]) == {32}
+    form = warp_form(w, tune) or ((("CAT eigenbasis" if int(tune[1][0]) == 1 else "matrix")) if cat_warp else None)
     fp32_ops = (FMA_OPS_PER_SITE_RATE[form] * R * site_evals / args.steps / t_trials
                 if form and t_trials > 0 else None)
     fp32_peak = 128 * N_SM * SM_MAX_HZ

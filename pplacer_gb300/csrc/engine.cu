@@ -1020,7 +1020,7 @@ __global__ void __launch_bounds__(32, MINB) k_place_warp(TrialCtx c, PlaceCtx p)
   extern __shared__ __align__(16) char t_smem[];
   TrialSmem sm;
   float4 *ring;
-  warp_trial_setup(c, t_smem, sm, ring);
+  warp_trial_setup(c, t_smem, sm, ring, !(CAT && EIG));
   WarpTeam<RP, CAT, EIG> tm{c, sm, ring, (int)(threadIdx.x & 31)};
   place_queries(tm, c, p);
 }
@@ -1611,7 +1611,8 @@ bool warp_eig_ok(const pgb_engine *e) { return warp_trials_ok(e) && e->eig_ok; }
 // tensor-core kernel (20 states) and the eigenbasis warp form (nucleotides,
 // the permuted and premultiplied layout of k_eigen_glvs_dna).
 pgb_status ensure_eigen_glvs(pgb_engine *e) {
-  const bool tc = tc_trials_ok(e), dna = warp_eig_ok(e) && e->warp_variant != 0;
+  const bool tc = tc_trials_ok(e),
+             dna = (warp_eig_ok(e) && e->warp_variant != 0) || (warp_cat_ok(e) && e->eig_ok && e->warp_variant == 1);
   if (e->eig_ready || (!tc && !dna)) return PGB_OK;
   const long rows = (long)e->n_nodes * e->S * e->RP;
   pgb_status s;
@@ -1867,7 +1868,7 @@ pgb_status ensure_prior_means(pgb_engine *e, int prior, double prior_lower) {
 
 template <int RP, bool CAT = false, int EIG = 0, int MINB = kWarpTrialMinCtas>
 pgb_status launch_place_warp_rp(pgb_engine *e, TrialCtx c, const PlaceCtx &pc) {
-  size_t smem = warp_trial_smem_bytes(e->NM, e->ncode, c.zcodes);
+  size_t smem = warp_trial_smem_bytes(e->NM, e->ncode, c.zcodes, !(CAT && EIG));
   auto kern = k_place_warp<RP, CAT, EIG, MINB>;
   int per_sm = 0;
   pgb_status s = kernel_fit(e, (const void *)kern, 32, smem, &per_sm);
@@ -1883,6 +1884,7 @@ pgb_status launch_place_warp_rp(pgb_engine *e, TrialCtx c, const PlaceCtx &pc) {
 // 16 warps per SM (255, 168 and 128 registers); 4, 5 the eigenbasis on
 // packed FP32 pairs at 12 and 16 warps per SM.
 constexpr int kWarpForms = 6;
+constexpr int kCatEigMinCtas = 12;  // the CAT eigenbasis form: one-warp CTAs per SM it aims for
 template <int RP>
 pgb_status launch_place_warp_gmix(pgb_engine *e, TrialCtx c, const PlaceCtx &pc) {
   if (e->warp_variant == 1) return launch_place_warp_rp<RP, false, 1, 8>(e, c, pc);
@@ -1988,7 +1990,9 @@ pgb_status run_whole_queries(pgb_engine *e, const pgb_prefs *p, const BBCtx &c, 
   if (tc.pp_rule == 1) s = launch_place_cta(e, tc, pc, max_sq);  // the CTA kernels carry the QNG replica
   else if (e->tune_threads[0] == kTuneTc && tc_trials_ok(e)) s = launch_place_tc(e, tc, pc, max_sq);
   else if (e->tune_threads[0] != 32 || !warp_form_ok(e)) s = launch_place_cta(e, tc, pc, max_sq);
-  else if (e->gcat) s = launch_place_warp_rp<1, true>(e, tc, pc);
+  else if (e->gcat)  // the CAT forms: 0 matrices per category, 1 the eigenbasis
+    s = e->warp_variant == 1 && e->eig_ok ? launch_place_warp_rp<1, true, 1, kCatEigMinCtas>(e, tc, pc)
+                                          : launch_place_warp_rp<1, true>(e, tc, pc);
   else
     switch (e->RP) {
       case 1: s = launch_place_warp_gmix<1>(e, tc, pc); break;
@@ -2111,7 +2115,9 @@ pgb_status pgb_engine_create(const pgb_model_desc *m, const pgb_tree_desc *t, pg
         if (k != kz) ord |= k << (8 * s++);
       e->eig_ok = true;
       e->eig_ord = ord;
-      e->warp_variant = 4;  // the eigenbasis form on packed FP32 pairs, 12 warps per SM, until the autotuner says otherwise
+      // until the autotuner says otherwise: the eigenbasis form on packed FP32
+      // pairs at 12 warps per SM (Gamma mixtures), the CAT eigenbasis form
+      e->warp_variant = e->gcat ? 1 : 4;
       double mean = 0;
       for (int i = 0; i < K; i++) mean += e->X[i * K + kz];
       e->eig_c0 = mean / K;
@@ -2889,6 +2895,21 @@ pgb_status pgb_engine_autotune(pgb_engine *e, const pgb_prefs *p) {
     e->tune_threads[b] = best_cfg < 0 ? per_bin_t[b] : uni_t[best_cfg];
     e->tune_win[b] = best_cfg < 0 ? per_bin_w[b] : uni_w[best_cfg];
   }
+  if (best_cfg == 0 && warp_cat_ok(e) && e->eig_ok) {
+    // the CAT warp form: its matrix and eigenbasis variants on whole runs
+    float bf = 1e30f;
+    int bv = 0;
+    for (int v = 0; v < 2; v++) {
+      if (v != e->warp_variant) { e->warp_variant = v; e->eig_ready = false; }
+      float ms_best = 1e30f;
+      for (int rep = 0; rep < 2; rep++) {
+        if ((s = pgb_queries_run(e, p))) return s;
+        ms_best = std::min(ms_best, (float)e->t_ms[3]);
+      }
+      if (ms_best < bf) { bf = ms_best; bv = v; }
+    }
+    if (bv != e->warp_variant) { e->warp_variant = bv; e->eig_ready = false; }
+  }
   return check_tc_err(e);
 }
 
@@ -2896,7 +2917,9 @@ pgb_status pgb_engine_get_tuning(pgb_engine *e, int *threads, int *smem_windows)
   if (!e) return PGB_ERR_ARG;
   for (int b = 0; b < kBins; b++) {
     threads[b] = e->tune_threads[b];
-    smem_windows[b] = e->tune_threads[b] == 32 && warp_trials_ok(e) ? e->warp_variant : e->tune_win[b];
+    smem_windows[b] = e->tune_threads[b] == 32 && (warp_trials_ok(e) || warp_cat_ok(e))
+                          ? (warp_trials_ok(e) ? e->warp_variant : (e->warp_variant == 1 ? 1 : 0))
+                          : e->tune_win[b];
   }
   return PGB_OK;
 }
@@ -2914,11 +2937,18 @@ pgb_status pgb_engine_set_tuning(pgb_engine *e, const int *threads, const int *s
       return PGB_ERR_ARG;
     }
   }
+  if (threads[0] == 32 && warp_cat_ok(e) && smem_windows[0] == 1 && !e->eig_ok) {
+    set_error("set_tuning: the CAT eigenbasis form needs a rate matrix with one zero eigenvalue");
+    return PGB_ERR_ARG;
+  }
   for (int b = 0; b < kBins; b++) {
     e->tune_threads[b] = threads[b];
-    e->tune_win[b] = threads[b] == 32 && warp_forms ? 0 : smem_windows[b];
+    e->tune_win[b] = threads[b] == 32 && (warp_forms || warp_cat_ok(e)) ? 0 : smem_windows[b];
   }
-  if (threads[0] == 32 && warp_forms && smem_windows[0] != e->warp_variant) {
+  // smem_windows of a warp bin selects the form: the nucleotide Gamma forms
+  // 0 .. 5, or the CAT form (0 matrices per category, 1 the eigenbasis)
+  const bool cat_forms = warp_cat_ok(e);
+  if (threads[0] == 32 && (warp_forms || cat_forms) && smem_windows[0] != e->warp_variant) {
     e->warp_variant = smem_windows[0];
     e->eig_ready = false;  // the eigen-coordinate layout follows the form
   }

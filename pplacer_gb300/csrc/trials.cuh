@@ -92,6 +92,7 @@ struct TrialSmem {
   float *Md, *Mp, *Md1, *Md2, *Mp1, *Mp2;  // [NM][K][K]
   float *Z, *Z1, *Z2;        // [NM][ncode][K] statd-weighted evolved query vectors
   float *E, *Em1, *Lr;       // exp / expm1 factors [3][NM][K]; rate * lambda [NM][K]
+  float *Tc;                 // the CAT eigenbasis form: per category [12] (exp factors, rate * lambda)
   float *X, *W, *Lt, *lv, *statd;  // model constants (W only for K = 4)
   float *red;                // [warps][8]
   int *redi;                 // [warps]

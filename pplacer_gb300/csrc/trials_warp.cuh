@@ -37,9 +37,11 @@ constexpr int kWarpRing = 8;        // site iterations in flight per warp
 __host__ __device__ inline size_t warp_trial_const_floats(int NM, int ncode) {
   return 16 + 64 + 2 * (size_t)ncode * 4 + 4 + (size_t)NM * 4;
 }
-// zc: the character codes the query-vector tables hold (c.zcodes)
-__host__ __device__ inline size_t warp_trial_table_floats(int NM, int zc) {
-  return 6 * (size_t)NM * 16 + 3 * (size_t)NM * zc * 4 + 2 * 3 * (size_t)NM * 4;
+// zc: the character codes the query-vector tables hold (c.zcodes); mats:
+// the per-model transition matrices (every form but the CAT eigenbasis
+// form, which holds 12 floats per category instead)
+__host__ __device__ inline size_t warp_trial_table_floats(int NM, int zc, bool mats = true) {
+  return (mats ? 6 * (size_t)NM * 16 : 12 * (size_t)NM) + 3 * (size_t)NM * zc * 4 + 2 * 3 * (size_t)NM * 4;
 }
 static_assert(kWarpRing == 8, "ring depth 8: the codes in flight fill one 64-bit register");
 
@@ -53,11 +55,11 @@ struct WarpSegs {
 };
 // per warp: its tables, the ring of D / P float4s [2][kWarpRing][32], and
 // the optimiser state
-__host__ __device__ inline size_t warp_trial_warp_bytes(int NM, int zc) {
-  return align16(4 * warp_trial_table_floats(NM, zc)) + 2 * kWarpRing * 32 * 16 + align16(sizeof(Optimiser));
+__host__ __device__ inline size_t warp_trial_warp_bytes(int NM, int zc, bool mats = true) {
+  return align16(4 * warp_trial_table_floats(NM, zc, mats)) + 2 * kWarpRing * 32 * 16 + align16(sizeof(Optimiser));
 }
-__host__ __device__ inline size_t warp_trial_smem_bytes(int NM, int ncode, int zc) {
-  return align16(4 * warp_trial_const_floats(NM, ncode)) + kWarpTrialWarps * warp_trial_warp_bytes(NM, zc);
+__host__ __device__ inline size_t warp_trial_smem_bytes(int NM, int ncode, int zc, bool mats = true) {
+  return align16(4 * warp_trial_const_floats(NM, ncode)) + kWarpTrialWarps * warp_trial_warp_bytes(NM, zc, mats);
 }
 
 __device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
@@ -658,9 +660,136 @@ __device__ __forceinline__ void sites_warp_cat(const TrialCtx &c, const TrialSme
   cp_async_wait<0>();  // drain the copies issued past the end
 }
 
+// The CAT model in the eigenbasis: every category shares the rate matrix's
+// eigenvectors, so the windows are stored as eigen-coordinates (one plane,
+// the layout of k_eigen_glvs_dna) and a site's category enters only through
+// three exp factors per window and three r lambda scalings, read from the
+// warp's 12-float table of the category (Tc: exp(r lambda_k dist),
+// exp(r lambda_k prox), r lambda_k for the three non-zero eigenvalues in
+// eig_ord order) -- 3 shared loads per site instead of the 24 of six 4x4
+// matrices, and tables small enough for more warps per SM.
+__device__ __forceinline__ void cat_eig_tables(const TrialCtx &c, const TrialSmem &sm, int NM, int lane) {
+  constexpr int K = 4;
+  const int o1 = (c.eig_ord >> 8) & 255, o2 = (c.eig_ord >> 16) & 255, o3 = (c.eig_ord >> 24) & 255;
+  for (int it = lane; it < 12 * NM; it += 32) {
+    const int cat = it / 12, j = it - cat * 12, g = j / 3, kk = j - g * 3;
+    const int o = kk == 0 ? o1 : (kk == 1 ? o2 : o3);
+    sm.Tc[it] = g == 0 ? sm.E[cat * K + o] : (g == 1 ? sm.E[(NM + cat) * K + o] : (g == 2 ? sm.Lr[cat * K + o] : 0.f));
+  }
+}
+
+template <bool DER>
+__device__ __forceinline__ void sites_warp_cat_eig(const TrialCtx &c, const TrialSmem &sm, float4 *ring, int q,
+                                                   int node, int Sq, int lane, SiteAcc &acc) {
+  constexpr int K = 4;
+  const int zc = c.zcodes;
+  int ord[3];
+  ord[0] = (c.eig_ord >> 8) & 255; ord[1] = (c.eig_ord >> 16) & 255; ord[2] = (c.eig_ord >> 24) & 255;
+  float xr[4][3];
+#pragma unroll
+  for (int k = 0; k < 3; k++)
+#pragma unroll
+    for (int i = 0; i < 4; i++) xr[i][k] = sm.X[i * K + ord[k]];
+  const float *gd = c.darr_e + (long)node * c.S * K;
+  const float *gp = c.parr_e + (long)node * c.S * K;
+  const uint32_t *rc = c.rcode + (long)q * c.S;
+  const int last = Sq - 1;
+  // byte k of cq / kq: the character / category of the k-th next iteration
+  unsigned long long cq = 0ull, kq = 0ull;
+  auto issue = [&](int stage, uint32_t pk) {
+    const long col = (long)((pk >> 8) & 0xffffu);
+    cp_async16(ring + (stage * 32 + lane), gd + col * K);
+    cp_async16(ring + ((kWarpRing + stage) * 32 + lane), gp + col * K);
+    cp_async_commit();
+  };
+#pragma unroll
+  for (int j = 0; j < kWarpRing - 1; j++) {
+    const uint32_t pk = rc[min(j * 32 + lane, last)];
+    issue(j, pk);
+    cq |= (unsigned long long)(pk & 255u) << (8 * j);
+    kq |= (unsigned long long)(pk >> 24) << (8 * j);
+  }
+  uint32_t pk_next = rc[min((kWarpRing - 1) * 32 + lane, last)];
+  uint32_t pk_next2 = rc[min(kWarpRing * 32 + lane, last)];
+  int st = 0;
+  for (int base = 0; base < Sq; base += 32) {
+    issue((st + kWarpRing - 1) & (kWarpRing - 1), pk_next);
+    cq |= (unsigned long long)(pk_next & 255u) << (8 * (kWarpRing - 1));
+    kq |= (unsigned long long)(pk_next >> 24) << (8 * (kWarpRing - 1));
+    const int code = (int)(cq & 255ull), cat = (int)(kq & 255ull);
+    cq >>= 8;
+    kq >>= 8;
+    pk_next = pk_next2;
+    pk_next2 = rc[min(base + 32 + kWarpRing * 32 + lane, last)];
+    cp_async_wait<kWarpRing - 1>();  // this iteration's copies have landed
+    const float4 dcur = ring[st * 32 + lane];
+    const float4 pcur = ring[(kWarpRing + st) * 32 + lane];
+    st = (st + 1) & (kWarpRing - 1);
+    const float4 t0 = *reinterpret_cast<const float4 *>(sm.Tc + cat * 12);
+    const float4 t1 = *reinterpret_cast<const float4 *>(sm.Tc + cat * 12 + 4);
+    const float ed[3] = {t0.x, t0.y, t0.z}, ep[3] = {t0.w, t1.x, t1.y};
+    const float4 Z4 = *reinterpret_cast<const float4 *>(sm.Z + (cat * zc + code) * K);
+    const float z[4] = {Z4.x, Z4.y, Z4.z, Z4.w};
+    float z1[4], z2[4], lr[3];
+    if (DER) {
+      const float4 t2 = *reinterpret_cast<const float4 *>(sm.Tc + cat * 12 + 8);
+      lr[0] = t1.z; lr[1] = t1.w; lr[2] = t2.x;
+      const float4 a = *reinterpret_cast<const float4 *>(sm.Z1 + (cat * zc + code) * K);
+      const float4 b = *reinterpret_cast<const float4 *>(sm.Z2 + (cat * zc + code) * K);
+      z1[0] = a.x; z1[1] = a.y; z1[2] = a.z; z1[3] = a.w;
+      z2[0] = b.x; z2[1] = b.y; z2[2] = b.z; z2[3] = b.w;
+    }
+    const float dv[3] = {dcur.y, dcur.z, dcur.w}, pv[3] = {pcur.y, pcur.z, pcur.w};
+    float ud[3], wp[3], ud1[3], ud2[3], wp1[3], wp2[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      ud[k] = ed[k] * dv[k];
+      wp[k] = ep[k] * pv[k];
+      if (DER) {
+        ud1[k] = lr[k] * ud[k];
+        ud2[k] = lr[k] * ud1[k];
+        wp1[k] = lr[k] * wp[k];
+        wp2[k] = lr[k] * wp1[k];
+      }
+    }
+    float v[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+    for (int ii = 0; ii < 4; ii++) {
+      float x = dcur.x, y = pcur.x;
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        x = fmaf(xr[ii][k], ud[k], x);
+        y = fmaf(xr[ii][k], wp[k], y);
+      }
+      const float xy = x * y;
+      v[0] = fmaf(z[ii], xy, v[0]);
+      if (DER) {
+        float x1 = xr[ii][0] * ud1[0], x2 = xr[ii][0] * ud2[0], y1 = xr[ii][0] * wp1[0], y2 = xr[ii][0] * wp2[0];
+#pragma unroll
+        for (int k = 1; k < 3; k++) {
+          x1 = fmaf(xr[ii][k], ud1[k], x1);
+          x2 = fmaf(xr[ii][k], ud2[k], x2);
+          y1 = fmaf(xr[ii][k], wp1[k], y1);
+          y2 = fmaf(xr[ii][k], wp2[k], y2);
+        }
+        const float aa = x1 * y - x * y1;
+        const float bb = x2 * y - 2.f * x1 * y1 + x * y2;
+        v[1] = fmaf(z[ii], aa, v[1]);
+        v[2] = fmaf(z[ii], bb, v[2]);
+        v[3] = fmaf(z1[ii], xy, v[3]);
+        v[4] = fmaf(z2[ii], xy, v[4]);
+        v[5] = fmaf(z1[ii], aa, v[5]);
+      }
+    }
+    if (base + lane < Sq) acc.add(v[0], v[1], v[2], v[3], v[4], v[5], DER);
+  }
+  cp_async_wait<0>();  // drain the copies issued past the end
+}
+
 // Per-CTA constants and this warp's tables and ring; returns after a block
 // barrier, the only one the warp kernels take.
-__device__ __forceinline__ void warp_trial_setup(const TrialCtx &c, char *t_smem, TrialSmem &sm, float4 *&ring) {
+__device__ __forceinline__ void warp_trial_setup(const TrialCtx &c, char *t_smem, TrialSmem &sm, float4 *&ring,
+                                                 bool mats = true) {
   constexpr int K = 4;
   const int tid = threadIdx.x, warp = tid >> 5;
   const int NM = c.NM, nc = c.ncode;
@@ -678,14 +807,20 @@ __device__ __forceinline__ void warp_trial_setup(const TrialCtx &c, char *t_smem
   for (int i = tid; i < NM * K; i += blockDim.x) sm.Lr[i] = c.rates[i / K] * c.lam[i % K];
   if (tid < K) sm.statd[tid] = c.statd[tid];
   const int zc = c.zcodes;
-  char *wb = t_smem + align16(4 * warp_trial_const_floats(NM, nc)) + warp * warp_trial_warp_bytes(NM, zc);
+  char *wb = t_smem + align16(4 * warp_trial_const_floats(NM, nc)) + warp * warp_trial_warp_bytes(NM, zc, mats);
   float *tb = reinterpret_cast<float *>(wb);
-  ring = reinterpret_cast<float4 *>(wb + align16(4 * warp_trial_table_floats(NM, zc)));
-  sm.opt = wb + align16(4 * warp_trial_table_floats(NM, zc)) + 2 * kWarpRing * 32 * 16;
+  ring = reinterpret_cast<float4 *>(wb + align16(4 * warp_trial_table_floats(NM, zc, mats)));
+  sm.opt = wb + align16(4 * warp_trial_table_floats(NM, zc, mats)) + 2 * kWarpRing * 32 * 16;
   const int mb = NM * 16, zb = NM * zc * K;
-  sm.Md = tb; sm.Mp = tb + mb; sm.Md1 = tb + 2 * mb; sm.Md2 = tb + 3 * mb; sm.Mp1 = tb + 4 * mb;
-  sm.Mp2 = tb + 5 * mb;
-  sm.Z = tb + 6 * mb; sm.Z1 = sm.Z + zb; sm.Z2 = sm.Z1 + zb;
+  if (mats) {
+    sm.Md = tb; sm.Mp = tb + mb; sm.Md1 = tb + 2 * mb; sm.Md2 = tb + 3 * mb; sm.Mp1 = tb + 4 * mb;
+    sm.Mp2 = tb + 5 * mb;
+    sm.Z = tb + 6 * mb;
+  } else {
+    sm.Tc = tb;
+    sm.Z = tb + 12 * NM;
+  }
+  sm.Z1 = sm.Z + zb; sm.Z2 = sm.Z1 + zb;
   sm.E = sm.Z2 + zb; sm.Em1 = sm.E + 3 * NM * K;
   __syncthreads();
 }
@@ -769,11 +904,15 @@ __device__ TrialRes trial_warp(const TrialCtx &c, const TrialSmem &sm, float4 *r
     trial_exps(sm, NM, K, ctl, lane, 32);
     __syncwarp();
     trial_tables(sm, sm.W, NM, c.zcodes, ncz, K, derivs, lane, 32, !EIG);  // Z rows of stride zcodes
+    if (CAT && EIG) cat_eig_tables(c, sm, NM, lane);
     __syncwarp();
     SiteAcc acc;
     acc.init();
     if (Sq > 0) {
-      if (CAT) {
+      if (CAT && EIG) {
+        if (derivs) sites_warp_cat_eig<true>(c, sm, ring, q, node, Sq, lane, acc);
+        else sites_warp_cat_eig<false>(c, sm, ring, q, node, Sq, lane, acc);
+      } else if (CAT) {
         if (derivs) sites_warp_cat<true>(c, sm, ring, q, node, Sq, lane, acc);
         else sites_warp_cat<false>(c, sm, ring, q, node, Sq, lane, acc);
       } else if (EIG == 2) {
