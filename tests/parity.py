@@ -132,15 +132,23 @@ def compare(O, oref, seqs, res_gpu, res_orc, keep_at_most=7, keep_factor=0.01, d
         if not newton:
             # the Brent replica ranks stage-2 results of the reference's own
             # search: its kept set is the oracle's, up to near-ties at a
-            # keep boundary
+            # keep boundary, and up to the oracle's stage-2 Brent stopping
+            # short of an edge the GPU keeps (the same search on FP32
+            # likelihoods can stop elsewhere on a long query)
             o_min = min(Ls[e] for e in oset)
             for e in set(gset) ^ set(oset):
                 other_min = o_min if e in gset else g_min
                 other_n = len(oset) if e in gset else len(gset)
                 bounds = [thr] + ([other_min] if other_n >= keep_at_most else [])
                 st["gpu_only" if e in gset else "oracle_only"] += 1
-                if min(abs(Ls[e] - b) for b in bounds) > delta_keep:
-                    bad.append("q%d: edge %d (polished %.4f) kept by one side only" % (q, e, Ls[e]))
+                if min(abs(Ls[e] - b) for b in bounds) <= delta_keep:
+                    continue
+                s2 = oracle_stage2(q) if (oracle_stage2 and e in gset) else None
+                if s2 is not None and e in s2 and s2[e] < Ls[e] - delta_keep:
+                    st["gpu_only_oracle_brent_short"] += 1
+                    st["max_oracle_stage2_shortfall"] = max(st["max_oracle_stage2_shortfall"], Ls[e] - s2[e])
+                    continue
+                bad.append("q%d: edge %d (polished %.4f) kept by one side only" % (q, e, Ls[e]))
         # the GPU's keep decisions, judged on the polished optima: every kept
         # edge clears the keep_factor threshold, and an edge only the oracle
         # keeps lies below that threshold or below the GPU's weakest kept
