@@ -328,23 +328,30 @@ typedef struct {
 pgb_status pgb_queries_trials(pgb_engine *e, const pgb_prefs *prefs, int optimizer, int mode, int n_trials,
                               const pgb_trial *trials, pgb_trial_out *out);
 
-/* Autotuner of the stage-2 trial kernel.  Nucleotide models whose Gamma
- * mixture has 1, 2, 4 or 8 rates always use the whole-query warp kernel (one
- * warp runs a query's baseball trials, keep and refinement); autotune sets
- * that and returns.  For the other models (CAT, which also has a warp form,
- * and 20 states): for each of the 6 query-length bins
- * (<= 256, 512, 768, 1024, 1536 informative sites, longer; 128, 256, 384,
- * 512, 640 for 20 states and CAT), time one CTA of
- * 128 or 256 threads per trial with the query's sites of darr / parr staged
- * in shared memory or read from L2, and for 20-state Gamma mixtures the
- * tensor-core CTA (tcgen05 evolves, 128 threads), on the loaded queries'
- * first baseball round; then time the whole round for that choice and for
- * each uniform form, and keep the fastest one with a single CTA size in every
- * bin for later runs.  get_tuning reports the table (threads[6],
- * smem_windows[6]); set_tuning imposes one (threads 1 = tensor-core CTA, 32,
- * 128 or 256; smem_windows 0 or 1).  When every bin has the same threads,
- * pgb_queries_run places whole queries in one persistent launch (a warp, a
- * tensor-core CTA or a CTA per query, windows as bin 0 says); otherwise it
+/* Autotuner of the stage-2 trial kernel, timed on whole placement runs of
+ * the loaded queries.  Nucleotide models whose Gamma mixture has 1, 2, 4 or
+ * 8 rates use the whole-query warp kernel (one warp runs a query's baseball
+ * trials, keep and refinement) in one of six forms, which autotune times and
+ * picks from: 0 the transition matrices in registers (8 warps per SM); 1, 2,
+ * 3 the eigenbasis form (eigen-coordinate windows) at 8, 12 and 16 warps per
+ * SM; 4, 5 the eigenbasis form on packed FP32 pairs at 12 and 16 (the
+ * default is 4).  For the other models (CAT and 20 states): for each of the
+ * 6 query-length bins (<= 256, 512, 768, 1024, 1536 informative sites,
+ * longer; 128, 256, 384, 512, 640 for 20 states and CAT), time the warp form
+ * (CAT), one CTA of 128 or 256 threads per trial with the query's sites of
+ * darr / parr staged in shared memory or read from L2, and for 20-state
+ * Gamma mixtures the tensor-core team (tcgen05 evolves), on the loaded
+ * queries' first baseball round; then time the whole round for that choice
+ * and for each uniform form, keep the fastest one with a single CTA size in
+ * every bin, and for a CAT warp choice time its two forms (0 matrices per
+ * category, 1 the eigenbasis, the default).  get_tuning reports the table
+ * (threads[6], smem_windows[6]: for a warp bin the form); set_tuning imposes
+ * one (threads 1 = tensor-core team, 32, 128 or 256; smem_windows 0 or 1,
+ * or 0 .. 5 for the nucleotide Gamma warp forms).  When every bin has the
+ * same threads, pgb_queries_run places whole queries in one persistent
+ * launch (a warp, a tensor-core team or a CTA per query, windows as bin 0
+ * says) -- except every-edge runs (max_strikes 0) of fewer queries than the
+ * GPU has trial warps, which run all their trials as one batch; otherwise it
  * runs the baseball in speculative rounds of per-trial CTAs.  Where the warp
  * or tensor-core form does not apply it falls back to 256.  20-state Gamma
  * mixtures start with the tensor-core form.  No reference counterpart:
