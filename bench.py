@@ -173,7 +173,8 @@ def stage2_kernel(w, tune):
                 "then the refinement trials)")
     if th == {32}:
         return "k_place_warp (stage 2 + refinement, whole queries, one warp each%s)" % (
-            ", per-site categories, %s form" % ("eigenbasis" if int(tune[1][0]) == 1 else "matrix")
+            ", per-site categories, %s form" % {0: "matrix", 1: "eigenbasis", 2: "eigenbasis on packed FP32 pairs"}[
+                int(tune[1][0])]
             if w.site_cats is not None else
             ", %s form%s, %d warps per SM" % (warp_form(w, tune), " on packed FP32 pairs" if int(tune[1][0]) >= 4 else "",
                                              WARP_FORM_WARPS[int(tune[1][0])]))
@@ -416,7 +417,7 @@ def run_ours(args):
     # derivatives), against 128 lanes per SM; CAT runs the matrix arithmetic
     # on its one plane, the 20-state tensor-core form has no such count
     cat_warp = w.site_cats is not None and set(int(v) for v in tune[0]) == {32}
-    form = warp_form(w, tune) or ((("CAT eigenbasis" if int(tune[1][0]) == 1 else "matrix")) if cat_warp else None)
+    form = warp_form(w, tune) or ((("CAT eigenbasis" if int(tune[1][0]) >= 1 else "matrix")) if cat_warp else None)
     fp32_ops = (FMA_OPS_PER_SITE_RATE[form] * R * site_evals / args.steps / t_trials
                 if form and t_trials > 0 else None)
     fp32_peak = 128 * N_SM * SM_MAX_HZ

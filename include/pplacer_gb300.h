@@ -343,11 +343,12 @@ pgb_status pgb_queries_trials(pgb_engine *e, const pgb_prefs *prefs, int optimiz
  * Gamma mixtures the tensor-core team (tcgen05 evolves), on the loaded
  * queries' first baseball round; then time the whole round for that choice
  * and for each uniform form, keep the fastest one with a single CTA size in
- * every bin, and for a CAT warp choice time its two forms (0 matrices per
- * category, 1 the eigenbasis, the default).  get_tuning reports the table
- * (threads[6], smem_windows[6]: for a warp bin the form); set_tuning imposes
- * one (threads 1 = tensor-core team, 32, 128 or 256; smem_windows 0 or 1,
- * or 0 .. 5 for the nucleotide Gamma warp forms).  When every bin has the
+ * every bin, and for a CAT warp choice time its three forms (0 matrices per
+ * category, 1 the eigenbasis, 2 the eigenbasis on packed FP32 pairs, the
+ * default).  get_tuning reports the table (threads[6], smem_windows[6]: for a
+ * warp bin the form); set_tuning imposes one (threads 1 = tensor-core team,
+ * 32, 128 or 256; smem_windows 0 or 1, 0 .. 5 for the nucleotide Gamma warp
+ * forms, 0 .. 2 for the CAT warp forms).  When every bin has the
  * same threads, pgb_queries_run places whole queries in one persistent
  * launch (a warp, a tensor-core team or a CTA per query, windows as bin 0
  * says) -- except every-edge runs (max_strikes 0) of fewer queries than the

@@ -1612,7 +1612,7 @@ bool warp_eig_ok(const pgb_engine *e) { return warp_trials_ok(e) && e->eig_ok; }
 // the permuted and premultiplied layout of k_eigen_glvs_dna).
 pgb_status ensure_eigen_glvs(pgb_engine *e) {
   const bool tc = tc_trials_ok(e),
-             dna = (warp_eig_ok(e) && e->warp_variant != 0) || (warp_cat_ok(e) && e->eig_ok && e->warp_variant == 1);
+             dna = (warp_eig_ok(e) && e->warp_variant != 0) || (warp_cat_ok(e) && e->eig_ok && e->warp_variant != 0);
   if (e->eig_ready || (!tc && !dna)) return PGB_OK;
   const long rows = (long)e->n_nodes * e->S * e->RP;
   pgb_status s;
@@ -1884,6 +1884,9 @@ pgb_status launch_place_warp_rp(pgb_engine *e, TrialCtx c, const PlaceCtx &pc) {
 // 16 warps per SM (255, 168 and 128 registers); 4, 5 the eigenbasis on
 // packed FP32 pairs at 12 and 16 warps per SM.
 constexpr int kWarpForms = 6;
+// The CAT warp forms: 0 matrices per category, 1 the eigenbasis, 2 the
+// eigenbasis on packed FP32 pairs.
+constexpr int kCatForms = 3;
 constexpr int kCatEigMinCtas = 12;  // the CAT eigenbasis form: one-warp CTAs per SM it aims for
 template <int RP>
 pgb_status launch_place_warp_gmix(pgb_engine *e, TrialCtx c, const PlaceCtx &pc) {
@@ -1990,9 +1993,10 @@ pgb_status run_whole_queries(pgb_engine *e, const pgb_prefs *p, const BBCtx &c, 
   if (tc.pp_rule == 1) s = launch_place_cta(e, tc, pc, max_sq);  // the CTA kernels carry the QNG replica
   else if (e->tune_threads[0] == kTuneTc && tc_trials_ok(e)) s = launch_place_tc(e, tc, pc, max_sq);
   else if (e->tune_threads[0] != 32 || !warp_form_ok(e)) s = launch_place_cta(e, tc, pc, max_sq);
-  else if (e->gcat)  // the CAT forms: 0 matrices per category, 1 the eigenbasis
-    s = e->warp_variant == 1 && e->eig_ok ? launch_place_warp_rp<1, true, 1, kCatEigMinCtas>(e, tc, pc)
-                                          : launch_place_warp_rp<1, true>(e, tc, pc);
+  else if (e->gcat)  // the CAT forms: 0 matrices per category, 1 the eigenbasis, 2 on packed FP32 pairs
+    s = e->warp_variant == 1 && e->eig_ok   ? launch_place_warp_rp<1, true, 1, kCatEigMinCtas>(e, tc, pc)
+        : e->warp_variant == 2 && e->eig_ok ? launch_place_warp_rp<1, true, 2, kCatEigMinCtas>(e, tc, pc)
+                                            : launch_place_warp_rp<1, true>(e, tc, pc);
   else
     switch (e->RP) {
       case 1: s = launch_place_warp_gmix<1>(e, tc, pc); break;
@@ -2116,8 +2120,9 @@ pgb_status pgb_engine_create(const pgb_model_desc *m, const pgb_tree_desc *t, pg
       e->eig_ok = true;
       e->eig_ord = ord;
       // until the autotuner says otherwise: the eigenbasis form on packed FP32
-      // pairs at 12 warps per SM (Gamma mixtures), the CAT eigenbasis form
-      e->warp_variant = e->gcat ? 1 : 4;
+      // pairs at 12 warps per SM (Gamma mixtures), the CAT eigenbasis form on
+      // packed FP32 pairs
+      e->warp_variant = e->gcat ? 2 : 4;
       double mean = 0;
       for (int i = 0; i < K; i++) mean += e->X[i * K + kz];
       e->eig_c0 = mean / K;
@@ -2896,10 +2901,11 @@ pgb_status pgb_engine_autotune(pgb_engine *e, const pgb_prefs *p) {
     e->tune_win[b] = best_cfg < 0 ? per_bin_w[b] : uni_w[best_cfg];
   }
   if (best_cfg == 0 && warp_cat_ok(e) && e->eig_ok) {
-    // the CAT warp form: its matrix and eigenbasis variants on whole runs
+    // the CAT warp form: its matrix, eigenbasis and packed eigenbasis
+    // variants on whole runs
     float bf = 1e30f;
     int bv = 0;
-    for (int v = 0; v < 2; v++) {
+    for (int v = 0; v < kCatForms; v++) {
       if (v != e->warp_variant) { e->warp_variant = v; e->eig_ready = false; }
       float ms_best = 1e30f;
       for (int rep = 0; rep < 2; rep++) {
@@ -2918,7 +2924,7 @@ pgb_status pgb_engine_get_tuning(pgb_engine *e, int *threads, int *smem_windows)
   for (int b = 0; b < kBins; b++) {
     threads[b] = e->tune_threads[b];
     smem_windows[b] = e->tune_threads[b] == 32 && (warp_trials_ok(e) || warp_cat_ok(e))
-                          ? (warp_trials_ok(e) ? e->warp_variant : (e->warp_variant == 1 ? 1 : 0))
+                          ? e->warp_variant
                           : e->tune_win[b];
   }
   return PGB_OK;
@@ -2929,15 +2935,18 @@ pgb_status pgb_engine_set_tuning(pgb_engine *e, const int *threads, const int *s
   const bool warp_forms = warp_trials_ok(e);
   for (int b = 0; b < kBins; b++) {
     const bool wf = threads[b] == 32 && warp_forms;  // smem_windows selects the warp form
+    const bool cf = threads[b] == 32 && warp_cat_ok(e);  // ... or the CAT warp form
     if ((threads[b] != 32 && threads[b] != kTuneTc && threads[b] != 128 && threads[b] != 256) ||
-        (!wf && (smem_windows[b] & ~1)) || (wf && (smem_windows[b] < 0 || smem_windows[b] >= kWarpForms)) ||
+        (!wf && !cf && (smem_windows[b] & ~1)) || (wf && (smem_windows[b] < 0 || smem_windows[b] >= kWarpForms)) ||
+        (cf && (smem_windows[b] < 0 || smem_windows[b] >= kCatForms)) ||
         (wf && smem_windows[b] > 0 && !warp_eig_ok(e))) {
       set_error("set_tuning: bin %d: threads must be 1, 32, 128 or 256 and smem_windows 0 or 1 (for the "
-                "nucleotide Gamma warp form 0 .. 5 where the eigenbasis forms apply)", b);
+                "nucleotide Gamma warp form 0 .. 5 where the eigenbasis forms apply, for the CAT warp "
+                "form 0 .. 2)", b);
       return PGB_ERR_ARG;
     }
   }
-  if (threads[0] == 32 && warp_cat_ok(e) && smem_windows[0] == 1 && !e->eig_ok) {
+  if (threads[0] == 32 && warp_cat_ok(e) && smem_windows[0] != 0 && !e->eig_ok) {
     set_error("set_tuning: the CAT eigenbasis form needs a rate matrix with one zero eigenvalue");
     return PGB_ERR_ARG;
   }
@@ -2946,7 +2955,8 @@ pgb_status pgb_engine_set_tuning(pgb_engine *e, const int *threads, const int *s
     e->tune_win[b] = threads[b] == 32 && (warp_forms || warp_cat_ok(e)) ? 0 : smem_windows[b];
   }
   // smem_windows of a warp bin selects the form: the nucleotide Gamma forms
-  // 0 .. 5, or the CAT form (0 matrices per category, 1 the eigenbasis)
+  // 0 .. 5, or the CAT form (0 matrices per category, 1 the eigenbasis, 2
+  // the eigenbasis on packed FP32 pairs)
   const bool cat_forms = warp_cat_ok(e);
   if (threads[0] == 32 && (warp_forms || cat_forms) && smem_windows[0] != e->warp_variant) {
     e->warp_variant = smem_windows[0];

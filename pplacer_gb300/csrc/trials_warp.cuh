@@ -786,6 +786,127 @@ __device__ __forceinline__ void sites_warp_cat_eig(const TrialCtx &c, const Tria
   cp_async_wait<0>();  // drain the copies issued past the end
 }
 
+// The CAT eigenbasis form on packed FP32 pairs: the arithmetic of
+// sites_warp_cat_eig with two states of the site per fma.rn.f32x2 (X's
+// columns paired across the states, the site's scaled eigen-coordinates
+// duplicated into both halves, the proximal first derivative formed
+// negated as in sites_warp_eig2).
+template <bool DER>
+__device__ __forceinline__ void sites_warp_cat_eig2(const TrialCtx &c, const TrialSmem &sm, float4 *ring, int q,
+                                                    int node, int Sq, int lane, SiteAcc &acc) {
+  constexpr int K = 4;
+  const int zc = c.zcodes;
+  int ord[3];
+  ord[0] = (c.eig_ord >> 8) & 255; ord[1] = (c.eig_ord >> 16) & 255; ord[2] = (c.eig_ord >> 24) & 255;
+  float2 xp[2][3];
+#pragma unroll
+  for (int k = 0; k < 3; k++)
+#pragma unroll
+    for (int h = 0; h < 2; h++) xp[h][k] = make_float2(sm.X[(2 * h) * K + ord[k]], sm.X[(2 * h + 1) * K + ord[k]]);
+  const float *gd = c.darr_e + (long)node * c.S * K;
+  const float *gp = c.parr_e + (long)node * c.S * K;
+  const uint32_t *rc = c.rcode + (long)q * c.S;
+  const int last = Sq - 1;
+  unsigned long long cq = 0ull, kq = 0ull;
+  auto issue = [&](int stage, uint32_t pk) {
+    const long col = (long)((pk >> 8) & 0xffffu);
+    cp_async16(ring + (stage * 32 + lane), gd + col * K);
+    cp_async16(ring + ((kWarpRing + stage) * 32 + lane), gp + col * K);
+    cp_async_commit();
+  };
+#pragma unroll
+  for (int j = 0; j < kWarpRing - 1; j++) {
+    const uint32_t pk = rc[min(j * 32 + lane, last)];
+    issue(j, pk);
+    cq |= (unsigned long long)(pk & 255u) << (8 * j);
+    kq |= (unsigned long long)(pk >> 24) << (8 * j);
+  }
+  uint32_t pk_next = rc[min((kWarpRing - 1) * 32 + lane, last)];
+  uint32_t pk_next2 = rc[min(kWarpRing * 32 + lane, last)];
+  int st = 0;
+  for (int base = 0; base < Sq; base += 32) {
+    issue((st + kWarpRing - 1) & (kWarpRing - 1), pk_next);
+    cq |= (unsigned long long)(pk_next & 255u) << (8 * (kWarpRing - 1));
+    kq |= (unsigned long long)(pk_next >> 24) << (8 * (kWarpRing - 1));
+    const int code = (int)(cq & 255ull), cat = (int)(kq & 255ull);
+    cq >>= 8;
+    kq >>= 8;
+    pk_next = pk_next2;
+    pk_next2 = rc[min(base + 32 + kWarpRing * 32 + lane, last)];
+    cp_async_wait<kWarpRing - 1>();  // this iteration's copies have landed
+    const float4 dcur = ring[st * 32 + lane];
+    const float4 pcur = ring[(kWarpRing + st) * 32 + lane];
+    st = (st + 1) & (kWarpRing - 1);
+    const float4 t0 = *reinterpret_cast<const float4 *>(sm.Tc + cat * 12);
+    const float4 t1 = *reinterpret_cast<const float4 *>(sm.Tc + cat * 12 + 4);
+    const float ed[3] = {t0.x, t0.y, t0.z}, ep[3] = {t0.w, t1.x, t1.y};
+    const float4 Z4 = *reinterpret_cast<const float4 *>(sm.Z + (cat * zc + code) * K);
+    const float2 zz[2] = {make_float2(Z4.x, Z4.y), make_float2(Z4.z, Z4.w)};
+    float2 z1p[2], z2p[2];
+    float lr[3];
+    if (DER) {
+      const float4 t2 = *reinterpret_cast<const float4 *>(sm.Tc + cat * 12 + 8);
+      lr[0] = t1.z; lr[1] = t1.w; lr[2] = t2.x;
+      const float4 a = *reinterpret_cast<const float4 *>(sm.Z1 + (cat * zc + code) * K);
+      const float4 b = *reinterpret_cast<const float4 *>(sm.Z2 + (cat * zc + code) * K);
+      z1p[0] = make_float2(a.x, a.y); z1p[1] = make_float2(a.z, a.w);
+      z2p[0] = make_float2(b.x, b.y); z2p[1] = make_float2(b.z, b.w);
+    }
+    const float dv[3] = {dcur.y, dcur.z, dcur.w}, pv[3] = {pcur.y, pcur.z, pcur.w};
+    float2 ud[3], wp[3], ud1[3], ud2[3], wn1[3], wp2[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      const float u = ed[k] * dv[k], w = ep[k] * pv[k];
+      ud[k] = make_float2(u, u);
+      wp[k] = make_float2(w, w);
+      if (DER) {
+        const float u1 = lr[k] * u, w1 = lr[k] * w;
+        const float u2 = lr[k] * u1, w2 = lr[k] * w1;
+        ud1[k] = make_float2(u1, u1);
+        ud2[k] = make_float2(u2, u2);
+        wn1[k] = make_float2(-w1, -w1);
+        wp2[k] = make_float2(w2, w2);
+      }
+    }
+    float2 V[6];
+#pragma unroll
+    for (int k = 0; k < 6; k++) V[k] = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      float2 X = make_float2(dcur.x, dcur.x), Y = make_float2(pcur.x, pcur.x);
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        X = __ffma2_rn(xp[h][k], ud[k], X);
+        Y = __ffma2_rn(xp[h][k], wp[k], Y);
+      }
+      const float2 XY = __fmul2_rn(X, Y);
+      V[0] = __ffma2_rn(zz[h], XY, V[0]);
+      if (DER) {
+        float2 X1 = __fmul2_rn(xp[h][0], ud1[0]), X2 = __fmul2_rn(xp[h][0], ud2[0]);
+        float2 Y1n = __fmul2_rn(xp[h][0], wn1[0]), Y2 = __fmul2_rn(xp[h][0], wp2[0]);
+#pragma unroll
+        for (int k = 1; k < 3; k++) {
+          X1 = __ffma2_rn(xp[h][k], ud1[k], X1);
+          X2 = __ffma2_rn(xp[h][k], ud2[k], X2);
+          Y1n = __ffma2_rn(xp[h][k], wn1[k], Y1n);
+          Y2 = __ffma2_rn(xp[h][k], wp2[k], Y2);
+        }
+        const float2 AA = __ffma2_rn(X, Y1n, __fmul2_rn(X1, Y));
+        const float2 BB = __ffma2_rn(X, Y2, __ffma2_rn(X1, __fadd2_rn(Y1n, Y1n), __fmul2_rn(X2, Y)));
+        V[1] = __ffma2_rn(zz[h], AA, V[1]);
+        V[2] = __ffma2_rn(zz[h], BB, V[2]);
+        V[3] = __ffma2_rn(z1p[h], XY, V[3]);
+        V[4] = __ffma2_rn(z2p[h], XY, V[4]);
+        V[5] = __ffma2_rn(z1p[h], AA, V[5]);
+      }
+    }
+    if (base + lane < Sq)
+      acc.add(V[0].x + V[0].y, V[1].x + V[1].y, V[2].x + V[2].y, V[3].x + V[3].y, V[4].x + V[4].y,
+              V[5].x + V[5].y, DER);
+  }
+  cp_async_wait<0>();  // drain the copies issued past the end
+}
+
 // Per-CTA constants and this warp's tables and ring; returns after a block
 // barrier, the only one the warp kernels take.
 __device__ __forceinline__ void warp_trial_setup(const TrialCtx &c, char *t_smem, TrialSmem &sm, float4 *&ring,
@@ -909,7 +1030,10 @@ __device__ TrialRes trial_warp(const TrialCtx &c, const TrialSmem &sm, float4 *r
     SiteAcc acc;
     acc.init();
     if (Sq > 0) {
-      if (CAT && EIG) {
+      if (CAT && EIG == 2) {
+        if (derivs) sites_warp_cat_eig2<true>(c, sm, ring, q, node, Sq, lane, acc);
+        else sites_warp_cat_eig2<false>(c, sm, ring, q, node, Sq, lane, acc);
+      } else if (CAT && EIG) {
         if (derivs) sites_warp_cat_eig<true>(c, sm, ring, q, node, Sq, lane, acc);
         else sites_warp_cat_eig<false>(c, sm, ring, q, node, Sq, lane, acc);
       } else if (CAT) {

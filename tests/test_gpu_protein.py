@@ -154,13 +154,14 @@ def test_round_based_path(oracle_lib):
     _check_pp(O, oref, w, res, prior, None)
 
 
-@pytest.mark.parametrize("form", [(32, 0), (32, 1), (128, 1)], ids=["warp", "warp_eig", "cta"])
+@pytest.mark.parametrize("form", [(32, 0), (32, 1), (32, 2), (128, 1)], ids=["warp", "warp_eig", "warp_eig2", "cta"])
 def test_cat_forms(oracle_lib, form):
     """Per-site CAT placements in the whole-query warp forms (sites_warp_cat:
     each lane's site reads its category's matrices; sites_warp_cat_eig: the
-    eigenbasis, each site's category entering through its exp factors) and
-    the whole-query CTA form, against the oracle; queries long enough to span
-    many categories."""
+    eigenbasis, each site's category entering through its exp factors;
+    sites_warp_cat_eig2: the same on packed FP32 pairs) and the whole-query
+    CTA form, against the oracle; queries long enough to span many
+    categories."""
     from pplacer_gb300 import engine as E
     from pplacer_gb300 import synth
     O = oracle_lib
