@@ -476,7 +476,8 @@ def run_ours(args):
         "cpu_baseline": {"value": cpu_v, "unit": "placements/s", "cores": cpu_threads, "kind": "port",
                          "sample": "%d queries of %s (%.1f s)" % (cpu_n, args.workload, cpu_dt)},
         "e2e": {"value": e2e, "unit": "placements/s", "h2d_bytes_per_step": Q * S,
-                "d2h_bytes_per_step": Q * kam * C.sizeof(L.Placement) + 8 * Q},
+                "d2h_bytes_per_step": Q * kam * C.sizeof(L.Placement) + 8 * Q,
+                "device_batch": args.batch if args.batch else "automatic"},
         "brent_replica": brent,
         "with_posterior_probabilities": pp,
         "newton_evals_per_trial": counts[2] / counts[1] if counts[1] else None,
