@@ -71,6 +71,8 @@ def parse():
                     help="queries placed by pplacer's flow over the plain per-call drop-in (untimed region)")
     ap.add_argument("--batch", type=int, default=0,
                     help="device batch of the end-to-end pgb_place_batch calls (0: automatic)")
+    ap.add_argument("--precompute-steps", type=int, default=2,
+                    help="untimed-region comparison: reference-tree precomputes (and CAT category refinements)")
     return ap.parse_args()
 
 
@@ -213,11 +215,26 @@ def cpu_baseline(w, n_sample, prefs_kw):
     O.build(with_ref=True)
     n = min(n_sample, len(w.query_seqs))
     threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
     ref = O.Reference(O.Model(w.exch, w.statd, w.rates, w.site_cats), w.parent, w.bl, w.leaf_row, w.ref_seqs)
+    t_pre = time.perf_counter() - t0
     t0 = time.perf_counter()
     ref.place(w.query_seqs[:n], O.make_prefs(**prefs_kw), n_threads=threads)
     dt = time.perf_counter() - t0
-    return n / dt, threads, n, dt
+    return n / dt, threads, n, dt, t_pre
+
+
+def cpu_refine_pass(w):
+    """One of the oracle's category passes of the CAT site-category
+    refinement (gcat_model.ml:387-419: the whole tree's per-site likelihood
+    with every site in one category), one thread; the refinement runs one
+    per category."""
+    import numpy as np
+    from oracle import oracle as O
+    t0 = time.perf_counter()
+    cat = np.zeros(w.n_sites, dtype=np.int32)
+    O.Reference(O.Model(w.exch, w.statd, w.rates, cat), w.parent, w.bl, w.leaf_row, w.ref_seqs).root_site_loglike()
+    return time.perf_counter() - t0
 
 
 def run_reference(args):
@@ -392,6 +409,26 @@ def run_ours(args):
     hb_in.close()
     hb_out.close()
     e2e = Q * world * args.steps / t_e2e
+    # ---- the reference-tree precompute (like_stree.ml:43-110: distal and
+    # proximal GLVs, exponent pulls, supernodes) and, for CAT models, the
+    # site-category refinement (gcat_model.ml:387-419), by wall clock through
+    # the C ABI: host preparation, uploads, kernels and the final
+    # synchronisation; last, as the refinement replaces the categories ----
+    pre = None
+    if args.precompute_steps > 0:
+        tp = []
+        for _ in range(args.precompute_steps):
+            t0 = time.perf_counter()
+            eng.precompute(w.leaf_row, w.ref_seqs)
+            tp.append(time.perf_counter() - t0)
+        pre = {"gpu_ms": 1e3 * min(tp), "steps": args.precompute_steps}
+        if w.site_cats is not None:
+            tr = []
+            for _ in range(args.precompute_steps):
+                t0 = time.perf_counter()
+                eng.refine_categories(w.leaf_row, w.ref_seqs)
+                tr.append(time.perf_counter() - t0)
+            pre["refine_categories_gpu_ms"] = 1e3 * min(tr)
     if rank != 0:
         return
     # ---- roofline of the dominant kernel ----
@@ -433,7 +470,14 @@ def run_ours(args):
     t_s1 = phase[0] / 1e3 / args.steps
     bf16_peak, bf16_kind = load_bf16_peak()
     s1_tflops = s1_flops / t_s1 / 1e12 if t_s1 > 0 else 0.0
-    cpu_v, cpu_threads, cpu_n, cpu_dt = cpu_baseline(w, args.cpu_sample, dict(w.prefs))
+    cpu_v, cpu_threads, cpu_n, cpu_dt, cpu_pre = cpu_baseline(w, args.cpu_sample, dict(w.prefs))
+    if pre is not None:
+        pre["cpu_ms"] = 1e3 * cpu_pre
+        pre["cpu"] = "the oracle's FP64 precompute (reference construction), one thread"
+        if "refine_categories_gpu_ms" in pre:
+            pre["refine_categories_cpu_ms"] = 1e3 * cpu_refine_pass(w) * len(w.rates)
+            pre["refine_categories_cpu"] = ("one category pass of the oracle's refinement, one thread, "
+                                            "times the %d categories" % len(w.rates))
     line = {
         "metric": "query placements/s", "value": value, "unit": "placements/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps,
@@ -480,6 +524,7 @@ def run_ours(args):
                 "device_batch": args.batch if args.batch else "automatic"},
         "brent_replica": brent,
         "with_posterior_probabilities": pp,
+        "tree_precompute": pre,
         "newton_evals_per_trial": counts[2] / counts[1] if counts[1] else None,
         "gpu_launches": int(launches),
         "clocks": clocks,
